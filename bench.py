@@ -1,0 +1,332 @@
+"""Benchmark of the FDTD time-stepping path: Yee cell-steps per second on the 512^3 plain-method
+workload (thin-wire dipole with a 50-ohm pulsed feed among 5% random dielectric blocks, 16-cell
+absorber, port series recorded every step), with the HBM roofline of the fused Yee kernel and the
+CPU restatement's throughput beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--size 512]
+
+One JSON line on rank 0. A step is one leapfrog step (B, E, sources) plus the per-step monitors,
+over the whole grid. Inputs (6.4 GB of field state) are far larger than L2 (129 MB), so no flush
+is needed between steps. Multi-GPU runs are replicas: each rank steps its own copy of the scene
+(weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+BYTES_PER_CELL_STEP = 60  # E and B read + write in FP32 (48 B) + six binary16 edge materials (12 B)
+METRIC = "Yee Mcells/s (cell-steps per second, 1e6)"
+
+
+def _rank_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        rows = []
+        for line in (getattr(self, "out", "") or "").splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def build_scene(size: int, steps: int):
+    from em_lab_gb300 import configs
+    return configs.plain_large(steps=steps, size=size)
+
+
+def load_grid(grid, sc):
+    m = sc.materials
+    grid.upload_materials(m.sigma, m.epsilon_r, sc.edges, sc.wires)
+    grid.set_sources(sc.sources)
+
+
+def cpu_sample(sc, seconds_budget: float = 20.0, max_steps: int = 8):
+    """The FP32 CPU restatement on every host thread, over the full grid, for a few steps."""
+    import oracle
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    o = oracle.Oracle(sc.grid, "f32")
+    t0 = time.perf_counter()
+    oracle.load_scene(o, sc)
+    ports = [p.to_c() for p in sc.ports]
+    o.ports_configure(ports, sc.ports[0].wavelength if sc.ports else 16.0, 4.0, sweep=True)
+    setup = time.perf_counter() - t0
+    cells = float(np.prod(sc.grid.size))
+    o.step(1)  # warm-up (first touch of every page)
+    steps = 0
+    t0 = time.perf_counter()
+    while steps < max_steps:
+        o.step(1)
+        steps += 1
+        if time.perf_counter() - t0 > seconds_budget:
+            break
+    el = time.perf_counter() - t0
+    o.close()
+    return {"value": cells * steps / el / 1e6, "unit": "Mcells/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} full-grid steps of the {sc.grid.nx}^3 workload after 1 warm-up step "
+                      f"(oracle/emlab_oracle.c FP32, OpenMP {threads} threads, set-up {setup:.1f} s excluded)"}
+
+
+def run_reference(args):
+    """The reference's CPU implementation of the path on the host cores."""
+    rank, world, _ = _rank_env()
+    if rank != 0:
+        return 0
+    sc = build_scene(args.size, args.steps)
+    kind = "port"
+    try:
+        from oracle import ref as refmod  # the reference's shaders compiled through the GLSL shim
+        if refmod.available():
+            kind = "reference"
+    except Exception:
+        refmod = None
+    cells = float(np.prod(sc.grid.size))
+    threads = os.cpu_count() or 1
+    if kind == "reference":
+        runner = refmod.RefGrid(sc.grid)
+        refmod.set_threads(threads)
+        runner.load_scene(sc)
+    else:
+        import oracle
+        oracle.set_threads(threads)
+        runner = oracle.Oracle(sc.grid, "f32")
+        oracle.load_scene(runner, sc)
+    ports = [p.to_c() for p in sc.ports]
+    runner.ports_configure(ports, sc.ports[0].wavelength, 4.0, sweep=True)
+    # each bench step is a bounded sample: one full-grid leapfrog step
+    for _ in range(max(1, min(args.warmup, 1))):
+        runner.step(1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        runner.step(1)
+    el = time.perf_counter() - t0
+    value = cells * args.steps / el / 1e6
+    sample = (f"{args.steps} full-grid leapfrog steps (B, E, sources, port monitor) of the {args.size}^3 workload, "
+              f"{'reference shaders compiled as C++ (oracle/_ref)' if kind == 'reference' else 'CPU restatement oracle/emlab_oracle.c FP32'}, "
+              f"{threads} host threads")
+    line = {"metric": METRIC, "value": value, "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"plain_large {args.size}^3, 16-cell absorber, thin-wire dipole + 50-ohm pulsed "
+                                   f"feed, 5% random dielectric blocks (seed 12345)", "cells": int(cells)},
+            "cpu_baseline": {"value": value, "unit": "Mcells/s", "cores": threads, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--kernel", default="fused", choices=["fused", "split"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end leg (default: --steps)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    args.warmup = max(args.warmup, 3)
+
+    import torch
+    rank, world, local = _rank_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+
+    from em_lab_gb300 import SimulationGrid, abi, launch_count
+
+    sc = build_scene(args.size, args.steps)
+    cells = float(np.prod(sc.grid.size))
+    grid = SimulationGrid(sc.grid)
+    grid.set_kernel(abi.KERNEL_SPLIT if args.kernel == "split" else abi.KERNEL_FUSED)
+    load_grid(grid, sc)
+    ports = [p.to_c() for p in sc.ports]
+    wl = sc.ports[0].wavelength
+    grid.ports_configure(ports, wl, 4.0, sweep=True)
+    stream = torch.cuda.ExternalStream(grid.stream_handle())
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+        grid.synchronize(600000)
+
+    # --- device-resident leg: inputs already in HBM -----------------------------------------
+    grid.step(args.warmup)
+    barrier()
+    grid.set_timing(True)
+    grid.kernel_time(reset=True)
+    l0 = launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        grid.step(args.steps)
+        ev1.record(stream)
+        barrier()
+    launches = launch_count() - l0
+    elapsed_ms = ev0.elapsed_time(ev1)
+    kernel_ms, kernel_n = grid.kernel_time(reset=True)
+    grid.set_timing(False)
+    if dist is not None:
+        t = torch.tensor([elapsed_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed_ms = float(t.item())
+    value = cells * args.steps * world / (elapsed_ms * 1e-3) / 1e6
+    peak, peak_kind = _peaks()
+    per_launch_ms = kernel_ms / max(kernel_n, 1)
+    achieved = BYTES_PER_CELL_STEP * cells / (per_launch_ms * 1e-3) / 1e9
+
+    # --- end-to-end leg through the C ABI with host buffers ------------------------------------
+    # The headless frame loop of the reference (Main.cpp:1074-1099): each frame steps the grid
+    # (the host computes the source signals and monitor rotations in FP64 and uploads them), then
+    # reads back the probe neighbourhood and the flux box; the port (V, I) series is read back at
+    # the end. Host<->device copies are inside the timed region.
+    e2e_steps = args.e2e_steps or args.steps
+    frame = 2
+    probe = [(int(sc.grid.nx * 0.25), sc.grid.ny // 2, sc.grid.nz // 2)]
+    n = sc.grid.nx
+    b0, b1 = n // 2 - 12, n // 2 + 12
+    planes = []
+    for ax in range(3):
+        for idx in (b0, b1):
+            planes.append(abi.FluxPlane(ax, idx, (b0, b0), (b1 + 1, b1 + 1)))
+    grid.ports_configure(ports, wl, 4.0, sweep=True)
+    barrier()
+    t0 = time.perf_counter()
+    frames = 0
+    for _ in range(e2e_steps // frame):
+        grid.step(frame)
+        grid.probe_gather(probe)
+        grid.flux_planes(planes)
+        frames += 1
+    series = grid.ports_series()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = cells * frames * frame * world / e2e_s / 1e6
+    nsrc = len(sc.sources)
+    h2d = 4 * nsrc + 16 + 16 * (2 if sc.far_field else 1)  # signals + rotations per step (+ blends per call)
+    d2h = (len(probe) * 54 * 16 + 6 * 4 * ((b1 - b0 + 16) // 16) ** 2) / frame + 8 * len(ports)
+    finite = grid.check_finite()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_sample(sc)
+        except Exception as e:  # pragma: no cover - reported, not fatal
+            cpu = {"value": None, "unit": "Mcells/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {e}"}
+
+    if rank == 0:
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(prof):
+            try:
+                with open(prof) as f:
+                    tj = json.load(f)
+                traffic = tj.get(f"{args.kernel}_{args.size}")
+            except Exception:
+                traffic = None
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"plain_large {args.size}^3, 16-cell absorber, thin-wire half-wave dipole with a "
+                                   f"50-ohm Gaussian-pulse feed, 5% seeded random dielectric blocks, port series "
+                                   f"recorded every step", "cells": int(cells), "kernel": args.kernel,
+                       "l2": "inputs larger than L2 (6.4 GB of field state per step)",
+                       "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": f"yee_{args.kernel}", "kernel_ms_per_launch": per_launch_ms,
+                         "algorithmic_bytes_per_cell_step": BYTES_PER_CELL_STEP},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "Mcells/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "frames": frames, "steps_per_frame": frame, "series_steps": int(series.shape[0])},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "finite": bool(finite),
+        }
+        print(json.dumps(line), flush=True)
+    grid.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,131 @@
+"""Scene builders for the benchmark workloads and the parity-test scenes.
+
+`plain_small` is the 128^3 point-dipole + dielectric-sphere scene (the scene of README.md:39-48
+with eps_r = 2.25); `plain_large` is the 512^3 thin-wire half-wave dipole with a 50-ohm pulsed
+feed among seeded random dielectric blocks. Both use seeded synthetic geometry; there is no
+external dataset. `random_scene` builds small seeded scenes that exercise every solver feature
+(lossy and metal cells, absorber, thin wires, feeds, several sources) for the parity tests.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import abi
+from .scene import EnvironmentBuilder, Material, SourceDesc, resolve_material
+
+f32 = np.float32
+
+
+def plain_small(steps: int = 2000):
+    """128^3 grid, FP32, vacuum, 10-cell absorber, Courant 0.5; eps_r 2.25 sphere of radius 10 at
+    centre + 30 x; z point dipole at the centre, CW lambda = 16, amplitude 7, 3-period ramp; probe at
+    centre - 30 x; 24-cell flux box; far-field box with the default 4-cell margin."""
+    grid = abi.GridConfig((128, 128, 128), courant=0.5, pml_thickness=10, pml_sigma_max=1.6, pml_grading=3.0)
+    b = EnvironmentBuilder("plain_small", grid, wavelength=16.0)
+    c = (64.0, 64.0, 64.0)
+    b.sphere((94.0, 64.0, 64.0), 10.0, Material(0.0, 2.25))
+    src = SourceDesc.dipole(c, (0.0, 0.0, 1.0), 16.0, 7.0, 0.0)
+    b.scene.sources.append(src)
+    b.scene.probes.append(("behind", (34.0, 64.0, 64.0)))
+    b.scene.fluxes.append(("radiated", (52, 52, 52), (76, 76, 76)))
+    L = grid.pml_thickness
+    b.scene.far_field = {"box_min": (L + 1 + 4,) * 3, "box_max": tuple(n - L - 2 - 4 for n in grid.size),
+                         "wavelength": 16.0, "averaging": 4.0}
+    sc = b.build()
+    sc.steps = steps
+    return sc
+
+
+def random_blocks(builder: EnvironmentBuilder, fraction: float, seed: int, lo: int, hi: int, keep_out=None,
+                  cell_size=1.0e-3, edge_range=(4, 24)):
+    """Seeded dielectric blocks until `fraction` of the cells is filled: edges uniform in
+    edge_range, eps_r uniform in [1, 10], sigma log-uniform in [1e-4, 1e-1] S/m."""
+    rng = np.random.default_rng(seed)
+    mats = builder.scene.materials
+    nx, ny, nz = builder.scene.grid.size
+    target = fraction * nx * ny * nz
+    filled = np.zeros((nz, ny, nx), bool)
+    count = 0
+    blocks = 0
+    while count < target and blocks < 1_000_000:
+        e = rng.integers(edge_range[0], edge_range[1] + 1, size=3)
+        p = np.array([rng.integers(lo, max(lo + 1, hi - e[a])) for a in range(3)])
+        if keep_out is not None:
+            kc, kr = keep_out
+            if np.all(p + e > np.asarray(kc) - kr) and np.all(p < np.asarray(kc) + kr):
+                continue
+        eps = float(rng.uniform(1.0, 10.0))
+        sig_si = float(10.0 ** rng.uniform(-4.0, -1.0))
+        m = resolve_material(eps, cell_size, builder.scene.wavelength, conductivity=sig_si)
+        builder.box(tuple(float(v) for v in p), tuple(float(v) for v in p + e), m)
+        sl = (slice(p[2], p[2] + e[2]), slice(p[1], p[1] + e[1]), slice(p[0], p[0] + e[0]))
+        count += int((~filled[sl]).sum())
+        filled[sl] = True
+        blocks += 1
+    return blocks, count / float(nx * ny * nz)
+
+
+def plain_large(steps: int = 20000, size: int = 512, seed: int = 12345):
+    """512^3 grid, 16-cell absorber; thin-wire half-wave z dipole (lambda = 40, length 20, radius
+    0.05) with a 50-ohm resistive voltage feed driven by a Gaussian pulse (pulse_width 0.4 periods:
+    the spectrum covers about 0.3-1.7 f0); 5% of the cells in seeded random dielectric blocks; port
+    sweep at 128 frequencies; far-field box 20 cells inside the absorber."""
+    L = 16
+    grid = abi.GridConfig((size, size, size), courant=0.5, pml_thickness=L, pml_sigma_max=1.6, pml_grading=3.0)
+    wl = 40.0
+    b = EnvironmentBuilder("plain_large", grid, wavelength=wl)
+    c = (size * 0.5,) * 3
+    box_lo, box_hi = L + 20, size - L - 21
+    random_blocks(b, 0.05, seed, box_lo + 1, box_hi - 1, keep_out=(c, 24), edge_range=(4, 24))
+    wave = SourceDesc(wavelength=wl, waveform=abi.WAVE_PULSE, ramp_periods=0.4)
+    b.thin_dipole(wave, c, 2, 20.0, radius=0.05, impedance_ohm=50.0, drive=1.0, name="dipole")
+    b.scene.far_field = {"box_min": (box_lo,) * 3, "box_max": (box_hi,) * 3, "wavelength": wl, "averaging": 4.0}
+    b.scene.sweep = {"wavelength_min": wl / 1.7, "wavelength_max": wl / 0.3, "points": 128}
+    sc = b.build()
+    sc.steps = steps
+    return sc
+
+
+def random_scene(size=(24, 20, 18), pml=4, seed=1, thin_wire=True, lossy=True, sources=2, courant=0.5):
+    """Small seeded scene exercising every solver feature (parity tests)."""
+    rng = np.random.default_rng(seed)
+    grid = abi.GridConfig(size, courant=courant, pml_thickness=pml, pml_sigma_max=1.6, pml_grading=3.0)
+    b = EnvironmentBuilder(f"random{seed}", grid, wavelength=12.0)
+    nx, ny, nz = size
+    for _ in range(4):
+        e = rng.integers(2, 6, size=3)
+        p = np.array([rng.integers(0, max(1, n - 2)) for n in size])
+        m = Material(float(10 ** rng.uniform(-3, 0.5)) if lossy else 0.0, float(rng.uniform(1.0, 6.0)))
+        b.box(tuple(float(v) for v in p), tuple(float(v) for v in p + e), m)
+    if lossy:
+        p = np.array([rng.integers(pml, max(pml + 1, n - pml - 3)) for n in size])
+        b.box(tuple(float(v) for v in p), tuple(float(v) for v in p + 2), Material(100.0, 1.0))  # metal block
+    b.sphere((nx * 0.3, ny * 0.6, nz * 0.5), 3.0, Material(0.02, 2.25))
+    srcs = []
+    for k in range(sources):
+        cpos = tuple(float(v) for v in rng.uniform(pml + 2, np.asarray(size) - pml - 2))
+        ax = [0.0, 0.0, 0.0]
+        ax[k % 3] = 1.0
+        s = SourceDesc.dipole(cpos, ax, 12.0, float(rng.uniform(0.5, 3.0)), float(rng.integers(0, 4)))
+        s.phase = float(rng.uniform(0, 6.28))
+        if k % 2:
+            s.waveform = abi.WAVE_PULSE
+            s.ramp_periods = 0.5
+        srcs.append(s)
+    b.scene.sources.extend(srcs)
+    if thin_wire:
+        c = (nx * 0.5 + 0.3, ny * 0.5 - 0.2, nz * 0.5)
+        wave = SourceDesc(wavelength=12.0, waveform=abi.WAVE_CW, ramp_periods=1.0)
+        b.thin_dipole(wave, c, 2, 7.0, radius=0.05, impedance_ohm=50.0, drive=1.0, name="feed")
+    sc = b.build()
+    return sc
+
+
+def fibonacci_directions(n: int) -> np.ndarray:
+    """n unit vectors spread over the sphere (far-field test directions)."""
+    i = np.arange(n) + 0.5
+    phi = np.arccos(1 - 2 * i / n)
+    th = math.pi * (1 + 5 ** 0.5) * i
+    return np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], 1).astype(np.float32)

@@ -1,0 +1,960 @@
+// capi.cu - the C ABI (include/emlab.h): device buffers, the step loop and the monitors.
+//
+// SimulationGrid (src/SimulationGrid.cpp) keeps its state in GL textures and dispatches one compute
+// pass per kernel per sub-step from the host. Here the state lives in plain device arrays owned by
+// the handle, every launch goes to the handle's own CUDA stream, and the host only precomputes the
+// per-step scalars the reference also computes on the host (source signals and monitor rotations,
+// in FP64), uploading them once per chunk of steps.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/emlab.h"
+#include "emlab_internal.h"
+#include "setup.h"
+
+using namespace emlab;
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define EMLAB_CUDA(call)                                                                                      \
+    do {                                                                                                      \
+        cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess)                                                                                \
+            return fail(e_ == cudaErrorMemoryAllocation ? EMLAB_ERR_OOM : EMLAB_ERR_CUDA,                     \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                                  \
+    } while (0)
+
+#define EMLAB_REQUIRE(cond, msg) \
+    do {                         \
+        if (!(cond)) return fail(EMLAB_ERR_INVALID, msg); \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        release();
+        if (count == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        else p = nullptr;
+        return e;
+    }
+};
+
+constexpr int kChunk = 1024;  // sub-steps whose host-side scalars are uploaded together
+
+}  // namespace
+
+struct emlab_grid {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    emlab_grid_config cfg{};
+    bool configured = false;
+    int pitch = 0;
+    long long plane = 0;
+    long long padded = 0;  // floats per component array
+    DevBuf<float> fields;  // 12 component arrays: generation 0 (Ex..Bz), generation 1
+    int cur = 0;
+    int kernel = EMLAB_KERNEL_FUSED;
+    // materials
+    DevBuf<uint8_t> cls;
+    bool wide = false;
+    DevBuf<float4> tabE, tabM, tabW;
+    uint32_t classes = 0, wire_start = 0;
+    DevBuf<float> pml;
+    int pml_stride = 0;
+    std::vector<float> cell_sigma, cell_eps;  // alpha channels of the textures (read-back only)
+    // sources
+    std::vector<emlab_source> desc;
+    std::vector<float> packed;
+    DevBuf<float4> d_src;
+    DevBuf<int4> d_cells;
+    DevBuf<int> d_lists;
+    int nsrc = 0, ncells = 0;
+    // per-chunk scalars: signals[k][nsrc], port rot[k], ntff rot[k], line rot[k], blends
+    DevBuf<uint8_t> d_stage;
+    uint8_t* h_stage[2] = {nullptr, nullptr};
+    cudaEvent_t stage_done[2] = {nullptr, nullptr};
+    size_t stage_bytes = 0;
+    int stage_slot = 0;
+    uint64_t step = 0;
+    // ports
+    int nports = 0;
+    DevBuf<int4> d_ports;
+    DevBuf<float> d_port_ph, d_series;
+    size_t series_cap = 0, recorded = 0;
+    bool recording = false;
+    float port_wl = 16.0f, port_avg = 4.0f;
+    // ntff
+    bool ntff_on = false;
+    int box[13] = {};
+    int points = 0;
+    DevBuf<int> d_box;
+    DevBuf<float> d_ntff;
+    float ntff_wl = 16.0f, ntff_avg = 4.0f;
+    // lines
+    int nq = 0;
+    DevBuf<int4> d_q, d_terms;
+    DevBuf<float> d_weights, d_line_ph, d_line_now;
+    float line_wl = 16.0f, line_avg = 4.0f;
+    // scratch
+    DevBuf<unsigned> d_flag;
+    // solver-pass timing: event pairs recorded around each Yee launch, read back lazily
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_start, ev_stop;
+    size_t ev_used = 0;
+    double timed_ms = 0.0;
+    uint64_t timed_launches = 0;
+
+    float* comp(int gen, int c) { return fields.p + (size_t)(gen * 6 + c) * padded; }
+    long long cells() const { return (long long)cfg.nx * cfg.ny * cfg.nz; }
+};
+
+namespace {
+
+YeeArgs yee_args(emlab_grid* g) {
+    YeeArgs a{};
+    a.nx = g->cfg.nx, a.ny = g->cfg.ny, a.nz = g->cfg.nz;
+    a.pitch = g->pitch;
+    a.plane = g->plane;
+    const int c = g->cur, n = g->cur ^ 1;
+    a.ex = g->comp(c, 0), a.ey = g->comp(c, 1), a.ez = g->comp(c, 2);
+    a.bx = g->comp(c, 3), a.by = g->comp(c, 4), a.bz = g->comp(c, 5);
+    a.nex = g->comp(n, 0), a.ney = g->comp(n, 1), a.nez = g->comp(n, 2);
+    a.nbx = g->comp(n, 3), a.nby = g->comp(n, 4), a.nbz = g->comp(n, 5);
+    a.wex = g->comp(c, 0), a.wey = g->comp(c, 1), a.wez = g->comp(c, 2);
+    a.wbx = g->comp(c, 3), a.wby = g->comp(c, 4), a.wbz = g->comp(c, 5);
+    a.cls = g->cls.p;
+    a.tabE = g->tabE.p, a.tabM = g->tabM.p, a.tabW = g->tabW.p;
+    a.wire_start = g->wire_start;
+    a.pml = g->pml.p;
+    a.pml_stride = g->pml_stride;
+    a.L = g->cfg.pml_thickness;
+    a.dt = g->cfg.courant;
+    // z chunks: enough CTAs for ~4 per SM, but at least 8 planes each (one plane is recomputed)
+    const int ty = a.ny >= 256 ? 16 : 8;
+    const long long xy = (long long)((a.nx + 31) / 32) * ((a.ny + ty - 1) / ty);
+    const long long want = 152 * 4;
+    int chunks = (int)std::max<long long>(1, (want + xy - 1) / xy);
+    int zc = (a.nz + chunks - 1) / chunks;
+    zc = std::max(zc, std::min(8, a.nz));
+    a.zchunk = zc;
+    return a;
+}
+
+MonitorArgs monitor_args(emlab_grid* g) {
+    MonitorArgs m{};
+    m.nx = g->cfg.nx, m.ny = g->cfg.ny, m.nz = g->cfg.nz, m.pitch = g->pitch, m.plane = g->plane;
+    const int c = g->cur;
+    m.ex = g->comp(c, 0), m.ey = g->comp(c, 1), m.ez = g->comp(c, 2);
+    m.bx = g->comp(c, 3), m.by = g->comp(c, 4), m.bz = g->comp(c, 5);
+    return m;
+}
+
+int check_launch() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(EMLAB_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return EMLAB_OK;
+}
+
+int upload_class_table(emlab_grid* g, const ClassTable& t) {
+    const long long ncls = (long long)t.cls.size();
+    g->wide = t.classes > 65536u;
+    EMLAB_CUDA(g->cls.alloc((size_t)ncls * (g->wide ? 4 : 2)));
+    if (g->wide) {
+        EMLAB_CUDA(cudaMemcpyAsync(g->cls.p, t.cls.data(), (size_t)ncls * 4, cudaMemcpyHostToDevice, g->stream));
+        EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    } else {
+        std::vector<uint16_t> narrow((size_t)ncls);
+        for (long long i = 0; i < ncls; ++i) narrow[(size_t)i] = (uint16_t)t.cls[(size_t)i];
+        EMLAB_CUDA(cudaMemcpyAsync(g->cls.p, narrow.data(), (size_t)ncls * 2, cudaMemcpyHostToDevice, g->stream));
+        EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    }
+    EMLAB_CUDA(g->tabE.alloc(t.classes * 2));
+    EMLAB_CUDA(g->tabM.alloc(t.classes * 2));
+    EMLAB_CUDA(g->tabW.alloc(t.classes * 2));
+    EMLAB_CUDA(cudaMemcpy(g->tabE.p, t.tabE.data(), t.tabE.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpy(g->tabM.p, t.tabM.data(), t.tabM.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpy(g->tabW.p, t.tabW.data(), t.tabW.size() * 4, cudaMemcpyHostToDevice));
+    g->classes = t.classes;
+    g->wire_start = t.wire_start;
+    return EMLAB_OK;
+}
+
+int clear_fields(emlab_grid* g) {
+    EMLAB_CUDA(cudaMemsetAsync(g->fields.p, 0, g->fields.n * sizeof(float), g->stream));
+    g->cur = 0;
+    return EMLAB_OK;
+}
+
+void rotation(double w, double tE, double dt, float4& r) {
+    const double tH = tE - 0.5 * dt;
+    r = make_float4((float)std::cos(w * tE), (float)std::sin(w * tE), (float)std::cos(w * tH), (float)std::sin(w * tH));
+}
+
+float blend_of(float avg, float wl, double dt) {
+    const double tau = (double)avg * (double)wl;
+    return (float)(1.0 - std::exp(-dt / (0.5 * tau)));
+}
+
+int ensure_stage(emlab_grid* g, size_t bytes) {
+    if (bytes <= g->stage_bytes) return EMLAB_OK;
+    for (int s = 0; s < 2; ++s) {
+        if (g->stage_done[s]) cudaEventSynchronize(g->stage_done[s]);
+        if (g->h_stage[s]) cudaFreeHost(g->h_stage[s]);
+        g->h_stage[s] = nullptr;
+        EMLAB_CUDA(cudaMallocHost(&g->h_stage[s], bytes));
+    }
+    EMLAB_CUDA(g->d_stage.alloc(bytes));
+    g->stage_bytes = bytes;
+    return EMLAB_OK;
+}
+
+// Folds the recorded event pairs into timed_ms (waits for the last one).
+int drain_timing(emlab_grid* g) {
+    if (!g->ev_used) return EMLAB_OK;
+    EMLAB_CUDA(cudaEventSynchronize(g->ev_stop[g->ev_used - 1]));
+    for (size_t i = 0; i < g->ev_used; ++i) {
+        float ms = 0.0f;
+        EMLAB_CUDA(cudaEventElapsedTime(&ms, g->ev_start[i], g->ev_stop[i]));
+        g->timed_ms += ms;
+    }
+    g->timed_launches += g->ev_used;
+    g->ev_used = 0;
+    return EMLAB_OK;
+}
+
+int timing_pair(emlab_grid* g, cudaEvent_t* start, cudaEvent_t* stop) {
+    if (g->ev_used == 4096)
+        if (int rc = drain_timing(g)) return rc;
+    while (g->ev_start.size() <= g->ev_used) {
+        cudaEvent_t a, b;
+        EMLAB_CUDA(cudaEventCreate(&a));
+        EMLAB_CUDA(cudaEventCreate(&b));
+        g->ev_start.push_back(a);
+        g->ev_stop.push_back(b);
+    }
+    *start = g->ev_start[g->ev_used];
+    *stop = g->ev_stop[g->ev_used];
+    ++g->ev_used;
+    return EMLAB_OK;
+}
+
+int require_grid(const emlab_grid* g) {
+    if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
+    if (!g->configured) return fail(EMLAB_ERR_INVALID, "grid is not configured");
+    return EMLAB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* emlab_last_error(void) { return g_last_error.c_str(); }
+int emlab_version(void) { return 1; }
+uint64_t emlab_launch_count(void) { return g_launches.load(); }
+
+int emlab_grid_create(emlab_grid** out) {
+    if (!out) return fail(EMLAB_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return fail(EMLAB_ERR_NO_DEVICE, "no CUDA device is visible");
+    emlab_grid* g = new (std::nothrow) emlab_grid();
+    if (!g) return fail(EMLAB_ERR_OOM, "host allocation failed");
+    cudaGetDevice(&g->device);
+    if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g->stage_done[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g->stage_done[1], cudaEventDisableTiming) != cudaSuccess ||
+        g->d_flag.alloc(1) != cudaSuccess) {
+        delete g;
+        return fail(EMLAB_ERR_CUDA, "stream or event creation failed");
+    }
+    *out = g;
+    return EMLAB_OK;
+}
+
+int emlab_grid_destroy(emlab_grid* g) {
+    if (!g) return EMLAB_OK;
+    cudaSetDevice(g->device);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    for (int s = 0; s < 2; ++s) {
+        if (g->h_stage[s]) cudaFreeHost(g->h_stage[s]);
+        if (g->stage_done[s]) cudaEventDestroy(g->stage_done[s]);
+    }
+    for (size_t i = 0; i < g->ev_start.size(); ++i) cudaEventDestroy(g->ev_start[i]), cudaEventDestroy(g->ev_stop[i]);
+    cudaStream_t s = g->stream;
+    delete g;
+    if (s) cudaStreamDestroy(s);
+    return EMLAB_OK;
+}
+
+int emlab_grid_configure(emlab_grid* g, const emlab_grid_config* req) {
+    if (!g || !req) return fail(EMLAB_ERR_INVALID, "null argument");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    emlab_grid_config c = *req;
+    clamp_config(c);
+    const int pitch = row_pitch(c.nx);
+    const long long plane = (long long)pitch * c.ny;
+    const long long padded = plane * c.nz;
+    if (!g->configured || c.nx != g->cfg.nx || c.ny != g->cfg.ny || c.nz != g->cfg.nz || !g->fields.p) {
+        g->fields.release();
+        g->cls.release();
+        cudaError_t e = g->fields.alloc((size_t)padded * 12);
+        if (e != cudaSuccess) {
+            g->configured = false;
+            return fail(EMLAB_ERR_OOM, "SimulationGrid: field allocation failed (grid too large for device memory)");
+        }
+    }
+    g->cfg = c;
+    g->pitch = pitch, g->plane = plane, g->padded = padded;
+    g->pml_stride = std::max(c.nx, std::max(c.ny, c.nz));
+    const std::vector<float> pt = pml_tables(c, g->pml_stride);
+    EMLAB_CUDA(g->pml.alloc(pt.size()));
+    EMLAB_CUDA(cudaMemcpy(g->pml.p, pt.data(), pt.size() * 4, cudaMemcpyHostToDevice));
+    // vacuum materials: class 0 everywhere (SimulationGrid.cpp:185-192)
+    const long long n = g->cells();
+    try {
+        g->cell_sigma.assign((size_t)n, 0.0f);
+        g->cell_eps.assign((size_t)n, 1.0f);
+    } catch (const std::bad_alloc&) {
+        return fail(EMLAB_ERR_OOM, "host allocation failed");
+    }
+    ClassTable t;
+    t.classes = 1, t.wire_start = 1;
+    t.tabM = {0, 0, 0, 1, 1, 1, 0, 0};
+    t.tabW = {1, 1, 1, 1, 1, 1, 0, 0};
+    t.tabE.assign(8, 0.0f);
+    class_coefficients(t, c.courant);
+    g->wide = false;
+    EMLAB_CUDA(g->cls.alloc((size_t)padded * 2));
+    EMLAB_CUDA(cudaMemsetAsync(g->cls.p, 0, (size_t)padded * 2, g->stream));
+    EMLAB_CUDA(g->tabE.alloc(2));
+    EMLAB_CUDA(g->tabM.alloc(2));
+    EMLAB_CUDA(g->tabW.alloc(2));
+    EMLAB_CUDA(cudaMemcpy(g->tabE.p, t.tabE.data(), 32, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpy(g->tabM.p, t.tabM.data(), 32, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpy(g->tabW.p, t.tabW.data(), 32, cudaMemcpyHostToDevice));
+    g->classes = 1, g->wire_start = 1;
+    int rc = clear_fields(g);
+    if (rc) return rc;
+    g->step = 0;
+    g->configured = true;
+    // the source lists index cells of the old size: rebuild them for the new one
+    if (!g->desc.empty()) {
+        std::vector<emlab_source> d = g->desc;
+        rc = emlab_grid_set_sources(g, d.data(), d.size());
+        if (rc) return rc;
+    }
+    emlab_ports_configure(g, nullptr, 0, 16.0f, 4.0f, 0, 0);
+    int zero[3] = {0, 0, 0};
+    emlab_ntff_configure(g, zero, zero, 0.0f, 4.0f, nullptr);
+    emlab_lines_configure(g, nullptr, 0, nullptr, nullptr, 0, 16.0f, 4.0f);
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    return EMLAB_OK;
+}
+
+int emlab_grid_get_config(const emlab_grid* g, emlab_grid_config* out) {
+    if (int rc = require_grid(g)) return rc;
+    if (!out) return fail(EMLAB_ERR_INVALID, "null output");
+    *out = g->cfg;
+    return EMLAB_OK;
+}
+
+int emlab_grid_upload_materials(emlab_grid* g, const float* sigma, const float* eps_r, int nx, int ny, int nz,
+                                const emlab_edge_override* edges, size_t n_edges, const emlab_wire_term* wires,
+                                size_t n_wires) {
+    if (int rc = require_grid(g)) return rc;
+    if (nx != g->cfg.nx || ny != g->cfg.ny || nz != g->cfg.nz)
+        return fail(EMLAB_ERR_INVALID, "SimulationGrid: material volume size does not match the grid");
+    EMLAB_REQUIRE(sigma && eps_r, "null material array");
+    EMLAB_REQUIRE((edges || n_edges == 0) && (wires || n_wires == 0), "null override array");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    ClassTable t;
+    std::string err;
+    if (!build_classes(sigma, eps_r, nx, ny, nz, edges, n_edges, wires, n_wires, g->cfg.courant, t, err))
+        return fail(EMLAB_ERR_OOM, err);
+    if (int rc = upload_class_table(g, t)) return rc;
+    const long long n = g->cells();
+    std::memcpy(g->cell_sigma.data(), sigma, (size_t)n * 4);
+    std::memcpy(g->cell_eps.data(), eps_r, (size_t)n * 4);
+    if (int rc = clear_fields(g)) return rc;
+    g->step = 0;
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    return EMLAB_OK;
+}
+
+int emlab_grid_set_sources(emlab_grid* g, const emlab_source* sources, size_t n) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(sources || n == 0, "null source array");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    std::vector<emlab_source> desc;
+    std::vector<float> packed;
+    g->nsrc = pack_sources(sources, n, desc, packed);
+    g->desc = desc;
+    g->packed = packed;
+    std::vector<int32_t> cells, lists;
+    const int dims[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+    source_lists(packed, g->nsrc, dims, cells, lists);
+    g->ncells = (int)(cells.size() / 4) - 1;
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));  // buffers may be in use by queued steps
+    EMLAB_CUDA(g->d_src.alloc(std::max<size_t>(1, packed.size() / 4)));
+    if (!packed.empty())
+        EMLAB_CUDA(cudaMemcpy(g->d_src.p, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_cells.alloc(cells.size() / 4));
+    EMLAB_CUDA(cudaMemcpy(g->d_cells.p, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_lists.alloc(lists.size()));
+    EMLAB_CUDA(cudaMemcpy(g->d_lists.p, lists.data(), lists.size() * 4, cudaMemcpyHostToDevice));
+    return EMLAB_OK;
+}
+
+int emlab_grid_reset_fields(emlab_grid* g) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    if (int rc = clear_fields(g)) return rc;
+    g->step = 0;
+    return EMLAB_OK;
+}
+
+int emlab_grid_step(emlab_grid* g, int count) {
+    if (int rc = require_grid(g)) return rc;
+    if (count <= 0) return EMLAB_OK;
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    const double dt = (double)g->cfg.courant;
+    const int nsrc = g->nsrc;
+    for (int base = 0; base < count; base += kChunk) {
+        const int m = std::min(kChunk, count - base);
+        // stage layout: signals m*nsrc floats | port rot m float4 | ntff rot | line rot | 3 blends
+        const size_t sig_bytes = ((size_t)m * nsrc * 4 + 15) / 16 * 16;
+        const size_t rot_bytes = (size_t)m * 16;
+        const size_t bytes = sig_bytes + 3 * rot_bytes + 16 * 3;
+        if (int rc = ensure_stage(g, bytes)) return rc;
+        const int slot = g->stage_slot;
+        g->stage_slot ^= 1;
+        EMLAB_CUDA(cudaEventSynchronize(g->stage_done[slot]));  // the slot's previous copy has finished
+        uint8_t* h = g->h_stage[slot];
+        float* sig = reinterpret_cast<float*>(h);
+        float4* prot = reinterpret_cast<float4*>(h + sig_bytes);
+        float4* nrot = prot + m;
+        float4* lrot = nrot + m;
+        float* blends = reinterpret_cast<float*>(lrot + m);
+        for (int k = 0; k < m; ++k) {
+            // E^{n+1} uses J at t = (n + 1/2) dt (SimulationGrid.cpp:371-387)
+            const double t = ((double)(g->step + (uint64_t)k) + 0.5) * dt;
+            for (int s = 0; s < nsrc; ++s) sig[(size_t)k * nsrc + s] = (float)source_signal(g->desc[s], t);
+            // monitors see the time of the completed step: t_E = n dt, t_H = t_E - dt/2
+            const double tE = (double)(g->step + (uint64_t)k + 1) * dt;
+            if (g->nports) rotation(6.28318530717958647692 / g->port_wl, tE, dt, prot[k]);
+            if (g->ntff_on) rotation(6.28318530717958647692 / g->ntff_wl, tE, dt, nrot[k]);
+            if (g->nq) rotation(6.28318530717958647692 / g->line_wl, tE, dt, lrot[k]);
+        }
+        blends[0] = blend_of(g->port_avg, g->port_wl, dt);
+        blends[1] = blend_of(g->ntff_avg, g->ntff_wl, dt);
+        blends[2] = blend_of(g->line_avg, g->line_wl, dt);
+        uint8_t* d = g->d_stage.p;
+        EMLAB_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g->stream));
+        EMLAB_CUDA(cudaEventRecord(g->stage_done[slot], g->stream));
+        const float* d_sig = reinterpret_cast<const float*>(d);
+        const float4* d_prot = reinterpret_cast<const float4*>(d + sig_bytes);
+        const float4* d_nrot = d_prot + m;
+        const float4* d_lrot = d_nrot + m;
+        const float* d_bl = reinterpret_cast<const float*>(d_lrot + m);
+        // monitor kernels get this sub-step's rotation and their blend by pointer (index 0)
+        for (int k = 0; k < m; ++k) {
+            YeeArgs a = yee_args(g);
+            cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+            if (g->timing) {
+                if (int rc = timing_pair(g, &ev0, &ev1)) return rc;
+                EMLAB_CUDA(cudaEventRecord(ev0, g->stream));
+            }
+            if (g->kernel == EMLAB_KERNEL_SPLIT) {
+                launch_yee_split(a, g->wide, g->stream);
+                g_launches += 2;
+            } else {
+                launch_yee_fused(a, g->wide, g->stream);
+                g_launches += 1;
+                g->cur ^= 1;
+                a = yee_args(g);  // sources act on the new generation
+            }
+            if (g->timing) EMLAB_CUDA(cudaEventRecord(ev1, g->stream));
+            if (g->ncells > 0) {
+                SourceArgs sa{};
+                sa.cells = g->d_cells.p, sa.lists = g->d_lists.p, sa.src = g->d_src.p;
+                sa.signals = d_sig, sa.nsrc = nsrc, sa.ncells = g->ncells;
+                launch_sources(a, sa, k, g->wide, g->stream);
+                g_launches += 1;
+            }
+            ++g->step;
+            const MonitorArgs mon = monitor_args(g);
+            if (g->ntff_on) {
+                launch_ntff(mon, g->d_box.p, g->points, g->d_ntff.p, d_nrot + k, d_bl + 1, 0, g->stream);
+                g_launches += 1;
+            }
+            if (g->nports) {
+                long long rec = -1;
+                if (g->recording && g->recorded < g->series_cap) rec = (long long)g->recorded++;
+                launch_ports(mon, g->d_ports.p, g->nports, g->d_port_ph.p, g->d_series.p, rec, d_prot + k, d_bl, 0,
+                             g->stream);
+                g_launches += 1;
+            }
+            if (g->nq) {
+                launch_lines(mon, g->d_q.p, g->nq, g->d_terms.p, g->d_weights.p, g->d_line_ph.p, g->d_line_now.p,
+                             d_lrot + k, d_bl + 2, 0, g->stream);
+                g_launches += 1;
+            }
+            if (int rc = check_launch()) return rc;
+        }
+    }
+    return EMLAB_OK;
+}
+
+int emlab_grid_synchronize(emlab_grid* g, int timeout_ms) {
+    if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
+    const auto limit = std::chrono::milliseconds(timeout_ms > 0 ? timeout_ms : 60000);
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(g->stream);
+        if (e == cudaSuccess) return EMLAB_OK;
+        if (e != cudaErrorNotReady) return fail(EMLAB_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
+        if (std::chrono::steady_clock::now() - t0 > limit) return fail(EMLAB_ERR_TIMEOUT, "grid stream wait timed out");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
+int emlab_grid_get_state(const emlab_grid* g, emlab_grid_state* out) {
+    if (int rc = require_grid(g)) return rc;
+    if (!out) return fail(EMLAB_ERR_INVALID, "null output");
+    out->dt = g->cfg.courant;
+    out->step_count = g->step;
+    out->time = (double)g->step * (double)g->cfg.courant;
+    out->nx = g->cfg.nx, out->ny = g->cfg.ny, out->nz = g->cfg.nz;
+    out->device_bytes = g->fields.n * 4 + g->cls.n + (g->tabE.n + g->tabM.n + g->tabW.n) * 16 + g->pml.n * 4 +
+                        g->d_ntff.n * 4 + g->d_series.n * 4;
+    out->source_cells = g->ncells;
+    out->kernel = g->kernel;
+    return EMLAB_OK;
+}
+
+static int read_comp(emlab_grid* g, int c, float* host, int stride, int offset) {
+    const int nx = g->cfg.nx, ny = g->cfg.ny, nz = g->cfg.nz;
+    std::vector<float> tmp((size_t)g->padded);
+    EMLAB_CUDA(cudaMemcpyAsync(tmp.data(), g->comp(g->cur, c), (size_t)g->padded * 4, cudaMemcpyDeviceToHost, g->stream));
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y) {
+            const float* src = tmp.data() + (size_t)z * g->plane + (size_t)y * g->pitch;
+            const size_t row = ((size_t)z * ny + y) * nx;
+            for (int x = 0; x < nx; ++x) host[(row + x) * stride + offset] = src[x];
+        }
+    return EMLAB_OK;
+}
+
+int emlab_grid_read_fields(emlab_grid* g, float* e_rgba, float* b_rgba) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    const long long n = g->cells();
+    for (int c = 0; c < 6; ++c) {
+        float* dst = c < 3 ? e_rgba : b_rgba;
+        if (!dst) continue;
+        if (int rc = read_comp(g, c, dst, 4, c % 3)) return rc;
+    }
+    for (long long i = 0; i < n; ++i) {
+        if (e_rgba) e_rgba[i * 4 + 3] = g->cell_sigma[(size_t)i];
+        if (b_rgba) b_rgba[i * 4 + 3] = g->cell_eps[(size_t)i];
+    }
+    return EMLAB_OK;
+}
+
+int emlab_grid_read_components(emlab_grid* g, float* ex, float* ey, float* ez, float* bx, float* by, float* bz) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    float* out[6] = {ex, ey, ez, bx, by, bz};
+    for (int c = 0; c < 6; ++c)
+        if (out[c])
+            if (int rc = read_comp(g, c, out[c], 1, 0)) return rc;
+    return EMLAB_OK;
+}
+
+int emlab_grid_write_components(emlab_grid* g, const float* ex, const float* ey, const float* ez, const float* bx,
+                                const float* by, const float* bz) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    const float* in[6] = {ex, ey, ez, bx, by, bz};
+    const int nx = g->cfg.nx, ny = g->cfg.ny, nz = g->cfg.nz;
+    std::vector<float> tmp((size_t)g->padded, 0.0f);
+    for (int c = 0; c < 6; ++c) {
+        if (!in[c]) continue;
+        for (int z = 0; z < nz; ++z)
+            for (int y = 0; y < ny; ++y)
+                std::memcpy(tmp.data() + (size_t)z * g->plane + (size_t)y * g->pitch, in[c] + ((size_t)z * ny + y) * nx,
+                            (size_t)nx * 4);
+        EMLAB_CUDA(cudaMemcpyAsync(g->comp(g->cur, c), tmp.data(), (size_t)g->padded * 4, cudaMemcpyHostToDevice,
+                                   g->stream));
+        EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    }
+    return EMLAB_OK;
+}
+
+int emlab_grid_set_kernel(emlab_grid* g, int kernel) {
+    if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
+    EMLAB_REQUIRE(kernel == EMLAB_KERNEL_FUSED || kernel == EMLAB_KERNEL_SPLIT, "unknown kernel");
+    g->kernel = kernel;
+    return EMLAB_OK;
+}
+
+int emlab_grid_stream(emlab_grid* g, void** stream) {
+    if (!g || !stream) return fail(EMLAB_ERR_INVALID, "null argument");
+    *stream = (void*)g->stream;
+    return EMLAB_OK;
+}
+
+int emlab_grid_set_timing(emlab_grid* g, int enabled) {
+    if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
+    if (!enabled)
+        if (int rc = drain_timing(g)) return rc;
+    g->timing = enabled != 0;
+    return EMLAB_OK;
+}
+
+int emlab_grid_kernel_time(emlab_grid* g, double* ms, uint64_t* launches, int reset) {
+    if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
+    if (int rc = drain_timing(g)) return rc;
+    if (ms) *ms = g->timed_ms;
+    if (launches) *launches = g->timed_launches;
+    if (reset) g->timed_ms = 0.0, g->timed_launches = 0;
+    return EMLAB_OK;
+}
+
+int emlab_grid_check_finite(emlab_grid* g) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    EMLAB_CUDA(cudaMemsetAsync(g->d_flag.p, 0, 4, g->stream));
+    launch_check_finite(monitor_args(g), g->d_flag.p, g->stream);
+    ++g_launches;
+    if (int rc = check_launch()) return rc;
+    unsigned flag = 0;
+    EMLAB_CUDA(cudaMemcpyAsync(&flag, g->d_flag.p, 4, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    if (flag) return fail(EMLAB_ERR_NONFINITE, "non-finite field values detected");
+    return EMLAB_OK;
+}
+
+// ---- ports ---------------------------------------------------------------------------------
+int emlab_ports_configure(emlab_grid* g, const emlab_port* ports, size_t n, float wavelength, float averaging_periods,
+                          int sweep, size_t record_steps) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(ports || n == 0, "null port array");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    n = std::min<size_t>(n, 256);
+    g->nports = (int)n;
+    g->port_avg = std::max(averaging_periods, 0.5f);
+    g->port_wl = std::max(wavelength, 2.0f);
+    g->recorded = 0, g->series_cap = 0, g->recording = false;
+    g->d_ports.release(), g->d_port_ph.release(), g->d_series.release();
+    if (!n) return EMLAB_OK;
+    std::vector<int4> pk;
+    for (size_t i = 0; i < n; ++i) {
+        pk.push_back(make_int4(ports[i].x, ports[i].y, ports[i].z, ports[i].axis));
+        pk.push_back(make_int4(ports[i].edges, ports[i].sign >= 0 ? 1 : -1, 0, 0));
+    }
+    EMLAB_CUDA(g->d_ports.alloc(pk.size()));
+    EMLAB_CUDA(cudaMemcpy(g->d_ports.p, pk.data(), pk.size() * 16, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_port_ph.alloc(n * 8));
+    EMLAB_CUDA(cudaMemset(g->d_port_ph.p, 0, n * 32));
+    if (sweep || record_steps > 0) {
+        size_t cap = ((size_t)1 << 23) / (2 * n);  // Ports.cpp:16, 209-210
+        if (!sweep) cap = std::min(cap, record_steps);
+        EMLAB_CUDA(g->d_series.alloc(cap * n * 2));
+        g->series_cap = cap;
+        g->recording = true;
+    }
+    return EMLAB_OK;
+}
+
+int emlab_ports_read_phasors(emlab_grid* g, float* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(out || g->nports == 0, "null output");
+    if (!g->nports) return EMLAB_OK;
+    EMLAB_CUDA(cudaMemcpyAsync(out, g->d_port_ph.p, (size_t)g->nports * 32, cudaMemcpyDeviceToHost, g->stream));
+    return emlab_grid_synchronize(g, 0);
+}
+
+int emlab_ports_read_series(emlab_grid* g, float* out, size_t max_steps, size_t* steps) {
+    if (int rc = require_grid(g)) return rc;
+    if (steps) *steps = g->recorded;
+    if (!out || !g->recorded) return EMLAB_OK;
+    const size_t s = std::min(max_steps, g->recorded);
+    EMLAB_CUDA(cudaMemcpyAsync(out, g->d_series.p, s * g->nports * 8, cudaMemcpyDeviceToHost, g->stream));
+    return emlab_grid_synchronize(g, 0);
+}
+
+int emlab_ports_sweep_sums(emlab_grid* g, double lambda_min, double lambda_max, int points, double* out,
+                           double* residual) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(g->nports > 0 && g->recorded > 0, "no recorded port series");
+    EMLAB_REQUIRE(out, "null output");
+    points = std::max(points, 2);
+    const double nu_lo = 1.0 / std::max(lambda_max, lambda_min), nu_hi = 1.0 / std::min(lambda_max, lambda_min);
+    DevBuf<double> d_out;
+    EMLAB_CUDA(d_out.alloc((size_t)g->nports * points * 4));
+    launch_sweep_sums(g->d_series.p, (long long)g->recorded, g->nports, nu_lo, nu_hi, points, (double)g->cfg.courant,
+                      d_out.p, g->stream);
+    ++g_launches;
+    if (int rc = check_launch()) return rc;
+    EMLAB_CUDA(cudaMemcpyAsync(out, d_out.p, d_out.n * 8, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    if (residual) {
+        // ring-down: late-time |V| of port 0 relative to its peak (Ports.cpp:346-353)
+        std::vector<float> series(g->recorded * g->nports * 2);
+        EMLAB_CUDA(cudaMemcpy(series.data(), g->d_series.p, series.size() * 4, cudaMemcpyDeviceToHost));
+        const size_t n = g->recorded, tail = std::max<size_t>(n / 20, 1);
+        double peak = 0.0, late = 0.0;
+        for (size_t k = 0; k < n; ++k) {
+            const double v = std::abs((double)series[k * g->nports * 2]);
+            peak = std::max(peak, v);
+            if (k >= n - tail) late = std::max(late, v);
+        }
+        *residual = peak > 0.0 ? late / peak : 1.0;
+    }
+    return EMLAB_OK;
+}
+
+// ---- far field -----------------------------------------------------------------------------
+int emlab_ntff_configure(emlab_grid* g, const int box_min[3], const int box_max[3], float wavelength,
+                         float averaging_periods, int box_out[6]) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    g->ntff_on = false;
+    g->d_ntff.release();
+    if (!(wavelength > 0.0f)) return EMLAB_OK;
+    EMLAB_REQUIRE(box_min && box_max, "null box");
+    const int n[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+    const int L = g->cfg.pml_thickness;
+    int bmin[3], bmax[3];
+    for (int a = 0; a < 3; ++a) {
+        // FarField.cpp:263-268: keep every node and its -1 neighbours out of the absorber
+        const int lo = L + 1, hi = n[a] - L - 2;
+        bmin[a] = std::clamp(std::min(box_min[a], box_max[a]), lo, hi);
+        bmax[a] = std::clamp(std::max(box_min[a], box_max[a]), lo, hi);
+        if (bmax[a] - bmin[a] < 4)
+            return fail(EMLAB_ERR_INVALID,
+                        "far_field box is degenerate after clamping to the region inside the absorbing layer");
+    }
+    for (int a = 0; a < 3; ++a) g->box[a] = bmin[a], g->box[3 + a] = bmax[a];
+    if (box_out)
+        for (int a = 0; a < 3; ++a) box_out[a] = bmin[a], box_out[3 + a] = bmax[a];
+    g->box[6] = 0;
+    for (int f = 0; f < 6; ++f) {
+        const int a = f >> 1, u = a == 0 ? 1 : 0, v = a == 2 ? 1 : 2;
+        g->box[7 + f] = g->box[6 + f] + (bmax[u] - bmin[u] + 1) * (bmax[v] - bmin[v] + 1);
+    }
+    g->points = g->box[12];
+    g->ntff_wl = std::max(wavelength, 2.0f);
+    g->ntff_avg = std::max(averaging_periods, 0.5f);
+    EMLAB_CUDA(g->d_box.alloc(13));
+    EMLAB_CUDA(cudaMemcpy(g->d_box.p, g->box, 13 * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_ntff.alloc((size_t)g->points * 32));
+    EMLAB_CUDA(cudaMemset(g->d_ntff.p, 0, (size_t)g->points * 128));
+    g->ntff_on = true;
+    return EMLAB_OK;
+}
+
+int emlab_ntff_point_count(emlab_grid* g, int* points) {
+    if (int rc = require_grid(g)) return rc;
+    if (!points) return fail(EMLAB_ERR_INVALID, "null output");
+    *points = g->ntff_on ? g->points : 0;
+    return EMLAB_OK;
+}
+
+int emlab_ntff_read_phasors(emlab_grid* g, float* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(g->ntff_on, "far-field monitor is not configured");
+    EMLAB_REQUIRE(out, "null output");
+    EMLAB_CUDA(cudaMemcpyAsync(out, g->d_ntff.p, (size_t)g->points * 128, cudaMemcpyDeviceToHost, g->stream));
+    return emlab_grid_synchronize(g, 0);
+}
+
+int emlab_ntff_evaluate(emlab_grid* g, const float* directions, int n_dirs, float* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(g->ntff_on, "far-field monitor is not configured");
+    EMLAB_REQUIRE(directions && out && n_dirs > 0, "bad direction arguments");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    const int slices = std::clamp((g->points + 4095) / 4096, 1, 64);  // FarField.cpp:297
+    const int chunk = 4096;
+    DevBuf<float4> d_dirs, d_part;
+    DevBuf<float> d_out;
+    EMLAB_CUDA(d_dirs.alloc((size_t)n_dirs));
+    EMLAB_CUDA(cudaMemcpyAsync(d_dirs.p, directions, (size_t)n_dirs * 16, cudaMemcpyHostToDevice, g->stream));
+    EMLAB_CUDA(d_part.alloc((size_t)chunk * slices * 4));
+    EMLAB_CUDA(d_out.alloc((size_t)n_dirs * 2));
+    const float k = (float)(6.28318530717958647692 / (double)g->ntff_wl);
+    for (int first = 0; first < n_dirs; first += chunk) {
+        const int count = std::min(chunk, n_dirs - first);
+        launch_ntff_pattern(g->d_box.p, g->points, g->d_ntff.p, d_dirs.p, first, count, slices, k, d_part.p, g->stream);
+        launch_ntff_reduce(d_dirs.p, d_part.p, first, count, slices, d_out.p, g->stream);
+        g_launches += 2;
+        if (int rc = check_launch()) return rc;
+    }
+    std::vector<float> tmp((size_t)n_dirs * 2);
+    EMLAB_CUDA(cudaMemcpyAsync(tmp.data(), d_out.p, tmp.size() * 4, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    // only the dispatch starting at direction 0 carries the power (ntff_pattern.comp:52)
+    for (int d = 0; d < n_dirs; ++d) out[2 * d] = tmp[2 * (size_t)d], out[2 * d + 1] = d == 0 ? tmp[1] : 0.0f;
+    return EMLAB_OK;
+}
+
+// ---- probes and flux ----------------------------------------------------------------------
+int emlab_probe_gather(emlab_grid* g, const int* origins, int n_probes, float* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(origins && out && n_probes > 0, "bad probe arguments");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    DevBuf<int4> d_o;
+    DevBuf<float4> d_out;
+    EMLAB_CUDA(d_o.alloc((size_t)n_probes));
+    EMLAB_CUDA(d_out.alloc((size_t)n_probes * 54));
+    EMLAB_CUDA(cudaMemcpyAsync(d_o.p, origins, (size_t)n_probes * 16, cudaMemcpyHostToDevice, g->stream));
+    launch_probe_gather(monitor_args(g), d_o.p, n_probes, d_out.p, nullptr, nullptr, g->stream);
+    ++g_launches;
+    if (int rc = check_launch()) return rc;
+    EMLAB_CUDA(cudaMemcpyAsync(out, d_out.p, (size_t)n_probes * 54 * 16, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    const int nx = g->cfg.nx, ny = g->cfg.ny, nz = g->cfg.nz;
+    for (int id = 0; id < n_probes * 54; ++id) {
+        const int probe = id / 54, k = id % 54, t = k % 27;
+        const int* o = origins + probe * 4;
+        const int x = std::clamp(o[0] + t % 3, 0, nx - 1), y = std::clamp(o[1] + (t / 3) % 3, 0, ny - 1),
+                  z = std::clamp(o[2] + t / 9, 0, nz - 1);
+        const size_t ci = ((size_t)z * ny + y) * nx + x;
+        out[(size_t)id * 4 + 3] = k < 27 ? g->cell_sigma[ci] : g->cell_eps[ci];
+    }
+    return EMLAB_OK;
+}
+
+int emlab_flux_planes(emlab_grid* g, const emlab_flux_plane* planes, int n_planes, double* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(planes && out && n_planes >= 0, "bad flux arguments");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    const int size[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+    struct Rect {
+        int axis, index, m0, m1, r0, r1;
+        size_t groups, offset;
+    };
+    std::vector<Rect> rects;
+    size_t total = 0;
+    for (int i = 0; i < n_planes; ++i) {
+        const emlab_flux_plane& p = planes[i];
+        Rect r{std::clamp(p.axis, 0, 2), p.index, 0, 0, 0, 0, 0, total};
+        const int u = r.axis == 0 ? 1 : 0, v = r.axis == 2 ? 1 : 2;
+        r.m0 = std::max(p.rect_min[0], 0), r.m1 = std::max(p.rect_min[1], 0);
+        r.r0 = std::min(p.rect_max[0], size[u]) - r.m0, r.r1 = std::min(p.rect_max[1], size[v]) - r.m1;
+        if (p.index < 0 || p.index >= size[r.axis] || r.r0 <= 0 || r.r1 <= 0) r.groups = 0;
+        else r.groups = (size_t)((r.r0 + 15) / 16) * ((r.r1 + 15) / 16);
+        total += r.groups;
+        rects.push_back(r);
+    }
+    DevBuf<float> d_part;
+    EMLAB_CUDA(d_part.alloc(std::max<size_t>(total, 1)));
+    const MonitorArgs m = monitor_args(g);
+    for (const Rect& r : rects) {
+        if (!r.groups) continue;
+        launch_flux_plane(m, r.axis, r.index, r.m0, r.m1, r.r0, r.r1, d_part.p + r.offset, g->stream);
+        ++g_launches;
+    }
+    if (int rc = check_launch()) return rc;
+    std::vector<float> part(std::max<size_t>(total, 1));
+    EMLAB_CUDA(cudaMemcpyAsync(part.data(), d_part.p, part.size() * 4, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    for (int i = 0; i < n_planes; ++i) {
+        double s = 0.0;  // FP64 sum of the FP32 workgroup partials (FieldAnalyzer.cpp:395-399)
+        for (size_t k = 0; k < rects[i].groups; ++k) s += (double)part[rects[i].offset + k];
+        out[i] = s;
+    }
+    return EMLAB_OK;
+}
+
+// ---- coax lines ----------------------------------------------------------------------------
+int emlab_lines_configure(emlab_grid* g, const int* quantities, int n_quantities, const int* terms,
+                          const float* weights, int n_terms, float wavelength, float averaging_periods) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    g->nq = 0;
+    g->d_q.release(), g->d_terms.release(), g->d_weights.release(), g->d_line_ph.release(), g->d_line_now.release();
+    if (n_quantities <= 0) return EMLAB_OK;
+    EMLAB_REQUIRE(quantities && (n_terms == 0 || (terms && weights)), "null line arrays");
+    for (int q = 0; q < n_quantities; ++q) {
+        const int* info = quantities + 4 * q;
+        EMLAB_REQUIRE(info[0] >= 0 && info[1] >= 0 && info[0] + info[1] <= n_terms, "line quantity term range");
+    }
+    for (int t = 0; t < n_terms; ++t) EMLAB_REQUIRE(terms[4 * t + 3] >= 0 && terms[4 * t + 3] < 6, "line term component");
+    EMLAB_CUDA(g->d_q.alloc((size_t)n_quantities));
+    EMLAB_CUDA(cudaMemcpy(g->d_q.p, quantities, (size_t)n_quantities * 16, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_terms.alloc((size_t)std::max(n_terms, 1)));
+    EMLAB_CUDA(g->d_weights.alloc((size_t)std::max(n_terms, 1)));
+    if (n_terms > 0) {
+        EMLAB_CUDA(cudaMemcpy(g->d_terms.p, terms, (size_t)n_terms * 16, cudaMemcpyHostToDevice));
+        EMLAB_CUDA(cudaMemcpy(g->d_weights.p, weights, (size_t)n_terms * 4, cudaMemcpyHostToDevice));
+    }
+    EMLAB_CUDA(g->d_line_ph.alloc((size_t)n_quantities * 4));
+    EMLAB_CUDA(cudaMemset(g->d_line_ph.p, 0, (size_t)n_quantities * 16));
+    EMLAB_CUDA(g->d_line_now.alloc((size_t)n_quantities));
+    EMLAB_CUDA(cudaMemset(g->d_line_now.p, 0, (size_t)n_quantities * 4));
+    g->nq = n_quantities;
+    g->line_wl = std::max(wavelength, 2.0f);
+    g->line_avg = averaging_periods;
+    return EMLAB_OK;
+}
+
+int emlab_lines_read(emlab_grid* g, float* phasors, float* now) {
+    if (int rc = require_grid(g)) return rc;
+    if (!g->nq) return EMLAB_OK;
+    if (phasors)
+        EMLAB_CUDA(cudaMemcpyAsync(phasors, g->d_line_ph.p, (size_t)g->nq * 16, cudaMemcpyDeviceToHost, g->stream));
+    if (now) EMLAB_CUDA(cudaMemcpyAsync(now, g->d_line_now.p, (size_t)g->nq * 4, cudaMemcpyDeviceToHost, g->stream));
+    return emlab_grid_synchronize(g, 0);
+}
+
+// ---- self-checks ---------------------------------------------------------------------------
+int emlab_debug_expf(const float* in, float* out, size_t n) {
+    if (!in || !out) return fail(EMLAB_ERR_INVALID, "null argument");
+    if (!n) return EMLAB_OK;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return fail(EMLAB_ERR_NO_DEVICE, "no CUDA device");
+    DevBuf<float> d_in, d_out;
+    EMLAB_CUDA(d_in.alloc(n));
+    EMLAB_CUDA(d_out.alloc(n));
+    EMLAB_CUDA(cudaMemcpy(d_in.p, in, n * 4, cudaMemcpyHostToDevice));
+    launch_debug_expf(d_in.p, d_out.p, n, 0);
+    ++g_launches;
+    if (int rc = check_launch()) return rc;
+    EMLAB_CUDA(cudaMemcpy(out, d_out.p, n * 4, cudaMemcpyDeviceToHost));
+    return EMLAB_OK;
+}
+
+}  // extern "C"

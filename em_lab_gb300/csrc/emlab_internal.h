@@ -1,0 +1,88 @@
+// emlab_internal.h - device layout and kernel entry points shared by the library's translation units.
+//
+// Field layout in HBM: six FP32 component arrays (Ex, Ey, Ez, Bx, By, Bz), x fastest, rows padded
+// to a multiple of 32 floats (128 bytes) so every warp-wide row access is one aligned line.
+// Two copies of the six arrays: the fused kernel reads generation `cur` and writes `cur ^ 1`
+// (in-place updates are impossible when one pass computes B and then E from it across tile halos).
+// Materials: one class index per cell (uint16, or uint32 above 65535 classes) into a table holding,
+// per class, the edge conductivity/permittivity (after binary16 rounding), the exponential
+// integrator coefficients ca/cb for cells outside the absorber (computed on the host by the very
+// formula the kernel would evaluate, so the values are bit-identical), and thin-wire factors.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "emlab_math.h"
+
+namespace emlab {
+
+// Per-class table entries (float4 pairs, see build_classes in setup.cpp):
+//   tabE[2c]   = (ca.x, ca.y, ca.z, cb.x)     tabE[2c+1] = (cb.y, cb.z, 0, 0)
+//   tabM[2c]   = (sig.x, sig.y, sig.z, eps.x) tabM[2c+1] = (eps.y, eps.z, 0, 0)
+//   tabW[2c]   = (w0.x, w0.y, w0.z, w1.x)     tabW[2c+1] = (w1.y, w1.z, 0, 0)
+// Classes >= wire_start carry thin-wire factors other than 1.
+struct YeeArgs {
+    int nx, ny, nz;
+    int pitch;          // floats per row
+    long long plane;    // floats per z plane (pitch * ny)
+    const float* ex; const float* ey; const float* ez;
+    const float* bx; const float* by; const float* bz;
+    float* nex; float* ney; float* nez;   // fused kernel: next generation (split kernels: unused)
+    float* nbx; float* nby; float* nbz;
+    float* wex; float* wey; float* wez;   // split kernels: in-place targets
+    float* wbx; float* wby; float* wbz;
+    const void* cls;
+    const float4* tabE;
+    const float4* tabM;
+    const float4* tabW;
+    unsigned wire_start;
+    const float* pml;   // [6][pml_stride]: I_x, I_y, I_z (integer positions), H_x, H_y, H_z (half)
+    int pml_stride;
+    int L;
+    float dt;
+    int zchunk;
+};
+
+struct SourceArgs {
+    const int4* cells;       // xyz = cell, w = first list entry; entry n is the sentinel
+    const int* lists;
+    const float4* src;       // 4 float4 per source: center, halfExtent, polAmp, softness
+    const float* signals;    // [step][nsrc]
+    int nsrc;
+    int ncells;
+};
+
+struct MonitorArgs {
+    int nx, ny, nz, pitch;
+    long long plane;
+    const float* ex; const float* ey; const float* ez;
+    const float* bx; const float* by; const float* bz;
+};
+
+void launch_yee_fused(const YeeArgs& a, bool wide, cudaStream_t s);
+void launch_yee_split(const YeeArgs& a, bool wide, cudaStream_t s);
+void launch_sources(const YeeArgs& a, const SourceArgs& sa, int k, bool wide, cudaStream_t s);
+
+// ports: ports[2i] = (x, y, z, axis), ports[2i+1] = (edges, sign, 0, 0); phasors 8 per port;
+// params[k] = (cos wtE, sin wtE, cos wtH, sin wtH) and blend for sub-step k.
+void launch_ports(const MonitorArgs& m, const int4* ports, int n, float* phasors, float* series, long long rec_index,
+                  const float4* rot, const float* blend, int k, cudaStream_t s);
+void launch_ntff(const MonitorArgs& m, const int* box, int points, float* phasors, const float4* rot,
+                 const float* blend, int k, cudaStream_t s);
+void launch_lines(const MonitorArgs& m, const int4* q, int nq, const int4* terms, const float* weights,
+                  float* phasors, float* now, const float4* rot, const float* blend, int k, cudaStream_t s);
+void launch_probe_gather(const MonitorArgs& m, const int4* origins, int n, float4* out, const float* cell_sig,
+                         const float* cell_eps, cudaStream_t s);
+void launch_flux_plane(const MonitorArgs& m, int axis, int index, int rmin0, int rmin1, int rs0, int rs1,
+                       float* partials, cudaStream_t s);
+void launch_ntff_pattern(const int* box, int points, const float* phasors, const float4* dirs, int first, int count,
+                         int slices, float k, float4* partials, cudaStream_t s);
+void launch_ntff_reduce(const float4* dirs, const float4* partials, int first, int count, int slices, float* out,
+                        cudaStream_t s);
+void launch_sweep_sums(const float* series, long long steps, int nports, double nu_lo, double nu_hi, int points,
+                       double dt, double* out, cudaStream_t s);
+void launch_check_finite(const MonitorArgs& m, unsigned* flag, cudaStream_t s);
+void launch_debug_expf(const float* in, float* out, size_t n, cudaStream_t s);
+
+}  // namespace emlab

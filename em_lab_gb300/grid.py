@@ -1,0 +1,342 @@
+"""Python mirror of EM_Lab's solver interface over the native C ABI (include/emlab.h).
+
+`SimulationGrid` keeps the member names and semantics of src/SimulationGrid.hpp:155-216
+(configure, uploadMaterials, setSources, resetFields, step, time, dt, stepCount, size, config,
+gpuMemoryBytes); the monitors attach to the grid and run inside `step` on the device.
+The library is loaded from the package's own `_lib/` directory; there is no fallback: if it is
+missing or no CUDA device is visible, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+
+_LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libemlab_gb300.so"
+_lib = None
+
+
+class EmlabError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"emlab error {code}: {message}")
+        self.code = code
+
+
+def library_path() -> Path:
+    return _LIB_PATH
+
+
+def load_library() -> C.CDLL:
+    """Loads libemlab_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not _LIB_PATH.exists():
+        raise RuntimeError(f"{_LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(_LIB_PATH))
+    P, I, SZ, F, D = C.c_void_p, C.c_int, C.c_size_t, C.c_float, C.c_double
+    fp, dp, ip = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int)
+    sig = {
+        "emlab_last_error": ([], C.c_char_p),
+        "emlab_version": ([], I),
+        "emlab_launch_count": ([], C.c_uint64),
+        "emlab_grid_create": ([C.POINTER(P)], I),
+        "emlab_grid_destroy": ([P], I),
+        "emlab_grid_configure": ([P, C.POINTER(abi.GridConfig)], I),
+        "emlab_grid_get_config": ([P, C.POINTER(abi.GridConfig)], I),
+        "emlab_grid_upload_materials": ([P, fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ,
+                                         C.POINTER(abi.WireTerm), SZ], I),
+        "emlab_grid_set_sources": ([P, C.POINTER(abi.Source), SZ], I),
+        "emlab_grid_reset_fields": ([P], I),
+        "emlab_grid_step": ([P, I], I),
+        "emlab_grid_synchronize": ([P, I], I),
+        "emlab_grid_get_state": ([P, C.POINTER(abi.GridState)], I),
+        "emlab_grid_read_fields": ([P, fp, fp], I),
+        "emlab_grid_read_components": ([P, fp, fp, fp, fp, fp, fp], I),
+        "emlab_grid_write_components": ([P, fp, fp, fp, fp, fp, fp], I),
+        "emlab_grid_set_kernel": ([P, I], I),
+        "emlab_grid_stream": ([P, C.POINTER(P)], I),
+        "emlab_grid_check_finite": ([P], I),
+        "emlab_grid_set_timing": ([P, I], I),
+        "emlab_grid_kernel_time": ([P, dp, C.POINTER(C.c_uint64), I], I),
+        "emlab_ports_configure": ([P, C.POINTER(abi.Port), SZ, F, F, I, SZ], I),
+        "emlab_ports_read_phasors": ([P, fp], I),
+        "emlab_ports_read_series": ([P, fp, SZ, C.POINTER(SZ)], I),
+        "emlab_ports_sweep_sums": ([P, D, D, I, dp, dp], I),
+        "emlab_ntff_configure": ([P, ip, ip, F, F, ip], I),
+        "emlab_ntff_point_count": ([P, ip], I),
+        "emlab_ntff_read_phasors": ([P, fp], I),
+        "emlab_ntff_evaluate": ([P, fp, I, fp], I),
+        "emlab_probe_gather": ([P, ip, I, fp], I),
+        "emlab_flux_planes": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
+        "emlab_lines_configure": ([P, ip, I, ip, fp, I, F, F], I),
+        "emlab_lines_read": ([P, fp, fp], I),
+        "emlab_debug_expf": ([fp, fp, SZ], I),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != abi.EMLAB_OK:
+        raise EmlabError(rc, load_library().emlab_last_error().decode())
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float)) if a is not None else None
+
+
+def _f32(a, n=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if n is not None and a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def launch_count() -> int:
+    return int(load_library().emlab_launch_count())
+
+
+def device_expf(x) -> np.ndarray:
+    x = _f32(np.asarray(x).ravel())
+    out = np.empty_like(x)
+    _check(load_library().emlab_debug_expf(_fptr(x), _fptr(out), x.size))
+    return out
+
+
+class SimulationGrid:
+    """The FDTD solver (src/SimulationGrid.hpp:155-216) on one CUDA device."""
+
+    kMaxSources = 256
+
+    def __init__(self, config: abi.GridConfig | None = None):
+        self._lib = load_library()
+        h = C.c_void_p()
+        _check(self._lib.emlab_grid_create(C.byref(h)))
+        self._h = h
+        self._sources = []
+        if config is not None:
+            self.configure(config)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.emlab_grid_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # --- SimulationGrid ---------------------------------------------------------------------
+    def configure(self, config: abi.GridConfig):
+        cfg = abi.GridConfig()
+        C.memmove(C.byref(cfg), C.byref(config), C.sizeof(cfg))
+        _check(self._lib.emlab_grid_configure(self._h, C.byref(cfg)))
+
+    def config(self) -> abi.GridConfig:
+        cfg = abi.GridConfig()
+        _check(self._lib.emlab_grid_get_config(self._h, C.byref(cfg)))
+        return cfg
+
+    def size(self):
+        c = self.config()
+        return (c.nx, c.ny, c.nz)
+
+    def upload_materials(self, sigma, eps_r, edges=(), wires=()):
+        """uploadMaterials: sigma/eps_r are (nz, ny, nx) cell arrays (MaterialVolume)."""
+        nx, ny, nz = self.size()
+        s = _f32(sigma, nx * ny * nz)
+        e = _f32(eps_r, nx * ny * nz)
+        ea, ne = abi.array_of(abi.EdgeOverride, edges)
+        wa, nw = abi.array_of(abi.WireTerm, wires)
+        _check(self._lib.emlab_grid_upload_materials(self._h, _fptr(s), _fptr(e), nx, ny, nz, ea, ne, wa, nw))
+
+    def set_sources(self, sources):
+        arr, n = abi.array_of(abi.Source, [s.to_c() if hasattr(s, "to_c") else s for s in sources])
+        _check(self._lib.emlab_grid_set_sources(self._h, arr, n))
+        self._sources = list(sources)
+
+    def sources(self):
+        return list(self._sources)
+
+    def reset_fields(self):
+        _check(self._lib.emlab_grid_reset_fields(self._h))
+
+    def step(self, count: int = 1, after_each_step=None):
+        """step(count, afterEachStep): attached monitors run on the device inside every step; a
+        Python callback, if given, runs on the host after each completed step."""
+        if after_each_step is None:
+            _check(self._lib.emlab_grid_step(self._h, int(count)))
+            return
+        for _ in range(int(count)):
+            _check(self._lib.emlab_grid_step(self._h, 1))
+            after_each_step()
+
+    def synchronize(self, timeout_ms: int = 0):
+        _check(self._lib.emlab_grid_synchronize(self._h, int(timeout_ms)))
+
+    def state(self) -> abi.GridState:
+        st = abi.GridState()
+        _check(self._lib.emlab_grid_get_state(self._h, C.byref(st)))
+        return st
+
+    def time(self) -> float:
+        return self.state().time
+
+    def dt(self) -> float:
+        return self.config().courant
+
+    def step_count(self) -> int:
+        return int(self.state().step_count)
+
+    def gpu_memory_bytes(self) -> int:
+        return int(self.state().device_bytes)
+
+    def set_kernel(self, kernel: int):
+        _check(self._lib.emlab_grid_set_kernel(self._h, int(kernel)))
+
+    def stream_handle(self) -> int:
+        p = C.c_void_p()
+        _check(self._lib.emlab_grid_stream(self._h, C.byref(p)))
+        return int(p.value or 0)
+
+    def set_timing(self, enabled: bool):
+        _check(self._lib.emlab_grid_set_timing(self._h, 1 if enabled else 0))
+
+    def kernel_time(self, reset: bool = False):
+        """(accumulated device ms of the solver launches, number of timed launches)."""
+        ms = C.c_double()
+        n = C.c_uint64()
+        _check(self._lib.emlab_grid_kernel_time(self._h, C.byref(ms), C.byref(n), 1 if reset else 0))
+        return ms.value, int(n.value)
+
+    def check_finite(self) -> bool:
+        rc = self._lib.emlab_grid_check_finite(self._h)
+        if rc == abi.EMLAB_ERR_NONFINITE:
+            return False
+        _check(rc)
+        return True
+
+    # --- field access -----------------------------------------------------------------------
+    def read_components(self):
+        """(Ex, Ey, Ez, Bx, By, Bz), each (nz, ny, nx) float32."""
+        nx, ny, nz = self.size()
+        out = [np.empty((nz, ny, nx), np.float32) for _ in range(6)]
+        _check(self._lib.emlab_grid_read_components(self._h, *[_fptr(o) for o in out]))
+        return out
+
+    def read_textures(self):
+        """The E and B textures (nz, ny, nx, 4) in the reference's RGBA32F layout."""
+        nx, ny, nz = self.size()
+        e = np.empty((nz, ny, nx, 4), np.float32)
+        b = np.empty((nz, ny, nx, 4), np.float32)
+        _check(self._lib.emlab_grid_read_fields(self._h, _fptr(e), _fptr(b)))
+        return e, b
+
+    def write_components(self, comps):
+        nx, ny, nz = self.size()
+        arrs = [None if c is None else _f32(c, nx * ny * nz) for c in comps]
+        _check(self._lib.emlab_grid_write_components(self._h, *[_fptr(a) for a in arrs]))
+
+    # --- monitors (device side) -------------------------------------------------------------
+    def ports_configure(self, ports, wavelength, averaging_periods=4.0, sweep=False, record_steps=0):
+        arr, n = abi.array_of(abi.Port, ports)
+        _check(self._lib.emlab_ports_configure(self._h, arr, n, float(wavelength), float(averaging_periods),
+                                               1 if sweep else 0, int(record_steps)))
+        self._nports = n
+
+    def ports_phasors(self) -> np.ndarray:
+        out = np.zeros((max(1, getattr(self, "_nports", 0)), 8), np.float32)
+        _check(self._lib.emlab_ports_read_phasors(self._h, _fptr(out)))
+        return out[: getattr(self, "_nports", 0)]
+
+    def ports_series(self) -> np.ndarray:
+        steps = C.c_size_t()
+        _check(self._lib.emlab_ports_read_series(self._h, None, 0, C.byref(steps)))
+        n = getattr(self, "_nports", 0)
+        out = np.zeros((max(1, steps.value), max(1, n), 2), np.float32)
+        _check(self._lib.emlab_ports_read_series(self._h, _fptr(out), steps.value, C.byref(steps)))
+        return out[: steps.value, :n]
+
+    def ports_sweep_sums(self, lambda_min, lambda_max, points):
+        n = getattr(self, "_nports", 0)
+        out = np.zeros((n, points, 4), np.float64)
+        res = C.c_double()
+        _check(self._lib.emlab_ports_sweep_sums(self._h, float(lambda_min), float(lambda_max), int(points),
+                                                out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res)))
+        return out, res.value
+
+    def ntff_configure(self, box_min, box_max, wavelength, averaging_periods=4.0):
+        mn = (C.c_int * 3)(*[int(v) for v in box_min])
+        mx = (C.c_int * 3)(*[int(v) for v in box_max])
+        out = (C.c_int * 6)()
+        _check(self._lib.emlab_ntff_configure(self._h, mn, mx, float(wavelength), float(averaging_periods), out))
+        return tuple(out[:3]), tuple(out[3:])
+
+    def ntff_point_count(self) -> int:
+        p = C.c_int()
+        _check(self._lib.emlab_ntff_point_count(self._h, C.byref(p)))
+        return p.value
+
+    def ntff_phasors(self) -> np.ndarray:
+        n = self.ntff_point_count()
+        out = np.zeros((max(1, n), 32), np.float32)
+        _check(self._lib.emlab_ntff_read_phasors(self._h, _fptr(out)))
+        return out[:n]
+
+    def ntff_evaluate(self, directions) -> np.ndarray:
+        d = np.zeros((len(directions), 4), np.float32)
+        d[:, :3] = np.asarray(directions, np.float32)[:, :3]
+        out = np.zeros((len(directions), 2), np.float32)
+        _check(self._lib.emlab_ntff_evaluate(self._h, _fptr(d), len(d), _fptr(out)))
+        return out
+
+    def probe_gather(self, origins) -> np.ndarray:
+        o = np.zeros((len(origins), 4), np.int32)
+        o[:, :3] = np.asarray(origins, np.int32)[:, :3]
+        out = np.zeros((len(origins), 54, 4), np.float32)
+        _check(self._lib.emlab_probe_gather(self._h, o.ctypes.data_as(C.POINTER(C.c_int)), len(o), _fptr(out)))
+        return out
+
+    def flux_planes(self, planes) -> np.ndarray:
+        arr, n = abi.array_of(abi.FluxPlane, planes)
+        out = np.zeros(max(1, n), np.float64)
+        _check(self._lib.emlab_flux_planes(self._h, arr, n, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out[:n]
+
+    def lines_configure(self, quantities, terms, weights, wavelength, averaging_periods=4.0):
+        q = np.ascontiguousarray(np.asarray(quantities, np.int32).reshape(-1, 4))
+        t = np.ascontiguousarray(np.asarray(terms, np.int32).reshape(-1, 4))
+        w = _f32(weights)
+        _check(self._lib.emlab_lines_configure(self._h, q.ctypes.data_as(C.POINTER(C.c_int)), len(q),
+                                               t.ctypes.data_as(C.POINTER(C.c_int)), _fptr(w), len(t),
+                                               float(wavelength), float(averaging_periods)))
+        self._nq = len(q)
+
+    def lines_read(self):
+        n = getattr(self, "_nq", 0)
+        ph = np.zeros((max(1, n), 4), np.float32)
+        now = np.zeros(max(1, n), np.float32)
+        _check(self._lib.emlab_lines_read(self._h, _fptr(ph), _fptr(now)))
+        return ph[:n], now[:n]
+
+

@@ -1,0 +1,226 @@
+/* emlab.h - C ABI of the GB300 FDTD solver (the drop-in boundary for EM_Lab's time-stepping path).
+ *
+ * Every entry point replaces one member of the reference's solver or monitor classes; the comment
+ * on each names the reference function (src/ or shaders/ file:line) whose behaviour it keeps.
+ * Conventions:
+ *   - lattice layout and units follow shaders/common.glsl:4-12 (c = eps0 = mu0 = 1, dx = 1,
+ *     dt = Courant number, B stored as c*B; texel (i,j,k) holds Ex at (i+1/2,j,k), Ey at (i,j+1/2,k),
+ *     Ez at (i,j,k+1/2), Bx at (i,j+1/2,k+1/2), By at (i+1/2,j,k+1/2), Bz at (i+1/2,j+1/2,k));
+ *   - host arrays are x-fastest: index = (z * ny + y) * nx + x (MaterialVolume::index,
+ *     src/SimulationGrid.hpp:55-57);
+ *   - every function returns EMLAB_OK (0) or an EMLAB_ERR_* code; emlab_last_error() gives the
+ *     message of the calling thread's last failure (the reference throws std::runtime_error);
+ *   - caller arrays are borrowed for the duration of the call only;
+ *   - one handle is used by one thread at a time; distinct handles are independent.
+ */
+#ifndef EMLAB_H
+#define EMLAB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EMLAB_OK 0
+#define EMLAB_ERR_INVALID 1   /* bad argument: size mismatch, out-of-range value, null pointer */
+#define EMLAB_ERR_OOM 2       /* device or host allocation failed (grid too large) */
+#define EMLAB_ERR_CUDA 3      /* a CUDA call failed; the message names it */
+#define EMLAB_ERR_TIMEOUT 4   /* a bounded host wait ran out */
+#define EMLAB_ERR_NONFINITE 5 /* non-finite field values detected */
+#define EMLAB_ERR_NO_DEVICE 6 /* no CUDA device is visible */
+
+/* Solver kernels: the fused single-pass Yee step (default) or the reference's two-pass layout. */
+#define EMLAB_KERNEL_FUSED 0
+#define EMLAB_KERNEL_SPLIT 1
+
+/* Waveforms of emlab_source (src/SimulationGrid.hpp:108-111). */
+#define EMLAB_WAVE_CW 0
+#define EMLAB_WAVE_PULSE 1
+
+/* GridConfig (src/SimulationGrid.hpp:25-31). */
+typedef struct emlab_grid_config {
+    int nx, ny, nz;
+    float courant;       /* c dt / dx, clamped to [0.05, 0.99/sqrt(3)] */
+    int pml_thickness;   /* absorbing layer depth in cells, clamped to [0, 64] */
+    float pml_sigma_max; /* conductivity at the outer edge of the layer */
+    float pml_grading;   /* exponential grading g, clamped to [0.25, 12] */
+} emlab_grid_config;
+
+/* EdgeOverride (src/SimulationGrid.hpp:76-81): replaces the averaged conductivity of one E edge. */
+typedef struct emlab_edge_override {
+    int x, y, z; /* owning texel: the edge E_axis sits at texel + 0.5 e_axis */
+    int axis;    /* 0, 1, 2 */
+    float sigma; /* normalised conductivity */
+} emlab_edge_override;
+
+/* WireCoefficient (src/SimulationGrid.hpp:86-94): thin-wire factor on one curl term of one B
+ * component; with c1 = c+1, c2 = c+2 (mod 3): curl_c E = term0 - term1, term0 = d_{c1} E_{c2}. */
+typedef struct emlab_wire_term {
+    int x, y, z;
+    int component; /* 0, 1, 2 = Bx, By, Bz */
+    int term;      /* 0 or 1 */
+    float factor;  /* 2 / ln(cell / radius) */
+} emlab_wire_term;
+
+/* SourceDesc (src/SimulationGrid.hpp:113-150): J(x,t) = p A w(x) s(t). */
+typedef struct emlab_source {
+    float center[3];       /* cell coordinates */
+    float half_extent[3];  /* flat-top half extents (0 = point) */
+    float softness[3];     /* per-axis Gaussian edge width, clamped >= 0.25 */
+    float polarization[3]; /* normalised on upload; zero-length sources are dropped */
+    float amplitude;       /* J0 */
+    float wavelength;      /* cells; omega = 2 pi / wavelength */
+    float phase;           /* radians */
+    int waveform;          /* EMLAB_WAVE_CW or EMLAB_WAVE_PULSE */
+    float ramp_periods;    /* CW: smooth turn-on; pulse: 1/e half-width tau in periods */
+    float repeat_periods;  /* pulse repetition interval (0 = single shot) */
+    float delay_periods;   /* start delay */
+    int enabled;
+} emlab_source;
+
+/* Port of port_accumulate.comp:20-23 / PortSetup (src/Ports.hpp:30-40), solver-facing part. */
+typedef struct emlab_port {
+    int x, y, z; /* owning texel of the (first) gap edge */
+    int axis;
+    int edges;   /* 1 = thin-wire gap edge, 4 = corner edges of a 1x1-cell rod gap */
+    int sign;    /* +1 / -1 feed orientation */
+} emlab_port;
+
+/* One flux plane of poynting_flux.comp:21-26 (box faces are six of these). */
+typedef struct emlab_flux_plane {
+    int axis;        /* plane normal 0, 1, 2 */
+    int index;       /* lattice index along the normal */
+    int rect_min[2]; /* first cell along the tangential axes (u, v) = (x,y,z) order skipping axis */
+    int rect_max[2]; /* one past the last cell */
+} emlab_flux_plane;
+
+/* Solver state read-back: time(), dt(), stepCount(), size(), gpuMemoryBytes()
+ * (src/SimulationGrid.hpp:183-188). */
+typedef struct emlab_grid_state {
+    double time;
+    float dt;
+    uint64_t step_count;
+    int nx, ny, nz;
+    uint64_t device_bytes;
+    int source_cells; /* cells in the source lists (SimulationGrid.cpp:348) */
+    int kernel;       /* EMLAB_KERNEL_* in use */
+} emlab_grid_state;
+
+typedef struct emlab_grid emlab_grid;
+
+/* ---- library ---------------------------------------------------------------------------- */
+const char* emlab_last_error(void);
+int emlab_version(void);
+/* Kernels this library has launched since load (graph launches count their kernel nodes). */
+uint64_t emlab_launch_count(void);
+
+/* ---- solver: SimulationGrid (src/SimulationGrid.hpp:155-216) ------------------------------ */
+/* SimulationGrid::SimulationGrid (src/SimulationGrid.cpp:135-147): binds the current CUDA device
+ * and creates the handle's stream. */
+int emlab_grid_create(emlab_grid** out);
+int emlab_grid_destroy(emlab_grid* g);
+/* SimulationGrid::configure (src/SimulationGrid.cpp:149-199): clamps the request, reallocates
+ * when the size changed, clears fields and materials (vacuum), rewinds time. Monitors are reset. */
+int emlab_grid_configure(emlab_grid* g, const emlab_grid_config* cfg);
+/* config() (src/SimulationGrid.hpp:183): the clamped configuration in use. */
+int emlab_grid_get_config(const emlab_grid* g, emlab_grid_config* out);
+/* SimulationGrid::uploadMaterials (src/SimulationGrid.cpp:209-295): per-cell sigma and eps_r
+ * (nx*ny*nz each), edge averaging, sub-cell overrides (invalid ones silently skipped), binary16
+ * rounding, thin-wire factors; clears E and B and time. EMLAB_ERR_INVALID on a size mismatch. */
+int emlab_grid_upload_materials(emlab_grid* g, const float* sigma, const float* eps_r, int nx, int ny, int nz,
+                                const emlab_edge_override* edges, size_t n_edges, const emlab_wire_term* wires,
+                                size_t n_wires);
+/* SimulationGrid::setSources (src/SimulationGrid.cpp:297-357): drops disabled and zero-polarisation
+ * sources, keeps at most 256, builds the per-cell source lists; fields are kept. */
+int emlab_grid_set_sources(emlab_grid* g, const emlab_source* sources, size_t n);
+/* SimulationGrid::resetFields (src/SimulationGrid.cpp:359-366). */
+int emlab_grid_reset_fields(emlab_grid* g);
+/* SimulationGrid::step (src/SimulationGrid.cpp:368-433): count leapfrog steps (B, E, sources),
+ * then every monitor attached to the grid samples the step, on the device. Returns when the work
+ * is queued on the grid's stream; emlab_grid_synchronize waits for it. */
+int emlab_grid_step(emlab_grid* g, int count);
+/* Bounded wait for the grid's stream (EMLAB_ERR_TIMEOUT after timeout_ms; <= 0 waits 60 s). */
+int emlab_grid_synchronize(emlab_grid* g, int timeout_ms);
+int emlab_grid_get_state(const emlab_grid* g, emlab_grid_state* out);
+/* Read-back of the E and B textures in the reference's RGBA32F layout (E.a = cell sigma,
+ * B.a = cell eps_r; src/SimulationGrid.hpp:4-6), 4 floats per cell. Either pointer may be NULL. */
+int emlab_grid_read_fields(emlab_grid* g, float* e_rgba, float* b_rgba);
+/* Read-back as six component arrays (nx*ny*nz floats each); NULL pointers are skipped. */
+int emlab_grid_read_components(emlab_grid* g, float* ex, float* ey, float* ez, float* bx, float* by, float* bz);
+/* Overwrites the field components (for checkpoints and tests); materials and time are kept. */
+int emlab_grid_write_components(emlab_grid* g, const float* ex, const float* ey, const float* ez, const float* bx,
+                                const float* by, const float* bz);
+/* Selects the solver kernel (EMLAB_KERNEL_FUSED or EMLAB_KERNEL_SPLIT); results are identical. */
+int emlab_grid_set_kernel(emlab_grid* g, int kernel);
+/* The cudaStream_t the grid launches on (for events and for ordering caller work). */
+int emlab_grid_stream(emlab_grid* g, void** stream);
+/* Kernel timing of the solver pass: when enabled, CUDA events bracket every Yee launch (the fused
+ * kernel, or the split pair) on the grid's stream; emlab_grid_kernel_time returns the accumulated
+ * device time in ms and the number of timed launches since the last reset (reset = 1 clears). */
+int emlab_grid_set_timing(emlab_grid* g, int enabled);
+int emlab_grid_kernel_time(emlab_grid* g, double* ms, uint64_t* launches, int reset);
+/* Non-finite check over E and B on the device (Instruments::applyMeasurement's stability check,
+ * src/Instruments.cpp:271-275): EMLAB_ERR_NONFINITE if any component is NaN or infinite. */
+int emlab_grid_check_finite(emlab_grid* g);
+
+/* ---- port monitor: PortMonitor (src/Ports.hpp:84-140) ------------------------------------- */
+/* PortMonitor::configure (src/Ports.cpp:183-215): at most 256 ports; phasors cleared; the (V, I)
+ * series is recorded every step when record_steps > 0 (capacity 2^23 floats, src/Ports.cpp:16)
+ * or when sweep != 0 (whole capacity). n = 0 disables the monitor. */
+int emlab_ports_configure(emlab_grid* g, const emlab_port* ports, size_t n, float wavelength, float averaging_periods,
+                          int sweep, size_t record_steps);
+/* Phasor state (port_accumulate.comp:24-27): 8 floats per port, stage1 (V re, V im, I re, I im)
+ * then stage2. */
+int emlab_ports_read_phasors(emlab_grid* g, float* out);
+/* Recorded (V, I) pairs, [step][port], recordedSteps() x ports x 2 floats (PortMonitor::readSeries,
+ * src/Ports.cpp:138-143). *steps receives recordedSteps(); out may be NULL to query it. */
+int emlab_ports_read_series(emlab_grid* g, float* out, size_t max_steps, size_t* steps);
+/* Running DFT of the recorded series at `points` frequencies evenly spaced in 1/lambda between
+ * 1/lambda_max and 1/lambda_min, in FP64 on the device (the sums of PortMonitor::evaluateSweep,
+ * src/Ports.cpp:215-242, I corrected by e^{i w dt/2}): out[(port * points + f) * 4 + {0..3}] =
+ * (sumV re, sumV im, sumI re, sumI im). Also returns the ring-down residual of port 0. */
+int emlab_ports_sweep_sums(emlab_grid* g, double lambda_min, double lambda_max, int points, double* out,
+                           double* residual);
+
+/* ---- far-field monitor: FarFieldMonitor (src/FarField.hpp:75-133) ------------------------ */
+/* FarFieldMonitor::configure (src/FarField.cpp:259-307): box clamped into [L+1, n-L-2];
+ * EMLAB_ERR_INVALID if degenerate (< 4 cells on an axis). box_out receives the clamped box.
+ * wavelength <= 0 disables the monitor. */
+int emlab_ntff_configure(emlab_grid* g, const int box_min[3], const int box_max[3], float wavelength,
+                         float averaging_periods, int box_out[6]);
+/* Huygens-box point count (FarField.cpp:274-282). */
+int emlab_ntff_point_count(emlab_grid* g, int* points);
+/* PhasorPair per point (ntff_common.glsl:17-28): 32 floats each. */
+int emlab_ntff_read_phasors(emlab_grid* g, float* out);
+/* ntff_pattern.comp + ntff_reduce.comp (FarField.cpp:226-243, 359-376): for each direction
+ * (4 floats, xyz used) out[2d] = |N_perp - r x L|^2 and out[1] = radiated power P. */
+int emlab_ntff_evaluate(emlab_grid* g, const float* directions, int n_dirs, float* out);
+
+/* ---- probes and flux: FieldAnalyzer (src/FieldAnalyzer.hpp:73-130) ----------------------- */
+/* probe_gather.comp (FieldAnalyzer.cpp:274-303): origins are 4 ints per probe (xyz used); out
+ * receives 54 texels (27 E, then 27 B, 4 floats each) per probe. */
+int emlab_probe_gather(emlab_grid* g, const int* origins, int n_probes, float* out);
+/* poynting_flux.comp per plane (FieldAnalyzer.cpp:230-254, 391-400): out[i] = FP64 sum of the
+ * FP32 16x16-workgroup partial sums of plane i (without the box orientation sign). */
+int emlab_flux_planes(emlab_grid* g, const emlab_flux_plane* planes, int n_planes, double* out);
+
+/* ---- coax line monitor: line_accumulate.comp (src/Coax.cpp:179-197) ---------------------- */
+/* quantities: 4 ints each (first term, term count, 0 = E integral / 1 = B integral, unused);
+ * terms: 4 ints each (x, y, z, component 0-5 = Ex..Ez, Bx..Bz); weights: one per term.
+ * n_quantities = 0 disables the monitor. */
+int emlab_lines_configure(emlab_grid* g, const int* quantities, int n_quantities, const int* terms,
+                          const float* weights, int n_terms, float wavelength, float averaging_periods);
+/* Phasors (4 floats per quantity: stage1 re, im, stage2 re, im) and instantaneous values. */
+int emlab_lines_read(emlab_grid* g, float* phasors, float* now);
+
+/* ---- self-checks ------------------------------------------------------------------------- */
+/* Evaluates the device emlab_expf on n inputs (bit-exactness check against the host). */
+int emlab_debug_expf(const float* in, float* out, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EMLAB_H */

@@ -1,0 +1,114 @@
+"""Compiles the reference's own compute shaders as C++ (test infrastructure; the pin of the oracle).
+
+Reads the shader files where they lie in the reference tree (default /root/reference/shaders, or
+$EMLAB_REFERENCE/shaders), rewrites the GLSL-only syntax mechanically (resource declarations ->
+globals, `out` parameters -> references, swizzles -> calls, float literals -> float suffix,
+array constructors -> brace lists) into oracle/_ref/*.hpp, and builds oracle/_ref/libemlab_ref.so
+from oracle/ref_driver.cpp, which runs every dispatch of SimulationGrid::step and the monitors over
+the CPU with those shader bodies and the GLSL semantics of oracle/glsl_shim.hpp. Nothing under
+oracle/_ref is committed. Without the reference tree the recipe does nothing.
+
+    python oracle/build_ref.py [--force]
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+LIB = OUT / "libemlab_ref.so"
+SHADERS = ["common.glsl", "field_sampling.glsl", "ntff_common.glsl", "update_B.comp", "update_E.comp",
+           "apply_sources.comp", "clear_fields.comp", "port_accumulate.comp", "probe_gather.comp",
+           "poynting_flux.comp", "ntff_accumulate.comp", "ntff_pattern.comp", "ntff_reduce.comp",
+           "line_accumulate.comp"]
+
+
+def reference_shaders() -> Path | None:
+    base = Path(os.environ.get("EMLAB_REFERENCE", "/root/reference"))
+    d = base / "shaders"
+    return d if d.is_dir() else None
+
+
+_FLOAT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])")
+
+
+def _array_ctor(src: str) -> str:
+    """`T[N](a, b, ...)` -> `{a, b, ...}`."""
+    out = []
+    i = 0
+    pat = re.compile(r"\b\w+\[\d+\]\(")
+    while True:
+        m = pat.search(src, i)
+        if not m:
+            out.append(src[i:])
+            return "".join(out)
+        out.append(src[i:m.start()])
+        depth, j = 1, m.end()
+        while depth:
+            depth += {"(": 1, ")": -1}.get(src[j], 0)
+            j += 1
+        out.append("{" + src[m.end():j - 1] + "}")
+        i = j
+
+
+def transform(text: str) -> str:
+    lines = []
+    for line in text.splitlines():
+        s = line
+        if s.lstrip().startswith("#version"):
+            continue
+        s = re.sub(r'#include\s+"([\w.]+)"', r'#include "\1.hpp"', s)
+        if re.match(r"\s*layout\s*\(\s*local_size", s):
+            continue
+        s = re.sub(r"layout\s*\(\s*std430[^)]*\)\s*(?:(?:readonly|writeonly|restrict)\s+)*buffer\s+\w+\s*\{\s*(\w+)\s+"
+                   r"(\w+)\s*\[\s*\]\s*;\s*\}\s*;", r"\1* \2 = nullptr;", s)
+        s = re.sub(r"layout\s*\([^)]*\)\s*uniform\s+(?:restrict\s+)?(\w+)\s+(\w+)\s*;", r"\1 \2;", s)
+        s = re.sub(r"^(\s*)uniform\s+", r"\1", s)
+        s = re.sub(r"^(\s*)shared\s+", r"\1thread_local ", s)
+        s = re.sub(r"\bout\s+(\w+)\s+(\w+)", r"\1& \2", s)
+        code, sep, comment = s.partition("//")
+        code = re.sub(r"\.(xyz|xy|zw)\b(?!\s*\()", r".\1()", code)
+        code = _FLOAT.sub(lambda m: m.group(1) + "f", code)
+        lines.append(code + sep + comment)
+    return _array_ctor("\n".join(lines)) + "\n"
+
+
+def build(force: bool = False, verbose: bool = False) -> Path | None:
+    src = reference_shaders()
+    if src is None:
+        return None
+    OUT.mkdir(parents=True, exist_ok=True)
+    deps = [HERE / "ref_driver.cpp", HERE / "glsl_shim.hpp", HERE / "emlab_oracle.c", HERE / "oracle_impl.h",
+            HERE.parent / "em_lab_gb300" / "csrc" / "emlab_math.h", Path(__file__)]
+    changed = force or not LIB.exists()
+    for name in SHADERS:
+        dst = OUT / (name + ".hpp")
+        text = transform((src / name).read_text())
+        if not dst.exists() or dst.read_text() != text:
+            dst.write_text(text)
+            changed = True
+    if not changed and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return LIB
+    # the host-side set-up comes from the restatement: link its object into the same library
+    obj = OUT / "emlab_oracle.o"
+    cmds = [[os.environ.get("CC", "gcc"), "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-c",
+             str(HERE / "emlab_oracle.c"), "-o", str(obj)],
+            [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+             "-I", str(OUT), "-I", str(HERE), str(HERE / "ref_driver.cpp"), str(obj), "-o", str(LIB)]]
+    for cmd in cmds:
+        if verbose:
+            print(" ".join(cmd))
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            sys.stderr.write(res.stdout + res.stderr)
+            raise RuntimeError("building the reference shaders failed")
+    return LIB
+
+
+if __name__ == "__main__":
+    lib = build(force="--force" in sys.argv, verbose=True)
+    print(lib if lib else "reference tree not found: nothing built")

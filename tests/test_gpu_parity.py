@@ -1,0 +1,113 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU restatement, on the same inputs.
+
+The FP32 oracle evaluates the reference's update in the shaders' operation order with the same
+deterministic exp(); the kernels are compiled without contraction, so the bar is bit equality.
+The FP64 oracle gives the error floor that is reported (and bounded) beside every result.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from em_lab_gb300 import SimulationGrid, abi, configs, device_expf
+
+pytestmark = pytest.mark.gpu
+
+COMP = ["Ex", "Ey", "Ez", "Bx", "By", "Bz"]
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    n = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / n) if n > 0 else float(np.linalg.norm(a))
+
+
+def run_gpu(sc, steps, kernel=abi.KERNEL_FUSED, chunks=1):
+    g = SimulationGrid(sc.grid)
+    g.set_kernel(kernel)
+    oracle.load_scene(g, sc)
+    for _ in range(chunks):
+        g.step(steps // chunks)
+    g.synchronize(120000)
+    out = g.read_components()
+    g.close()
+    return out
+
+
+def run_oracle(sc, steps, precision="f32"):
+    o = oracle.Oracle(sc.grid, precision)
+    oracle.load_scene(o, sc)
+    o.step(steps)
+    return o.read_components()
+
+
+def assert_bitwise(got, want, what=""):
+    for c, (a, b) in enumerate(zip(got, want)):
+        if not np.array_equal(a, b):
+            bad = np.argwhere(a != b)
+            z, y, x = bad[0]
+            raise AssertionError(f"{what} {COMP[c]}: {len(bad)} cells differ, first at x={x} y={y} z={z}: "
+                                 f"gpu {a[z, y, x]!r} oracle {b[z, y, x]!r}")
+
+
+def test_device_expf_bit_exact():
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.uniform(-110, 90, 200000), rng.uniform(-1, 1, 100000), rng.uniform(-1e-3, 1e-3, 10000),
+                        np.array([0.0, -0.0, 88.72, 88.7228394, -103.9, -103.972084, -87.3, 1e-30, -1e-30])])
+    x = x.astype(np.float32)
+    got = device_expf(x)
+    want = np.array([oracle.expf(float(v)) for v in x[:20000]], np.float32)
+    assert np.array_equal(got[:20000], want)
+    # against FP64: within 2 ulp everywhere the result is normal
+    ref = np.exp(x.astype(np.float64))
+    ok = (ref > 1.2e-38) & (ref < 3e38)
+    ulp = np.spacing(ref[ok].astype(np.float32)).astype(np.float64)
+    assert np.max(np.abs(got[ok] - ref[ok]) / ulp) <= 2.0
+
+
+@pytest.mark.parametrize("kernel", [abi.KERNEL_FUSED, abi.KERNEL_SPLIT])
+@pytest.mark.parametrize("seed,size,pml", [(1, (24, 20, 18), 4), (2, (37, 29, 23), 5), (3, (64, 40, 33), 8)])
+def test_random_scene_bit_exact(kernel, seed, size, pml):
+    sc = configs.random_scene(size=size, pml=pml, seed=seed)
+    steps = 80
+    got = run_gpu(sc, steps, kernel)
+    want = run_oracle(sc, steps)
+    assert_bitwise(got, want, f"seed {seed} kernel {kernel}")
+    ref = run_oracle(sc, steps, "f64")
+    for c in range(6):
+        assert rel_l2(got[c], ref[c]) < 1e-5, (COMP[c], rel_l2(got[c], ref[c]))
+
+
+def test_fused_equals_split_and_chunking():
+    sc = configs.random_scene(size=(70, 300, 26), pml=6, seed=11)
+    a = run_gpu(sc, 30, abi.KERNEL_FUSED, chunks=3)
+    b = run_gpu(sc, 30, abi.KERNEL_SPLIT, chunks=1)
+    assert_bitwise(a, b, "fused vs split")
+
+
+def test_random_initial_fields_no_materials():
+    """Arbitrary E/B state in vacuum with the absorber: every stencil term is exercised."""
+    grid = abi.GridConfig((33, 34, 35), courant=0.55, pml_thickness=3)
+    rng = np.random.default_rng(5)
+    comps = [rng.standard_normal((35, 34, 33)).astype(np.float32) for _ in range(6)]
+    g = SimulationGrid(grid)
+    g.write_components(comps)
+    g.step(25)
+    g.synchronize(60000)
+    got = g.read_components()
+    o = oracle.Oracle(grid, "f32")
+    o.write_components(comps)
+    o.step(25)
+    assert_bitwise(got, o.read_components(), "random fields")
+
+
+def test_zero_thickness_absorber_and_minimum_size():
+    grid = abi.GridConfig((4, 4, 4), courant=0.3, pml_thickness=0)  # clamped up to 8 cells per axis
+    sc = configs.random_scene(size=(8, 8, 8), pml=0, seed=4, thin_wire=False, sources=1)
+    sc.grid = grid
+    g = SimulationGrid(grid)
+    assert g.size() == (8, 8, 8)
+    oracle.load_scene(g, sc)
+    g.step(40)
+    g.synchronize(60000)
+    assert_bitwise(g.read_components(), run_oracle(sc, 40), "tiny grid")
