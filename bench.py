@@ -93,6 +93,19 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def replica_throughput(cells_done: float, elapsed_s: float, dist=None, device=None):
+    """Whole-job throughput of independent replicas: the cell-steps every rank processed, divided by
+    the slowest rank's time (max over ranks). Returns (Mcells/s, max elapsed seconds)."""
+    if dist is None:
+        return cells_done / elapsed_s / 1e6, elapsed_s
+    import torch
+    t = torch.tensor([elapsed_s], dtype=torch.float64, device=device)
+    c = torch.tensor([cells_done], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(c, op=dist.ReduceOp.SUM)
+    return float(c.item()) / float(t.item()) / 1e6, float(t.item())
+
+
 def build_scene(size: int, steps: int):
     from em_lab_gb300 import configs
     return configs.plain_large(steps=steps, size=size)
@@ -235,14 +248,10 @@ def main():
         ev1.record(stream)
         barrier()
     launches = launch_count() - l0
-    elapsed_ms = ev0.elapsed_time(ev1)
     kernel_ms, kernel_n = grid.kernel_time(reset=True)
     grid.set_timing(False)
-    if dist is not None:
-        t = torch.tensor([elapsed_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed_ms = float(t.item())
-    value = cells * args.steps * world / (elapsed_ms * 1e-3) / 1e6
+    value, elapsed_s = replica_throughput(cells * args.steps, ev0.elapsed_time(ev1) * 1e-3, dist, "cuda")
+    elapsed_ms = elapsed_s * 1e3
     peak, peak_kind = _peaks()
     per_launch_ms = kernel_ms / max(kernel_n, 1)
     achieved = BYTES_PER_CELL_STEP * cells / (per_launch_ms * 1e-3) / 1e9
@@ -272,12 +281,7 @@ def main():
         frames += 1
     series = grid.ports_series()
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = cells * frames * frame * world / e2e_s / 1e6
+    e2e_value, e2e_s = replica_throughput(cells * frames * frame, time.perf_counter() - t0, dist, "cuda")
     nsrc = len(sc.sources)
     h2d = 4 * nsrc + 16 + 16 * (2 if sc.far_field else 1)  # signals + rotations per step (+ blends per call)
     d2h = (len(probe) * 54 * 16 + 6 * 4 * ((b1 - b0 + 16) // 16) ** 2) / frame + 8 * len(ports)

@@ -49,7 +49,9 @@ def random_blocks(builder: EnvironmentBuilder, fraction: float, seed: int, lo: i
     filled = np.zeros((nz, ny, nx), bool)
     count = 0
     blocks = 0
-    while count < target and blocks < 1_000_000:
+    attempts = 0
+    while count < target and attempts < 200_000:
+        attempts += 1
         e = rng.integers(edge_range[0], edge_range[1] + 1, size=3)
         p = np.array([rng.integers(lo, max(lo + 1, hi - e[a])) for a in range(3)])
         if keep_out is not None:

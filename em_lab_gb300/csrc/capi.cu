@@ -87,6 +87,11 @@ struct emlab_grid {
     uint32_t classes = 0, wire_start = 0;
     DevBuf<float> pml;
     int pml_stride = 0;
+    DevBuf<uint8_t> pml_cls;
+    DevBuf<float2> pml_coef;
+    int pml_K = 0;
+    TmaMaps* tma = nullptr;
+    DevBuf<unsigned> d_err;  // set by a solver kernel whose bounded on-device wait ran out
     std::vector<float> cell_sigma, cell_eps;  // alpha channels of the textures (read-back only)
     // sources
     std::vector<emlab_source> desc;
@@ -153,6 +158,9 @@ YeeArgs yee_args(emlab_grid* g) {
     a.wire_start = g->wire_start;
     a.pml = g->pml.p;
     a.pml_stride = g->pml_stride;
+    a.pml_cls = g->pml_cls.p;
+    a.pml_coef = g->pml_coef.p;
+    a.pml_K = g->pml_K;
     a.L = g->cfg.pml_thickness;
     a.dt = g->cfg.courant;
     // z chunks: enough CTAs for ~4 per SM, but at least 8 planes each (one plane is recomputed)
@@ -203,6 +211,17 @@ int upload_class_table(emlab_grid* g, const ClassTable& t) {
     g->classes = t.classes;
     g->wire_start = t.wire_start;
     return EMLAB_OK;
+}
+
+// Tensor maps of both field generations and the class index (the TMA kernel's inputs).
+void refresh_tma(emlab_grid* g) {
+    if (!g->tma) g->tma = tma_maps_create();
+    const int cur = g->cur;
+    for (int gen = 0; gen < 2; ++gen) {
+        g->cur = gen;
+        tma_maps_encode(g->tma, gen, yee_args(g), g->wide);
+    }
+    g->cur = cur;
 }
 
 int clear_fields(emlab_grid* g) {
@@ -290,7 +309,8 @@ int emlab_grid_create(emlab_grid** out) {
     if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&g->stage_done[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&g->stage_done[1], cudaEventDisableTiming) != cudaSuccess ||
-        g->d_flag.alloc(1) != cudaSuccess) {
+        g->d_flag.alloc(1) != cudaSuccess || g->d_err.alloc(1) != cudaSuccess ||
+        cudaMemset(g->d_err.p, 0, 4) != cudaSuccess) {
         delete g;
         return fail(EMLAB_ERR_CUDA, "stream or event creation failed");
     }
@@ -307,6 +327,7 @@ int emlab_grid_destroy(emlab_grid* g) {
         if (g->stage_done[s]) cudaEventDestroy(g->stage_done[s]);
     }
     for (size_t i = 0; i < g->ev_start.size(); ++i) cudaEventDestroy(g->ev_start[i]), cudaEventDestroy(g->ev_stop[i]);
+    if (g->tma) tma_maps_destroy(g->tma);
     cudaStream_t s = g->stream;
     delete g;
     if (s) cudaStreamDestroy(s);
@@ -336,6 +357,15 @@ int emlab_grid_configure(emlab_grid* g, const emlab_grid_config* req) {
     const std::vector<float> pt = pml_tables(c, g->pml_stride);
     EMLAB_CUDA(g->pml.alloc(pt.size()));
     EMLAB_CUDA(cudaMemcpy(g->pml.p, pt.data(), pt.size() * 4, cudaMemcpyHostToDevice));
+    {
+        std::vector<uint8_t> pcls;
+        std::vector<float> coef;
+        pml_class_tables(c, g->pml_stride, pcls, coef, g->pml_K);
+        EMLAB_CUDA(g->pml_cls.alloc(pcls.size()));
+        EMLAB_CUDA(cudaMemcpy(g->pml_cls.p, pcls.data(), pcls.size(), cudaMemcpyHostToDevice));
+        EMLAB_CUDA(g->pml_coef.alloc(coef.size() / 2));
+        EMLAB_CUDA(cudaMemcpy(g->pml_coef.p, coef.data(), coef.size() * 4, cudaMemcpyHostToDevice));
+    }
     // vacuum materials: class 0 everywhere (SimulationGrid.cpp:185-192)
     const long long n = g->cells();
     try {
@@ -362,6 +392,7 @@ int emlab_grid_configure(emlab_grid* g, const emlab_grid_config* req) {
     g->classes = 1, g->wire_start = 1;
     int rc = clear_fields(g);
     if (rc) return rc;
+    refresh_tma(g);
     g->step = 0;
     g->configured = true;
     // the source lists index cells of the old size: rebuild them for the new one
@@ -399,6 +430,7 @@ int emlab_grid_upload_materials(emlab_grid* g, const float* sigma, const float* 
     if (!build_classes(sigma, eps_r, nx, ny, nz, edges, n_edges, wires, n_wires, g->cfg.courant, t, err))
         return fail(EMLAB_ERR_OOM, err);
     if (int rc = upload_class_table(g, t)) return rc;
+    refresh_tma(g);
     const long long n = g->cells();
     std::memcpy(g->cell_sigma.data(), sigma, (size_t)n * 4);
     std::memcpy(g->cell_eps.data(), eps_r, (size_t)n * 4);
@@ -495,7 +527,9 @@ int emlab_grid_step(emlab_grid* g, int count) {
                 launch_yee_split(a, g->wide, g->stream);
                 g_launches += 2;
             } else {
-                launch_yee_fused(a, g->wide, g->stream);
+                const bool tma = g->kernel == EMLAB_KERNEL_FUSED &&
+                                 launch_yee_tma(a, g->tma, g->cur, g->wide, g->d_err.p, g->stream);
+                if (!tma) launch_yee_fused(a, g->wide, g->stream);
                 g_launches += 1;
                 g->cur ^= 1;
                 a = yee_args(g);  // sources act on the new generation
@@ -538,7 +572,15 @@ int emlab_grid_synchronize(emlab_grid* g, int timeout_ms) {
     const auto t0 = std::chrono::steady_clock::now();
     for (;;) {
         cudaError_t e = cudaStreamQuery(g->stream);
-        if (e == cudaSuccess) return EMLAB_OK;
+        if (e == cudaSuccess) {
+            unsigned err = 0;
+            EMLAB_CUDA(cudaMemcpy(&err, g->d_err.p, 4, cudaMemcpyDeviceToHost));
+            if (err) {
+                EMLAB_CUDA(cudaMemset(g->d_err.p, 0, 4));
+                return fail(EMLAB_ERR_TIMEOUT, "a solver kernel gave up a bounded wait on the device");
+            }
+            return EMLAB_OK;
+        }
         if (e != cudaErrorNotReady) return fail(EMLAB_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e));
         if (std::chrono::steady_clock::now() - t0 > limit) return fail(EMLAB_ERR_TIMEOUT, "grid stream wait timed out");
         std::this_thread::sleep_for(std::chrono::microseconds(50));
@@ -621,7 +663,8 @@ int emlab_grid_write_components(emlab_grid* g, const float* ex, const float* ey,
 
 int emlab_grid_set_kernel(emlab_grid* g, int kernel) {
     if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
-    EMLAB_REQUIRE(kernel == EMLAB_KERNEL_FUSED || kernel == EMLAB_KERNEL_SPLIT, "unknown kernel");
+    EMLAB_REQUIRE(kernel == EMLAB_KERNEL_FUSED || kernel == EMLAB_KERNEL_SPLIT || kernel == EMLAB_KERNEL_FUSED_LDG,
+                  "unknown kernel");
     g->kernel = kernel;
     return EMLAB_OK;
 }
@@ -939,6 +982,38 @@ int emlab_lines_read(emlab_grid* g, float* phasors, float* now) {
     if (now) EMLAB_CUDA(cudaMemcpyAsync(now, g->d_line_now.p, (size_t)g->nq * 4, cudaMemcpyDeviceToHost, g->stream));
     return emlab_grid_synchronize(g, 0);
 }
+
+// ---- host-side set-up ----------------------------------------------------------------------
+int emlab_edge_materials(const float* sigma, const float* eps_r, int nx, int ny, int nz,
+                         const emlab_edge_override* edges, size_t n_edges, const emlab_wire_term* wires,
+                         size_t n_wires, float* edge_sigma, float* edge_eps, float* wire0, float* wire1,
+                         uint32_t* classes) {
+    EMLAB_REQUIRE(sigma && eps_r && nx > 0 && ny > 0 && nz > 0, "bad material arguments");
+    EMLAB_REQUIRE((edges || n_edges == 0) && (wires || n_wires == 0), "null override array");
+    ClassTable t;
+    std::string err;
+    if (!build_classes(sigma, eps_r, nx, ny, nz, edges, n_edges, wires, n_wires, 0.5f, t, err))
+        return fail(EMLAB_ERR_OOM, err);
+    const int pitch = row_pitch(nx);
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const size_t i = ((size_t)z * ny + y) * nx + x;
+                const uint32_t c = t.cls[((size_t)z * ny + y) * pitch + x];
+                const float* m = &t.tabM[(size_t)c * 8];
+                const float* w = &t.tabW[(size_t)c * 8];
+                for (int a = 0; a < 3; ++a) {
+                    if (edge_sigma) edge_sigma[i * 3 + a] = m[a];
+                    if (edge_eps) edge_eps[i * 3 + a] = m[3 + a];
+                    if (wire0) wire0[i * 3 + a] = w[a];
+                    if (wire1) wire1[i * 3 + a] = w[3 + a];
+                }
+            }
+    if (classes) *classes = t.classes;
+    return EMLAB_OK;
+}
+
+double emlab_source_signal(const emlab_source* source, double t) { return source ? source_signal(*source, t) : 0.0; }
 
 // ---- self-checks ---------------------------------------------------------------------------
 int emlab_debug_expf(const float* in, float* out, size_t n) {

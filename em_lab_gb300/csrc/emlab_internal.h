@@ -39,6 +39,9 @@ struct YeeArgs {
     unsigned wire_start;
     const float* pml;   // [6][pml_stride]: I_x, I_y, I_z (integer positions), H_x, H_y, H_z (half)
     int pml_stride;
+    const unsigned char* pml_cls;  // [6][pml_stride]: depth class of each position (same order)
+    const float2* pml_coef;        // [K][K][K]: (e^{-x}, dt phi(x)), x = dt ((V_i + V_j) + V_k)
+    int pml_K;
     int L;
     float dt;
     int zchunk;
@@ -61,6 +64,15 @@ struct MonitorArgs {
 };
 
 void launch_yee_fused(const YeeArgs& a, bool wide, cudaStream_t s);
+
+// TMA-staged fused kernel: tensor maps of one field generation and the class index.
+struct TmaMaps;
+TmaMaps* tma_maps_create();
+void tma_maps_destroy(TmaMaps* m);
+// Encodes the maps for generation `gen` (0 or 1); returns false if TMA cannot be used.
+bool tma_maps_encode(TmaMaps* m, int gen, const YeeArgs& a, bool wide);
+// Launches the TMA kernel reading generation `gen`; err receives a nonzero word if a wait timed out.
+bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsigned* err, cudaStream_t s);
 void launch_yee_split(const YeeArgs& a, bool wide, cudaStream_t s);
 void launch_sources(const YeeArgs& a, const SourceArgs& sa, int k, bool wide, cudaStream_t s);
 

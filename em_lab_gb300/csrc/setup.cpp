@@ -206,6 +206,37 @@ std::vector<float> pml_tables(const emlab_grid_config& c, int stride) {
     return t;
 }
 
+void pml_class_tables(const emlab_grid_config& c, int stride, std::vector<uint8_t>& cls, std::vector<float>& coef,
+                      int& K) {
+    const int L = c.pml_thickness;
+    K = 2 * L + 2;
+    std::vector<float> V((size_t)K, 0.0f);
+    for (int k = 1; k <= L; ++k) V[(size_t)k] = emlab_pml_profile((float)k, L, c.pml_sigma_max, c.pml_grading);
+    for (int m = 0; m <= L; ++m)
+        V[(size_t)(L + 1 + m)] = emlab_pml_profile((float)m + 0.5f, L, c.pml_sigma_max, c.pml_grading);
+    cls.assign((size_t)6 * stride, 0);
+    const int n[3] = {c.nx, c.ny, c.nz};
+    for (int a = 0; a < 3; ++a)
+        for (int i = 0; i < n[a]; ++i) {
+            const float di = emlab_pml_depth((float)i, n[a], L);
+            const float dh = emlab_pml_depth((float)i + 0.5f, n[a], L);
+            // integer depths are whole numbers, half-integer depths are m + 0.5 (both at most L + 0.5)
+            cls[(size_t)a * stride + i] = (uint8_t)(di <= 0.0f ? 0 : (int)di);
+            cls[(size_t)(3 + a) * stride + i] = (uint8_t)(dh <= 0.0f ? 0 : L + 1 + (int)(dh - 0.5f));
+        }
+    const float dt = c.courant;
+    coef.assign((size_t)K * K * K * 2, 0.0f);
+    for (int i = 0; i < K; ++i)
+        for (int j = 0; j < K; ++j)
+            for (int k = 0; k < K; ++k) {
+                const float sigma = (V[(size_t)i] + V[(size_t)j]) + V[(size_t)k];
+                const float x = sigma * dt;
+                float* e = &coef[(((size_t)i * K + j) * K + k) * 2];
+                e[0] = emlab_expf(-x);
+                e[1] = dt * emlab_phi(x);
+            }
+}
+
 int pack_sources(const emlab_source* s, size_t n, std::vector<emlab_source>& desc, std::vector<float>& packed) {
     desc.clear();
     packed.clear();

@@ -40,6 +40,14 @@ void class_coefficients(ClassTable& t, float dt);
 // (common.glsl:23-36): 6 tables of `stride` floats: I_x, I_y, I_z, H_x, H_y, H_z.
 std::vector<float> pml_tables(const emlab_grid_config& c, int stride);
 
+// Absorber coefficients by depth class: each axis position (integer or half-integer) maps to a
+// class k in [0, K), K = 2L + 2 (0: outside the layer, 1..L: integer depths, L+1..2L+1: depths
+// 0.5..L+0.5), and coef[(i K + j) K + k] = (e^{-x}, dt phi(x)) with x = ((V_i + V_j) + V_k) dt,
+// V the profile of common.glsl:23-27 at the class depth. cls: 6 tables of `stride` bytes in the
+// order of pml_tables.
+void pml_class_tables(const emlab_grid_config& c, int stride, std::vector<uint8_t>& cls, std::vector<float>& coef,
+                      int& K);
+
 // setSources (src/SimulationGrid.cpp:302-349): packed sources (16 floats: center, halfExtent,
 // polAmp, softness) and the sorted per-cell lists (cells: 4 ints per cell + sentinel).
 int pack_sources(const emlab_source* s, size_t n, std::vector<emlab_source>& desc, std::vector<float>& packed);

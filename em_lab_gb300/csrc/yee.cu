@@ -12,80 +12,11 @@
 //    generation: 50 bytes of HBM traffic per cell-step with a 16-bit class index.
 //  * yee_split_b / yee_split_e: the reference's two in-place passes (84+ bytes per cell-step),
 //    kept as the layout-for-layout counterpart and as a cross-check of the fused kernel.
-#include "emlab_internal.h"
+#include "yee_common.cuh"
 
 namespace emlab {
 
 namespace {
-
-__device__ __forceinline__ bool in_pml(const YeeArgs& a, int x, int y, int z) {
-    // common.glsl:40-43
-    return x < a.L || y < a.L || z < a.L || x >= a.nx - (a.L + 1) || y >= a.ny - (a.L + 1) || z >= a.nz - (a.L + 1);
-}
-
-template <typename Idx>
-__device__ __forceinline__ unsigned load_class(const YeeArgs& a, long long i) {
-    return (unsigned)__ldg(static_cast<const Idx*>(a.cls) + i);
-}
-
-// Exponential-integrator B update inside the absorber (update_B.comp:58-64).
-__device__ __forceinline__ float b_pml(float b, float curl, float sm, float dt) {
-    const float x = sm * dt;
-    return emlab_expf(-x) * b - (dt * emlab_phi(x)) * curl;
-}
-
-// E update inside the absorber (update_E.comp:51-64).
-__device__ __forceinline__ float e_pml(float e, float curl, float sigma, float eps, float dt) {
-    const float dtEps = dt / eps;
-    const float x = sigma * dtEps;
-    return emlab_expf(-x) * e + (dtEps * emlab_phi(x)) * curl;
-}
-
-// B^{n+1/2} at cell (x,y,z) from E^n at the cell and its +x, +y, +z neighbours (update_B.comp:35-67).
-__device__ __forceinline__ void b_cell(const YeeArgs& a, float& bx, float& by, float& bz, float e0x, float e0y,
-                                       float e0z, float exy, float exz, float eyx, float eyz, float ezx, float ezy,
-                                       unsigned c, int x, int y, int z) {
-    float t0x = eyz - e0z, t0y = ezx - e0x, t0z = exy - e0y;
-    float t1x = ezy - e0y, t1y = exz - e0z, t1z = eyx - e0x;
-    if (c >= a.wire_start) {
-        const float4 w0 = __ldg(a.tabW + 2 * c), w1 = __ldg(a.tabW + 2 * c + 1);
-        t0x = t0x * w0.x, t0y = t0y * w0.y, t0z = t0z * w0.z;
-        t1x = t1x * w0.w, t1y = t1y * w1.x, t1z = t1z * w1.y;
-    }
-    const float cx = t0x - t1x, cy = t0y - t1y, cz = t0z - t1z;
-    const float dt = a.dt;
-    if (in_pml(a, x, y, z)) {
-        const int S = a.pml_stride;
-        const float ix = __ldg(a.pml + x), iy = __ldg(a.pml + S + y), iz = __ldg(a.pml + 2 * S + z);
-        const float hx = __ldg(a.pml + 3 * S + x), hy = __ldg(a.pml + 4 * S + y), hz = __ldg(a.pml + 5 * S + z);
-        bx = b_pml(bx, cx, (ix + hy) + hz, dt);
-        by = b_pml(by, cy, (hx + iy) + hz, dt);
-        bz = b_pml(bz, cz, (hx + hy) + iz, dt);
-    } else {
-        bx = bx - dt * cx;
-        by = by - dt * cy;
-        bz = bz - dt * cz;
-    }
-}
-
-// E^{n+1} at cell (x,y,z) from curl B^{n+1/2} (update_E.comp:41-64).
-__device__ __forceinline__ void e_cell(const YeeArgs& a, float& ex, float& ey, float& ez, float cx, float cy, float cz,
-                                       unsigned c, int x, int y, int z) {
-    if (!in_pml(a, x, y, z)) {
-        const float4 t0 = __ldg(a.tabE + 2 * c), t1 = __ldg(a.tabE + 2 * c + 1);
-        ex = t0.x * ex + t0.w * cx;
-        ey = t0.y * ey + t1.x * cy;
-        ez = t0.z * ez + t1.y * cz;
-    } else {
-        const float4 m0 = __ldg(a.tabM + 2 * c), m1 = __ldg(a.tabM + 2 * c + 1);
-        const int S = a.pml_stride;
-        const float ix = __ldg(a.pml + x), iy = __ldg(a.pml + S + y), iz = __ldg(a.pml + 2 * S + z);
-        const float hx = __ldg(a.pml + 3 * S + x), hy = __ldg(a.pml + 4 * S + y), hz = __ldg(a.pml + 5 * S + z);
-        ex = e_pml(ex, cx, m0.x + ((hx + iy) + iz), m0.w, a.dt);
-        ey = e_pml(ey, cy, m0.y + ((ix + hy) + iz), m1.x, a.dt);
-        ez = e_pml(ez, cz, m0.z + ((ix + iy) + hz), m1.y, a.dt);
-    }
-}
 
 // ----------------------------------------------------------------------------------------------
 // Fused single-pass kernel.

@@ -75,6 +75,9 @@ def load_library() -> C.CDLL:
         "emlab_lines_configure": ([P, ip, I, ip, fp, I, F, F], I),
         "emlab_lines_read": ([P, fp, fp], I),
         "emlab_debug_expf": ([fp, fp, SZ], I),
+        "emlab_edge_materials": ([fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ, C.POINTER(abi.WireTerm), SZ,
+                                  fp, fp, fp, fp, C.POINTER(C.c_uint32)], I),
+        "emlab_source_signal": ([C.POINTER(abi.Source), D], D),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -109,6 +112,28 @@ def device_expf(x) -> np.ndarray:
     out = np.empty_like(x)
     _check(load_library().emlab_debug_expf(_fptr(x), _fptr(out), x.size))
     return out
+
+
+def edge_materials(sigma, eps_r, edges=(), wires=()):
+    """Host-side uploadMaterials arithmetic: (edge sigma, edge eps, wire0, wire1, classes), each
+    array (nz, ny, nx, 3) as the solver sees it; needs no device."""
+    sigma = np.asarray(sigma, np.float32)
+    nz, ny, nx = sigma.shape
+    s = _f32(sigma)
+    e = _f32(eps_r, s.size)
+    ea, ne = abi.array_of(abi.EdgeOverride, edges)
+    wa, nw = abi.array_of(abi.WireTerm, wires)
+    outs = [np.empty((nz, ny, nx, 3), np.float32) for _ in range(4)]
+    classes = C.c_uint32()
+    _check(load_library().emlab_edge_materials(_fptr(s), _fptr(e), nx, ny, nz, ea, ne, wa, nw,
+                                               *[_fptr(o) for o in outs], C.byref(classes)))
+    return (*outs, int(classes.value))
+
+
+def source_signal(src, t: float) -> float:
+    """SourceDesc::signal through the library (FP64)."""
+    s = src.to_c() if hasattr(src, "to_c") else src
+    return float(load_library().emlab_source_signal(C.byref(s), float(t)))
 
 
 class SimulationGrid:

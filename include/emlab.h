@@ -31,9 +31,12 @@ extern "C" {
 #define EMLAB_ERR_NONFINITE 5 /* non-finite field values detected */
 #define EMLAB_ERR_NO_DEVICE 6 /* no CUDA device is visible */
 
-/* Solver kernels: the fused single-pass Yee step (default) or the reference's two-pass layout. */
+/* Solver kernels, all bit-identical: the fused single-pass Yee step with TMA-staged z planes
+ * (default; falls back to the load-staged variant where tensor maps cannot be built), the
+ * load-staged fused step, or the reference's two-pass layout. */
 #define EMLAB_KERNEL_FUSED 0
 #define EMLAB_KERNEL_SPLIT 1
+#define EMLAB_KERNEL_FUSED_LDG 2
 
 /* Waveforms of emlab_source (src/SimulationGrid.hpp:108-111). */
 #define EMLAB_WAVE_CW 0
@@ -141,7 +144,8 @@ int emlab_grid_reset_fields(emlab_grid* g);
  * then every monitor attached to the grid samples the step, on the device. Returns when the work
  * is queued on the grid's stream; emlab_grid_synchronize waits for it. */
 int emlab_grid_step(emlab_grid* g, int count);
-/* Bounded wait for the grid's stream (EMLAB_ERR_TIMEOUT after timeout_ms; <= 0 waits 60 s). */
+/* Bounded wait for the grid's stream (EMLAB_ERR_TIMEOUT after timeout_ms; <= 0 waits 60 s). Also
+ * EMLAB_ERR_TIMEOUT if a solver kernel gave up a bounded on-device wait since the last call. */
 int emlab_grid_synchronize(emlab_grid* g, int timeout_ms);
 int emlab_grid_get_state(const emlab_grid* g, emlab_grid_state* out);
 /* Read-back of the E and B textures in the reference's RGBA32F layout (E.a = cell sigma,
@@ -214,6 +218,18 @@ int emlab_lines_configure(emlab_grid* g, const int* quantities, int n_quantities
                           const float* weights, int n_terms, float wavelength, float averaging_periods);
 /* Phasors (4 floats per quantity: stage1 re, im, stage2 re, im) and instantaneous values. */
 int emlab_lines_read(emlab_grid* g, float* phasors, float* now);
+
+/* ---- host-side set-up (no device needed) ------------------------------------------------- */
+/* The edge materials uploadMaterials derives (src/SimulationGrid.cpp:224-291), as the shaders see
+ * them after unpackHalf2x16: per cell 3 conductivities (x, y, z edges, >= 0), 3 permittivities
+ * (>= 1) and the thin-wire factors of term0 and term1 (3 each); any output pointer may be NULL.
+ * Also returns the number of distinct material classes the device table will hold. */
+int emlab_edge_materials(const float* sigma, const float* eps_r, int nx, int ny, int nz,
+                         const emlab_edge_override* edges, size_t n_edges, const emlab_wire_term* wires,
+                         size_t n_wires, float* edge_sigma, float* edge_eps, float* wire0, float* wire1,
+                         uint32_t* classes);
+/* SourceDesc::signal (src/SimulationGrid.cpp:103-130): the FP64 source waveform at time t. */
+double emlab_source_signal(const emlab_source* source, double t);
 
 /* ---- self-checks ------------------------------------------------------------------------- */
 /* Evaluates the device emlab_expf on n inputs (bit-exactness check against the host). */

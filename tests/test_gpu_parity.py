@@ -65,8 +65,12 @@ def test_device_expf_bit_exact():
     assert np.max(np.abs(got[ok] - ref[ok]) / ulp) <= 2.0
 
 
-@pytest.mark.parametrize("kernel", [abi.KERNEL_FUSED, abi.KERNEL_SPLIT])
-@pytest.mark.parametrize("seed,size,pml", [(1, (24, 20, 18), 4), (2, (37, 29, 23), 5), (3, (64, 40, 33), 8)])
+KERNELS = [abi.KERNEL_FUSED, abi.KERNEL_FUSED_LDG, abi.KERNEL_SPLIT]
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("seed,size,pml", [(1, (24, 20, 18), 4), (2, (37, 29, 23), 5), (3, (64, 40, 33), 8),
+                                           (4, (40, 260, 16), 3)])
 def test_random_scene_bit_exact(kernel, seed, size, pml):
     sc = configs.random_scene(size=size, pml=pml, seed=seed)
     steps = 80
@@ -78,19 +82,22 @@ def test_random_scene_bit_exact(kernel, seed, size, pml):
         assert rel_l2(got[c], ref[c]) < 1e-5, (COMP[c], rel_l2(got[c], ref[c]))
 
 
-def test_fused_equals_split_and_chunking():
+@pytest.mark.parametrize("kernel", [abi.KERNEL_FUSED, abi.KERNEL_FUSED_LDG])
+def test_fused_equals_split_and_chunking(kernel):
     sc = configs.random_scene(size=(70, 300, 26), pml=6, seed=11)
-    a = run_gpu(sc, 30, abi.KERNEL_FUSED, chunks=3)
+    a = run_gpu(sc, 30, kernel, chunks=3)
     b = run_gpu(sc, 30, abi.KERNEL_SPLIT, chunks=1)
     assert_bitwise(a, b, "fused vs split")
 
 
-def test_random_initial_fields_no_materials():
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_random_initial_fields_no_materials(kernel):
     """Arbitrary E/B state in vacuum with the absorber: every stencil term is exercised."""
     grid = abi.GridConfig((33, 34, 35), courant=0.55, pml_thickness=3)
     rng = np.random.default_rng(5)
     comps = [rng.standard_normal((35, 34, 33)).astype(np.float32) for _ in range(6)]
     g = SimulationGrid(grid)
+    g.set_kernel(kernel)
     g.write_components(comps)
     g.step(25)
     g.synchronize(60000)
