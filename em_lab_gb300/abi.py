@@ -18,6 +18,10 @@ KERNEL_FUSED_LDG = 2
 WAVE_CW = 0
 WAVE_PULSE = 1
 
+# fixed scratch of emlab_flux_planes_noalloc
+FLUX_NOALLOC_MAX_PLANES = 64
+FLUX_NOALLOC_MAX_PARTIALS = 65536
+
 
 class GridConfig(C.Structure):
     """GridConfig (src/SimulationGrid.hpp:25-31); defaults are the reference's."""

@@ -291,6 +291,20 @@ int require_grid(const emlab_grid* g) {
 
 }  // namespace
 
+namespace emlab {
+int grid_view(emlab_grid* g, MonitorArgs* m, cudaStream_t* stream, int* device) {
+    if (int rc = require_grid(g)) return rc;
+    cudaError_t e = cudaSetDevice(g->device);
+    if (e != cudaSuccess) return fail(EMLAB_ERR_CUDA, cudaGetErrorString(e));
+    *m = monitor_args(g);
+    *stream = g->stream;
+    *device = g->device;
+    return EMLAB_OK;
+}
+int report_error(int code, const char* msg) { return fail(code, msg); }
+void count_launches(int n) { g_launches += (uint64_t)n; }
+}  // namespace emlab
+
 extern "C" {
 
 const char* emlab_last_error(void) { return g_last_error.c_str(); }

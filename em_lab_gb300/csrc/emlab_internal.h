@@ -98,3 +98,13 @@ void launch_check_finite(const MonitorArgs& m, unsigned* flag, cudaStream_t s);
 void launch_debug_expf(const float* in, float* out, size_t n, cudaStream_t s);
 
 }  // namespace emlab
+
+struct emlab_grid;
+
+namespace emlab {
+// The current field generation, stream and device of a configured grid (EMLAB_OK or an error code
+// with the message set); records an error message for the calling thread; counts kernel launches.
+int grid_view(emlab_grid* g, MonitorArgs* m, cudaStream_t* stream, int* device);
+int report_error(int code, const char* msg);
+void count_launches(int n);
+}  // namespace emlab

@@ -72,6 +72,7 @@ def load_library() -> C.CDLL:
         "emlab_ntff_evaluate": ([P, fp, I, fp], I),
         "emlab_probe_gather": ([P, ip, I, fp], I),
         "emlab_flux_planes": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
+        "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_lines_configure": ([P, ip, I, ip, fp, I, F, F], I),
         "emlab_lines_read": ([P, fp, fp], I),
         "emlab_debug_expf": ([fp, fp, SZ], I),
@@ -346,6 +347,14 @@ class SimulationGrid:
         arr, n = abi.array_of(abi.FluxPlane, planes)
         out = np.zeros(max(1, n), np.float64)
         _check(self._lib.emlab_flux_planes(self._h, arr, n, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out[:n]
+
+    def flux_planes_noalloc(self, planes) -> np.ndarray:
+        """flux_planes without device allocation, for callers that must not allocate: scratch is a
+        fixed device array (at most 64 planes / 65536 workgroup partials) shared by all calls."""
+        arr, n = abi.array_of(abi.FluxPlane, planes)
+        out = np.zeros(max(1, n), np.float64)
+        _check(self._lib.emlab_flux_planes_noalloc(self._h, arr, n, out.ctypes.data_as(C.POINTER(C.c_double))))
         return out[:n]
 
     def lines_configure(self, quantities, terms, weights, wavelength, averaging_periods=4.0):

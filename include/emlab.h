@@ -210,6 +210,22 @@ int emlab_probe_gather(emlab_grid* g, const int* origins, int n_probes, float* o
  * FP32 16x16-workgroup partial sums of plane i (without the box orientation sign). */
 int emlab_flux_planes(emlab_grid* g, const emlab_flux_plane* planes, int n_planes, double* out);
 
+/* Flux through planes for callers that must not allocate device memory (no counterpart in the
+ * reference). emlab_flux_planes allocates and frees its per-workgroup partial sums on every call;
+ * cudaMalloc/cudaFree synchronise the whole device (a frame loop that measures flux every other
+ * frame would stall the solver each time), are not allowed during a CUDA stream capture, and are
+ * unwelcome in applications that budget all device memory themselves. This entry point allocates
+ * nothing: its scratch is a fixed file-scope device array of EMLAB_FLUX_NOALLOC_MAX_PARTIALS FP32
+ * workgroup partials (256 KB) plus EMLAB_FLUX_NOALLOC_MAX_PLANES FP64 sums, held by every device
+ * that loads the library until the process exits. Requests needing more planes or partials fail
+ * with EMLAB_ERR_INVALID. The first call on a device looks the scratch up (cudaGetSymbolAddress,
+ * with the grid's device current); make that first call before any stream capture. Every call
+ * shares the scratch and overwrites all of it that it reads, so calls whose kernels overlap on the
+ * GPU (grids on different streams of one device) race. Results equal emlab_flux_planes bit for bit. */
+#define EMLAB_FLUX_NOALLOC_MAX_PLANES 64
+#define EMLAB_FLUX_NOALLOC_MAX_PARTIALS 65536
+int emlab_flux_planes_noalloc(emlab_grid* g, const emlab_flux_plane* planes, int n_planes, double* out);
+
 /* ---- coax line monitor: line_accumulate.comp (src/Coax.cpp:179-197) ---------------------- */
 /* quantities: 4 ints each (first term, term count, 0 = E integral / 1 = B integral, unused);
  * terms: 4 ints each (x, y, z, component 0-5 = Ex..Ez, Bx..Bz); weights: one per term.
