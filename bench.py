@@ -200,7 +200,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--size", type=int, default=512)
-    ap.add_argument("--kernel", default="fused", choices=["fused", "split"])
+    ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
+    ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end leg (default: --steps)")
     args = ap.parse_args()
@@ -221,7 +222,8 @@ def main():
     sc = build_scene(args.size, args.steps)
     cells = float(np.prod(sc.grid.size))
     grid = SimulationGrid(sc.grid)
-    grid.set_kernel(abi.KERNEL_SPLIT if args.kernel == "split" else abi.KERNEL_FUSED)
+    grid.set_kernel({"fused": abi.KERNEL_FUSED, "fused_ldg": abi.KERNEL_FUSED_LDG, "split": abi.KERNEL_SPLIT}[args.kernel])
+    grid.set_tiling(args.tile_rows)
     load_grid(grid, sc)
     ports = [p.to_c() for p in sc.ports]
     wl = sc.ports[0].wavelength

@@ -80,6 +80,7 @@ struct emlab_grid {
     DevBuf<float> fields;  // 12 component arrays: generation 0 (Ex..Bz), generation 1
     int cur = 0;
     int kernel = EMLAB_KERNEL_FUSED;
+    int tile_rows = 0;  // 0: automatic
     // materials
     DevBuf<uint8_t> cls;
     bool wide = false;
@@ -163,8 +164,10 @@ YeeArgs yee_args(emlab_grid* g) {
     a.pml_K = g->pml_K;
     a.L = g->cfg.pml_thickness;
     a.dt = g->cfg.courant;
-    // z chunks: enough CTAs for ~4 per SM, but at least 8 planes each (one plane is recomputed)
-    const int ty = a.ny >= 256 ? 16 : 8;
+    // tile height and z chunks: enough CTAs for ~4 per SM, but at least 8 planes each (the first
+    // plane of a chunk is recomputed)
+    const int ty = g->tile_rows == 16 ? 16 : 8;
+    a.tile_rows = ty;
     const long long xy = (long long)((a.nx + 31) / 32) * ((a.ny + ty - 1) / ty);
     const long long want = 152 * 4;
     int chunks = (int)std::max<long long>(1, (want + xy - 1) / xy);
@@ -680,6 +683,14 @@ int emlab_grid_set_kernel(emlab_grid* g, int kernel) {
     EMLAB_REQUIRE(kernel == EMLAB_KERNEL_FUSED || kernel == EMLAB_KERNEL_SPLIT || kernel == EMLAB_KERNEL_FUSED_LDG,
                   "unknown kernel");
     g->kernel = kernel;
+    return EMLAB_OK;
+}
+
+int emlab_grid_set_tiling(emlab_grid* g, int tile_rows) {
+    if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
+    EMLAB_REQUIRE(tile_rows == 0 || tile_rows == 8 || tile_rows == 16, "tile rows must be 0 (automatic), 8 or 16");
+    g->tile_rows = tile_rows;
+    if (g->configured) refresh_tma(g);  // the TMA boxes depend on the tile height
     return EMLAB_OK;
 }
 

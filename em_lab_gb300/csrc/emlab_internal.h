@@ -45,6 +45,7 @@ struct YeeArgs {
     int L;
     float dt;
     int zchunk;
+    int tile_rows;   // rows of cells per CTA tile of the fused kernels (8 or 16)
 };
 
 struct SourceArgs {

@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(64) apply_sources(YeeArgs a, SourceArgs sa, in
 
 template <typename Idx>
 void fused_launch(const YeeArgs& a, cudaStream_t s) {
-    if (a.ny >= 256) {
+    if (a.tile_rows == 16) {
         constexpr int TY = 16;
         const dim3 grid((a.nx + 31) / 32, (a.ny + TY - 1) / TY, (a.nz + a.zchunk - 1) / a.zchunk);
         yee_fused<Idx, TY><<<grid, dim3(32, TY), 0, s>>>(a);

@@ -3,11 +3,12 @@
 // Same arithmetic and traversal as yee_fused (yee.cu): a CTA owns a 32 x TY column of cells and
 // marches it along z, computing B^{n+1/2} for its cells plus the -x/-y halo cells, then E^{n+1}.
 // Difference: the inputs of each z plane (E^n with a one-cell halo, B^n and the class index with
-// the low halo) arrive by cp.async.bulk.tensor into a STAGES-deep shared-memory ring, issued by
-// one thread and completed on per-stage mbarriers, so several planes are in flight while the CTA
-// computes; threads never form global addresses for loads. B^{n+1/2} of the plane is kept in a
-// double-buffered shared tile so one __syncthreads per plane suffices. Results go to the other
-// field generation with coalesced 128-byte warp stores.
+// the low halo) arrive by cp.async.bulk.tensor into a 4- or 6-deep shared-memory ring, issued by
+// a control warp and completed on per-stage mbarriers, so several planes are in flight while the
+// CTA computes; threads never form global addresses for loads. The control warp also computes the
+// halo B components, so the cell warps run a branch-free update with hoisted invariants.
+// B^{n+1/2} of the plane is kept in a double-buffered shared tile so one __syncthreads per plane
+// suffices. Results go to the other field generation with coalesced 128-byte warp stores.
 //
 // TMA boxes start at x0-4 (x0-8 for a 16-bit class index) so the innermost coordinate stays
 // 16-byte aligned; coordinates outside the grid read zeros, which is exactly the reference's
@@ -28,8 +29,6 @@ struct TmaMaps {
 };
 
 namespace {
-
-constexpr int kStages = 4;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -68,6 +67,7 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 
 template <int TY, typename Idx>
 struct Layout {
+    static constexpr int STAGES = TY <= 8 ? 6 : 4;           // planes in the shared-memory ring
     static constexpr int EW = 40;                         // E box: x0-4 .. x0+35, TY+2 rows
     static constexpr int BW = 36;                         // B box: x0-4 .. x0+31, TY+1 rows
     static constexpr int CW = sizeof(Idx) == 2 ? 40 : 36;  // class box width
@@ -83,40 +83,40 @@ struct Layout {
     static constexpr int C_OFF = B_OFF + 3 * BP;
     static constexpr int STAGE = C_OFF + CP;
     static constexpr uint32_t TX_BYTES = 3 * E_BYTES + 3 * B_BYTES + C_BYTES;
-    static constexpr int SB_OFF = kStages * STAGE;                   // B^{n+1/2}: [2][3][TY+1][33]
+    static constexpr int SB_OFF = STAGES * STAGE;                    // B^{n+1/2}: [2][3][TY+1][33]
     static constexpr int SB_BYTES = 2 * 3 * (TY + 1) * 33 * 4;
     static constexpr int BAR_OFF = (SB_OFF + SB_BYTES + 127) / 128 * 128;
-    static constexpr int SMEM = BAR_OFF + 8 * kStages;
+    static constexpr int SMEM = BAR_OFF + 8 * STAGES;
 };
 
+// Warps 0..TY-1 own the tile's cells (warp w = row y0+w, lane = x0+lane). Warp TY is the halo and
+// control warp: it issues the TMA copies, waits on the mbarriers (so no other warp ever polls), and
+// computes the B^{n+1/2} components of the -y row and -x column that the E update of the tile
+// needs (Bx, Bz at (x0+lane, y0-1); By, Bz at (x0-1, y0+lane)).
 template <int TY, typename Idx>
-__global__ void __launch_bounds__(32 * TY) yee_tma(const __grid_constant__ CUtensorMap tex,
-                                                   const __grid_constant__ CUtensorMap tey,
-                                                   const __grid_constant__ CUtensorMap tez,
-                                                   const __grid_constant__ CUtensorMap tbx,
-                                                   const __grid_constant__ CUtensorMap tby,
-                                                   const __grid_constant__ CUtensorMap tbz,
-                                                   const __grid_constant__ CUtensorMap tcls, YeeArgs a, unsigned* err) {
+__global__ void __launch_bounds__(32 * (TY + 1), TY <= 8 ? 3 : 1)
+    yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUtensorMap tey,
+            const __grid_constant__ CUtensorMap tez, const __grid_constant__ CUtensorMap tbx,
+            const __grid_constant__ CUtensorMap tby, const __grid_constant__ CUtensorMap tbz,
+            const __grid_constant__ CUtensorMap tcls, YeeArgs a, unsigned* err) {
     using Lay = Layout<TY, Idx>;
-    constexpr int TX = 32, NW = TY;
+    constexpr int S_ = Lay::STAGES;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Lay::BAR_OFF);
     float* sB = reinterpret_cast<float*>(smem + Lay::SB_OFF);
 
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const bool ctl = warp == TY;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * TY;
     const int zs = blockIdx.z * a.zchunk;
     const int ze = min(a.nz, zs + a.zchunk);
     if (zs >= ze) return;
     const int zstart = zs > 0 ? zs - 1 : zs;  // a chunk above z = 0 first rebuilds B^{n+1/2}(zs-1)
     const int zlast = ze;                      // planes zstart .. ze are read (ze as the "z+1" plane)
-    const int x = x0 + tx, y = y0 + ty;
-    const bool own = x < a.nx && y < a.ny;
 
-    auto stage_ptr = [&](int p) { return smem + ((p - zstart) % kStages) * Lay::STAGE; };
     auto issue = [&](int p) {
-        unsigned char* st = stage_ptr(p);
-        uint64_t* bar = bars + (p - zstart) % kStages;
+        unsigned char* st = smem + ((p - zstart) % S_) * Lay::STAGE;
+        uint64_t* bar = bars + (p - zstart) % S_;
         mbar_expect_tx(bar, Lay::TX_BYTES);
         tma_load_3d(st + Lay::E_OFF + 0 * Lay::EP, &tex, x0 - 4, y0 - 1, p, bar);
         tma_load_3d(st + Lay::E_OFF + 1 * Lay::EP, &tey, x0 - 4, y0 - 1, p, bar);
@@ -126,95 +126,190 @@ __global__ void __launch_bounds__(32 * TY) yee_tma(const __grid_constant__ CUten
         tma_load_3d(st + Lay::B_OFF + 2 * Lay::BP, &tbz, x0 - 4, y0 - 1, p, bar);
         tma_load_3d(st + Lay::C_OFF, &tcls, x0 - Lay::CX, y0 - 1, p, bar);
     };
-
-    if (tid == 0) {
-        for (int s = 0; s < kStages; ++s) mbar_init(bars + s, 1);
+    const bool leader = ctl && lane == 0;
+    if (leader) {
+        for (int s = 0; s < S_; ++s) mbar_init(bars + s, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid == 0)
-        for (int p = zstart; p <= zlast && p < zstart + kStages; ++p) issue(p);
+    bool failed = false;
+    if (leader) {
+        for (int p = zstart; p <= zlast && p < zstart + S_; ++p) issue(p);
+        // planes zstart and zstart+1 before the first B phase; later planes one iteration ahead,
+        // just before the per-plane barrier, which passes the TMA writes on to the other warps
+        failed = !mbar_wait(bars + 0, 0) || !mbar_wait(bars + 1, 0);
+    }
+    if (__syncthreads_or(failed)) {
+        if (leader) atomicOr(err, 1u);
+        return;
+    }
 
-    // typed views of a stage
-    auto E = [&](unsigned char* st, int c, int r, int col) -> float {
-        return reinterpret_cast<const float*>(st + Lay::E_OFF + c * Lay::EP)[r * Lay::EW + col];
-    };
-    auto Bo = [&](unsigned char* st, int c, int r, int col) -> float {
-        return reinterpret_cast<const float*>(st + Lay::B_OFF + c * Lay::BP)[r * Lay::BW + col];
-    };
-    auto CL = [&](unsigned char* st, int r, int col) -> unsigned {
-        return (unsigned)reinterpret_cast<const Idx*>(st + Lay::C_OFF)[r * Lay::CW + col];
-    };
     auto SB = [&](int buf, int c, int r, int col) -> float& { return sB[((buf * 3 + c) * (TY + 1) + r) * 33 + col]; };
+    constexpr int EPF = Lay::EP / 4, BPF = Lay::BP / 4;
+    const int L = a.L, K = a.pml_K, PS = a.pml_stride;
+    const unsigned char* pcls = a.pml_cls;
+    const float2* T = a.pml_coef;
+    const float dt = a.dt;
 
-    // halo cells handled by this thread: item h = ty + NW * lane for lanes covering 32 + TY items
-    // (items 0..31: (x0+h, y0-1); items 32..: (x0-1, y0+h-32)); spread so every warp does one share.
-    const int nitems = 32 + TY;
-    const int h = ty + NW * tx;
-    const bool has_halo = h < nitems;
+    // ---- per-thread invariants of the z march ----
+    // own warps: cell (x, y); halo warp: row cell (x0+lane, y0-1) and column cell (x0-1, y0+lane)
+    const int x = ctl ? x0 + lane : x0 + lane;
+    const int y = ctl ? y0 - 1 : y0 + warp;
+    const bool own = !ctl && x < a.nx && y < a.ny;
+    const bool row_live = ctl && y0 > 0 && x < a.nx;                        // (x0+lane, y0-1)
+    const int cy = y0 + lane;                                               // column cell y
+    const bool col_live = ctl && lane < TY && x0 > 0 && cy < a.ny;          // (x0-1, y0+lane)
+    auto pml_rows = [&](int px, int py, int& R1, int& R2, int& R3, int& R4) {
+        const int ix = __ldg(pcls + px), iy = __ldg(pcls + PS + py), hx = __ldg(pcls + 3 * PS + px),
+                  hy = __ldg(pcls + 4 * PS + py);
+        R1 = (ix * K + hy) * K, R2 = (hx * K + iy) * K, R3 = (hx * K + hy) * K, R4 = (ix * K + iy) * K;
+    };
+    auto pml_xy_of = [&](int px, int py) { return px < L || py < L || px >= a.nx - (L + 1) || py >= a.ny - (L + 1); };
+    int R1 = 0, R2 = 0, R3 = 0, R4 = 0, C1 = 0, C2 = 0, C3 = 0, C4 = 0;
+    if (own || row_live) pml_rows(x, y, R1, R2, R3, R4);
+    if (col_live) pml_rows(x0 - 1, cy, C1, C2, C3, C4);
+    const bool pml_xy = (own || row_live) && pml_xy_of(x, y);
+    const bool pml_xy_c = col_live && pml_xy_of(x0 - 1, cy);
+    // shared-memory offsets: own/row cell and column cell (E/B box column 3 = x0-1)
+    const int me = (ctl ? 0 : warp + 1) * Lay::EW + lane + 4;
+    const int mb = (ctl ? 0 : warp + 1) * Lay::BW + lane + 4;
+    const int mc = (ctl ? 0 : warp + 1) * Lay::CW + lane + Lay::CX;
+    const int ce = (lane + 1) * Lay::EW + 3, cb = (lane + 1) * Lay::BW + 3, cc = (lane + 1) * Lay::CW + Lay::CX - 1;
+    const long long row_off = (long long)y * a.pitch + x;
 
     float bpx = 0.0f, bpy = 0.0f;  // B^{n+1/2}(x, y, z-1).xy (B below the lower face is 0)
-    bool failed = false;
     for (int z = zstart; z < ze; ++z) {
-        const int use = (z - zstart) / kStages;
-        unsigned char* st = stage_ptr(z);
-        unsigned char* st1 = stage_ptr(z + 1);
-        if (!mbar_wait(bars + (z - zstart) % kStages, use & 1)) failed = true;
-        if (!mbar_wait(bars + (z + 1 - zstart) % kStages, ((z + 1 - zstart) / kStages) & 1)) failed = true;
+        const int rel = z - zstart;
+        const unsigned char* st = smem + (rel % S_) * Lay::STAGE;
+        const unsigned char* st1 = smem + ((rel + 1) % S_) * Lay::STAGE;
         const bool emit = z >= zs;
-        const int buf = (z - zstart) & 1;
-        const int r = ty + 1, col = tx + 4;
-        const float e0x = E(st, 0, r, col), e0y = E(st, 1, r, col), e0z = E(st, 2, r, col);
-        float bx = 0.0f, by = 0.0f, bz = 0.0f;
+        const int buf = rel & 1;
+        const bool pz = z < L || z >= a.nz - (L + 1);
+        const int iz = __ldg(pcls + 2 * PS + z), hz = __ldg(pcls + 5 * PS + z);
+        const float* Es = reinterpret_cast<const float*>(st + Lay::E_OFF);
+        const float* E1 = reinterpret_cast<const float*>(st1 + Lay::E_OFF);
+        const float* Bs = reinterpret_cast<const float*>(st + Lay::B_OFF);
+        const Idx* Cs = reinterpret_cast<const Idx*>(st + Lay::C_OFF);
+        const long long off = (long long)z * a.plane + row_off;
+        float bx = 0.0f, by = 0.0f, bz = 0.0f, e0x = 0.0f, e0y = 0.0f, e0z = 0.0f;
         unsigned c = 0;
         if (own) {
-            bx = Bo(st, 0, r, col), by = Bo(st, 1, r, col), bz = Bo(st, 2, r, col);
-            c = CL(st, r, tx + Lay::CX);
-            b_cell(a, bx, by, bz, e0x, e0y, e0z, E(st, 1, r, col + 1), E(st, 2, r, col + 1), E(st, 0, r + 1, col),
-                   E(st, 2, r + 1, col), E(st1, 0, r, col), E(st1, 1, r, col), c, x, y, z);
-            SB(buf, 0, r, tx + 1) = bx, SB(buf, 1, r, tx + 1) = by, SB(buf, 2, r, tx + 1) = bz;
-            if (emit) {
-                const long long i = (long long)z * a.plane + (long long)y * a.pitch + x;
-                a.nbx[i] = bx, a.nby[i] = by, a.nbz[i] = bz;
+            // update_B.comp:35-67 for the own cell
+            e0x = Es[me], e0y = Es[EPF + me], e0z = Es[2 * EPF + me];
+            bx = Bs[mb], by = Bs[BPF + mb], bz = Bs[2 * BPF + mb];
+            c = (unsigned)Cs[mc];
+            const float exy = Es[EPF + me + 1], exz = Es[2 * EPF + me + 1];
+            const float eyx = Es[me + Lay::EW], eyz = Es[2 * EPF + me + Lay::EW];
+            const float ezx = E1[me], ezy = E1[EPF + me];
+            float t0x = eyz - e0z, t0y = ezx - e0x, t0z = exy - e0y;
+            float t1x = ezy - e0y, t1y = exz - e0z, t1z = eyx - e0x;
+            if (c >= a.wire_start) {
+                const float4 w0 = __ldg(a.tabW + 2 * c), w1 = __ldg(a.tabW + 2 * c + 1);
+                t0x = t0x * w0.x, t0y = t0y * w0.y, t0z = t0z * w0.z;
+                t1x = t1x * w0.w, t1y = t1y * w1.x, t1z = t1z * w1.y;
+            }
+            const float cx = t0x - t1x, cy_ = t0y - t1y, cz = t0z - t1z;
+            if (pml_xy || pz) {
+                const float2 kx = __ldg(T + R1 + hz), ky = __ldg(T + R2 + hz), kz = __ldg(T + R3 + iz);
+                bx = kx.x * bx - kx.y * cx;
+                by = ky.x * by - ky.y * cy_;
+                bz = kz.x * bz - kz.y * cz;
+            } else {
+                bx = bx - dt * cx;
+                by = by - dt * cy_;
+                bz = bz - dt * cz;
+            }
+            SB(buf, 0, warp + 1, lane + 1) = bx, SB(buf, 1, warp + 1, lane + 1) = by, SB(buf, 2, warp + 1, lane + 1) = bz;
+            if (emit) a.nbx[off] = bx, a.nby[off] = by, a.nbz[off] = bz;
+        } else if (ctl && emit) {
+            // -y row: Bx, Bz at (x0+lane, y0-1) (update_B.comp:41-66, components x and z)
+            float hbx = 0.0f, hbz = 0.0f;  // B below the lower faces is 0
+            if (row_live) {
+                const float f0x = Es[me], f0y = Es[EPF + me], f0z = Es[2 * EPF + me];
+                const unsigned hc = (unsigned)Cs[mc];
+                float t0x = Es[2 * EPF + me + Lay::EW] - f0z, t1x = E1[EPF + me] - f0y;  // d_y Ez, d_z Ey
+                float t0z = Es[EPF + me + 1] - f0y, t1z = Es[me + Lay::EW] - f0x;      // d_x Ey, d_y Ex
+                if (hc >= a.wire_start) {
+                    const float4 w0 = __ldg(a.tabW + 2 * hc), w1 = __ldg(a.tabW + 2 * hc + 1);
+                    t0x = t0x * w0.x, t0z = t0z * w0.z, t1x = t1x * w0.w, t1z = t1z * w1.y;
+                }
+                const float cx = t0x - t1x, cz = t0z - t1z;
+                hbx = Bs[mb], hbz = Bs[2 * BPF + mb];
+                if (pml_xy || pz) {
+                    const float2 kx = __ldg(T + R1 + hz), kz = __ldg(T + R3 + iz);
+                    hbx = kx.x * hbx - kx.y * cx;
+                    hbz = kz.x * hbz - kz.y * cz;
+                } else {
+                    hbx = hbx - dt * cx;
+                    hbz = hbz - dt * cz;
+                }
+            }
+            SB(buf, 0, 0, lane + 1) = hbx, SB(buf, 2, 0, lane + 1) = hbz;
+            // -x column: By, Bz at (x0-1, y0+lane)
+            if (lane < TY) {
+                float hby = 0.0f, hbz2 = 0.0f;
+                if (col_live) {
+                    const float f0x = Es[ce], f0y = Es[EPF + ce], f0z = Es[2 * EPF + ce];
+                    const unsigned hc = (unsigned)Cs[cc];
+                    float t0y = E1[ce] - f0x, t1y = Es[2 * EPF + ce + 1] - f0z;   // d_z Ex, d_x Ez
+                    float t0z = Es[EPF + ce + 1] - f0y, t1z = Es[ce + Lay::EW] - f0x;  // d_x Ey, d_y Ex
+                    if (hc >= a.wire_start) {
+                        const float4 w0 = __ldg(a.tabW + 2 * hc), w1 = __ldg(a.tabW + 2 * hc + 1);
+                        t0y = t0y * w0.y, t0z = t0z * w0.z, t1y = t1y * w1.x, t1z = t1z * w1.y;
+                    }
+                    const float cyy = t0y - t1y, cz = t0z - t1z;
+                    hby = Bs[BPF + cb], hbz2 = Bs[2 * BPF + cb];
+                    if (pml_xy_c || pz) {
+                        const float2 ky = __ldg(T + C2 + hz), kz = __ldg(T + C3 + iz);
+                        hby = ky.x * hby - ky.y * cyy;
+                        hbz2 = kz.x * hbz2 - kz.y * cz;
+                    } else {
+                        hby = hby - dt * cyy;
+                        hbz2 = hbz2 - dt * cz;
+                    }
+                }
+                SB(buf, 1, lane + 1, 0) = hby, SB(buf, 2, lane + 1, 0) = hbz2;
             }
         }
-        if (emit && has_halo) {
-            int hr, hc, gx, gy;  // tile row/column (E/B box coordinates) and lattice cell
-            if (h < 32) hr = 0, hc = h + 4, gx = x0 + h, gy = y0 - 1;
-            else hr = h - 32 + 1, hc = 3, gx = x0 - 1, gy = y0 + h - 32;
-            float hbx = 0.0f, hby = 0.0f, hbz = 0.0f;  // B below the lower faces is 0
-            if (gx >= 0 && gy >= 0 && gx < a.nx && gy < a.ny) {
-                hbx = Bo(st, 0, hr, hc), hby = Bo(st, 1, hr, hc), hbz = Bo(st, 2, hr, hc);
-                b_cell(a, hbx, hby, hbz, E(st, 0, hr, hc), E(st, 1, hr, hc), E(st, 2, hr, hc), E(st, 1, hr, hc + 1),
-                       E(st, 2, hr, hc + 1), E(st, 0, hr + 1, hc), E(st, 2, hr + 1, hc), E(st1, 0, hr, hc),
-                       E(st1, 1, hr, hc), CL(st, hr, hc - 4 + Lay::CX), gx, gy, z);
-            }
-            const int sr = h < 32 ? 0 : h - 32 + 1, sc = h < 32 ? h + 1 : 0;
-            SB(buf, 0, sr, sc) = hbx, SB(buf, 1, sr, sc) = hby, SB(buf, 2, sr, sc) = hbz;
-        }
+        // the next iteration's B phase reads plane z+2: the leader waits for it before the barrier
+        if (leader && z + 1 < ze) failed = !mbar_wait(bars + (rel + 2) % S_, ((rel + 2) / S_) & 1);
         if (__syncthreads_or(failed)) {
-            if (tid == 0) atomicOr(err, 1u);
+            if (leader) atomicOr(err, 1u);
             return;
         }
-        // every thread is past its reads of plane z-1's stage (E phase of the previous plane and
-        // B phase of this one): refill it with plane z-1+kStages
-        if (tid == 0 && z > zstart) {
-            const int p = z - 1 + kStages;
-            if (p <= zlast) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue(p);
-            }
+        // every warp is past its reads of plane z-1's stage: refill it with plane z-1+STAGES
+        if (leader && z > zstart && z - 1 + S_ <= zlast) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(z - 1 + S_);
         }
         if (emit && own) {
-            const float bxm_y = SB(buf, 1, r, tx), bxm_z = SB(buf, 2, r, tx);          // B(x-1)
-            const float bym_x = SB(buf, 0, r - 1, tx + 1), bym_z = SB(buf, 2, r - 1, tx + 1);  // B(y-1)
+            // update_E.comp:41-64 for the own cell
+            const float bxm_y = SB(buf, 1, warp + 1, lane), bxm_z = SB(buf, 2, warp + 1, lane);  // B(x-1)
+            const float bym_x = SB(buf, 0, warp, lane + 1), bym_z = SB(buf, 2, warp, lane + 1);  // B(y-1)
             const float cx = (bz - bym_z) - (by - bpy);
-            const float cy = (bx - bpx) - (bz - bxm_z);
+            const float cy_ = (bx - bpx) - (bz - bxm_z);
             const float cz = (by - bxm_y) - (bx - bym_x);
             float ex = e0x, ey = e0y, ez = e0z;
-            e_cell(a, ex, ey, ez, cx, cy, cz, c, x, y, z);
-            const long long i = (long long)z * a.plane + (long long)y * a.pitch + x;
-            a.nex[i] = ex, a.ney[i] = ey, a.nez[i] = ez;
+            if (!(pml_xy || pz)) {
+                if (c == 0) {  // vacuum: ca = 1 and cb = dt exactly, so 1 * e + dt * curl == e + dt * curl
+                    ex = ex + dt * cx;
+                    ey = ey + dt * cy_;
+                    ez = ez + dt * cz;
+                } else {
+                    const float4 t0 = __ldg(a.tabE + 2 * c), t1 = __ldg(a.tabE + 2 * c + 1);
+                    ex = t0.x * ex + t0.w * cx;
+                    ey = t0.y * ey + t1.x * cy_;
+                    ez = t0.z * ez + t1.y * cz;
+                }
+            } else if (c == 0) {
+                const float2 kx = __ldg(T + R2 + iz), ky = __ldg(T + R1 + iz), kz = __ldg(T + R4 + hz);
+                ex = kx.x * ex + kx.y * cx;
+                ey = ky.x * ey + ky.y * cy_;
+                ez = kz.x * ez + kz.y * cz;
+            } else {
+                e_cell(a, ex, ey, ez, cx, cy_, cz, c, x, y, z);
+            }
+            a.nex[off] = ex, a.ney[off] = ey, a.nez[off] = ez;
         }
         bpx = bx, bpy = by;
     }
@@ -252,7 +347,7 @@ bool encode(CUtensorMap* m, CUtensorMapDataType type, int elem, const void* base
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-int tile_rows(const YeeArgs& a) { return a.ny >= 256 ? 16 : 8; }
+int tile_rows(const YeeArgs& a) { return a.tile_rows == 16 ? 16 : 8; }
 
 template <int TY, typename Idx>
 bool launch_t(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaStream_t s) {
@@ -265,7 +360,7 @@ bool launch_t(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaSt
         configured = true;
     }
     const dim3 grid((a.nx + 31) / 32, (a.ny + TY - 1) / TY, (a.nz + a.zchunk - 1) / a.zchunk);
-    yee_tma<TY, Idx><<<grid, dim3(32, TY), Lay::SMEM, s>>>(m->e[gen][0], m->e[gen][1], m->e[gen][2], m->b[gen][0],
+    yee_tma<TY, Idx><<<grid, dim3(32, TY + 1), Lay::SMEM, s>>>(m->e[gen][0], m->e[gen][1], m->e[gen][2], m->b[gen][0],
                                                            m->b[gen][1], m->b[gen][2], m->cls, a, err);
     return true;
 }

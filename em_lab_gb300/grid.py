@@ -58,6 +58,7 @@ def load_library() -> C.CDLL:
         "emlab_grid_read_components": ([P, fp, fp, fp, fp, fp, fp], I),
         "emlab_grid_write_components": ([P, fp, fp, fp, fp, fp, fp], I),
         "emlab_grid_set_kernel": ([P, I], I),
+        "emlab_grid_set_tiling": ([P, I], I),
         "emlab_grid_stream": ([P, C.POINTER(P)], I),
         "emlab_grid_check_finite": ([P], I),
         "emlab_grid_set_timing": ([P, I], I),
@@ -239,6 +240,10 @@ class SimulationGrid:
 
     def set_kernel(self, kernel: int):
         _check(self._lib.emlab_grid_set_kernel(self._h, int(kernel)))
+
+    def set_tiling(self, tile_rows: int):
+        """Tile height of the fused kernels (8, 16, or 0 = automatic); results do not depend on it."""
+        _check(self._lib.emlab_grid_set_tiling(self._h, int(tile_rows)))
 
     def stream_handle(self) -> int:
         p = C.c_void_p()

@@ -22,9 +22,10 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / n) if n > 0 else float(np.linalg.norm(a))
 
 
-def run_gpu(sc, steps, kernel=abi.KERNEL_FUSED, chunks=1):
+def run_gpu(sc, steps, kernel=abi.KERNEL_FUSED, chunks=1, rows=0):
     g = SimulationGrid(sc.grid)
     g.set_kernel(kernel)
+    g.set_tiling(rows)
     oracle.load_scene(g, sc)
     for _ in range(chunks):
         g.step(steps // chunks)
@@ -69,12 +70,12 @@ KERNELS = [abi.KERNEL_FUSED, abi.KERNEL_FUSED_LDG, abi.KERNEL_SPLIT]
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
-@pytest.mark.parametrize("seed,size,pml", [(1, (24, 20, 18), 4), (2, (37, 29, 23), 5), (3, (64, 40, 33), 8),
-                                           (4, (40, 260, 16), 3)])
-def test_random_scene_bit_exact(kernel, seed, size, pml):
+@pytest.mark.parametrize("seed,size,pml,rows", [(1, (24, 20, 18), 4, 0), (2, (37, 29, 23), 5, 16),
+                                                (3, (64, 40, 33), 8, 8), (4, (40, 260, 16), 3, 16)])
+def test_random_scene_bit_exact(kernel, seed, size, pml, rows):
     sc = configs.random_scene(size=size, pml=pml, seed=seed)
     steps = 80
-    got = run_gpu(sc, steps, kernel)
+    got = run_gpu(sc, steps, kernel, rows=rows)
     want = run_oracle(sc, steps)
     assert_bitwise(got, want, f"seed {seed} kernel {kernel}")
     ref = run_oracle(sc, steps, "f64")
@@ -83,9 +84,10 @@ def test_random_scene_bit_exact(kernel, seed, size, pml):
 
 
 @pytest.mark.parametrize("kernel", [abi.KERNEL_FUSED, abi.KERNEL_FUSED_LDG])
-def test_fused_equals_split_and_chunking(kernel):
+@pytest.mark.parametrize("rows", [8, 16])
+def test_fused_equals_split_and_chunking(kernel, rows):
     sc = configs.random_scene(size=(70, 300, 26), pml=6, seed=11)
-    a = run_gpu(sc, 30, kernel, chunks=3)
+    a = run_gpu(sc, 30, kernel, chunks=3, rows=rows)
     b = run_gpu(sc, 30, abi.KERNEL_SPLIT, chunks=1)
     assert_bitwise(a, b, "fused vs split")
 
