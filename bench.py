@@ -201,7 +201,7 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
-    ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16])
+    ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 64])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end leg (default: --steps)")
     args = ap.parse_args()

@@ -14,6 +14,8 @@ EMLAB_ERR_NO_DEVICE = 6
 KERNEL_FUSED = 0
 KERNEL_SPLIT = 1
 KERNEL_FUSED_LDG = 2
+DFT_TENSOR = 0
+DFT_CUDA_CORES = 1
 
 WAVE_CW = 0
 WAVE_PULSE = 1

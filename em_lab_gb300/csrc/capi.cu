@@ -127,6 +127,19 @@ struct emlab_grid {
     DevBuf<int4> d_q, d_terms;
     DevBuf<float> d_weights, d_line_ph, d_line_now;
     float line_wl = 16.0f, line_avg = 4.0f;
+    // multi-frequency far-field DFT
+    bool dft_on = false;
+    int dft_box[13] = {};
+    int dft_points = 0, dft_nf = 0, dft_t = 0;
+    long long dft_n0 = 0;
+    uint64_t dft_samples = 0;
+    std::vector<double> dft_omega;
+    DevBuf<int> d_dft_box;
+    DevBuf<float2> d_dft_w;
+    DevBuf<double> d_dft_omega, d_dft_x;
+    DevBuf<float> d_dft_blk;
+    DevBuf<float> d_dft_bhi, d_dft_blo;  // tensor-core twiddles (split hi/lo, MMA operand layout)
+    int dft_engine = EMLAB_DFT_TENSOR;
     // scratch
     DevBuf<unsigned> d_flag;
     // solver-pass timing: event pairs recorded around each Yee launch, read back lazily
@@ -166,9 +179,11 @@ YeeArgs yee_args(emlab_grid* g) {
     a.dt = g->cfg.courant;
     // tile height and z chunks: enough CTAs for ~4 per SM, but at least 8 planes each (the first
     // plane of a chunk is recomputed)
-    const int ty = g->tile_rows == 16 ? 16 : 8;
-    a.tile_rows = ty;
-    const long long xy = (long long)((a.nx + 31) / 32) * ((a.ny + ty - 1) / ty);
+    const int mode = g->tile_rows == 0 ? 64 : g->tile_rows;  // automatic: 64 x 8 pair tiles
+    const int ty = mode == 16 ? 16 : 8;
+    const int tx = mode == 64 && g->kernel == EMLAB_KERNEL_FUSED ? 64 : 32;
+    a.tile_rows = g->kernel == EMLAB_KERNEL_FUSED ? mode : ty;
+    const long long xy = (long long)((a.nx + tx - 1) / tx) * ((a.ny + ty - 1) / ty);
     const long long want = 152 * 4;
     int chunks = (int)std::max<long long>(1, (want + xy - 1) / xy);
     int zc = (a.nz + chunks - 1) / chunks;
@@ -283,6 +298,23 @@ int timing_pair(emlab_grid* g, cudaEvent_t* start, cudaEvent_t* stop) {
     *start = g->ev_start[g->ev_used];
     *stop = g->ev_stop[g->ev_used];
     ++g->ev_used;
+    return EMLAB_OK;
+}
+
+constexpr int kDftBlock = 64;  // samples per time block (the fold kernel's register block)
+
+// Folds the samples gathered so far into the FP64 sums.
+int dft_fold(emlab_grid* g) {
+    if (!g->dft_on || g->dft_t == 0) return EMLAB_OK;
+    const double dt = (double)g->cfg.courant;
+    if (g->dft_engine != EMLAB_DFT_TENSOR ||
+        !launch_dft_fold_tc(g->d_dft_blk.p, g->dft_t, g->dft_points, g->dft_nf, g->d_dft_bhi.p, g->d_dft_blo.p,
+                            g->d_dft_omega.p, g->dft_n0, dt, g->d_dft_x.p, g->d_err.p, g->stream))
+        launch_dft_fold(g->d_dft_blk.p, g->dft_t, g->dft_points, g->dft_nf, g->d_dft_w.p, g->d_dft_omega.p,
+                        g->dft_n0, dt, g->d_dft_x.p, g->stream);
+    ++g_launches;
+    g->dft_samples += (uint64_t)g->dft_t;
+    g->dft_t = 0;
     return EMLAB_OK;
 }
 
@@ -422,6 +454,7 @@ int emlab_grid_configure(emlab_grid* g, const emlab_grid_config* req) {
     int zero[3] = {0, 0, 0};
     emlab_ntff_configure(g, zero, zero, 0.0f, 4.0f, nullptr);
     emlab_lines_configure(g, nullptr, 0, nullptr, nullptr, 0, 16.0f, 4.0f);
+    emlab_ntff_dft_configure(g, zero, zero, nullptr, 0, nullptr);
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
     return EMLAB_OK;
 }
@@ -577,6 +610,12 @@ int emlab_grid_step(emlab_grid* g, int count) {
                              d_lrot + k, d_bl + 2, 0, g->stream);
                 g_launches += 1;
             }
+            if (g->dft_on) {
+                if (g->dft_t == 0) g->dft_n0 = (long long)g->step;  // time index of the block's first sample
+                launch_dft_sample(mon, g->d_dft_box.p, g->dft_points, g->d_dft_blk.p, g->dft_t, g->stream);
+                g_launches += 1;
+                if (++g->dft_t == kDftBlock) dft_fold(g);
+            }
             if (int rc = check_launch()) return rc;
         }
     }
@@ -683,12 +722,14 @@ int emlab_grid_set_kernel(emlab_grid* g, int kernel) {
     EMLAB_REQUIRE(kernel == EMLAB_KERNEL_FUSED || kernel == EMLAB_KERNEL_SPLIT || kernel == EMLAB_KERNEL_FUSED_LDG,
                   "unknown kernel");
     g->kernel = kernel;
+    if (g->configured) refresh_tma(g);
     return EMLAB_OK;
 }
 
 int emlab_grid_set_tiling(emlab_grid* g, int tile_rows) {
     if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
-    EMLAB_REQUIRE(tile_rows == 0 || tile_rows == 8 || tile_rows == 16, "tile rows must be 0 (automatic), 8 or 16");
+    EMLAB_REQUIRE(tile_rows == 0 || tile_rows == 8 || tile_rows == 16 || tile_rows == 64,
+                  "tiling must be 0 (automatic), 8 or 16 (32-cell rows), or 64 (64 x 8 tiles of cell pairs)");
     g->tile_rows = tile_rows;
     if (g->configured) refresh_tma(g);  // the TMA boxes depend on the tile height
     return EMLAB_OK;
@@ -893,6 +934,136 @@ int emlab_ntff_evaluate(emlab_grid* g, const float* directions, int n_dirs, floa
     EMLAB_CUDA(cudaMemcpyAsync(tmp.data(), d_out.p, tmp.size() * 4, cudaMemcpyDeviceToHost, g->stream));
     if (int rc = emlab_grid_synchronize(g, 0)) return rc;
     // only the dispatch starting at direction 0 carries the power (ntff_pattern.comp:52)
+    for (int d = 0; d < n_dirs; ++d) out[2 * d] = tmp[2 * (size_t)d], out[2 * d + 1] = d == 0 ? tmp[1] : 0.0f;
+    return EMLAB_OK;
+}
+
+// ---- multi-frequency far-field DFT ------------------------------------------------------------
+int emlab_ntff_dft_configure(emlab_grid* g, const int box_min[3], const int box_max[3], const float* wavelengths,
+                             int n_freq, int box_out[6]) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    g->dft_on = false;
+    g->d_dft_x.release(), g->d_dft_blk.release();
+    if (n_freq <= 0) return EMLAB_OK;
+    EMLAB_REQUIRE(box_min && box_max && wavelengths, "null DFT argument");
+    EMLAB_REQUIRE(n_freq <= 128, "at most 128 DFT frequencies");
+    const int n[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+    const int L = g->cfg.pml_thickness;
+    int* b = g->dft_box;
+    for (int a = 0; a < 3; ++a) {
+        const int lo = L + 1, hi = n[a] - L - 2;
+        b[a] = std::clamp(std::min(box_min[a], box_max[a]), lo, hi);
+        b[3 + a] = std::clamp(std::max(box_min[a], box_max[a]), lo, hi);
+        if (b[3 + a] - b[a] < 4)
+            return fail(EMLAB_ERR_INVALID, "far-field DFT box is degenerate after clamping to the region inside the "
+                                           "absorbing layer");
+        if (box_out) box_out[a] = b[a], box_out[3 + a] = b[3 + a];
+    }
+    b[6] = 0;
+    for (int f = 0; f < 6; ++f) {
+        const int a = f >> 1, u = a == 0 ? 1 : 0, v = a == 2 ? 1 : 2;
+        b[7 + f] = b[6 + f] + (b[3 + u] - b[u] + 1) * (b[3 + v] - b[v] + 1);
+    }
+    g->dft_points = b[12];
+    g->dft_nf = n_freq;
+    g->dft_omega.assign((size_t)n_freq, 0.0);
+    std::vector<float2> w((size_t)n_freq * kDftBlock);
+    const double dt = (double)g->cfg.courant;
+    for (int f = 0; f < n_freq; ++f) {
+        g->dft_omega[(size_t)f] = 6.28318530717958647692 / (double)std::max(wavelengths[f], 2.0f);
+        for (int k = 0; k < kDftBlock; ++k) {
+            const double ph = g->dft_omega[(size_t)f] * dt * k;
+            w[(size_t)f * kDftBlock + k] = make_float2((float)std::cos(ph), (float)-std::sin(ph));
+        }
+    }
+    EMLAB_CUDA(g->d_dft_box.alloc(13));
+    EMLAB_CUDA(cudaMemcpy(g->d_dft_box.p, b, 13 * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_dft_w.alloc(w.size()));
+    EMLAB_CUDA(cudaMemcpy(g->d_dft_w.p, w.data(), w.size() * 8, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_dft_omega.alloc((size_t)n_freq));
+    EMLAB_CUDA(cudaMemcpy(g->d_dft_omega.p, g->dft_omega.data(), (size_t)n_freq * 8, cudaMemcpyHostToDevice));
+    std::vector<float> bhi, blo;
+    dft_tc_twiddles(n_freq, g->dft_omega.data(), dt, bhi, blo);
+    EMLAB_CUDA(g->d_dft_bhi.alloc(bhi.size()));
+    EMLAB_CUDA(g->d_dft_blo.alloc(blo.size()));
+    EMLAB_CUDA(cudaMemcpy(g->d_dft_bhi.p, bhi.data(), bhi.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpy(g->d_dft_blo.p, blo.data(), blo.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_dft_blk.alloc((size_t)kDftBlock * 6 * g->dft_points));
+    EMLAB_CUDA(g->d_dft_x.alloc((size_t)n_freq * g->dft_points * 12));
+    EMLAB_CUDA(cudaMemset(g->d_dft_x.p, 0, g->d_dft_x.n * 8));
+    g->dft_t = 0, g->dft_samples = 0;
+    g->dft_on = true;
+    return EMLAB_OK;
+}
+
+int emlab_ntff_dft_info(emlab_grid* g, int* points, uint64_t* samples) {
+    if (int rc = require_grid(g)) return rc;
+    if (points) *points = g->dft_on ? g->dft_points : 0;
+    if (samples) *samples = g->dft_samples + (uint64_t)g->dft_t;
+    return EMLAB_OK;
+}
+
+int emlab_ntff_dft_read(emlab_grid* g, double* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(g->dft_on, "far-field DFT monitor is not configured");
+    EMLAB_REQUIRE(out, "null output");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    if (int rc = dft_fold(g)) return rc;
+    if (int rc = check_launch()) return rc;
+    std::vector<double> x(g->d_dft_x.n);  // device layout [f][c][i][2] -> [f][i][c][2]
+    EMLAB_CUDA(cudaMemcpyAsync(x.data(), g->d_dft_x.p, x.size() * 8, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    const size_t P = (size_t)g->dft_points;
+    for (size_t f = 0; f < (size_t)g->dft_nf; ++f)
+        for (size_t c = 0; c < 6; ++c)
+            for (size_t i = 0; i < P; ++i) {
+                const size_t src = ((f * 6 + c) * P + i) * 2, dst = ((f * P + i) * 6 + c) * 2;
+                out[dst] = x[src], out[dst + 1] = x[src + 1];
+            }
+    return EMLAB_OK;
+}
+
+int emlab_ntff_dft_engine(emlab_grid* g, int engine) {
+    if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
+    EMLAB_REQUIRE(engine == EMLAB_DFT_TENSOR || engine == EMLAB_DFT_CUDA_CORES, "unknown DFT engine");
+    g->dft_engine = engine;
+    return EMLAB_OK;
+}
+
+int emlab_ntff_dft_evaluate(emlab_grid* g, int f, const float* directions, int n_dirs, float* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(g->dft_on && f >= 0 && f < g->dft_nf, "far-field DFT frequency out of range");
+    EMLAB_REQUIRE(directions && out && n_dirs > 0, "bad direction arguments");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    if (int rc = dft_fold(g)) return rc;
+    const uint64_t samples = g->dft_samples;
+    EMLAB_REQUIRE(samples > 0, "no far-field DFT samples yet");
+    DevBuf<float> ph;
+    EMLAB_CUDA(ph.alloc((size_t)g->dft_points * 32));
+    launch_dft_to_phasor(g->d_dft_x.p, g->dft_points, f, 2.0 / (double)samples, ph.p, g->stream);
+    const int slices = std::clamp((g->dft_points + 4095) / 4096, 1, 64);
+    const int chunk = 4096;
+    DevBuf<float4> d_dirs, d_part;
+    DevBuf<float> d_out;
+    EMLAB_CUDA(d_dirs.alloc((size_t)n_dirs));
+    EMLAB_CUDA(cudaMemcpyAsync(d_dirs.p, directions, (size_t)n_dirs * 16, cudaMemcpyHostToDevice, g->stream));
+    EMLAB_CUDA(d_part.alloc((size_t)chunk * slices * 4));
+    EMLAB_CUDA(d_out.alloc((size_t)n_dirs * 2));
+    const float k = (float)g->dft_omega[(size_t)f];
+    for (int first = 0; first < n_dirs; first += chunk) {
+        const int count = std::min(chunk, n_dirs - first);
+        launch_ntff_pattern(g->d_dft_box.p, g->dft_points, ph.p, d_dirs.p, first, count, slices, k, d_part.p,
+                            g->stream);
+        launch_ntff_reduce(d_dirs.p, d_part.p, first, count, slices, d_out.p, g->stream);
+        g_launches += 2;
+    }
+    g_launches += 1;
+    if (int rc = check_launch()) return rc;
+    std::vector<float> tmp((size_t)n_dirs * 2);
+    EMLAB_CUDA(cudaMemcpyAsync(tmp.data(), d_out.p, tmp.size() * 4, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
     for (int d = 0; d < n_dirs; ++d) out[2 * d] = tmp[2 * (size_t)d], out[2 * d + 1] = d == 0 ? tmp[1] : 0.0f;
     return EMLAB_OK;
 }

@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "emlab_math.h"
 
 namespace emlab {
@@ -96,6 +98,17 @@ void launch_ntff_reduce(const float4* dirs, const float4* partials, int first, i
 void launch_sweep_sums(const float* series, long long steps, int nports, double nu_lo, double nu_hi, int points,
                        double dt, double* out, cudaStream_t s);
 void launch_check_finite(const MonitorArgs& m, unsigned* flag, cudaStream_t s);
+// multi-frequency far-field DFT: per-step sampling into a time block, FP64 fold of a block
+void launch_dft_sample(const MonitorArgs& m, const int* box, int points, float* blk, int t, cudaStream_t s);
+void launch_dft_fold(const float* blk, int T, int points, int nf, const float2* W, const double* omega, long long n0,
+                     double dt, double* X, cudaStream_t s);
+void launch_dft_to_phasor(const double* X, int points, int f, double scale, float* ph, cudaStream_t s);
+// tensor-core fold (dft_tc.cu): MMA N for nf frequencies, host twiddle tables (hi, lo) in the
+// kernel's shared-memory layout, and the launcher (false if nf is too large or set-up failed)
+int dft_tc_mma_n(int nf);
+void dft_tc_twiddles(int nf, const double* omega, double dt, std::vector<float>& hi, std::vector<float>& lo);
+bool launch_dft_fold_tc(const float* blk, int T, int points, int nf, const float* b_hi, const float* b_lo,
+                        const double* omega, long long n0, double dt, double* X, unsigned* err, cudaStream_t s);
 void launch_debug_expf(const float* in, float* out, size_t n, cudaStream_t s);
 
 }  // namespace emlab

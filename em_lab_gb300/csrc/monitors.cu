@@ -368,6 +368,83 @@ __global__ void finite_kernel(MonitorArgs m, unsigned* flag) {
     }
 }
 
+// Multi-frequency far-field DFT, per step: the co-located E and H (field_sampling.glsl:17-32) of
+// every Huygens-box node into slot t of the time block, component-major: blk[(t * 6 + c) * P + i].
+__global__ void __launch_bounds__(256) dft_sample_kernel(MonitorArgs m, const int* box, int points, float* blk, int t) {
+    __shared__ int sbox[13];
+    if (threadIdx.x < 13) sbox[threadIdx.x] = box[threadIdx.x];
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= points) return;
+    int node[3];
+    float n[3], w;
+    ntff_point(sbox, i, node, n, w);
+    float E[3], Hh[3];
+    e_at_node(m, node[0], node[1], node[2], E[0], E[1], E[2]);
+    b_at_node(m, node[0], node[1], node[2], Hh[0], Hh[1], Hh[2]);
+    float* o = blk + (size_t)t * 6 * points + i;
+    o[0] = E[0], o[(size_t)points] = E[1], o[2 * (size_t)points] = E[2];
+    o[3 * (size_t)points] = Hh[0], o[4 * (size_t)points] = Hh[1], o[5 * (size_t)points] = Hh[2];
+}
+
+// Folds T samples of every column (component c of node i) into the FP64 sums:
+//   X_f += e^{-i w_f t0} sum_k F(t0 + k dt) e^{-i w_f k dt},
+// t0 = n0 dt for E and (n0 - 1/2) dt for H (B lags half a step). The block-relative twiddles
+// W[f][k] = (cos w_f k dt, -sin w_f k dt) are FP32 (from FP64 on the host); the in-block sums are
+// FP32 (<= 64 terms); the block phase e^{-i w_f t0} is evaluated in FP64 once per CTA and applied in
+// FP32; the accumulation is FP64. X layout: [f][c][i][re, im]. The CUDA-core twin of the
+// tensor-core fold (dft_tc.cu), which differs only in how the in-block sums are formed.
+constexpr int kDftMaxT = 64;
+__global__ void __launch_bounds__(128) dft_fold_kernel(const float* blk, int T, int points, int nf, const float2* W,
+                                                       const double* omega, long long n0, double dt, double* X) {
+    extern __shared__ float2 sW[];  // [nf][kDftMaxT], then the block phases [nf][E, H]
+    float2* rot = sW + nf * kDftMaxT;
+    for (int j = threadIdx.x; j < nf * kDftMaxT; j += blockDim.x) sW[j] = W[j];
+    for (int j = threadIdx.x; j < 2 * nf; j += blockDim.x) {
+        const double t0 = ((double)n0 - ((j & 1) ? 0.5 : 0.0)) * dt;
+        double sn, cs;
+        sincos(omega[j >> 1] * t0, &sn, &cs);
+        rot[j] = make_float2((float)cs, (float)sn);
+    }
+    __syncthreads();
+    const long long col = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (col >= 6ll * points) return;
+    const int c = (int)(col / points), i = (int)(col % points), h = c >= 3 ? 1 : 0;
+    float v[kDftMaxT];
+#pragma unroll
+    for (int k = 0; k < kDftMaxT; ++k) v[k] = k < T ? blk[(size_t)k * 6 * points + col] : 0.0f;
+    for (int f = 0; f < nf; ++f) {
+        float re = 0.0f, im = 0.0f;
+#pragma unroll
+        for (int k = 0; k < kDftMaxT; ++k) {
+            const float2 w = sW[f * kDftMaxT + k];
+            re = re + w.x * v[k];
+            im = im + w.y * v[k];
+        }
+        const float2 r = rot[2 * f + h];
+        const float xr = re * r.x + im * r.y, xi = im * r.x - re * r.y;  // (re + i im)(cos - i sin)
+        double2* o = reinterpret_cast<double2*>(X) + ((size_t)f * 6 + c) * points + i;
+        double2 a = *o;
+        a.x += (double)xr, a.y += (double)xi;
+        *o = a;
+    }
+}
+
+// Stage-2 phasor layout of ntff_pattern.comp (PhasorPair, 8 float4 per node) from the DFT sums of
+// one frequency, scaled by `scale` (2 / samples turns a sum into the amplitude of a steady tone).
+__global__ void dft_to_phasor_kernel(const double* X, int points, int f, double scale, float4* ph) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= points) return;
+    const double2* x = reinterpret_cast<const double2*>(X) + (size_t)f * 6 * points + i;
+    double2 v[6];
+    for (int c = 0; c < 6; ++c) v[c] = x[(size_t)c * points];
+    float4* p = ph + 8 * (size_t)i;
+    p[4] = make_float4((float)(v[0].x * scale), (float)(v[1].x * scale), (float)(v[2].x * scale), 0.0f);  // E re
+    p[5] = make_float4((float)(v[0].y * scale), (float)(v[1].y * scale), (float)(v[2].y * scale), 0.0f);  // E im
+    p[6] = make_float4((float)(v[3].x * scale), (float)(v[4].x * scale), (float)(v[5].x * scale), 0.0f);  // H re
+    p[7] = make_float4((float)(v[3].y * scale), (float)(v[4].y * scale), (float)(v[5].y * scale), 0.0f);  // H im
+}
+
 __global__ void expf_kernel(const float* in, float* out, size_t n) {
     const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (i < n) out[i] = emlab_expf(in[i]);
@@ -421,6 +498,25 @@ void launch_sweep_sums(const float* series, long long steps, int nports, double 
 
 void launch_check_finite(const MonitorArgs& m, unsigned* flag, cudaStream_t s) {
     finite_kernel<<<152 * 8, 256, 0, s>>>(m, flag);
+}
+
+void launch_dft_sample(const MonitorArgs& m, const int* box, int points, float* blk, int t, cudaStream_t s) {
+    dft_sample_kernel<<<(points + 255) / 256, 256, 0, s>>>(m, box, points, blk, t);
+}
+
+void launch_dft_fold(const float* blk, int T, int points, int nf, const float2* W, const double* omega, long long n0,
+                     double dt, double* X, cudaStream_t s) {
+    const long long cols = 6ll * points;
+    const size_t smem = (size_t)(nf * kDftMaxT + 2 * nf) * sizeof(float2);
+    static size_t smem_set = 48 * 1024;
+    if (smem > smem_set &&
+        cudaFuncSetAttribute(dft_fold_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess)
+        smem_set = smem;
+    dft_fold_kernel<<<(unsigned)((cols + 127) / 128), 128, smem, s>>>(blk, T, points, nf, W, omega, n0, dt, X);
+}
+
+void launch_dft_to_phasor(const double* X, int points, int f, double scale, float* ph, cudaStream_t s) {
+    dft_to_phasor_kernel<<<(points + 255) / 256, 256, 0, s>>>(X, points, f, scale, reinterpret_cast<float4*>(ph));
 }
 
 void launch_debug_expf(const float* in, float* out, size_t n, cudaStream_t s) {

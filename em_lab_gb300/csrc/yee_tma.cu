@@ -16,6 +16,8 @@
 // on expiry the CTA records an error word and leaves (the host reports EMLAB_ERR_TIMEOUT).
 #include <cuda.h>
 
+#include <algorithm>
+
 #include "yee_common.cuh"
 
 namespace emlab {
@@ -315,6 +317,376 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY <= 8 ? 3 : 1)
     }
 }
 
+// ------------------------------------------------------------------------------------------------
+// Two cells per thread along x: a CTA owns a 64 x TY tile (warp w = row y0+w, lane l = cells
+// x0+2l and x0+2l+1) and moves pairs with 64-bit shared and global accesses, so the per-plane
+// bookkeeping and most address arithmetic are paid once per two cells. Same arithmetic per cell.
+template <int TY, typename Idx>
+struct Layout2 {
+    static constexpr int STAGES = 4;
+    static constexpr int EW = 72;                         // E box: x0-4 .. x0+67, TY+2 rows
+    static constexpr int BW = 68;                         // B box: x0-4 .. x0+63, TY+1 rows
+    static constexpr int CW = sizeof(Idx) == 2 ? 72 : 68;  // class box width
+    static constexpr int CX = sizeof(Idx) == 2 ? 8 : 4;    // class box starts at x0 - CX
+    static constexpr int E_BYTES = EW * (TY + 2) * 4;
+    static constexpr int B_BYTES = BW * (TY + 1) * 4;
+    static constexpr int C_BYTES = CW * (TY + 1) * (int)sizeof(Idx);
+    static constexpr int EP = (E_BYTES + 127) / 128 * 128;
+    static constexpr int BP = (B_BYTES + 127) / 128 * 128;
+    static constexpr int CP = (C_BYTES + 127) / 128 * 128;
+    static constexpr int E_OFF = 0;
+    static constexpr int B_OFF = 3 * EP;
+    static constexpr int C_OFF = B_OFF + 3 * BP;
+    static constexpr int STAGE = C_OFF + CP;
+    static constexpr uint32_t TX_BYTES = 3 * E_BYTES + 3 * B_BYTES + C_BYTES;
+    static constexpr int SBW = 66;                        // B tile row: col 1 = x0-1, col 2+i = x0+i
+    static constexpr int SB_OFF = STAGES * STAGE;
+    static constexpr int SB_BYTES = 2 * 3 * (TY + 1) * SBW * 4;
+    static constexpr int BAR_OFF = (SB_OFF + SB_BYTES + 127) / 128 * 128;
+    static constexpr int SMEM = BAR_OFF + 8 * STAGES;
+};
+
+template <typename Idx>
+__device__ __forceinline__ void load_class_pair(const Idx* p, unsigned& a, unsigned& b);
+template <>
+__device__ __forceinline__ void load_class_pair<uint16_t>(const uint16_t* p, unsigned& a, unsigned& b) {
+    const unsigned v = *reinterpret_cast<const unsigned*>(p);
+    a = v & 0xffffu, b = v >> 16;
+}
+template <>
+__device__ __forceinline__ void load_class_pair<uint32_t>(const uint32_t* p, unsigned& a, unsigned& b) {
+    const uint2 v = *reinterpret_cast<const uint2*>(p);
+    a = v.x, b = v.y;
+}
+
+// B^{n+1/2} of one cell outside/inside the absorber from its curl terms (update_B.comp:47-67).
+__device__ __forceinline__ void b_update(const YeeArgs& a, float& bx, float& by, float& bz, float t0x, float t0y,
+                                         float t0z, float t1x, float t1y, float t1z, unsigned c, bool inp, int R1,
+                                         int R2, int R3, int iz, int hz) {
+    if (c >= a.wire_start) {
+        const float4 w0 = __ldg(a.tabW + 2 * c), w1 = __ldg(a.tabW + 2 * c + 1);
+        t0x = t0x * w0.x, t0y = t0y * w0.y, t0z = t0z * w0.z;
+        t1x = t1x * w0.w, t1y = t1y * w1.x, t1z = t1z * w1.y;
+    }
+    const float cx = t0x - t1x, cy = t0y - t1y, cz = t0z - t1z;
+    if (inp) {
+        const float2 kx = __ldg(a.pml_coef + R1 + hz), ky = __ldg(a.pml_coef + R2 + hz),
+                     kz = __ldg(a.pml_coef + R3 + iz);
+        bx = kx.x * bx - kx.y * cx;
+        by = ky.x * by - ky.y * cy;
+        bz = kz.x * bz - kz.y * cz;
+    } else {
+        const float dt = a.dt;
+        bx = bx - dt * cx;
+        by = by - dt * cy;
+        bz = bz - dt * cz;
+    }
+}
+
+// E^{n+1} of one cell from its curl (update_E.comp:41-64).
+__device__ __forceinline__ void e_update(const YeeArgs& a, float& ex, float& ey, float& ez, float cx, float cy,
+                                         float cz, unsigned c, bool inp, int R1, int R2, int R4, int iz, int hz, int x,
+                                         int y, int z) {
+    if (!inp) {
+        if (c == 0) {  // vacuum: ca = 1 and cb = dt exactly, so 1 * e + dt * curl == e + dt * curl
+            const float dt = a.dt;
+            ex = ex + dt * cx;
+            ey = ey + dt * cy;
+            ez = ez + dt * cz;
+        } else {
+            const float4 t0 = __ldg(a.tabE + 2 * c), t1 = __ldg(a.tabE + 2 * c + 1);
+            ex = t0.x * ex + t0.w * cx;
+            ey = t0.y * ey + t1.x * cy;
+            ez = t0.z * ez + t1.y * cz;
+        }
+    } else if (c == 0) {
+        const float2 kx = __ldg(a.pml_coef + R2 + iz), ky = __ldg(a.pml_coef + R1 + iz),
+                     kz = __ldg(a.pml_coef + R4 + hz);
+        ex = kx.x * ex + kx.y * cx;
+        ey = ky.x * ey + ky.y * cy;
+        ez = kz.x * ez + kz.y * cz;
+    } else {
+        e_cell(a, ex, ey, ez, cx, cy, cz, c, x, y, z);
+    }
+}
+
+// Static schedule of the persistent pair kernel: work items are (z chunk, tile) pairs, chunk-major,
+// and CTA b takes items b, b + G, b + 2G, ... (G = gridDim.x). CTAs resident at the same time then
+// work on neighbouring tiles of the same chunk, so the tile halos they share are L2 hits.
+struct PairSched {
+    int tiles_x;  // 64-cell tiles along x
+    int tiles;    // tiles per z chunk
+    int items;    // tiles * z chunks
+    int zc;       // planes per z chunk
+};
+
+struct PairItem {
+    int x0, y0, zs, ze, zstart;
+};
+
+template <int TY>
+__device__ __forceinline__ PairItem pair_item(const PairSched& ps, int nz, int item) {
+    const int c = item / ps.tiles, t = item - c * ps.tiles;
+    PairItem it;
+    it.x0 = (t % ps.tiles_x) * 64;
+    it.y0 = (t / ps.tiles_x) * TY;
+    it.zs = c * ps.zc;
+    it.ze = min(nz, it.zs + ps.zc);
+    it.zstart = it.zs > 0 ? it.zs - 1 : 0;  // a chunk above z = 0 first rebuilds B^{n+1/2}(zs-1)
+    return it;
+}
+
+// The CTA's loads form one sequence over its items: for each item, planes zstart .. ze (plane ze
+// is read as the "z+1" neighbour of the last plane; ze = nz reads TMA zeros). Load j goes to ring
+// stage j % STAGES and completes phase (j / STAGES) & 1 of that stage's mbarrier. The ring runs
+// on across item boundaries, so the pipeline never drains inside a launch.
+// Two 288-thread CTAs per SM: registers are allocated per SM quadrant, and 18 warps put 5 warps on
+// one quadrant, so 96 registers per thread at most.
+template <int TY, typename Idx>
+__global__ void __launch_bounds__(32 * (TY + 1), 2)
+    yee_tma2(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUtensorMap tey,
+             const __grid_constant__ CUtensorMap tez, const __grid_constant__ CUtensorMap tbx,
+             const __grid_constant__ CUtensorMap tby, const __grid_constant__ CUtensorMap tbz,
+             const __grid_constant__ CUtensorMap tcls, YeeArgs a, PairSched ps, unsigned* err) {
+    static_assert(TY == 8, "register budget assumes 9 warps per CTA");
+    using Lay = Layout2<TY, Idx>;
+    constexpr int S_ = Lay::STAGES;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Lay::BAR_OFF);
+    float* sB = reinterpret_cast<float*>(smem + Lay::SB_OFF);
+
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const bool ctl = warp == TY;
+    const bool leader = ctl && lane == 0;
+    const int G = gridDim.x;
+    if ((int)blockIdx.x >= ps.items) return;
+
+    // ---- producer (leader thread): cursor over the load sequence ----
+    int p_item = blockIdx.x, p_x0 = 0, p_y0 = 0, p_z = 0, p_zend = 0;
+    int issued = 0, waited = -1;
+    auto p_seek = [&]() {
+        if (p_item < ps.items) {
+            const PairItem it = pair_item<TY>(ps, a.nz, p_item);
+            p_x0 = it.x0, p_y0 = it.y0, p_z = it.zstart, p_zend = it.ze;
+        }
+    };
+    auto issue_upto = [&](int last) {  // issue loads up to index `last` while the sequence lasts
+        while (issued <= last && p_item < ps.items) {
+            unsigned char* st = smem + (issued % S_) * Lay::STAGE;
+            uint64_t* bar = bars + issued % S_;
+            mbar_expect_tx(bar, Lay::TX_BYTES);
+            tma_load_3d(st + Lay::E_OFF + 0 * Lay::EP, &tex, p_x0 - 4, p_y0 - 1, p_z, bar);
+            tma_load_3d(st + Lay::E_OFF + 1 * Lay::EP, &tey, p_x0 - 4, p_y0 - 1, p_z, bar);
+            tma_load_3d(st + Lay::E_OFF + 2 * Lay::EP, &tez, p_x0 - 4, p_y0 - 1, p_z, bar);
+            tma_load_3d(st + Lay::B_OFF + 0 * Lay::BP, &tbx, p_x0 - 4, p_y0 - 1, p_z, bar);
+            tma_load_3d(st + Lay::B_OFF + 1 * Lay::BP, &tby, p_x0 - 4, p_y0 - 1, p_z, bar);
+            tma_load_3d(st + Lay::B_OFF + 2 * Lay::BP, &tbz, p_x0 - 4, p_y0 - 1, p_z, bar);
+            tma_load_3d(st + Lay::C_OFF, &tcls, p_x0 - Lay::CX, p_y0 - 1, p_z, bar);
+            ++issued;
+            if (++p_z > p_zend) {
+                p_item += G;
+                p_seek();
+            }
+        }
+    };
+    auto wait_upto = [&](int last) {  // false if a load did not complete within the bound
+        bool ok = true;
+        while (ok && waited < last) {
+            ++waited;
+            ok = mbar_wait(bars + waited % S_, (waited / S_) & 1);
+        }
+        return ok;
+    };
+    // on an expired wait: record the error, give the copies still in flight a bounded time to land
+    auto bail = [&]() {
+        if (leader) {
+            atomicOr(err, 1u);
+            while (waited < issued - 1) {
+                ++waited;
+                mbar_wait(bars + waited % S_, (waited / S_) & 1);
+            }
+        }
+    };
+
+    if (leader) {
+        for (int s = 0; s < S_; ++s) mbar_init(bars + s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    bool failed = false;
+    if (leader) {
+        p_seek();
+        issue_upto(S_ - 1);
+        failed = !wait_upto(1);  // the first iteration reads loads 0 and 1
+    }
+    if (__syncthreads_or(failed)) {
+        bail();
+        return;
+    }
+
+    constexpr int EPF = Lay::EP / 4, BPF = Lay::BP / 4, SBW = Lay::SBW, SBC = (TY + 1) * SBW;
+    const int L = a.L, K = a.pml_K, PS = a.pml_stride;
+    const unsigned char* pcls = a.pml_cls;
+    const int r = ctl ? 0 : warp + 1;  // box row of the own / halo-row cells
+    const int me = r * Lay::EW + 2 * lane + 4, mb = r * Lay::BW + 2 * lane + 4, mc = r * Lay::CW + 2 * lane + Lay::CX;
+    const int ce = (lane + 1) * Lay::EW + 3, cbo = (lane + 1) * Lay::BW + 3, cc = (lane + 1) * Lay::CW + Lay::CX - 1;
+    const int so = r * SBW + 2 + 2 * lane;  // B tile slot of the pair
+    auto pml_rows = [&](int px, int py, int& R1, int& R2, int& R3, int& R4) {
+        const int ix = __ldg(pcls + px), iy = __ldg(pcls + PS + py), hx = __ldg(pcls + 3 * PS + px),
+                  hy = __ldg(pcls + 4 * PS + py);
+        R1 = (ix * K + hy) * K, R2 = (hx * K + iy) * K, R3 = (hx * K + hy) * K, R4 = (ix * K + iy) * K;
+    };
+    auto pml_xy_of = [&](int px, int py) { return px < L || py < L || px >= a.nx - (L + 1) || py >= a.ny - (L + 1); };
+
+    int k = 0;     // load index of the current iteration's plane z
+    int iter = 0;  // iteration counter: parity selects the B tile buffer
+    for (int item = blockIdx.x; item < ps.items; item += G) {
+        const PairItem itm = pair_item<TY>(ps, a.nz, item);
+        const int x0 = itm.x0, y0 = itm.y0, zs = itm.zs, ze = itm.ze;
+        const bool last_item = item + G >= ps.items;
+
+        // per-item invariants: own warps hold cells (xa, y), (xa+1, y); the halo warp holds the row
+        // cells (xa, y0-1), (xa+1, y0-1) and the column cell (x0-1, y0+lane)
+        const int xa = x0 + 2 * lane;
+        const int y = ctl ? y0 - 1 : y0 + warp;
+        const bool rowok = ctl ? y0 > 0 : y < a.ny;
+        const bool o0 = rowok && xa < a.nx, o1 = rowok && xa + 1 < a.nx;
+        const int cy = y0 + lane;
+        const bool col_live = ctl && lane < TY && x0 > 0 && cy < a.ny;
+        int A1 = 0, A2 = 0, A3 = 0, A4 = 0, B1 = 0, B2 = 0, B3 = 0, B4 = 0, C1 = 0, C2 = 0, C3 = 0, C4 = 0;
+        if (o0) pml_rows(xa, y, A1, A2, A3, A4);
+        if (o1) pml_rows(xa + 1, y, B1, B2, B3, B4);
+        if (col_live) pml_rows(x0 - 1, cy, C1, C2, C3, C4);
+        const bool pxy0 = o0 && pml_xy_of(xa, y), pxy1 = o1 && pml_xy_of(xa + 1, y);
+        const bool pxyc = col_live && pml_xy_of(x0 - 1, cy);
+        const long long row_off = (long long)y * a.pitch + xa;
+
+        float2 bp_x = make_float2(0.0f, 0.0f), bp_y = bp_x;  // B^{n+1/2}(z-1).x, .y of the pair
+        int iz = __ldg(pcls + 2 * PS + itm.zstart), hz = __ldg(pcls + 5 * PS + itm.zstart);
+        for (int z = itm.zstart; z < ze; ++z, ++k, ++iter) {
+            const unsigned char* st = smem + (k % S_) * Lay::STAGE;
+            const unsigned char* st1 = smem + ((k + 1) % S_) * Lay::STAGE;
+            const bool emit = z >= zs;
+            float* sb = sB + (iter & 1) * 3 * SBC;
+            const bool pz = z < L || z >= a.nz - (L + 1);
+            const int zn = min(z + 1, a.nz - 1);
+            const int iz_n = __ldg(pcls + 2 * PS + zn), hz_n = __ldg(pcls + 5 * PS + zn);
+            const float* Es = reinterpret_cast<const float*>(st + Lay::E_OFF);
+            const float* E1 = reinterpret_cast<const float*>(st1 + Lay::E_OFF);
+            const float* Bs = reinterpret_cast<const float*>(st + Lay::B_OFF);
+            const Idx* Cs = reinterpret_cast<const Idx*>(st + Lay::C_OFF);
+            const long long off = (long long)z * a.plane + row_off;
+            float2 e0x = make_float2(0.0f, 0.0f), e0y = e0x, e0z = e0x, bx = e0x, by = e0x, bz = e0x;
+            unsigned ca = 0, cb = 0;
+            if (!ctl) {
+                // update_B.comp:35-67 for both cells (halo values beyond the grid are TMA zeros)
+                e0x = *reinterpret_cast<const float2*>(Es + me);
+                e0y = *reinterpret_cast<const float2*>(Es + EPF + me);
+                e0z = *reinterpret_cast<const float2*>(Es + 2 * EPF + me);
+                bx = *reinterpret_cast<const float2*>(Bs + mb);
+                by = *reinterpret_cast<const float2*>(Bs + BPF + mb);
+                bz = *reinterpret_cast<const float2*>(Bs + 2 * BPF + mb);
+                load_class_pair<Idx>(Cs + mc, ca, cb);
+                const float e2y = Es[EPF + me + 2], e2z = Es[2 * EPF + me + 2];              // E(xa+2)
+                const float2 eyx = *reinterpret_cast<const float2*>(Es + me + Lay::EW);       // E(y+1)
+                const float2 eyz = *reinterpret_cast<const float2*>(Es + 2 * EPF + me + Lay::EW);
+                const float2 ezx = *reinterpret_cast<const float2*>(E1 + me);                // E(z+1)
+                const float2 ezy = *reinterpret_cast<const float2*>(E1 + EPF + me);
+                b_update(a, bx.x, by.x, bz.x, eyz.x - e0z.x, ezx.x - e0x.x, e0y.y - e0y.x, ezy.x - e0y.x,
+                         e0z.y - e0z.x, eyx.x - e0x.x, ca, pxy0 || pz, A1, A2, A3, iz, hz);
+                b_update(a, bx.y, by.y, bz.y, eyz.y - e0z.y, ezx.y - e0x.y, e2y - e0y.y, ezy.y - e0y.y, e2z - e0z.y,
+                         eyx.y - e0x.y, cb, pxy1 || pz, B1, B2, B3, iz, hz);
+                *reinterpret_cast<float2*>(sb + so) = bx;
+                *reinterpret_cast<float2*>(sb + SBC + so) = by;
+                *reinterpret_cast<float2*>(sb + 2 * SBC + so) = bz;
+                if (emit) {
+                    if (o1) {
+                        *reinterpret_cast<float2*>(a.nbx + off) = bx;
+                        *reinterpret_cast<float2*>(a.nby + off) = by;
+                        *reinterpret_cast<float2*>(a.nbz + off) = bz;
+                    } else if (o0) {
+                        a.nbx[off] = bx.x, a.nby[off] = by.x, a.nbz[off] = bz.x;
+                    }
+                }
+            } else if (emit) {
+                // -y row: Bx, Bz of (xa, y0-1) and (xa+1, y0-1); B below the lower faces is 0
+                float2 hx2 = make_float2(0.0f, 0.0f), hz2 = hx2;
+                if (o0) {
+                    const float2 f0x = *reinterpret_cast<const float2*>(Es + me);
+                    const float2 f0y = *reinterpret_cast<const float2*>(Es + EPF + me);
+                    const float2 f0z = *reinterpret_cast<const float2*>(Es + 2 * EPF + me);
+                    const float e2y = Es[EPF + me + 2];
+                    const float2 eyx = *reinterpret_cast<const float2*>(Es + me + Lay::EW);
+                    const float2 eyz = *reinterpret_cast<const float2*>(Es + 2 * EPF + me + Lay::EW);
+                    const float2 ezy = *reinterpret_cast<const float2*>(E1 + EPF + me);
+                    unsigned ha, hb;
+                    load_class_pair<Idx>(Cs + mc, ha, hb);
+                    hx2 = *reinterpret_cast<const float2*>(Bs + mb);
+                    hz2 = *reinterpret_cast<const float2*>(Bs + 2 * BPF + mb);
+                    float unused0 = 0.0f, unused1 = 0.0f;
+                    b_update(a, hx2.x, unused0, hz2.x, eyz.x - f0z.x, 0.0f, f0y.y - f0y.x, ezy.x - f0y.x, 0.0f,
+                             eyx.x - f0x.x, ha, pxy0 || pz, A1, A2, A3, iz, hz);
+                    if (o1)
+                        b_update(a, hx2.y, unused1, hz2.y, eyz.y - f0z.y, 0.0f, e2y - f0y.y, ezy.y - f0y.y, 0.0f,
+                                 eyx.y - f0x.y, hb, pxy1 || pz, B1, B2, B3, iz, hz);
+                    else
+                        hx2.y = 0.0f, hz2.y = 0.0f;
+                }
+                *reinterpret_cast<float2*>(sb + 2 + 2 * lane) = hx2;
+                *reinterpret_cast<float2*>(sb + 2 * SBC + 2 + 2 * lane) = hz2;
+                // -x column: By, Bz of (x0-1, y0+lane)
+                if (lane < TY) {
+                    float hby = 0.0f, hbz = 0.0f, hbx = 0.0f;
+                    if (col_live) {
+                        const float f0x = Es[ce], f0y = Es[EPF + ce], f0z = Es[2 * EPF + ce];
+                        hby = Bs[BPF + cbo], hbz = Bs[2 * BPF + cbo];
+                        b_update(a, hbx, hby, hbz, 0.0f, E1[ce] - f0x, Es[EPF + ce + 1] - f0y, 0.0f,
+                                 Es[2 * EPF + ce + 1] - f0z, Es[ce + Lay::EW] - f0x, (unsigned)Cs[cc], pxyc || pz, C1,
+                                 C2, C3, iz, hz);
+                    }
+                    sb[SBC + (lane + 1) * SBW + 1] = hby;
+                    sb[2 * SBC + (lane + 1) * SBW + 1] = hbz;
+                }
+            }
+            // the next iteration reads loads k+1, k+2 (or k+2, k+3 at the start of the next item)
+            if (leader) {
+                const int need = z + 1 < ze ? k + 2 : (last_item ? -1 : k + 3);
+                if (need >= 0) failed = !wait_upto(need);
+            }
+            if (__syncthreads_or(failed)) {
+                bail();
+                return;
+            }
+            // every warp is past its reads of loads <= k: refill up to k + STAGES
+            if (leader) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_upto(k + S_);
+            }
+            if (emit && !ctl && o0) {
+                // update_E.comp:41-64 for both cells
+                const float bxm_y = sb[SBC + so - 1], bxm_z = sb[2 * SBC + so - 1];               // B(xa-1).y, .z
+                const float2 bym_x = *reinterpret_cast<const float2*>(sb + so - SBW);            // B(y-1).x
+                const float2 bym_z = *reinterpret_cast<const float2*>(sb + 2 * SBC + so - SBW);  // B(y-1).z
+                float2 ex = e0x, ey = e0y, ez = e0z;
+                e_update(a, ex.x, ey.x, ez.x, (bz.x - bym_z.x) - (by.x - bp_y.x), (bx.x - bp_x.x) - (bz.x - bxm_z),
+                         (by.x - bxm_y) - (bx.x - bym_x.x), ca, pxy0 || pz, A1, A2, A4, iz, hz, xa, y, z);
+                e_update(a, ex.y, ey.y, ez.y, (bz.y - bym_z.y) - (by.y - bp_y.y), (bx.y - bp_x.y) - (bz.y - bz.x),
+                         (by.y - by.x) - (bx.y - bym_x.y), cb, pxy1 || pz, B1, B2, B4, iz, hz, xa + 1, y, z);
+                if (o1) {
+                    *reinterpret_cast<float2*>(a.nex + off) = ex;
+                    *reinterpret_cast<float2*>(a.ney + off) = ey;
+                    *reinterpret_cast<float2*>(a.nez + off) = ez;
+                } else {
+                    a.nex[off] = ex.x, a.ney[off] = ey.x, a.nez[off] = ez.x;
+                }
+            }
+            bp_x = bx, bp_y = by;
+            iz = iz_n, hz = hz_n;
+        }
+        ++k;  // the item's last load (plane ze) was only read as the z+1 neighbour
+    }
+}
+
 using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                               const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -348,6 +720,7 @@ bool encode(CUtensorMap* m, CUtensorMapDataType type, int elem, const void* base
 }
 
 int tile_rows(const YeeArgs& a) { return a.tile_rows == 16 ? 16 : 8; }
+bool pair_tiles(const YeeArgs& a) { return a.tile_rows == 64; }
 
 template <int TY, typename Idx>
 bool launch_t(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaStream_t s) {
@@ -365,6 +738,54 @@ bool launch_t(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaSt
     return true;
 }
 
+// Chooses the z chunk length of the persistent schedule: the CTA with the most items bounds the
+// launch, and every chunk above z = 0 re-reads one plane, so minimise ceil(items / G) * (zc + 1).
+PairSched pair_schedule(const YeeArgs& a, int TY, int G) {
+    PairSched ps;
+    ps.tiles_x = (a.nx + 63) / 64;
+    ps.tiles = ps.tiles_x * ((a.ny + TY - 1) / TY);
+    long long best = -1;
+    for (int chunks = 1; chunks <= std::max(1, a.nz / 4); ++chunks) {
+        const int zc = (a.nz + chunks - 1) / chunks;
+        const int n = (a.nz + zc - 1) / zc;
+        const long long items = (long long)n * ps.tiles;
+        const long long cost = (items + G - 1) / G * (zc + (n > 1 ? 1 : 0));
+        if (best < 0 || cost < best) best = cost, ps.zc = zc, ps.items = (int)items;
+    }
+    return ps;
+}
+
+template <int TY, typename Idx>
+bool launch_p(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaStream_t s) {
+    using Lay = Layout2<TY, Idx>;
+    static int resident = 0, sms = 0;  // per process: one device model
+    if (!resident) {
+        int dev = 0, smem_sm = 0;
+        // shared-memory carveout for exactly two CTAs: the rest of the SM's 256 KB stays L1, which
+        // caches the per-class and absorber tables
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+            smem_sm <= 0 ||
+            cudaFuncSetAttribute(yee_tma2<TY, Idx>, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(yee_tma2<TY, Idx>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 std::min(100, (200 * (Lay::SMEM + 1024) + smem_sm - 1) / smem_sm)) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, yee_tma2<TY, Idx>, 32 * (TY + 1), Lay::SMEM) !=
+                cudaSuccess ||
+            resident < 1) {
+            resident = 0;
+            return false;
+        }
+    }
+    const PairSched ps = pair_schedule(a, TY, resident * sms);
+    const int grid = std::min(ps.items, resident * sms);
+    yee_tma2<TY, Idx><<<grid, dim3(32, TY + 1), Lay::SMEM, s>>>(m->e[gen][0], m->e[gen][1], m->e[gen][2],
+                                                               m->b[gen][0], m->b[gen][1], m->b[gen][2], m->cls, a,
+                                                               ps, err);
+    return true;
+}
+
 }  // namespace
 
 TmaMaps* tma_maps_create() { return new TmaMaps(); }
@@ -372,16 +793,18 @@ void tma_maps_destroy(TmaMaps* m) { delete m; }
 
 bool tma_maps_encode(TmaMaps* m, int gen, const YeeArgs& a, bool wide) {
     const int ty = tile_rows(a);
+    const bool pair = pair_tiles(a);
+    const int ew = pair ? 72 : 40, bw = pair ? 68 : 36, cw16 = pair ? 72 : 40, cw32 = pair ? 68 : 36;
     bool ok = (a.pitch % 4) == 0;
     const float* e[3] = {a.ex, a.ey, a.ez};
     const float* b[3] = {a.bx, a.by, a.bz};
     for (int c = 0; c < 3 && ok; ++c) {
-        ok = encode(&m->e[gen][c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, e[c], a, 40, ty + 2) &&
-             encode(&m->b[gen][c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b[c], a, 36, ty + 1);
+        ok = encode(&m->e[gen][c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, e[c], a, ew, ty + 2) &&
+             encode(&m->b[gen][c], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, b[c], a, bw, ty + 1);
     }
     if (ok)
-        ok = wide ? encode(&m->cls, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, a.cls, a, 36, ty + 1)
-                  : encode(&m->cls, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, a.cls, a, 40, ty + 1);
+        ok = wide ? encode(&m->cls, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, a.cls, a, cw32, ty + 1)
+                  : encode(&m->cls, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, a.cls, a, cw16, ty + 1);
     m->ok[gen] = ok;
     m->cls_ok = ok;
     return ok;
@@ -389,6 +812,7 @@ bool tma_maps_encode(TmaMaps* m, int gen, const YeeArgs& a, bool wide) {
 
 bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsigned* err, cudaStream_t s) {
     if (!m || !m->ok[gen] || !m->cls_ok) return false;
+    if (pair_tiles(a)) return wide ? launch_p<8, uint32_t>(a, m, gen, err, s) : launch_p<8, uint16_t>(a, m, gen, err, s);
     if (tile_rows(a) == 16) return wide ? launch_t<16, uint32_t>(a, m, gen, err, s) : launch_t<16, uint16_t>(a, m, gen, err, s);
     return wide ? launch_t<8, uint32_t>(a, m, gen, err, s) : launch_t<8, uint16_t>(a, m, gen, err, s);
 }

@@ -71,6 +71,11 @@ def load_library() -> C.CDLL:
         "emlab_ntff_point_count": ([P, ip], I),
         "emlab_ntff_read_phasors": ([P, fp], I),
         "emlab_ntff_evaluate": ([P, fp, I, fp], I),
+        "emlab_ntff_dft_configure": ([P, ip, ip, fp, I, ip], I),
+        "emlab_ntff_dft_info": ([P, ip, C.POINTER(C.c_uint64)], I),
+        "emlab_ntff_dft_engine": ([P, I], I),
+        "emlab_ntff_dft_read": ([P, dp], I),
+        "emlab_ntff_dft_evaluate": ([P, I, fp, I, fp], I),
         "emlab_probe_gather": ([P, ip, I, fp], I),
         "emlab_flux_planes": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
@@ -339,6 +344,38 @@ class SimulationGrid:
         d[:, :3] = np.asarray(directions, np.float32)[:, :3]
         out = np.zeros((len(directions), 2), np.float32)
         _check(self._lib.emlab_ntff_evaluate(self._h, _fptr(d), len(d), _fptr(out)))
+        return out
+
+    def ntff_dft_configure(self, box_min, box_max, wavelengths):
+        mn = (C.c_int * 3)(*[int(v) for v in box_min])
+        mx = (C.c_int * 3)(*[int(v) for v in box_max])
+        out = (C.c_int * 6)()
+        wl = _f32(wavelengths)
+        _check(self._lib.emlab_ntff_dft_configure(self._h, mn, mx, _fptr(wl), len(wl), out))
+        self._dft_nf = len(wl)
+        return tuple(out[:3]), tuple(out[3:])
+
+    def ntff_dft_engine(self, engine: int):
+        """abi.DFT_TENSOR (tcgen05 split-precision TF32, the default) or abi.DFT_CUDA_CORES."""
+        _check(self._lib.emlab_ntff_dft_engine(self._h, int(engine)))
+
+    def ntff_dft_info(self):
+        p = C.c_int()
+        n = C.c_uint64()
+        _check(self._lib.emlab_ntff_dft_info(self._h, C.byref(p), C.byref(n)))
+        return p.value, int(n.value)
+
+    def ntff_dft_read(self) -> np.ndarray:
+        points, _ = self.ntff_dft_info()
+        out = np.zeros((self._dft_nf, points, 6, 2), np.float64)
+        _check(self._lib.emlab_ntff_dft_read(self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
+    def ntff_dft_evaluate(self, f, directions) -> np.ndarray:
+        d = np.zeros((len(directions), 4), np.float32)
+        d[:, :3] = np.asarray(directions, np.float32)[:, :3]
+        out = np.zeros((len(directions), 2), np.float32)
+        _check(self._lib.emlab_ntff_dft_evaluate(self._h, int(f), _fptr(d), len(d), _fptr(out)))
         return out
 
     def probe_gather(self, origins) -> np.ndarray:

@@ -158,8 +158,9 @@ int emlab_grid_write_components(emlab_grid* g, const float* ex, const float* ey,
                                 const float* by, const float* bz);
 /* Selects the solver kernel (EMLAB_KERNEL_FUSED or EMLAB_KERNEL_SPLIT); results are identical. */
 int emlab_grid_set_kernel(emlab_grid* g, int kernel);
-/* Tile height (rows of cells per CTA) of the fused kernels: 8, 16 or 0 for the automatic choice.
- * A tuning knob only: every choice gives bit-identical results. */
+/* Tile shape of the fused kernels: 8 or 16 (rows of 32 cells per CTA, one cell per thread), 64
+ * (64 x 8 tiles, two cells per thread; TMA kernel only) or 0 for the automatic choice. A tuning knob
+ * only: every choice gives bit-identical results. */
 int emlab_grid_set_tiling(emlab_grid* g, int tile_rows);
 /* The cudaStream_t the grid launches on (for events and for ordering caller work). */
 int emlab_grid_stream(emlab_grid* g, void** stream);
@@ -204,6 +205,29 @@ int emlab_ntff_read_phasors(emlab_grid* g, float* out);
 /* ntff_pattern.comp + ntff_reduce.comp (FarField.cpp:226-243, 359-376): for each direction
  * (4 floats, xyz used) out[2d] = |N_perp - r x L|^2 and out[1] = radiated power P. */
 int emlab_ntff_evaluate(emlab_grid* g, const float* directions, int n_dirs, float* out);
+
+/* Multi-frequency far-field DFT on a Huygens box (the reference's far-field monitor tracks one
+ * frequency with a two-stage running average, ntff_accumulate.comp; this one keeps exact DFT sums at
+ * up to 128 frequencies for pulsed runs). Every step samples the co-located E and H of each box node
+ * (ntff_common.glsl / field_sampling.glsl) into a 64-step time block; each full block is folded into
+ * FP64 sums X_f = sum_k F(t_k) e^{-i w_f t_k}, t_k = n_k dt for E and (n_k - 1/2) dt for H.
+ * Box clamped as FarFieldMonitor::configure; n_freq = 0 disables. box_out may be NULL. */
+int emlab_ntff_dft_configure(emlab_grid* g, const int box_min[3], const int box_max[3], const float* wavelengths,
+                             int n_freq, int box_out[6]);
+/* Engine of the block fold: EMLAB_DFT_TENSOR (default; tcgen05 TF32 MMAs with split hi/lo operands
+ * and FP32 accumulation in tensor memory, up to 128 frequencies) or EMLAB_DFT_CUDA_CORES (FP32
+ * FMA sums). Both apply the block phase in FP32 from FP64 cos/sin and accumulate in FP64. */
+#define EMLAB_DFT_TENSOR 0
+#define EMLAB_DFT_CUDA_CORES 1
+int emlab_ntff_dft_engine(emlab_grid* g, int engine);
+/* Box nodes and samples folded so far. */
+int emlab_ntff_dft_info(emlab_grid* g, int* points, uint64_t* samples);
+/* Folds any partial block and returns the sums: out[((f * points + i) * 6 + c) * 2 + {re, im}],
+ * c = Ex, Ey, Ez, Hx, Hy, Hz. */
+int emlab_ntff_dft_read(emlab_grid* g, double* out);
+/* ntff_pattern.comp + ntff_reduce.comp at frequency index f from the DFT sums scaled by 2/samples
+ * (the amplitude of a steady tone): out[2d] = |N_perp - r x L|^2, out[1] = radiated power. */
+int emlab_ntff_dft_evaluate(emlab_grid* g, int f, const float* directions, int n_dirs, float* out);
 
 /* ---- probes and flux: FieldAnalyzer (src/FieldAnalyzer.hpp:73-130) ----------------------- */
 /* probe_gather.comp (FieldAnalyzer.cpp:274-303): origins are 4 ints per probe (xyz used); out

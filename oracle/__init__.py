@@ -50,6 +50,9 @@ def _grid_spec(R):
         "oracle_lines_read": ([P, rp, rp], None),
         "oracle_probe_gather": ([P, ip, I, rp], None),
         "oracle_flux_planes": ([P, C.POINTER(abi.FluxPlane), I, dp], None),
+        "oracle_ntff_dft_configure": ([P, ip, ip, fp, I, ip], I),
+        "oracle_ntff_dft_points": ([P], I),
+        "oracle_ntff_dft_read": ([P, dp], None),
     }
 
 
@@ -67,7 +70,8 @@ def load_ref():
         raise FileNotFoundError(f"{_REF_PATH} is not built (python oracle/build_ref.py)")
     lib = C.CDLL(str(_REF_PATH))
     for name, (args, res) in _grid_spec(C.c_float).items():
-        if name == "oracle_ports_sweep_sums":
+        if name in ("oracle_ports_sweep_sums", "oracle_ntff_dft_configure", "oracle_ntff_dft_points",
+                    "oracle_ntff_dft_read"):
             continue
         fn = getattr(lib, f"{name}_ref")
         fn.argtypes, fn.restype = args, res
@@ -261,6 +265,23 @@ class Oracle:
         d[:, :3] = np.asarray(directions, np.float32)[:, :3]
         out = np.zeros((len(directions), 2), self.dtype)
         self._fn("oracle_ntff_evaluate")(self._h, d.ctypes.data_as(C.POINTER(C.c_float)), len(d), self._rp(out))
+        return out
+
+    def ntff_dft_configure(self, box_min, box_max, wavelengths, block_steps=64):
+        mn = (C.c_int * 3)(*[int(v) for v in box_min])
+        mx = (C.c_int * 3)(*[int(v) for v in box_max])
+        out = (C.c_int * 6)()
+        wl = np.ascontiguousarray(wavelengths, np.float32)
+        rc = self._fn("oracle_ntff_dft_configure")(self._h, mn, mx, wl.ctypes.data_as(C.POINTER(C.c_float)), len(wl), out)
+        if rc:
+            raise ValueError("far-field DFT box is degenerate")
+        self._dft_nf = len(wl)
+        return tuple(out[:3]), tuple(out[3:])
+
+    def ntff_dft_read(self):
+        n = int(self._fn("oracle_ntff_dft_points")(self._h))
+        out = np.zeros((self._dft_nf, n, 6, 2), np.float64)
+        self._fn("oracle_ntff_dft_read")(self._h, out.ctypes.data_as(C.POINTER(C.c_double)))
         return out
 
     def lines_configure(self, quantities, terms, weights, wavelength, averaging_periods=4.0):

@@ -53,6 +53,11 @@ typedef struct {
     float line_wavelength, line_avg;
     R* line_phasor;      /* 4 per quantity */
     R* line_now;
+    /* multi-frequency DFT of the Huygens-box fields (ntffPoint sampling, FP64 sums) */
+    int dft_on;
+    int dft_min[3], dft_max[3], dft_face[7], dft_points, dft_nf;
+    double* dft_w;       /* omega per frequency */
+    double* dft;         /* [f][point][6][2] */
 } NAME(grid);
 
 static inline R NAME(exp)(const NAME(grid) * g, R x) {
@@ -161,6 +166,7 @@ void NAME(oracle_destroy)(void* h) {
     NAME(free_buffers)(g);
     free(g->cells), free(g->lists), free(g->port_phasor), free(g->series), free(g->ntff);
     free(g->q), free(g->terms), free(g->weights), free(g->line_phasor), free(g->line_now);
+    free(g->dft_w), free(g->dft);
     free(g);
 }
 
@@ -383,6 +389,47 @@ static void NAME(ntff_point)(const NAME(grid) * g, int index, int node[3], R nor
     normal[a] = side == 1 ? (R)1 : (R)-1;
 }
 
+/* ntffPoint on an explicit box (same arithmetic as ntff_common.glsl:30-53) */
+static void NAME(box_point)(const int* mn, const int* mx, const int* face, int index, int node[3]) {
+    int f = 0;
+    for (int i = 1; i < 6; ++i)
+        if (index >= face[i]) f = i;
+    const int a = f >> 1, side = f & 1;
+    const int u = a == 0 ? 1 : 0, v = a == 2 ? 1 : 2;
+    const int nu = mx[u] - mn[u];
+    const int local = index - face[f];
+    const int iu = local % (nu + 1), iv = local / (nu + 1);
+    node[0] = mn[0], node[1] = mn[1], node[2] = mn[2];
+    node[a] = side == 1 ? mx[a] : mn[a];
+    node[u] = mn[u] + iu;
+    node[v] = mn[v] + iv;
+}
+
+/* multi-frequency running DFT: X_f += F(t) e^{-i w_f t}, t = n dt for E and (n - 1/2) dt for H,
+   with the fields co-located as field_sampling.glsl:17-32 does (FP32/FP64 samples, FP64 sums) */
+static void NAME(dft_accumulate)(NAME(grid) * g) {
+    const double dt = (double)g->cfg.courant;
+    const double tE = (double)g->step * dt, tH = tE - 0.5 * dt;
+    const int P = g->dft_points, nf = g->dft_nf;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < P; ++i) {
+        int node[3];
+        NAME(box_point)(g->dft_min, g->dft_max, g->dft_face, i, node);
+        R E[3], H[3];
+        NAME(e_at_node)(g, node[0], node[1], node[2], E);
+        NAME(b_at_node)(g, node[0], node[1], node[2], H);
+        for (int f = 0; f < nf; ++f) {
+            const double w = g->dft_w[f];
+            const double ce = cos(w * tE), se = sin(w * tE), ch = cos(w * tH), sh = sin(w * tH);
+            double* x = g->dft + ((size_t)f * P + (size_t)i) * 12;
+            for (int c = 0; c < 3; ++c) {
+                x[2 * c] += (double)E[c] * ce, x[2 * c + 1] -= (double)E[c] * se;
+                x[6 + 2 * c] += (double)H[c] * ch, x[6 + 2 * c + 1] -= (double)H[c] * sh;
+            }
+        }
+    }
+}
+
 /* FarFieldMonitor::accumulate (FarField.cpp:331-350) + ntff_accumulate.comp:30-52 */
 static void NAME(ntff_accumulate)(NAME(grid) * g) {
     const double w = 6.28318530717958647692 / (double)g->ntff_wavelength;
@@ -507,7 +554,48 @@ void NAME(oracle_step)(void* h, int count) {
         if (g->ntff_on) NAME(ntff_accumulate)(g);
         if (g->nports > 0) NAME(ports_accumulate)(g);
         if (g->nq > 0) NAME(lines_accumulate)(g);
+        if (g->dft_on) NAME(dft_accumulate)(g);
     }
+}
+
+/* the multi-frequency DFT monitor: box clamped like FarFieldMonitor::configure; nf = 0 disables */
+int NAME(oracle_ntff_dft_configure)(void* h, const int mn[3], const int mx[3], const float* wavelengths, int nf,
+                                    int box_out[6]) {
+    NAME(grid)* g = (NAME(grid)*)h;
+    free(g->dft_w), free(g->dft);
+    g->dft_w = NULL, g->dft = NULL, g->dft_on = 0;
+    if (nf <= 0) return EMLAB_OK;
+    const int n[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+    const int L = g->cfg.pml_thickness;
+    for (int a = 0; a < 3; ++a) {
+        const int lo = L + 1, hi = n[a] - L - 2;
+        int b0 = mn[a] < mx[a] ? mn[a] : mx[a], b1 = mn[a] < mx[a] ? mx[a] : mn[a];
+        b0 = b0 < lo ? lo : (b0 > hi ? hi : b0);
+        b1 = b1 < lo ? lo : (b1 > hi ? hi : b1);
+        if (b1 - b0 < 4) return EMLAB_ERR_INVALID;
+        g->dft_min[a] = b0, g->dft_max[a] = b1;
+        if (box_out) box_out[a] = b0, box_out[3 + a] = b1;
+    }
+    g->dft_face[0] = 0;
+    for (int f = 0; f < 6; ++f) {
+        const int a = f >> 1, u = a == 0 ? 1 : 0, v = a == 2 ? 1 : 2;
+        g->dft_face[f + 1] =
+            g->dft_face[f] + (g->dft_max[u] - g->dft_min[u] + 1) * (g->dft_max[v] - g->dft_min[v] + 1);
+    }
+    g->dft_points = g->dft_face[6];
+    g->dft_nf = nf;
+    g->dft_w = (double*)malloc((size_t)nf * sizeof(double));
+    for (int f = 0; f < nf; ++f) g->dft_w[f] = 6.28318530717958647692 / (double)(wavelengths[f] > 2.0f ? wavelengths[f] : 2.0f);
+    g->dft = (double*)calloc((size_t)nf * g->dft_points * 12, sizeof(double));
+    g->dft_on = 1;
+    return EMLAB_OK;
+}
+
+int NAME(oracle_ntff_dft_points)(void* h) { return ((NAME(grid)*)h)->dft_points; }
+
+void NAME(oracle_ntff_dft_read)(void* h, double* out) {
+    NAME(grid)* g = (NAME(grid)*)h;
+    memcpy(out, g->dft, (size_t)g->dft_nf * g->dft_points * 12 * sizeof(double));
 }
 
 /* ---------------------------------------------------------------------------------------- */

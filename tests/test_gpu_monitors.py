@@ -119,3 +119,60 @@ def test_plain_small_2000_steps():
         assert rel < 1e-4
     for k in ("probe", "flux", "ntff"):
         assert np.array_equal(out["gpu"][k], out["f32"][k]), k
+
+
+DFT_RTOL = 2e-6  # multi-frequency DFT sums, relative to the largest |sum| (FP32 in-block arithmetic)
+
+
+@pytest.mark.parametrize("engine", [abi.DFT_TENSOR, abi.DFT_CUDA_CORES])
+def test_multifrequency_dft_matches_fp64_oracle(engine):
+    """The time-blocked multi-frequency far-field DFT (FP32 samples; in-block sums on the tensor
+    cores with split TF32 operands, or FP32 FMA sums; block phase applied in FP32 from FP64 cos/sin;
+    FP64 accumulation) against the oracle's FP64 DFT with exact phases on the same FP32 samples; a
+    read in the middle folds a partial block and stepping continues."""
+    sc = configs.random_scene(size=(36, 32, 30), pml=4, seed=13)
+    wls = [9.0, 12.0, 16.0, 24.0, 40.0]
+    res = []
+    for t in (SimulationGrid(sc.grid), oracle.Oracle(sc.grid, "f32")):
+        oracle.load_scene(t, sc)
+        if isinstance(t, SimulationGrid):
+            t.ntff_dft_engine(engine)
+        box = t.ntff_dft_configure((6, 6, 6), (29, 25, 23), wls)
+        t.step(100)
+        mid = t.ntff_dft_read()
+        t.step(90)
+        res.append((box, mid, t.ntff_dft_read()))
+    (bg, mg_, xg), (bc, mc, xc) = res
+    assert bg == bc
+    for got, want in ((mg_, mc), (xg, xc)):
+        scale = np.abs(want).max()
+        assert scale > 0
+        err = np.max(np.abs(got - want)) / scale
+        print(f"engine {engine}: max |DFT - FP64 oracle| / max |DFT| = {err:.3e}")
+        assert err <= DFT_RTOL
+    g = SimulationGrid(sc.grid)
+    oracle.load_scene(g, sc)
+    g.ntff_dft_configure((6, 6, 6), (29, 25, 23), wls)
+    g.step(130)
+    pat = g.ntff_dft_evaluate(2, configs.fibonacci_directions(200))
+    assert np.all(np.isfinite(pat)) and pat[0, 1] != 0.0
+
+
+@pytest.mark.parametrize("nf", [1, 16, 48, 128])
+def test_dft_tensor_engine_equals_cuda_cores(nf):
+    """Tensor-core and CUDA-core folds of the same samples over several blocks and a partial one,
+    for MMA widths N = 32, 96 and 256: the two engines agree to the FP32 level of the in-block sums."""
+    sc = configs.random_scene(size=(44, 40, 38), pml=5, seed=17)
+    wls = list(np.linspace(6.0, 60.0, nf)) if nf > 1 else [16.0]
+    out = []
+    for engine in (abi.DFT_TENSOR, abi.DFT_CUDA_CORES):
+        g = SimulationGrid(sc.grid)
+        oracle.load_scene(g, sc)
+        g.ntff_dft_engine(engine)
+        g.ntff_dft_configure((7, 7, 7), (36, 32, 30), wls)
+        g.step(64 * 3 + 17)
+        out.append(g.ntff_dft_read())
+    a, b = out
+    scale = np.abs(b).max()
+    assert scale > 0 and np.all(np.isfinite(a))
+    assert np.max(np.abs(a - b)) <= DFT_RTOL * scale

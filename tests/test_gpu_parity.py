@@ -71,7 +71,8 @@ KERNELS = [abi.KERNEL_FUSED, abi.KERNEL_FUSED_LDG, abi.KERNEL_SPLIT]
 
 @pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("seed,size,pml,rows", [(1, (24, 20, 18), 4, 0), (2, (37, 29, 23), 5, 16),
-                                                (3, (64, 40, 33), 8, 8), (4, (40, 260, 16), 3, 16)])
+                                                (3, (64, 40, 33), 8, 8), (4, (40, 260, 16), 3, 16),
+                                                (5, (131, 45, 29), 6, 64), (6, (63, 17, 20), 4, 64)])
 def test_random_scene_bit_exact(kernel, seed, size, pml, rows):
     sc = configs.random_scene(size=size, pml=pml, seed=seed)
     steps = 80
@@ -84,12 +85,27 @@ def test_random_scene_bit_exact(kernel, seed, size, pml, rows):
 
 
 @pytest.mark.parametrize("kernel", [abi.KERNEL_FUSED, abi.KERNEL_FUSED_LDG])
-@pytest.mark.parametrize("rows", [8, 16])
+@pytest.mark.parametrize("rows", [8, 16, 64])
 def test_fused_equals_split_and_chunking(kernel, rows):
     sc = configs.random_scene(size=(70, 300, 26), pml=6, seed=11)
     a = run_gpu(sc, 30, kernel, chunks=3, rows=rows)
     b = run_gpu(sc, 30, abi.KERNEL_SPLIT, chunks=1)
     assert_bitwise(a, b, "fused vs split")
+
+
+@pytest.mark.parametrize("kernel,rows", [(abi.KERNEL_FUSED, 8), (abi.KERNEL_FUSED, 64), (abi.KERNEL_FUSED_LDG, 0),
+                                         (abi.KERNEL_SPLIT, 0)])
+def test_wide_class_index(kernel, rows):
+    """More than 65536 distinct edge materials switch the per-cell class index to 32 bits (a
+    distinct permittivity and conductivity in every cell)."""
+    sc = configs.random_scene(size=(75, 48, 40), pml=5, seed=21)
+    rng = np.random.default_rng(21)
+    shape = sc.materials.epsilon_r.shape
+    sc.materials.epsilon_r[...] = rng.uniform(1.0, 6.0, shape).astype(np.float32)
+    sc.materials.sigma[...] = rng.uniform(0.0, 0.02, shape).astype(np.float32)
+    assert len(np.unique(sc.materials.epsilon_r)) > 65536
+    got = run_gpu(sc, 40, kernel, rows=rows)
+    assert_bitwise(got, run_oracle(sc, 40), f"wide classes kernel {kernel} rows {rows}")
 
 
 @pytest.mark.parametrize("kernel", KERNELS)
