@@ -1,7 +1,8 @@
 """Benchmark of the FDTD time-stepping path: Yee cell-steps per second on the 512^3 plain-method
 workload (thin-wire dipole with a 50-ohm pulsed feed among 5% random dielectric blocks, 16-cell
-absorber, port series recorded every step), with the HBM roofline of the fused Yee kernel and the
-CPU restatement's throughput beside it.
+absorber, port series recorded every step, far-field DFT at 32 frequencies on a box 20 cells
+inside the absorber), with the HBM roofline of the fused Yee kernel and the CPU restatement's
+throughput beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--size 512]
 
@@ -117,6 +118,43 @@ def load_grid(grid, sc):
     grid.set_sources(sc.sources)
 
 
+DFT_FREQS = 32      # far-field spectrum: 32 frequencies over 0.3-1.7 x the design frequency
+SWEEP_POINTS = 128  # port Z / S11 sweep points
+DFT_MARGIN = 20     # Huygens box this many cells inside the absorber
+
+
+def dft_setup(grid, sc):
+    """Far-field DFT box 20 cells inside the absorber at 32 frequencies covering 0.3-1.7 f0."""
+    L = sc.grid.pml_thickness
+    lo = [L + DFT_MARGIN] * 3
+    hi = [n - L - DFT_MARGIN - 1 for n in sc.grid.size]
+    wl0 = sc.ports[0].wavelength
+    wls = [wl0 / f for f in np.linspace(0.3, 1.7, DFT_FREQS)]
+    grid.ntff_dft_configure(lo, hi, wls)
+    points, _ = grid.ntff_dft_info()
+    return wls, points
+
+
+def kernel_name(kernel: str, tiling: int) -> str:
+    if kernel == "fused":
+        return "yee_tma2" if tiling in (0, 64) else "yee_tma"
+    return {"fused_ldg": "yee_fused", "split": "yee_split_b+yee_split_e"}[kernel]
+
+
+def read_traffic(key: str):
+    """DRAM bytes per launch of the stencil kernel from an ncu capture, kept in profiles/traffic.txt
+    as lines `<kernel>_<size> <bytes per launch>`."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = line.split("#")[0].split()
+            if len(parts) == 2 and parts[0] == key:
+                return float(parts[1])
+    return None
+
+
 def cpu_sample(sc, seconds_budget: float = 20.0, max_steps: int = 8):
     """The FP32 CPU restatement on every host thread, over the full grid, for a few steps."""
     import oracle
@@ -228,6 +266,7 @@ def main():
     ports = [p.to_c() for p in sc.ports]
     wl = sc.ports[0].wavelength
     grid.ports_configure(ports, wl, 4.0, sweep=True)
+    dft_wls, dft_points = dft_setup(grid, sc)
     stream = torch.cuda.ExternalStream(grid.stream_handle())
 
     def barrier():
@@ -273,6 +312,9 @@ def main():
         for idx in (b0, b1):
             planes.append(abi.FluxPlane(ax, idx, (b0, b0), (b1 + 1, b1 + 1)))
     grid.ports_configure(ports, wl, 4.0, sweep=True)
+    dft_setup(grid, sc)
+    from em_lab_gb300 import configs
+    dirs = configs.fibonacci_directions(1024)
     barrier()
     t0 = time.perf_counter()
     frames = 0
@@ -282,11 +324,14 @@ def main():
         grid.flux_planes(planes)
         frames += 1
     series = grid.ports_series()
+    sweep, _ = grid.ports_sweep_sums(wl / 1.7, wl / 0.3, SWEEP_POINTS)
+    pattern = grid.ntff_dft_evaluate(DFT_FREQS // 2, dirs)
     barrier()
     e2e_value, e2e_s = replica_throughput(cells * frames * frame, time.perf_counter() - t0, dist, "cuda")
     nsrc = len(sc.sources)
     h2d = 4 * nsrc + 16 + 16 * (2 if sc.far_field else 1)  # signals + rotations per step (+ blends per call)
-    d2h = (len(probe) * 54 * 16 + 6 * 4 * ((b1 - b0 + 16) // 16) ** 2) / frame + 8 * len(ports)
+    d2h = ((len(probe) * 54 * 16 + 6 * 4 * ((b1 - b0 + 16) // 16) ** 2) / frame + 8 * len(ports)
+           + (sweep.nbytes + pattern.nbytes) / (frames * frame))
     finite = grid.check_finite()
 
     cpu = None
@@ -298,27 +343,25 @@ def main():
                    "sample": f"failed: {e}"}
 
     if rank == 0:
-        traffic = None
-        prof = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(prof):
-            try:
-                with open(prof) as f:
-                    tj = json.load(f)
-                traffic = tj.get(f"{args.kernel}_{args.size}")
-            except Exception:
-                traffic = None
+        kname = kernel_name(args.kernel, args.tile_rows)
+        traffic = read_traffic(f"{kname}_{args.size}")
         line = {
             "metric": METRIC, "value": value, "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"plain_large {args.size}^3, 16-cell absorber, thin-wire half-wave dipole with a "
                                    f"50-ohm Gaussian-pulse feed, 5% seeded random dielectric blocks, port series "
-                                   f"recorded every step", "cells": int(cells), "kernel": args.kernel,
+                                   f"recorded every step, far-field DFT at {DFT_FREQS} frequencies on a box "
+                                   f"{DFT_MARGIN} cells inside the absorber ({dft_points} nodes, tensor-core fold "
+                                   f"every 64 steps)", "cells": int(cells), "kernel": args.kernel,
+                       "tiling": args.tile_rows or "auto (64x8 pair tiles)",
                        "l2": "inputs larger than L2 (6.4 GB of field state per step)",
+                       "e2e_extra": f"probe + 6-plane flux box read every 2 steps; {SWEEP_POINTS}-point port sweep "
+                                    f"and a 1024-direction far-field pattern at the end",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": f"yee_{args.kernel}", "kernel_ms_per_launch": per_launch_ms,
+                         "kernel": kname, "kernel_ms_per_launch": per_launch_ms,
                          "algorithmic_bytes_per_cell_step": BYTES_PER_CELL_STEP},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcells/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -153,13 +153,19 @@ __global__ void __launch_bounds__(128) dft_fold_tc_kernel(const float* blk, int 
     const uint32_t tmem = *tslot;
     const uint32_t idesc = tf32_idesc(kRows, n_mma);
 
+    // the samples of the next tile are loaded while the current tile's MMAs and epilogue run
+    float v[kK];
+    auto load_rows = [&](long long tile) {
+        const long long row = tile * kRows + tid;
+        const bool live = tile < tiles && row < rows;
+#pragma unroll
+        for (int k = 0; k < kK; ++k) v[k] = (live && k < T) ? __ldg(blk + (size_t)k * rows + row) : 0.0f;
+    };
+    load_rows(blockIdx.x);
     uint32_t phase = 0;
     for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const long long row = tile * kRows + tid;
         const bool live = row < rows;
-        float v[kK];
-#pragma unroll
-        for (int k = 0; k < kK; ++k) v[k] = (live && k < T) ? __ldg(blk + (size_t)k * rows + row) : 0.0f;
         // K-major core-matrix layout: (row / 8) * 2048 B + (k / 4) * 128 B + (row % 8) * 16 B
         const int base = (tid >> 3) * 512 + (tid & 7) * 4;
 #pragma unroll
@@ -190,6 +196,7 @@ __global__ void __launch_bounds__(128) dft_fold_tc_kernel(const float* blk, int 
                              smem_addr(bar))
                          : "memory");
         }
+        load_rows(tile + gridDim.x);
         const bool ok = mbar_wait_bounded(bar, phase);
         phase ^= 1u;
         if (__syncthreads_or(!ok)) {
@@ -200,10 +207,17 @@ __global__ void __launch_bounds__(128) dft_fold_tc_kernel(const float* blk, int 
         int c = 0, i = 0;
         if (live) c = (int)(row / points), i = (int)(row - (long long)c * points);
         const int h = c >= 3 ? 1 : 0;
+        double2* xo = reinterpret_cast<double2*>(X) + (size_t)c * points + i;  // + f * 6 * points
+        const size_t fstride = (size_t)6 * points;
         for (int j = 0; j < n_mma / 32; ++j) {
             float d[32];
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(j * 32), d);
             if (!live) continue;
+            // all loads of the chunk before any store, so the 16 read-modify-writes overlap
+            double2 acc[16];
+#pragma unroll
+            for (int p = 0; p < 16; ++p)
+                if (j * 16 + p < nf) acc[p] = xo[(size_t)(j * 16 + p) * fstride];
 #pragma unroll
             for (int p = 0; p < 16; ++p) {
                 const int f = j * 16 + p;
@@ -211,10 +225,8 @@ __global__ void __launch_bounds__(128) dft_fold_tc_kernel(const float* blk, int 
                     const float2 r = rot[2 * f + h];
                     const float re = d[2 * p], im = d[2 * p + 1];
                     const float xr = re * r.x + im * r.y, xi = im * r.x - re * r.y;  // (re + i im)(cos - i sin)
-                    double2* o = reinterpret_cast<double2*>(X) + ((size_t)f * 6 + c) * points + i;
-                    double2 a = *o;
-                    a.x += (double)xr, a.y += (double)xi;
-                    *o = a;
+                    acc[p].x += (double)xr, acc[p].y += (double)xi;
+                    xo[(size_t)f * fstride] = acc[p];
                 }
             }
         }
@@ -258,21 +270,24 @@ bool launch_dft_fold_tc(const float* blk, int T, int points, int nf, const float
     const int n = dft_tc_mma_n(nf);
     if (n > 256) return false;
     const TcLayout lay = tc_layout(n, nf);
-    static int max_set = 0, sms = 0;
+    static int max_set = 0, sms = 0, smem_sm = 0;
     if (lay.smem > max_set) {
         int dev = 0;
         if (cudaFuncSetAttribute(dft_fold_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.smem) !=
                 cudaSuccess ||
             cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+            smem_sm <= 0)
             return false;
         max_set = lay.smem;
     }
-    int per_sm = 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dft_fold_tc_kernel, 128, lay.smem) != cudaSuccess ||
-        per_sm < 1)
-        per_sm = 1;
-    per_sm = std::min(per_sm, 512 / lay.ncols);  // tensor-memory columns per SM
+    // as many CTAs per SM as shared memory and tensor memory (512 columns) allow; the carveout asks
+    // for exactly that much shared memory
+    const int per_sm = std::max(1, std::min(smem_sm / (lay.smem + 1024), 512 / lay.ncols));
+    if (cudaFuncSetAttribute(dft_fold_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             std::min(100, (100 * per_sm * (lay.smem + 1024) + smem_sm - 1) / smem_sm)) != cudaSuccess)
+        return false;
     const long long tiles = (6ll * points + kRows - 1) / kRows;
     const int grid = (int)std::min<long long>(tiles, (long long)sms * per_sm);
     dft_fold_tc_kernel<<<grid, 128, lay.smem, s>>>(blk, T, points, nf, n, reinterpret_cast<const float4*>(b_hi),

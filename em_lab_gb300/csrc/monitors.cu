@@ -413,20 +413,30 @@ __global__ void __launch_bounds__(128) dft_fold_kernel(const float* blk, int T, 
     float v[kDftMaxT];
 #pragma unroll
     for (int k = 0; k < kDftMaxT; ++k) v[k] = k < T ? blk[(size_t)k * 6 * points + col] : 0.0f;
-    for (int f = 0; f < nf; ++f) {
-        float re = 0.0f, im = 0.0f;
+    double2* xo = reinterpret_cast<double2*>(X) + (size_t)c * points + i;  // + f * 6 * points
+    const size_t fstride = (size_t)6 * points;
+    constexpr int G = 4;  // frequencies per group: their X loads are issued before any store
+    for (int f0 = 0; f0 < nf; f0 += G) {
+        double2 acc[G];
 #pragma unroll
-        for (int k = 0; k < kDftMaxT; ++k) {
-            const float2 w = sW[f * kDftMaxT + k];
-            re = re + w.x * v[k];
-            im = im + w.y * v[k];
+        for (int g = 0; g < G; ++g)
+            if (f0 + g < nf) acc[g] = xo[(size_t)(f0 + g) * fstride];
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const int f = f0 + g;
+            if (f >= nf) break;
+            float re = 0.0f, im = 0.0f;
+#pragma unroll
+            for (int k = 0; k < kDftMaxT; ++k) {
+                const float2 w = sW[f * kDftMaxT + k];
+                re = re + w.x * v[k];
+                im = im + w.y * v[k];
+            }
+            const float2 r = rot[2 * f + h];
+            const float xr = re * r.x + im * r.y, xi = im * r.x - re * r.y;  // (re + i im)(cos - i sin)
+            acc[g].x += (double)xr, acc[g].y += (double)xi;
+            xo[(size_t)f * fstride] = acc[g];
         }
-        const float2 r = rot[2 * f + h];
-        const float xr = re * r.x + im * r.y, xi = im * r.x - re * r.y;  // (re + i im)(cos - i sin)
-        double2* o = reinterpret_cast<double2*>(X) + ((size_t)f * 6 + c) * points + i;
-        double2 a = *o;
-        a.x += (double)xr, a.y += (double)xi;
-        *o = a;
     }
 }
 

@@ -324,13 +324,12 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY <= 8 ? 3 : 1)
 template <int TY, typename Idx>
 struct Layout2 {
     static constexpr int STAGES = 4;
-    static constexpr int EW = 72;                         // E box: x0-4 .. x0+67, TY+2 rows
-    static constexpr int BW = 68;                         // B box: x0-4 .. x0+63, TY+1 rows
-    static constexpr int CW = sizeof(Idx) == 2 ? 72 : 68;  // class box width
-    static constexpr int CX = sizeof(Idx) == 2 ? 8 : 4;    // class box starts at x0 - CX
-    static constexpr int E_BYTES = EW * (TY + 2) * 4;
-    static constexpr int B_BYTES = BW * (TY + 1) * 4;
-    static constexpr int C_BYTES = CW * (TY + 1) * (int)sizeof(Idx);
+    static constexpr int W = 72;                        // box row width of E, B and the class index
+    static constexpr int CX = sizeof(Idx) == 2 ? 8 : 4;  // boxes start at x0 - 4 (16-bit class: x0 - 8)
+    static constexpr int DC = CX - 4;                   // class element offset from the E/B element
+    static constexpr int E_BYTES = W * (TY + 2) * 4;    // rows y0-1 .. y0+TY
+    static constexpr int B_BYTES = W * (TY + 1) * 4;    // rows y0-1 .. y0+TY-1
+    static constexpr int C_BYTES = W * (TY + 1) * (int)sizeof(Idx);
     static constexpr int EP = (E_BYTES + 127) / 128 * 128;
     static constexpr int BP = (B_BYTES + 127) / 128 * 128;
     static constexpr int CP = (C_BYTES + 127) / 128 * 128;
@@ -339,11 +338,13 @@ struct Layout2 {
     static constexpr int C_OFF = B_OFF + 3 * BP;
     static constexpr int STAGE = C_OFF + CP;
     static constexpr uint32_t TX_BYTES = 3 * E_BYTES + 3 * B_BYTES + C_BYTES;
-    static constexpr int SBW = 66;                        // B tile row: col 1 = x0-1, col 2+i = x0+i
+    // B tile row: element e of a box row maps to slot e - 2 (col 1 = x0-1, col 2+i = x0+i)
     static constexpr int SB_OFF = STAGES * STAGE;
-    static constexpr int SB_BYTES = 2 * 3 * (TY + 1) * SBW * 4;
+    static constexpr int SB_BYTES = 2 * 3 * (TY + 1) * W * 4;
     static constexpr int BAR_OFF = (SB_OFF + SB_BYTES + 127) / 128 * 128;
-    static constexpr int SMEM = BAR_OFF + 8 * STAGES;
+    static constexpr int PROD_OFF = BAR_OFF + 8 * STAGES;  // producer cursor (leader thread only)
+    static constexpr int COL_OFF = PROD_OFF + 8 * 4;        // column-halo absorber rows [TY][4]
+    static constexpr int SMEM = COL_OFF + TY * 16;
 };
 
 template <typename Idx>
@@ -454,6 +455,8 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Lay::BAR_OFF);
     float* sB = reinterpret_cast<float*>(smem + Lay::SB_OFF);
+    int* prod = reinterpret_cast<int*>(smem + Lay::PROD_OFF);  // item, x0, y0, z, zend, issued, waited
+    int4* colrow = reinterpret_cast<int4*>(smem + Lay::COL_OFF);
 
     const int lane = threadIdx.x, warp = threadIdx.y;
     const bool ctl = warp == TY;
@@ -461,56 +464,57 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
     const int G = gridDim.x;
     if ((int)blockIdx.x >= ps.items) return;
 
-    // ---- producer (leader thread): cursor over the load sequence ----
-    int p_item = blockIdx.x, p_x0 = 0, p_y0 = 0, p_z = 0, p_zend = 0;
-    int issued = 0, waited = -1;
+    // ---- producer (leader thread): cursor over the load sequence, kept in shared memory ----
     auto p_seek = [&]() {
-        if (p_item < ps.items) {
-            const PairItem it = pair_item<TY>(ps, a.nz, p_item);
-            p_x0 = it.x0, p_y0 = it.y0, p_z = it.zstart, p_zend = it.ze;
+        if (prod[0] < ps.items) {
+            const PairItem it = pair_item<TY>(ps, a.nz, prod[0]);
+            prod[1] = it.x0, prod[2] = it.y0, prod[3] = it.zstart, prod[4] = it.ze;
         }
     };
     auto issue_upto = [&](int last) {  // issue loads up to index `last` while the sequence lasts
-        while (issued <= last && p_item < ps.items) {
+        int issued = prod[5];
+        while (issued <= last && prod[0] < ps.items) {
             unsigned char* st = smem + (issued % S_) * Lay::STAGE;
             uint64_t* bar = bars + issued % S_;
+            const int px = prod[1] - 4, py = prod[2] - 1, pz = prod[3];
             mbar_expect_tx(bar, Lay::TX_BYTES);
-            tma_load_3d(st + Lay::E_OFF + 0 * Lay::EP, &tex, p_x0 - 4, p_y0 - 1, p_z, bar);
-            tma_load_3d(st + Lay::E_OFF + 1 * Lay::EP, &tey, p_x0 - 4, p_y0 - 1, p_z, bar);
-            tma_load_3d(st + Lay::E_OFF + 2 * Lay::EP, &tez, p_x0 - 4, p_y0 - 1, p_z, bar);
-            tma_load_3d(st + Lay::B_OFF + 0 * Lay::BP, &tbx, p_x0 - 4, p_y0 - 1, p_z, bar);
-            tma_load_3d(st + Lay::B_OFF + 1 * Lay::BP, &tby, p_x0 - 4, p_y0 - 1, p_z, bar);
-            tma_load_3d(st + Lay::B_OFF + 2 * Lay::BP, &tbz, p_x0 - 4, p_y0 - 1, p_z, bar);
-            tma_load_3d(st + Lay::C_OFF, &tcls, p_x0 - Lay::CX, p_y0 - 1, p_z, bar);
+            tma_load_3d(st + Lay::E_OFF + 0 * Lay::EP, &tex, px, py, pz, bar);
+            tma_load_3d(st + Lay::E_OFF + 1 * Lay::EP, &tey, px, py, pz, bar);
+            tma_load_3d(st + Lay::E_OFF + 2 * Lay::EP, &tez, px, py, pz, bar);
+            tma_load_3d(st + Lay::B_OFF + 0 * Lay::BP, &tbx, px, py, pz, bar);
+            tma_load_3d(st + Lay::B_OFF + 1 * Lay::BP, &tby, px, py, pz, bar);
+            tma_load_3d(st + Lay::B_OFF + 2 * Lay::BP, &tbz, px, py, pz, bar);
+            tma_load_3d(st + Lay::C_OFF, &tcls, px - Lay::DC, py, pz, bar);
             ++issued;
-            if (++p_z > p_zend) {
-                p_item += G;
+            if (++prod[3] > prod[4]) {
+                prod[0] += G;
                 p_seek();
             }
         }
+        prod[5] = issued;
     };
     auto wait_upto = [&](int last) {  // false if a load did not complete within the bound
+        int waited = prod[6];
         bool ok = true;
         while (ok && waited < last) {
             ++waited;
             ok = mbar_wait(bars + waited % S_, (waited / S_) & 1);
         }
+        prod[6] = waited;
         return ok;
     };
     // on an expired wait: record the error, give the copies still in flight a bounded time to land
     auto bail = [&]() {
         if (leader) {
             atomicOr(err, 1u);
-            while (waited < issued - 1) {
-                ++waited;
-                mbar_wait(bars + waited % S_, (waited / S_) & 1);
-            }
+            for (int w = prod[6] + 1; w < prod[5]; ++w) mbar_wait(bars + w % S_, (w / S_) & 1);
         }
     };
 
     if (leader) {
         for (int s = 0; s < S_; ++s) mbar_init(bars + s, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        prod[0] = blockIdx.x, prod[5] = 0, prod[6] = -1;
     }
     __syncthreads();
     bool failed = false;
@@ -524,13 +528,13 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
         return;
     }
 
-    constexpr int EPF = Lay::EP / 4, BPF = Lay::BP / 4, SBW = Lay::SBW, SBC = (TY + 1) * SBW;
+    constexpr int EPF = Lay::EP / 4, BPF = Lay::BP / 4, W = Lay::W, SBC = (TY + 1) * W;
     const int L = a.L, K = a.pml_K, PS = a.pml_stride;
     const unsigned char* pcls = a.pml_cls;
-    const int r = ctl ? 0 : warp + 1;  // box row of the own / halo-row cells
-    const int me = r * Lay::EW + 2 * lane + 4, mb = r * Lay::BW + 2 * lane + 4, mc = r * Lay::CW + 2 * lane + Lay::CX;
-    const int ce = (lane + 1) * Lay::EW + 3, cbo = (lane + 1) * Lay::BW + 3, cc = (lane + 1) * Lay::CW + Lay::CX - 1;
-    const int so = r * SBW + 2 + 2 * lane;  // B tile slot of the pair
+    // box element of the own / halo-row pair (E, B and 32-bit class boxes share it; the 16-bit class
+    // box is DC elements further) and of the column cell (x0-1, y0+lane); B tile slot = element - 2
+    const int me = (ctl ? 0 : warp + 1) * W + 2 * lane + 4;
+    const int ce = (lane + 1) * W + 3;
     auto pml_rows = [&](int px, int py, int& R1, int& R2, int& R3, int& R4) {
         const int ix = __ldg(pcls + px), iy = __ldg(pcls + PS + py), hx = __ldg(pcls + 3 * PS + px),
                   hy = __ldg(pcls + 4 * PS + py);
@@ -551,14 +555,20 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
         const int y = ctl ? y0 - 1 : y0 + warp;
         const bool rowok = ctl ? y0 > 0 : y < a.ny;
         const bool o0 = rowok && xa < a.nx, o1 = rowok && xa + 1 < a.nx;
-        const int cy = y0 + lane;
-        const bool col_live = ctl && lane < TY && x0 > 0 && cy < a.ny;
-        int A1 = 0, A2 = 0, A3 = 0, A4 = 0, B1 = 0, B2 = 0, B3 = 0, B4 = 0, C1 = 0, C2 = 0, C3 = 0, C4 = 0;
+        int A1 = 0, A2 = 0, A3 = 0, A4 = 0, B1 = 0, B2 = 0, B3 = 0, B4 = 0;
         if (o0) pml_rows(xa, y, A1, A2, A3, A4);
         if (o1) pml_rows(xa + 1, y, B1, B2, B3, B4);
-        if (col_live) pml_rows(x0 - 1, cy, C1, C2, C3, C4);
         const bool pxy0 = o0 && pml_xy_of(xa, y), pxy1 = o1 && pml_xy_of(xa + 1, y);
-        const bool pxyc = col_live && pml_xy_of(x0 - 1, cy);
+        if (ctl && lane < TY) {  // column cell: live flag | absorber flag, then its table rows
+            const int cy = y0 + lane;
+            int4 cr = make_int4(0, 0, 0, 0);
+            if (x0 > 0 && cy < a.ny) {
+                int r4;
+                pml_rows(x0 - 1, cy, cr.y, cr.z, cr.w, r4);
+                cr.x = 1 | (pml_xy_of(x0 - 1, cy) ? 2 : 0);
+            }
+            colrow[lane] = cr;  // read by the same thread only
+        }
         const long long row_off = (long long)y * a.pitch + xa;
 
         float2 bp_x = make_float2(0.0f, 0.0f), bp_y = bp_x;  // B^{n+1/2}(z-1).x, .y of the pair
@@ -567,14 +577,14 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
             const unsigned char* st = smem + (k % S_) * Lay::STAGE;
             const unsigned char* st1 = smem + ((k + 1) % S_) * Lay::STAGE;
             const bool emit = z >= zs;
-            float* sb = sB + (iter & 1) * 3 * SBC;
+            float* sb = sB + (iter & 1) * 3 * SBC - 2;  // indexed by box element
             const bool pz = z < L || z >= a.nz - (L + 1);
             const int zn = min(z + 1, a.nz - 1);
             const int iz_n = __ldg(pcls + 2 * PS + zn), hz_n = __ldg(pcls + 5 * PS + zn);
             const float* Es = reinterpret_cast<const float*>(st + Lay::E_OFF);
             const float* E1 = reinterpret_cast<const float*>(st1 + Lay::E_OFF);
             const float* Bs = reinterpret_cast<const float*>(st + Lay::B_OFF);
-            const Idx* Cs = reinterpret_cast<const Idx*>(st + Lay::C_OFF);
+            const Idx* Cs = reinterpret_cast<const Idx*>(st + Lay::C_OFF) + Lay::DC;
             const long long off = (long long)z * a.plane + row_off;
             float2 e0x = make_float2(0.0f, 0.0f), e0y = e0x, e0z = e0x, bx = e0x, by = e0x, bz = e0x;
             unsigned ca = 0, cb = 0;
@@ -583,22 +593,22 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
                 e0x = *reinterpret_cast<const float2*>(Es + me);
                 e0y = *reinterpret_cast<const float2*>(Es + EPF + me);
                 e0z = *reinterpret_cast<const float2*>(Es + 2 * EPF + me);
-                bx = *reinterpret_cast<const float2*>(Bs + mb);
-                by = *reinterpret_cast<const float2*>(Bs + BPF + mb);
-                bz = *reinterpret_cast<const float2*>(Bs + 2 * BPF + mb);
-                load_class_pair<Idx>(Cs + mc, ca, cb);
-                const float e2y = Es[EPF + me + 2], e2z = Es[2 * EPF + me + 2];              // E(xa+2)
-                const float2 eyx = *reinterpret_cast<const float2*>(Es + me + Lay::EW);       // E(y+1)
-                const float2 eyz = *reinterpret_cast<const float2*>(Es + 2 * EPF + me + Lay::EW);
-                const float2 ezx = *reinterpret_cast<const float2*>(E1 + me);                // E(z+1)
+                bx = *reinterpret_cast<const float2*>(Bs + me);
+                by = *reinterpret_cast<const float2*>(Bs + BPF + me);
+                bz = *reinterpret_cast<const float2*>(Bs + 2 * BPF + me);
+                load_class_pair<Idx>(Cs + me, ca, cb);
+                const float e2y = Es[EPF + me + 2], e2z = Es[2 * EPF + me + 2];          // E(xa+2)
+                const float2 eyx = *reinterpret_cast<const float2*>(Es + me + W);         // E(y+1)
+                const float2 eyz = *reinterpret_cast<const float2*>(Es + 2 * EPF + me + W);
+                const float2 ezx = *reinterpret_cast<const float2*>(E1 + me);            // E(z+1)
                 const float2 ezy = *reinterpret_cast<const float2*>(E1 + EPF + me);
                 b_update(a, bx.x, by.x, bz.x, eyz.x - e0z.x, ezx.x - e0x.x, e0y.y - e0y.x, ezy.x - e0y.x,
                          e0z.y - e0z.x, eyx.x - e0x.x, ca, pxy0 || pz, A1, A2, A3, iz, hz);
                 b_update(a, bx.y, by.y, bz.y, eyz.y - e0z.y, ezx.y - e0x.y, e2y - e0y.y, ezy.y - e0y.y, e2z - e0z.y,
                          eyx.y - e0x.y, cb, pxy1 || pz, B1, B2, B3, iz, hz);
-                *reinterpret_cast<float2*>(sb + so) = bx;
-                *reinterpret_cast<float2*>(sb + SBC + so) = by;
-                *reinterpret_cast<float2*>(sb + 2 * SBC + so) = bz;
+                *reinterpret_cast<float2*>(sb + me) = bx;
+                *reinterpret_cast<float2*>(sb + SBC + me) = by;
+                *reinterpret_cast<float2*>(sb + 2 * SBC + me) = bz;
                 if (emit) {
                     if (o1) {
                         *reinterpret_cast<float2*>(a.nbx + off) = bx;
@@ -616,13 +626,13 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
                     const float2 f0y = *reinterpret_cast<const float2*>(Es + EPF + me);
                     const float2 f0z = *reinterpret_cast<const float2*>(Es + 2 * EPF + me);
                     const float e2y = Es[EPF + me + 2];
-                    const float2 eyx = *reinterpret_cast<const float2*>(Es + me + Lay::EW);
-                    const float2 eyz = *reinterpret_cast<const float2*>(Es + 2 * EPF + me + Lay::EW);
+                    const float2 eyx = *reinterpret_cast<const float2*>(Es + me + W);
+                    const float2 eyz = *reinterpret_cast<const float2*>(Es + 2 * EPF + me + W);
                     const float2 ezy = *reinterpret_cast<const float2*>(E1 + EPF + me);
                     unsigned ha, hb;
-                    load_class_pair<Idx>(Cs + mc, ha, hb);
-                    hx2 = *reinterpret_cast<const float2*>(Bs + mb);
-                    hz2 = *reinterpret_cast<const float2*>(Bs + 2 * BPF + mb);
+                    load_class_pair<Idx>(Cs + me, ha, hb);
+                    hx2 = *reinterpret_cast<const float2*>(Bs + me);
+                    hz2 = *reinterpret_cast<const float2*>(Bs + 2 * BPF + me);
                     float unused0 = 0.0f, unused1 = 0.0f;
                     b_update(a, hx2.x, unused0, hz2.x, eyz.x - f0z.x, 0.0f, f0y.y - f0y.x, ezy.x - f0y.x, 0.0f,
                              eyx.x - f0x.x, ha, pxy0 || pz, A1, A2, A3, iz, hz);
@@ -632,20 +642,21 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
                     else
                         hx2.y = 0.0f, hz2.y = 0.0f;
                 }
-                *reinterpret_cast<float2*>(sb + 2 + 2 * lane) = hx2;
-                *reinterpret_cast<float2*>(sb + 2 * SBC + 2 + 2 * lane) = hz2;
+                *reinterpret_cast<float2*>(sb + me) = hx2;
+                *reinterpret_cast<float2*>(sb + 2 * SBC + me) = hz2;
                 // -x column: By, Bz of (x0-1, y0+lane)
                 if (lane < TY) {
                     float hby = 0.0f, hbz = 0.0f, hbx = 0.0f;
-                    if (col_live) {
+                    const int4 cr = colrow[lane];
+                    if (cr.x & 1) {
                         const float f0x = Es[ce], f0y = Es[EPF + ce], f0z = Es[2 * EPF + ce];
-                        hby = Bs[BPF + cbo], hbz = Bs[2 * BPF + cbo];
+                        hby = Bs[BPF + ce], hbz = Bs[2 * BPF + ce];
                         b_update(a, hbx, hby, hbz, 0.0f, E1[ce] - f0x, Es[EPF + ce + 1] - f0y, 0.0f,
-                                 Es[2 * EPF + ce + 1] - f0z, Es[ce + Lay::EW] - f0x, (unsigned)Cs[cc], pxyc || pz, C1,
-                                 C2, C3, iz, hz);
+                                 Es[2 * EPF + ce + 1] - f0z, Es[ce + W] - f0x, (unsigned)Cs[ce], (cr.x & 2) || pz,
+                                 cr.y, cr.z, cr.w, iz, hz);
                     }
-                    sb[SBC + (lane + 1) * SBW + 1] = hby;
-                    sb[2 * SBC + (lane + 1) * SBW + 1] = hbz;
+                    sb[SBC + ce] = hby;
+                    sb[2 * SBC + ce] = hbz;
                 }
             }
             // the next iteration reads loads k+1, k+2 (or k+2, k+3 at the start of the next item)
@@ -664,9 +675,9 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
             }
             if (emit && !ctl && o0) {
                 // update_E.comp:41-64 for both cells
-                const float bxm_y = sb[SBC + so - 1], bxm_z = sb[2 * SBC + so - 1];               // B(xa-1).y, .z
-                const float2 bym_x = *reinterpret_cast<const float2*>(sb + so - SBW);            // B(y-1).x
-                const float2 bym_z = *reinterpret_cast<const float2*>(sb + 2 * SBC + so - SBW);  // B(y-1).z
+                const float bxm_y = sb[SBC + me - 1], bxm_z = sb[2 * SBC + me - 1];             // B(xa-1).y, .z
+                const float2 bym_x = *reinterpret_cast<const float2*>(sb + me - W);            // B(y-1).x
+                const float2 bym_z = *reinterpret_cast<const float2*>(sb + 2 * SBC + me - W);  // B(y-1).z
                 float2 ex = e0x, ey = e0y, ez = e0z;
                 e_update(a, ex.x, ey.x, ez.x, (bz.x - bym_z.x) - (by.x - bp_y.x), (bx.x - bp_x.x) - (bz.x - bxm_z),
                          (by.x - bxm_y) - (bx.x - bym_x.x), ca, pxy0 || pz, A1, A2, A4, iz, hz, xa, y, z);
@@ -794,7 +805,7 @@ void tma_maps_destroy(TmaMaps* m) { delete m; }
 bool tma_maps_encode(TmaMaps* m, int gen, const YeeArgs& a, bool wide) {
     const int ty = tile_rows(a);
     const bool pair = pair_tiles(a);
-    const int ew = pair ? 72 : 40, bw = pair ? 68 : 36, cw16 = pair ? 72 : 40, cw32 = pair ? 68 : 36;
+    const int ew = pair ? 72 : 40, bw = pair ? 72 : 36, cw16 = pair ? 72 : 40, cw32 = pair ? 72 : 36;
     bool ok = (a.pitch % 4) == 0;
     const float* e[3] = {a.ex, a.ey, a.ez};
     const float* b[3] = {a.bx, a.by, a.bz};
