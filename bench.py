@@ -137,7 +137,7 @@ def dft_setup(grid, sc):
 
 def kernel_name(kernel: str, tiling: int) -> str:
     if kernel == "fused":
-        return "yee_tma2" if tiling in (0, 64) else "yee_tma"
+        return "yee_tma2" if tiling in (0, 64, 128) else "yee_tma"
     return {"fused_ldg": "yee_fused", "split": "yee_split_b+yee_split_e"}[kernel]
 
 
@@ -239,7 +239,7 @@ def main():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
-    ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 64])
+    ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 64, 128])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end leg (default: --steps)")
     args = ap.parse_args()

@@ -93,6 +93,8 @@ struct emlab_grid {
     int pml_K = 0;
     TmaMaps* tma = nullptr;
     DevBuf<unsigned> d_err;  // set by a solver kernel whose bounded on-device wait ran out
+    DevBuf<unsigned long long> d_work;  // ticket counter of the persistent Yee kernel (never reset)
+    unsigned long long work_base = 0;   // tickets consumed by the launches issued so far
     std::vector<float> cell_sigma, cell_eps;  // alpha channels of the textures (read-back only)
     // sources
     std::vector<emlab_source> desc;
@@ -180,8 +182,8 @@ YeeArgs yee_args(emlab_grid* g) {
     // tile height and z chunks: enough CTAs for ~4 per SM, but at least 8 planes each (the first
     // plane of a chunk is recomputed)
     const int mode = g->tile_rows == 0 ? 64 : g->tile_rows;  // automatic: 64 x 8 pair tiles
-    const int ty = mode == 16 ? 16 : 8;
-    const int tx = mode == 64 && g->kernel == EMLAB_KERNEL_FUSED ? 64 : 32;
+    const int ty = mode == 16 || mode == 128 ? 16 : 8;
+    const int tx = (mode == 64 || mode == 128) && g->kernel == EMLAB_KERNEL_FUSED ? 64 : 32;
     a.tile_rows = g->kernel == EMLAB_KERNEL_FUSED ? mode : ty;
     const long long xy = (long long)((a.nx + tx - 1) / tx) * ((a.ny + ty - 1) / ty);
     const long long want = 152 * 4;
@@ -189,6 +191,8 @@ YeeArgs yee_args(emlab_grid* g) {
     int zc = (a.nz + chunks - 1) / chunks;
     zc = std::max(zc, std::min(8, a.nz));
     a.zchunk = zc;
+    a.work = g->d_work.p;
+    a.work_base = g->work_base;
     return a;
 }
 
@@ -359,7 +363,8 @@ int emlab_grid_create(emlab_grid** out) {
         cudaEventCreateWithFlags(&g->stage_done[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&g->stage_done[1], cudaEventDisableTiming) != cudaSuccess ||
         g->d_flag.alloc(1) != cudaSuccess || g->d_err.alloc(1) != cudaSuccess ||
-        cudaMemset(g->d_err.p, 0, 4) != cudaSuccess) {
+        cudaMemset(g->d_err.p, 0, 4) != cudaSuccess || g->d_work.alloc(1) != cudaSuccess ||
+        cudaMemset(g->d_work.p, 0, 8) != cudaSuccess) {
         delete g;
         return fail(EMLAB_ERR_CUDA, "stream or event creation failed");
     }
@@ -577,8 +582,10 @@ int emlab_grid_step(emlab_grid* g, int count) {
                 launch_yee_split(a, g->wide, g->stream);
                 g_launches += 2;
             } else {
+                unsigned long long tickets = 0;
                 const bool tma = g->kernel == EMLAB_KERNEL_FUSED &&
-                                 launch_yee_tma(a, g->tma, g->cur, g->wide, g->d_err.p, g->stream);
+                                 launch_yee_tma(a, g->tma, g->cur, g->wide, g->d_err.p, g->stream, &tickets);
+                g->work_base += tickets;
                 if (!tma) launch_yee_fused(a, g->wide, g->stream);
                 g_launches += 1;
                 g->cur ^= 1;
@@ -728,8 +735,9 @@ int emlab_grid_set_kernel(emlab_grid* g, int kernel) {
 
 int emlab_grid_set_tiling(emlab_grid* g, int tile_rows) {
     if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
-    EMLAB_REQUIRE(tile_rows == 0 || tile_rows == 8 || tile_rows == 16 || tile_rows == 64,
-                  "tiling must be 0 (automatic), 8 or 16 (32-cell rows), or 64 (64 x 8 tiles of cell pairs)");
+    EMLAB_REQUIRE(tile_rows == 0 || tile_rows == 8 || tile_rows == 16 || tile_rows == 64 || tile_rows == 128,
+                  "tiling must be 0 (automatic), 8 or 16 (32-cell rows), 64 or 128 (64 x 8 or 64 x 16 tiles of "
+                  "cell pairs)");
     g->tile_rows = tile_rows;
     if (g->configured) refresh_tma(g);  // the TMA boxes depend on the tile height
     return EMLAB_OK;

@@ -47,7 +47,9 @@ struct YeeArgs {
     int L;
     float dt;
     int zchunk;
-    int tile_rows;   // rows of cells per CTA tile of the fused kernels (8 or 16)
+    int tile_rows;   // tiling mode of the fused kernels (8, 16: single-cell tiles; 64, 128: pair tiles)
+    unsigned long long* work;      // work-item ticket counter of the persistent kernel (monotonic)
+    unsigned long long work_base;  // tickets consumed by all earlier launches on this counter
 };
 
 struct SourceArgs {
@@ -75,7 +77,9 @@ void tma_maps_destroy(TmaMaps* m);
 // Encodes the maps for generation `gen` (0 or 1); returns false if TMA cannot be used.
 bool tma_maps_encode(TmaMaps* m, int gen, const YeeArgs& a, bool wide);
 // Launches the TMA kernel reading generation `gen`; err receives a nonzero word if a wait timed out.
-bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsigned* err, cudaStream_t s);
+// *tickets receives the work-counter tickets the launch consumes (0 for the non-persistent kernels)
+bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsigned* err, cudaStream_t s,
+                    unsigned long long* tickets);
 void launch_yee_split(const YeeArgs& a, bool wide, cudaStream_t s);
 void launch_sources(const YeeArgs& a, const SourceArgs& sa, int k, bool wide, cudaStream_t s);
 

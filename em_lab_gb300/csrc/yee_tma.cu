@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY <= 8 ? 3 : 1)
 // bookkeeping and most address arithmetic are paid once per two cells. Same arithmetic per cell.
 template <int TY, typename Idx>
 struct Layout2 {
-    static constexpr int STAGES = 4;
+    static constexpr int STAGES = TY == 8 ? 4 : 5;
     static constexpr int W = 72;                        // box row width of E, B and the class index
     static constexpr int CX = sizeof(Idx) == 2 ? 8 : 4;  // boxes start at x0 - 4 (16-bit class: x0 - 8)
     static constexpr int DC = CX - 4;                   // class element offset from the E/B element
@@ -342,10 +342,29 @@ struct Layout2 {
     static constexpr int SB_OFF = STAGES * STAGE;
     static constexpr int SB_BYTES = 2 * 3 * (TY + 1) * W * 4;
     static constexpr int BAR_OFF = (SB_OFF + SB_BYTES + 127) / 128 * 128;
-    static constexpr int PROD_OFF = BAR_OFF + 8 * STAGES;  // producer cursor (leader thread only)
-    static constexpr int COL_OFF = PROD_OFF + 8 * 4;        // column-halo absorber rows [TY][4]
+    static constexpr int PROD_OFF = BAR_OFF + 8 * STAGES;           // producer cursor (leader only)
+    static constexpr int QUEUE_OFF = PROD_OFF + 8 * 4;               // item numbers [8], -1 = done
+    static constexpr int COL_OFF = (QUEUE_OFF + 8 * 4 + 15) / 16 * 16;  // column-halo rows, int4 [TY]
     static constexpr int SMEM = COL_OFF + TY * 16;
+    static_assert(COL_OFF % 16 == 0 && BAR_OFF % 8 == 0 && SB_OFF % 16 == 0, "shared-memory alignment");
+    static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
 };
+
+// The next field generation is not read again in the launch: its stores leave L2 first, so the
+// current generation's planes stay for the neighbouring tiles' halo reads. The policy is made at
+// each use (one instruction) rather than held in a register across the z march.
+__device__ __forceinline__ uint64_t evict_first_policy() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ void st_pair(float* p, float2 v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(policy)
+                 : "memory");
+}
+__device__ __forceinline__ void st_one(float* p, float v, uint64_t policy) {
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(policy) : "memory");
+}
 
 template <typename Idx>
 __device__ __forceinline__ void load_class_pair(const Idx* p, unsigned& a, unsigned& b);
@@ -411,14 +430,20 @@ __device__ __forceinline__ void e_update(const YeeArgs& a, float& ex, float& ey,
     }
 }
 
-// Static schedule of the persistent pair kernel: work items are (z chunk, tile) pairs, chunk-major,
-// and CTA b takes items b, b + G, b + 2G, ... (G = gridDim.x). CTAs resident at the same time then
-// work on neighbouring tiles of the same chunk, so the tile halos they share are L2 hits.
+// Dynamic schedule of the persistent pair kernel: work items are (z chunk, tile) pairs, chunk-major,
+// handed out in order by a ticket counter. Items in progress at any moment are a window of
+// consecutive tiles at nearly the same z, so the halos that neighbouring tiles share are L2 hits;
+// a static assignment lets slow CTAs (absorber columns) drift planes apart from their neighbours.
+// The counter is never reset: launch n consumes exactly items + G tickets (every CTA's last grab
+// fails), and the host passes the sum over earlier launches as `base`. After a launch that stopped
+// early the counter lags; tickets below the base are skipped.
 struct PairSched {
     int tiles_x;  // 64-cell tiles along x
     int tiles;    // tiles per z chunk
     int items;    // tiles * z chunks
     int zc;       // planes per z chunk
+    unsigned long long* work;
+    unsigned long long base;
 };
 
 struct PairItem {
@@ -440,40 +465,49 @@ __device__ __forceinline__ PairItem pair_item(const PairSched& ps, int nz, int i
 // The CTA's loads form one sequence over its items: for each item, planes zstart .. ze (plane ze
 // is read as the "z+1" neighbour of the last plane; ze = nz reads TMA zeros). Load j goes to ring
 // stage j % STAGES and completes phase (j / STAGES) & 1 of that stage's mbarrier. The ring runs
-// on across item boundaries, so the pipeline never drains inside a launch.
-// Two 288-thread CTAs per SM: registers are allocated per SM quadrant, and 18 warps put 5 warps on
-// one quadrant, so 96 registers per thread at most.
+// on across item boundaries, so the pipeline never drains inside a launch. The leader takes the
+// next item when its loads reach it and posts the item number in a small shared ring that the
+// other warps read at their item boundary (always at least one barrier later).
+// 64 x 8 tiles: two 288-thread CTAs per SM; 64 x 16 tiles: one 544-thread CTA. Registers are
+// allocated per SM quadrant and 17-18 warps put 5 warps on one quadrant: 96 registers at most.
 template <int TY, typename Idx>
-__global__ void __launch_bounds__(32 * (TY + 1), 2)
+__global__ void __launch_bounds__(32 * (TY + 1), TY == 8 ? 2 : 1)
     yee_tma2(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUtensorMap tey,
              const __grid_constant__ CUtensorMap tez, const __grid_constant__ CUtensorMap tbx,
              const __grid_constant__ CUtensorMap tby, const __grid_constant__ CUtensorMap tbz,
              const __grid_constant__ CUtensorMap tcls, YeeArgs a, PairSched ps, unsigned* err) {
-    static_assert(TY == 8, "register budget assumes 9 warps per CTA");
+    static_assert(TY == 8 || TY == 16, "register budget assumes 9 or 17 warps per CTA");
     using Lay = Layout2<TY, Idx>;
     constexpr int S_ = Lay::STAGES;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem + Lay::BAR_OFF);
     float* sB = reinterpret_cast<float*>(smem + Lay::SB_OFF);
-    int* prod = reinterpret_cast<int*>(smem + Lay::PROD_OFF);  // item, x0, y0, z, zend, issued, waited
+    // producer cursor: item, x0, y0, z, zend, issued, waited, item ordinal
+    int* prod = reinterpret_cast<int*>(smem + Lay::PROD_OFF);
+    int* queue = reinterpret_cast<int*>(smem + Lay::QUEUE_OFF);  // item of ordinal n at [n & 7]
     int4* colrow = reinterpret_cast<int4*>(smem + Lay::COL_OFF);
 
     const int lane = threadIdx.x, warp = threadIdx.y;
     const bool ctl = warp == TY;
     const bool leader = ctl && lane == 0;
-    const int G = gridDim.x;
-    if ((int)blockIdx.x >= ps.items) return;
 
     // ---- producer (leader thread): cursor over the load sequence, kept in shared memory ----
+    auto grab = [&]() -> int {  // next work item, or -1 when all are taken
+        for (;;) {
+            const unsigned long long t = atomicAdd(ps.work, 1ull);
+            if (t < ps.base) continue;  // left over from a launch that stopped early
+            return t - ps.base < (unsigned long long)ps.items ? (int)(t - ps.base) : -1;
+        }
+    };
     auto p_seek = [&]() {
-        if (prod[0] < ps.items) {
+        if (prod[0] >= 0) {
             const PairItem it = pair_item<TY>(ps, a.nz, prod[0]);
             prod[1] = it.x0, prod[2] = it.y0, prod[3] = it.zstart, prod[4] = it.ze;
         }
     };
     auto issue_upto = [&](int last) {  // issue loads up to index `last` while the sequence lasts
         int issued = prod[5];
-        while (issued <= last && prod[0] < ps.items) {
+        while (issued <= last && prod[0] >= 0) {
             unsigned char* st = smem + (issued % S_) * Lay::STAGE;
             uint64_t* bar = bars + issued % S_;
             const int px = prod[1] - 4, py = prod[2] - 1, pz = prod[3];
@@ -486,8 +520,9 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
             tma_load_3d(st + Lay::B_OFF + 2 * Lay::BP, &tbz, px, py, pz, bar);
             tma_load_3d(st + Lay::C_OFF, &tcls, px - Lay::DC, py, pz, bar);
             ++issued;
-            if (++prod[3] > prod[4]) {
-                prod[0] += G;
+            if (++prod[3] > prod[4]) {  // item complete: take the next one and post it
+                prod[0] = grab();
+                queue[++prod[7] & 7] = prod[0];
                 p_seek();
             }
         }
@@ -514,9 +549,11 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
     if (leader) {
         for (int s = 0; s < S_; ++s) mbar_init(bars + s, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        prod[0] = blockIdx.x, prod[5] = 0, prod[6] = -1;
+        prod[0] = grab(), prod[5] = 0, prod[6] = -1, prod[7] = 0;
+        queue[0] = prod[0];
     }
     __syncthreads();
+    if (queue[0] < 0) return;  // uniform: no work for this CTA
     bool failed = false;
     if (leader) {
         p_seek();
@@ -544,10 +581,9 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
 
     int k = 0;     // load index of the current iteration's plane z
     int iter = 0;  // iteration counter: parity selects the B tile buffer
-    for (int item = blockIdx.x; item < ps.items; item += G) {
+    for (int ord = 0, item = queue[0]; item >= 0; item = queue[++ord & 7]) {
         const PairItem itm = pair_item<TY>(ps, a.nz, item);
         const int x0 = itm.x0, y0 = itm.y0, zs = itm.zs, ze = itm.ze;
-        const bool last_item = item + G >= ps.items;
 
         // per-item invariants: own warps hold cells (xa, y), (xa+1, y); the halo warp holds the row
         // cells (xa, y0-1), (xa+1, y0-1) and the column cell (x0-1, y0+lane)
@@ -610,12 +646,15 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
                 *reinterpret_cast<float2*>(sb + SBC + me) = by;
                 *reinterpret_cast<float2*>(sb + 2 * SBC + me) = bz;
                 if (emit) {
+                    const uint64_t evict_first = evict_first_policy();
                     if (o1) {
-                        *reinterpret_cast<float2*>(a.nbx + off) = bx;
-                        *reinterpret_cast<float2*>(a.nby + off) = by;
-                        *reinterpret_cast<float2*>(a.nbz + off) = bz;
+                        st_pair(a.nbx + off, bx, evict_first);
+                        st_pair(a.nby + off, by, evict_first);
+                        st_pair(a.nbz + off, bz, evict_first);
                     } else if (o0) {
-                        a.nbx[off] = bx.x, a.nby[off] = by.x, a.nbz[off] = bz.x;
+                        st_one(a.nbx + off, bx.x, evict_first);
+                        st_one(a.nby + off, by.x, evict_first);
+                        st_one(a.nbz + off, bz.x, evict_first);
                     }
                 }
             } else if (emit) {
@@ -660,8 +699,8 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
                 }
             }
             // the next iteration reads loads k+1, k+2 (or k+2, k+3 at the start of the next item)
-            if (leader) {
-                const int need = z + 1 < ze ? k + 2 : (last_item ? -1 : k + 3);
+            if (leader) {  // at the last plane the next item was taken when its first load was issued
+                const int need = z + 1 < ze ? k + 2 : (queue[(ord + 1) & 7] < 0 ? -1 : k + 3);
                 if (need >= 0) failed = !wait_upto(need);
             }
             if (__syncthreads_or(failed)) {
@@ -683,12 +722,15 @@ __global__ void __launch_bounds__(32 * (TY + 1), 2)
                          (by.x - bxm_y) - (bx.x - bym_x.x), ca, pxy0 || pz, A1, A2, A4, iz, hz, xa, y, z);
                 e_update(a, ex.y, ey.y, ez.y, (bz.y - bym_z.y) - (by.y - bp_y.y), (bx.y - bp_x.y) - (bz.y - bz.x),
                          (by.y - by.x) - (bx.y - bym_x.y), cb, pxy1 || pz, B1, B2, B4, iz, hz, xa + 1, y, z);
+                const uint64_t evict_first = evict_first_policy();
                 if (o1) {
-                    *reinterpret_cast<float2*>(a.nex + off) = ex;
-                    *reinterpret_cast<float2*>(a.ney + off) = ey;
-                    *reinterpret_cast<float2*>(a.nez + off) = ez;
+                    st_pair(a.nex + off, ex, evict_first);
+                    st_pair(a.ney + off, ey, evict_first);
+                    st_pair(a.nez + off, ez, evict_first);
                 } else {
-                    a.nex[off] = ex.x, a.ney[off] = ey.x, a.nez[off] = ez.x;
+                    st_one(a.nex + off, ex.x, evict_first);
+                    st_one(a.ney + off, ey.x, evict_first);
+                    st_one(a.nez + off, ez.x, evict_first);
                 }
             }
             bp_x = bx, bp_y = by;
@@ -730,8 +772,10 @@ bool encode(CUtensorMap* m, CUtensorMapDataType type, int elem, const void* base
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-int tile_rows(const YeeArgs& a) { return a.tile_rows == 16 ? 16 : 8; }
-bool pair_tiles(const YeeArgs& a) { return a.tile_rows == 64; }
+// tiling modes: 8, 16 = 32 x TY tiles of single cells (yee_tma); 64, 128 = 64 x 8 and 64 x 16 tiles
+// of cell pairs (yee_tma2)
+int tile_rows(const YeeArgs& a) { return a.tile_rows == 16 || a.tile_rows == 128 ? 16 : 8; }
+bool pair_tiles(const YeeArgs& a) { return a.tile_rows == 64 || a.tile_rows == 128; }
 
 template <int TY, typename Idx>
 bool launch_t(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaStream_t s) {
@@ -767,13 +811,14 @@ PairSched pair_schedule(const YeeArgs& a, int TY, int G) {
 }
 
 template <int TY, typename Idx>
-bool launch_p(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaStream_t s) {
+bool launch_p(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaStream_t s,
+              unsigned long long* tickets) {
     using Lay = Layout2<TY, Idx>;
     static int resident = 0, sms = 0;  // per process: one device model
     if (!resident) {
         int dev = 0, smem_sm = 0;
-        // shared-memory carveout for exactly two CTAs: the rest of the SM's 256 KB stays L1, which
-        // caches the per-class and absorber tables
+        // shared-memory carveout for exactly the CTAs wanted per SM (two 64 x 8 or one 64 x 16): the
+        // rest of the SM's 256 KB stays L1, which caches the per-class and absorber tables
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
@@ -781,7 +826,8 @@ bool launch_p(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaSt
             cudaFuncSetAttribute(yee_tma2<TY, Idx>, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(yee_tma2<TY, Idx>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 std::min(100, (200 * (Lay::SMEM + 1024) + smem_sm - 1) / smem_sm)) != cudaSuccess ||
+                                 std::min(100, (100 * (TY == 8 ? 2 : 1) * (Lay::SMEM + 1024) + smem_sm - 1) /
+                                                   smem_sm)) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, yee_tma2<TY, Idx>, 32 * (TY + 1), Lay::SMEM) !=
                 cudaSuccess ||
             resident < 1) {
@@ -789,11 +835,13 @@ bool launch_p(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaSt
             return false;
         }
     }
-    const PairSched ps = pair_schedule(a, TY, resident * sms);
+    PairSched ps = pair_schedule(a, TY, resident * sms);
     const int grid = std::min(ps.items, resident * sms);
+    ps.work = a.work, ps.base = a.work_base;
     yee_tma2<TY, Idx><<<grid, dim3(32, TY + 1), Lay::SMEM, s>>>(m->e[gen][0], m->e[gen][1], m->e[gen][2],
                                                                m->b[gen][0], m->b[gen][1], m->b[gen][2], m->cls, a,
                                                                ps, err);
+    *tickets = (unsigned long long)ps.items + (unsigned long long)grid;
     return true;
 }
 
@@ -821,9 +869,16 @@ bool tma_maps_encode(TmaMaps* m, int gen, const YeeArgs& a, bool wide) {
     return ok;
 }
 
-bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsigned* err, cudaStream_t s) {
+bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsigned* err, cudaStream_t s,
+                    unsigned long long* tickets) {
+    *tickets = 0;
     if (!m || !m->ok[gen] || !m->cls_ok) return false;
-    if (pair_tiles(a)) return wide ? launch_p<8, uint32_t>(a, m, gen, err, s) : launch_p<8, uint16_t>(a, m, gen, err, s);
+    if (pair_tiles(a) && tile_rows(a) == 16)
+        return wide ? launch_p<16, uint32_t>(a, m, gen, err, s, tickets)
+                    : launch_p<16, uint16_t>(a, m, gen, err, s, tickets);
+    if (pair_tiles(a))
+        return wide ? launch_p<8, uint32_t>(a, m, gen, err, s, tickets)
+                    : launch_p<8, uint16_t>(a, m, gen, err, s, tickets);
     if (tile_rows(a) == 16) return wide ? launch_t<16, uint32_t>(a, m, gen, err, s) : launch_t<16, uint16_t>(a, m, gen, err, s);
     return wide ? launch_t<8, uint32_t>(a, m, gen, err, s) : launch_t<8, uint16_t>(a, m, gen, err, s);
 }
