@@ -107,9 +107,57 @@ def replica_throughput(cells_done: float, elapsed_s: float, dist=None, device=No
     return float(c.item()) / float(t.item()) / 1e6, float(t.item())
 
 
-def build_scene(size: int, steps: int):
+def build_scene(args):
     from em_lab_gb300 import configs
-    return configs.plain_large(steps=steps, size=size)
+    if args.workload == "plain_small":
+        return configs.plain_small(steps=args.steps)
+    return configs.plain_large(steps=args.steps, size=args.size)
+
+
+def workload_text(args, sc, dft_points=None):
+    n = "x".join(str(v) for v in sc.grid.size)
+    if args.workload == "plain_small":
+        return (f"plain_small {n}, 10-cell absorber, vacuum, glass sphere eps 2.25 r 10, z point dipole "
+                f"CW lambda 16 amplitude 7 with 3-period ramp, far-field monitor at one frequency "
+                f"(two-stage running average, every step)")
+    text = (f"plain_large {n}, 16-cell absorber, thin-wire half-wave dipole with a 50-ohm Gaussian-pulse "
+            f"feed, 5% seeded random dielectric blocks, port series recorded every step")
+    if dft_points is not None:
+        text += (f", far-field DFT at {DFT_FREQS} frequencies on a box {DFT_MARGIN} cells inside the absorber "
+                 f"({dft_points} nodes, tensor-core fold every 64 steps)")
+    return text
+
+
+def attach_monitors(grid, sc, args):
+    """Per-step monitors of the workload. Returns the DFT node count (None without the DFT)."""
+    if sc.ports:
+        grid.ports_configure([p.to_c() for p in sc.ports], sc.ports[0].wavelength, 4.0, sweep=True)
+    if args.workload == "plain_small":
+        ff = sc.far_field
+        grid.ntff_configure(ff["box_min"], ff["box_max"], ff["wavelength"], ff["averaging"])
+        return None
+    _, points = dft_setup(grid, sc)
+    return points
+
+
+def frame_reads(sc):
+    """The headless frame loop's reads: the probe neighbourhood and the six planes of the flux box."""
+    from em_lab_gb300 import abi
+    if sc.probes:
+        probe = [tuple(int(v) - 1 for v in sc.probes[0][1])]
+    else:
+        probe = [(int(sc.grid.nx * 0.25), sc.grid.ny // 2, sc.grid.nz // 2)]
+    if sc.fluxes:
+        _, bmin, bmax = sc.fluxes[0]
+    else:
+        c = [v // 2 for v in sc.grid.size]
+        bmin, bmax = [v - 12 for v in c], [v + 12 for v in c]
+    planes = []
+    for ax in range(3):
+        u, v = (1, 2) if ax == 0 else ((0, 2) if ax == 1 else (0, 1))
+        for idx in (bmin[ax], bmax[ax]):
+            planes.append(abi.FluxPlane(ax, idx, (bmin[u], bmin[v]), (bmax[u] + 1, bmax[v] + 1)))
+    return probe, planes, bmin, bmax
 
 
 def load_grid(grid, sc):
@@ -163,8 +211,8 @@ def cpu_sample(sc, seconds_budget: float = 20.0, max_steps: int = 8):
     o = oracle.Oracle(sc.grid, "f32")
     t0 = time.perf_counter()
     oracle.load_scene(o, sc)
-    ports = [p.to_c() for p in sc.ports]
-    o.ports_configure(ports, sc.ports[0].wavelength if sc.ports else 16.0, 4.0, sweep=True)
+    if sc.ports:
+        o.ports_configure([p.to_c() for p in sc.ports], sc.ports[0].wavelength, 4.0, sweep=True)
     setup = time.perf_counter() - t0
     cells = float(np.prod(sc.grid.size))
     o.step(1)  # warm-up (first touch of every page)
@@ -178,16 +226,18 @@ def cpu_sample(sc, seconds_budget: float = 20.0, max_steps: int = 8):
     el = time.perf_counter() - t0
     o.close()
     return {"value": cells * steps / el / 1e6, "unit": "Mcells/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} full-grid steps of the {sc.grid.nx}^3 workload after 1 warm-up step "
+            "sample": f"{steps} full-grid steps (B, E, sources{', port monitor' if sc.ports else ''}) of the "
+                      f"{'x'.join(str(v) for v in sc.grid.size)} workload after 1 warm-up step "
                       f"(oracle/emlab_oracle.c FP32, OpenMP {threads} threads, set-up {setup:.1f} s excluded)"}
 
 
 def run_reference(args):
-    """The reference's CPU implementation of the path on the host cores."""
+    """The reference's CPU implementation of the path on the host cores: its shaders compiled as C++
+    (oracle/_ref) where that library was built, else the FP32 restatement, on every host thread."""
     rank, world, _ = _rank_env()
     if rank != 0:
         return 0
-    sc = build_scene(args.size, args.steps)
+    sc = build_scene(args)
     kind = "port"
     try:
         from oracle import ref as refmod  # the reference's shaders compiled through the GLSL shim
@@ -206,8 +256,8 @@ def run_reference(args):
         oracle.set_threads(threads)
         runner = oracle.Oracle(sc.grid, "f32")
         oracle.load_scene(runner, sc)
-    ports = [p.to_c() for p in sc.ports]
-    runner.ports_configure(ports, sc.ports[0].wavelength, 4.0, sweep=True)
+    if sc.ports:
+        runner.ports_configure([p.to_c() for p in sc.ports], sc.ports[0].wavelength, 4.0, sweep=True)
     # each bench step is a bounded sample: one full-grid leapfrog step
     for _ in range(max(1, min(args.warmup, 1))):
         runner.step(1)
@@ -216,15 +266,15 @@ def run_reference(args):
         runner.step(1)
     el = time.perf_counter() - t0
     value = cells * args.steps / el / 1e6
-    sample = (f"{args.steps} full-grid leapfrog steps (B, E, sources, port monitor) of the {args.size}^3 workload, "
+    sample = (f"{args.steps} full-grid leapfrog steps (B, E, sources{', port monitor' if sc.ports else ''}) of the "
+              f"{'x'.join(str(v) for v in sc.grid.size)} workload, "
               f"{'reference shaders compiled as C++ (oracle/_ref)' if kind == 'reference' else 'CPU restatement oracle/emlab_oracle.c FP32'}, "
               f"{threads} host threads")
     line = {"metric": METRIC, "value": value, "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": f"plain_large {args.size}^3, 16-cell absorber, thin-wire dipole + 50-ohm pulsed "
-                                   f"feed, 5% random dielectric blocks (seed 12345)", "cells": int(cells)},
+            "config": {"workload": workload_text(args, sc), "cells": int(cells)},
             "cpu_baseline": {"value": value, "unit": "Mcells/s", "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -237,7 +287,9 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--workload", default="plain_large", choices=["plain_large", "plain_small"],
+                    help="plain_large: the 512^3 dipole + blocks workload (default); plain_small: 128^3 sphere")
+    ap.add_argument("--size", type=int, default=512, help="edge of the plain_large grid")
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
     ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 64, 128])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -257,16 +309,13 @@ def main():
 
     from em_lab_gb300 import SimulationGrid, abi, launch_count
 
-    sc = build_scene(args.size, args.steps)
+    sc = build_scene(args)
     cells = float(np.prod(sc.grid.size))
     grid = SimulationGrid(sc.grid)
     grid.set_kernel({"fused": abi.KERNEL_FUSED, "fused_ldg": abi.KERNEL_FUSED_LDG, "split": abi.KERNEL_SPLIT}[args.kernel])
     grid.set_tiling(args.tile_rows)
     load_grid(grid, sc)
-    ports = [p.to_c() for p in sc.ports]
-    wl = sc.ports[0].wavelength
-    grid.ports_configure(ports, wl, 4.0, sweep=True)
-    dft_wls, dft_points = dft_setup(grid, sc)
+    dft_points = attach_monitors(grid, sc, args)
     stream = torch.cuda.ExternalStream(grid.stream_handle())
 
     def barrier():
@@ -304,15 +353,8 @@ def main():
     # the end. Host<->device copies are inside the timed region.
     e2e_steps = args.e2e_steps or args.steps
     frame = 2
-    probe = [(int(sc.grid.nx * 0.25), sc.grid.ny // 2, sc.grid.nz // 2)]
-    n = sc.grid.nx
-    b0, b1 = n // 2 - 12, n // 2 + 12
-    planes = []
-    for ax in range(3):
-        for idx in (b0, b1):
-            planes.append(abi.FluxPlane(ax, idx, (b0, b0), (b1 + 1, b1 + 1)))
-    grid.ports_configure(ports, wl, 4.0, sweep=True)
-    dft_setup(grid, sc)
+    probe, planes, bmin, bmax = frame_reads(sc)
+    attach_monitors(grid, sc, args)  # fresh monitor state for the end-to-end leg
     from em_lab_gb300 import configs
     dirs = configs.fibonacci_directions(1024)
     barrier()
@@ -323,15 +365,26 @@ def main():
         grid.probe_gather(probe)
         grid.flux_planes(planes)
         frames += 1
-    series = grid.ports_series()
-    sweep, _ = grid.ports_sweep_sums(wl / 1.7, wl / 0.3, SWEEP_POINTS)
-    pattern = grid.ntff_dft_evaluate(DFT_FREQS // 2, dirs)
+    tail = []  # end-of-run reads: port series and sweep, far-field pattern
+    if sc.ports:
+        wl = sc.ports[0].wavelength
+        tail.append(grid.ports_series())
+        tail.append(grid.ports_sweep_sums(wl / 1.7, wl / 0.3, SWEEP_POINTS)[0])
+    if dft_points is not None:
+        tail.append(grid.ntff_dft_evaluate(DFT_FREQS // 2, dirs))
+    else:
+        tail.append(grid.ntff_evaluate(dirs))
     barrier()
     e2e_value, e2e_s = replica_throughput(cells * frames * frame, time.perf_counter() - t0, dist, "cuda")
-    nsrc = len(sc.sources)
-    h2d = 4 * nsrc + 16 + 16 * (2 if sc.far_field else 1)  # signals + rotations per step (+ blends per call)
-    d2h = ((len(probe) * 54 * 16 + 6 * 4 * ((b1 - b0 + 16) // 16) ** 2) / frame + 8 * len(ports)
-           + (sweep.nbytes + pattern.nbytes) / (frames * frame))
+    # per step: FP64-evaluated source signals (FP32) and the monitor rotations (cos/sin pairs)
+    h2d = 4 * len(sc.sources) + 16 * (1 if sc.ports else 0) + 16 * (1 if args.workload == "plain_small" else 0)
+    # per frame: the probe's 54 texels and the flux planes' 16 x 16 workgroup partials; per step: the
+    # port series; once: the sweep and the pattern
+    parts = 0
+    for ax in range(3):
+        u, v = (1, 2) if ax == 0 else ((0, 2) if ax == 1 else (0, 1))
+        parts += 2 * ((bmax[u] - bmin[u] + 16) // 16) * ((bmax[v] - bmin[v] + 16) // 16)
+    d2h = (len(probe) * 54 * 16 + 4 * parts) / frame + sum(t.nbytes for t in tail) / (frames * frame)
     finite = grid.check_finite()
 
     cpu = None
@@ -344,20 +397,19 @@ def main():
 
     if rank == 0:
         kname = kernel_name(args.kernel, args.tile_rows)
-        traffic = read_traffic(f"{kname}_{args.size}")
+        traffic = read_traffic(f"{kname}_{args.workload}_{'x'.join(str(v) for v in sc.grid.size)}")
+        state_gb = 48.0 * cells / 1e9
         line = {
             "metric": METRIC, "value": value, "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"plain_large {args.size}^3, 16-cell absorber, thin-wire half-wave dipole with a "
-                                   f"50-ohm Gaussian-pulse feed, 5% seeded random dielectric blocks, port series "
-                                   f"recorded every step, far-field DFT at {DFT_FREQS} frequencies on a box "
-                                   f"{DFT_MARGIN} cells inside the absorber ({dft_points} nodes, tensor-core fold "
-                                   f"every 64 steps)", "cells": int(cells), "kernel": args.kernel,
+            "config": {"workload": workload_text(args, sc, dft_points), "cells": int(cells), "kernel": args.kernel,
                        "tiling": args.tile_rows or "auto (64x8 pair tiles)",
-                       "l2": "inputs larger than L2 (6.4 GB of field state per step)",
-                       "e2e_extra": f"probe + 6-plane flux box read every 2 steps; {SWEEP_POINTS}-point port sweep "
-                                    f"and a 1024-direction far-field pattern at the end",
+                       "l2": (f"inputs larger than L2 ({state_gb:.1f} GB of field state per step)" if state_gb > 0.129
+                              else f"field state {state_gb * 1e3:.0f} MB fits in L2 (129 MB); no flush between steps"),
+                       "e2e_extra": "probe + 6-plane flux box read every 2 steps; " + (
+                           f"port series, {SWEEP_POINTS}-point port sweep and " if sc.ports else "") +
+                                    "a 1024-direction far-field pattern at the end",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_kind,
@@ -365,7 +417,7 @@ def main():
                          "algorithmic_bytes_per_cell_step": BYTES_PER_CELL_STEP},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "Mcells/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "frames": frames, "steps_per_frame": frame, "series_steps": int(series.shape[0])},
+                    "frames": frames, "steps_per_frame": frame},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "finite": bool(finite),

@@ -3,7 +3,7 @@
 // The FDTD update of the reference (shaders/common.glsl:23-27, 50-54; update_E.comp:58-61;
 // update_B.comp:63-64; apply_sources.comp:37-40) calls exp() for the graded-absorber profile,
 // the exponential-integrator coefficients and the source footprint. GLSL leaves exp()'s accuracy
-// to the driver, so there is no single "right" bit pattern to reproduce. This header fixes one:
+// to the GL implementation, so there is no single "right" bit pattern to reproduce. This header fixes one:
 // emlab_expf is written only with IEEE operations that round identically on every conforming
 // machine (multiply, add, fmaf, rintf, exponent-field construction), so the GPU kernels, the host
 // coefficient tables and the CPU restatement used by the tests all get the same bits from the

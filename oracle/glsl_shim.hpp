@@ -4,7 +4,7 @@
 // Vector types follow the GLSL spec: component-wise arithmetic in float, swizzles .xyz/.xy/.zw (the
 // build step rewrites them to calls: writable proxies on lvalues, values on rvalues), mix() as
 // x * (1 - a) + y * a, step(), exp()/sin()/cos() per component, textures as flat RGBA arrays.
-// exp() is emlab_expf (or libm expf when GLSL_SHIM_LIBM_EXP is set by the driver).
+// exp() is emlab_expf, or libm expf when ref_driver.cpp sets g_libm_exp (the tolerance variant).
 #pragma once
 
 #include <cmath>
@@ -196,7 +196,7 @@ inline bool all(const bvec3& b) { return b.x && b.y && b.z; }
 inline vec2 unpackHalf2x16(uint v) {
     return vec2(emlab_half_to_float((uint16_t)(v & 0xffffu)), emlab_half_to_float((uint16_t)(v >> 16)));
 }
-// Workgroup barrier: the driver runs a workgroup's invocations as fibers and installs the hook
+// Workgroup barrier: ref_driver.cpp runs a workgroup's invocations as fibers and installs the hook
 // that suspends the calling invocation until all of them have arrived.
 extern thread_local void (*g_barrier_hook)();
 inline void barrier() {
