@@ -148,7 +148,7 @@ def frame_reads(sc):
     else:
         probe = [(int(sc.grid.nx * 0.25), sc.grid.ny // 2, sc.grid.nz // 2)]
     if sc.fluxes:
-        _, bmin, bmax = sc.fluxes[0]
+        bmin, bmax = sc.fluxes[0].box_min, sc.fluxes[0].box_max
     else:
         c = [v // 2 for v in sc.grid.size]
         bmin, bmax = [v - 12 for v in c], [v + 12 for v in c]

@@ -13,7 +13,7 @@ import math
 import numpy as np
 
 from . import abi
-from .scene import EnvironmentBuilder, Material, SourceDesc, resolve_material
+from .scene import EnvironmentBuilder, FluxSetup, Material, SourceDesc, resolve_material
 
 f32 = np.float32
 
@@ -29,7 +29,7 @@ def plain_small(steps: int = 2000):
     src = SourceDesc.dipole(c, (0.0, 0.0, 1.0), 16.0, 7.0, 0.0)
     b.scene.sources.append(src)
     b.scene.probes.append(("behind", (34.0, 64.0, 64.0)))
-    b.scene.fluxes.append(("radiated", (52, 52, 52), (76, 76, 76)))
+    b.scene.fluxes.append(FluxSetup("radiated", "box", (52, 52, 52), (76, 76, 76)))
     L = grid.pml_thickness
     b.scene.far_field = {"box_min": (L + 1 + 4,) * 3, "box_max": tuple(n - L - 2 - 4 for n in grid.size),
                          "wavelength": 16.0, "averaging": 4.0}

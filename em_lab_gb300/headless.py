@@ -1,0 +1,127 @@
+"""Headless runner: a scene script stepped for N frames with the reference's console output.
+
+    python -m em_lab_gb300 --script FILE.lua --frames N [--set NAME=VALUE ...] [--steps N]
+
+Follows the unattended `--frames` mode of the reference application (src/Main.cpp:40-103 options,
+464-540 scene load and header, 1043-1157 frame loop): each frame steps the grid (the monitors that
+need every step run on the device inside the step), measures probes and fluxes every second frame,
+evaluates the far field, port readings and sweep every 50th frame, prints the instrument report
+every 100th frame and once more after the last frame. Exit code 2 = non-finite fields, 3 = script
+error. There is no window and no renderer: the render timing is reported as 0.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+import time
+
+import numpy as np
+
+
+def _load(path, overrides):
+    from .script import ScriptEngine
+    return ScriptEngine(overrides, echo=True).run_file(path)
+
+
+def _value_string(p):
+    if p.kind == "bool":
+        return "on" if p.value else "off"
+    if p.kind == "choice":
+        return str(p.value)
+    return "%g" % p.value
+
+
+def print_header(res, grid, script_name):
+    sc = res.scene
+    s = grid.size()
+    print(f"\n=== {sc.name} ===  ({script_name})")
+    if sc.description:
+        print(sc.description)
+    n = s[0] * s[1] * s[2]
+    print(f"Grid {s[0]}x{s[1]}x{s[2]} ({n * 1e-6:.1f} M cells, {grid.gpu_memory_bytes() / (1 << 20):.0f} MB GPU), "
+          f"dt = {grid.dt():.3f}, PML {sc.grid.pml_thickness}, lambda_ref = {sc.wavelength:.1f} cells "
+          f"({299792458.0 / (sc.wavelength * sc.cell_size) * 1e-9:.4g} GHz at {sc.cell_size * 1e3:.3g} mm cells), "
+          f"{len(sc.sources)} source term(s)")
+    if res.params:
+        print("Parameters:")
+        for p in res.params:
+            print(f"  {'':<8s} {p.label:<24s} = {_value_string(p)}")
+
+
+def run(script, frames, overrides=None, steps_per_frame=None, quiet=False):
+    """Runs `script` for `frames` frames; returns (exit code, Instruments)."""
+    from . import SimulationGrid
+    from .instruments import NO_INSTRUMENTS_HINT, Instruments
+    from .script import ScriptError
+
+    try:
+        res = _load(script, overrides or {})
+    except ScriptError as e:
+        print(f"script error: {e}", file=sys.stderr)
+        return 3, None
+    sc = res.scene
+    grid = SimulationGrid(sc.grid)
+    m = sc.materials
+    grid.upload_materials(m.sigma, m.epsilon_r, sc.edges, sc.wires)
+    grid.set_sources(sc.sources)
+    inst = Instruments(grid, sc)
+    for w in res.warnings:
+        print(f"  warning: {w}", file=sys.stderr)
+    print_header(res, grid, os.path.basename(str(script)))
+    if inst.empty():
+        print(NO_INSTRUMENTS_HINT)
+    spf = steps_per_frame if steps_per_frame is not None else 2
+    if sc.view.get("steps_per_frame"):
+        spf = sc.view["steps_per_frame"]
+    every_step = bool(inst.ports or inst.ff)
+    sim_ms = 0.0
+    frame = 0
+    while frame < frames:
+        t0 = time.perf_counter()
+        if spf > 0:
+            grid.step(spf)
+        grid.synchronize(600000)
+        sim_ms = (time.perf_counter() - t0) * 1e3
+        if frame % 2 == 0 or spf == 0:
+            inst.measure()
+        if every_step and frame % 50 == 49:
+            inst.evaluate_far_field()
+            if inst.sweep_setup:
+                inst.evaluate_sweep()
+        frame += 1
+        if frame % 100 == 0 and not inst.empty():
+            inst.print_report()
+        if frame >= frames:
+            inst.measure()
+            inst.evaluate_far_field()
+            if inst.sweep_setup:
+                inst.evaluate_sweep()
+            if not inst.empty():
+                inst.print_report()
+            print(f"GPU timings: sim {sim_ms:.3f} ms/frame ({spf} steps), render 0.000 ms")
+    finite = grid.check_finite()
+    grid.close()
+    return (2 if (inst.unstable or not finite) else 0), inst
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m em_lab_gb300", description=__doc__.split("\n\n")[0])
+    ap.add_argument("--script", required=True, help="scene script (.lua)")
+    ap.add_argument("--set", action="append", default=[], metavar="NAME=VALUE", help="override a script param{}")
+    ap.add_argument("--frames", type=int, default=100, help="run this many frames, then exit")
+    ap.add_argument("--steps", type=int, default=2, help="simulation steps per frame (the scene's view{} wins)")
+    a = ap.parse_args(argv)
+    overrides = {}
+    for kv in a.set:
+        if "=" not in kv or kv.startswith("="):
+            print(f"--set expects NAME=VALUE (got '{kv}')", file=sys.stderr)
+            continue
+        k, v = kv.split("=", 1)
+        overrides[k] = v
+    code, _ = run(a.script, max(a.frames, 1), overrides, min(max(a.steps, 0), 64))
+    return code
+
+
+if __name__ == "__main__":
+    sys.exit(main())

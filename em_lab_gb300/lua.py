@@ -1473,12 +1473,12 @@ class Interpreter:
 
         def l_tonumber(v=None, base=None, *r):
             if base is None:
-                return tonum(v) if type(v) in (int, float) else (str2number(v) if type(v) is str else None)
+                return (tonum(v) if type(v) in (int, float) else (str2number(v) if type(v) is str else None),)
             s = str(v).strip().lower()
             try:
-                return int(s, int(base))
+                return (int(s, int(base)),)
             except ValueError:
-                return None
+                return (None,)
         self.register("tonumber", l_tonumber)
 
         def ipairs_step(args):
@@ -1498,7 +1498,7 @@ class Interpreter:
                 except ValueError:
                     raise LuaError("invalid key to 'next'")
             if idx >= len(keys):
-                return None
+                return (None,)
             kk = keys[idx]
             return (_unkey(kk), t.hash[kk])
         nextf = self.register("next", l_next)
@@ -1571,11 +1571,11 @@ class Interpreter:
         def l_getmetatable(v=None, *r):
             m = I.metatable(v)
             if m is None:
-                return None
+                return (None,)
             p = m.rawget("__metatable")
             return p if p is not None else m
         self.register("getmetatable", l_getmetatable)
-        self.register("rawget", lambda t, k=None, *r: t.rawget(k))
+        self.register("rawget", lambda t, k=None, *r: (t.rawget(k),))
         self.register("rawset", lambda t, k, v=None, *r: (t.rawset(k, v), t)[1])
         self.register("rawequal", lambda a=None, b=None, *r: a is b or (type(a) is type(b) and a == b
                                                                            and type(a) is not LuaTable))
@@ -1635,17 +1635,17 @@ class Interpreter:
                 init = max(len(s) + init + 1, 1)
             if plain or not any(c in pat for c in "^$*+?.([%-"):
                 k = s.find(pat, init - 1)
-                return None if k < 0 else (k + 1, k + len(pat))
+                return (None,) if k < 0 else (k + 1, k + len(pat))
             m = _lua_pattern(pat).search(s, init - 1)
             if not m:
-                return None
+                return (None,)
             return (m.start() + 1, m.end()) + tuple(m.groups())
         self.register("find", l_find, S)
 
         def l_match(s, pat, init=1, *r):
             m = _lua_pattern(pat).search(tostr(s), max(toint(init), 1) - 1)
             if not m:
-                return None
+                return (None,)
             return tuple(m.groups()) if m.groups() else m.group(0)
         self.register("match", l_match, S)
 
@@ -1786,9 +1786,9 @@ class Interpreter:
             ip = float(math.trunc(x))
             return (ip if not ip.is_integer() else (int(ip) if abs(ip) < 2 ** 63 else ip), x - ip)
         self.register("modf", lambda x, *r: (lambda v: (float(v[0]), v[1]))(l_modf(x)), M)
-        self.register("tointeger", lambda x=None, *r: toint(x) if type(x) in (int, float) else None, M)
-        self.register("type", lambda x=None, *r: ("integer" if type(x) is int else "float")
-                      if type(x) in (int, float) else None, M)
+        self.register("tointeger", lambda x=None, *r: (toint(x) if type(x) in (int, float) else None,), M)
+        self.register("type", lambda x=None, *r: (("integer" if type(x) is int else "float")
+                                                  if type(x) in (int, float) else None,), M)
         self.register("ult", lambda a, b, *r: (a & 0xFFFFFFFFFFFFFFFF) < (b & 0xFFFFFFFFFFFFFFFF), M)
         self.rng = Xoshiro256()
         self.rng.seed(0x5EED, 0)  # Lua seeds randomly; a fixed default keeps runs reproducible

@@ -102,6 +102,124 @@ class EllipsoidShape:
         return (dx * dx + dy * dy) + dz * dz <= f32(1.0)
 
 
+class CylinderShape:
+    """CylinderShape (Environment.hpp:64-75, Environment.cpp:11-22): |axial| <= h and radial^2 <= r^2."""
+
+    def __init__(self, c, axis, radius, half_length):
+        self.c = np.asarray(c, f32)
+        self.axis = int(axis)
+        self.r = f32(radius)
+        self.h = f32(half_length)
+
+    def bounds(self):
+        ext = np.full(3, self.r, f32)
+        ext[self.axis] = self.h
+        return self.c - ext, self.c + ext
+
+    def contains(self, x, y, z):
+        d = [x - self.c[0], y - self.c[1], z - self.c[2]]
+        a = d[self.axis]
+        r2 = ((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]) - a * a
+        return (np.abs(a) <= self.h) & (r2 <= self.r * self.r)
+
+
+class DifferenceShape:
+    """DifferenceShape (Environment.hpp:92-100): in `a` and not in `b`; bounds of `a`."""
+
+    def __init__(self, a, b):
+        self.a, self.b = a, b
+
+    def bounds(self):
+        return self.a.bounds()
+
+    def contains(self, x, y, z):
+        return self.a.contains(x, y, z) & ~self.b.contains(x, y, z)
+
+
+def rotation_from_euler_degrees(deg):
+    """rotationFromEulerDegrees (Environment.cpp:66-71): R = Rz Ry Rx (x first, then y, then z)."""
+    ax, ay, az = (math.radians(float(f32(v))) for v in deg)
+    cx, sx, cy, sy, cz, sz = math.cos(ax), math.sin(ax), math.cos(ay), math.sin(ay), math.cos(az), math.sin(az)
+    rx = np.array([[1, 0, 0], [0, cx, -sx], [0, sx, cx]])
+    ry = np.array([[cy, 0, sy], [0, 1, 0], [-sy, 0, cy]])
+    rz = np.array([[cz, -sz, 0], [sz, cz, 0], [0, 0, 1]])
+    return (rz @ ry @ rx).astype(f32)
+
+
+class TransformedShape:
+    """TransformedShape (Environment.hpp:78-89, Environment.cpp:24-39): a local shape around the
+    origin, rotated and moved to `center`; bounds = the rotated local box's 8 corners."""
+
+    def __init__(self, local, center, rotation):
+        self.local = local
+        self.center = np.asarray(center, f32)
+        self.rot = np.asarray(rotation, f32)
+        self.inv = self.rot.T
+        lo, hi = local.bounds()
+        corners = np.array([[hi[0] if i & 1 else lo[0], hi[1] if i & 2 else lo[1], hi[2] if i & 4 else lo[2]]
+                            for i in range(8)], f32)
+        w = self.center + corners @ self.rot.T
+        self.lo, self.hi = w.min(axis=0), w.max(axis=0)
+
+    def bounds(self):
+        return self.lo, self.hi
+
+    def contains(self, x, y, z):
+        d = [x - self.center[0], y - self.center[1], z - self.center[2]]
+        m = self.inv
+        lx = (m[0, 0] * d[0] + m[0, 1] * d[1]) + m[0, 2] * d[2]
+        ly = (m[1, 0] * d[0] + m[1, 1] * d[1]) + m[1, 2] * d[2]
+        lz = (m[2, 0] * d[0] + m[2, 1] * d[1]) + m[2, 2] * d[2]
+        return self.local.contains(lx, ly, lz)
+
+
+class WallShape:
+    """WallShape (Environment.hpp:115-135, Environment.cpp:41-64): the slab [x0, x1) normal to
+    `axis` minus rectangular (|d| < half size) and circular (|d|^2 <= r^2) apertures."""
+
+    def __init__(self, axis, x0, x1, apertures, grid_size):
+        self.axis = min(max(int(axis), 0), 2)
+        self.u = 1 if self.axis == 0 else 0
+        self.v = 1 if self.axis == 2 else 2
+        self.x0, self.x1 = f32(min(x0, x1)), f32(max(x0, x1))
+        self.apertures = apertures  # dicts: circular, center (u, v), half (u, v), radius
+        self.lo = np.zeros(3, f32)
+        self.hi = np.asarray(grid_size, f32).copy()
+        self.lo[self.axis], self.hi[self.axis] = self.x0, self.x1
+
+    def bounds(self):
+        return self.lo, self.hi
+
+    def contains(self, x, y, z):
+        p = (x, y, z)
+        a = p[self.axis]
+        inside = (a >= self.x0) & (a < self.x1)
+        tu, tv = p[self.u], p[self.v]
+        for ap in self.apertures:
+            du, dv = tu - f32(ap["center"][0]), tv - f32(ap["center"][1])
+            if ap["circular"]:
+                hole = du * du + dv * dv <= f32(ap["radius"]) * f32(ap["radius"])
+            else:
+                hole = (np.abs(du) < f32(ap["half"][0])) & (np.abs(dv) < f32(ap["half"][1]))
+            inside &= ~hole
+        return inside
+
+
+class LambdaShape:
+    """LambdaShape (Environment.hpp:102-110): a predicate over cell centres within given bounds.
+    `fn(x, y, z)` takes arrays and returns a boolean array."""
+
+    def __init__(self, lo, hi, fn):
+        self.lo, self.hi = np.asarray(lo, f32), np.asarray(hi, f32)
+        self.fn = fn
+
+    def bounds(self):
+        return self.lo, self.hi
+
+    def contains(self, x, y, z):
+        return self.fn(x, y, z)
+
+
 # ---------------------------------------------------------------------------------------------
 @dataclass
 class SourceDesc:
@@ -190,6 +308,36 @@ class ThinWireSpec:
 
 
 @dataclass
+class FluxSetup:
+    """FluxSetup / FluxSurface (Environment.hpp, FieldAnalyzer.hpp:28-45): a plane (axis, index,
+    rectangle in the two tangential coordinates) or a closed box (outward normal)."""
+
+    name: str
+    kind: str = "box"                  # "box" or "plane"
+    box_min: tuple = (0, 0, 0)
+    box_max: tuple = (0, 0, 0)
+    axis: int = 0
+    index: int = 0
+    rect_min: tuple = (0, 0)
+    rect_max: tuple = (0, 0)
+    log: str = ""
+
+    def planes(self):
+        """(sign, axis, index, rect_min, rect_max) per plane; a box has six with outward signs
+        (FieldAnalyzer.cpp:175-190)."""
+        if self.kind == "plane":
+            return [(1.0, self.axis, self.index, self.rect_min, self.rect_max)]
+        out = []
+        for ax in range(3):
+            u, v = (1, 2) if ax == 0 else ((0, 2) if ax == 1 else (0, 1))
+            rmin = (self.box_min[u], self.box_min[v])
+            rmax = (self.box_max[u] + 1, self.box_max[v] + 1)
+            out.append((-1.0, ax, self.box_min[ax], rmin, rmax))
+            out.append((1.0, ax, self.box_max[ax], rmin, rmax))
+        return out
+
+
+@dataclass
 class Scene:
     """The solver-facing part of Environment (src/Environment.hpp:165-187)."""
 
@@ -201,11 +349,13 @@ class Scene:
     sources: list = field(default_factory=list)    # SourceDesc
     ports: list = field(default_factory=list)      # PortSetup
     probes: list = field(default_factory=list)     # (name, position)
-    fluxes: list = field(default_factory=list)     # (name, box_min, box_max)
+    fluxes: list = field(default_factory=list)     # FluxSetup
     far_field: dict | None = None                  # box_min, box_max, wavelength, averaging
     sweep: dict | None = None                      # wavelength_min, wavelength_max, points
     cell_size: float = 1.0e-3
     wavelength: float = 16.0
+    description: str = ""
+    view: dict = field(default_factory=dict)       # ViewHints used by the headless runner
 
 
 class EnvironmentBuilder:

@@ -1,0 +1,64 @@
+"""The headless runner on the GPU: scene scripts stepped frame by frame with the reference's
+report, and the report's readings against the oracle stepping the same scene."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from em_lab_gb300 import headless
+from em_lab_gb300.instruments import Instruments
+from em_lab_gb300.script import ScriptEngine
+
+pytestmark = pytest.mark.gpu
+SCENES = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "em_lab_gb300", "scenes")
+
+
+def test_sphere_dipole_report_matches_oracle(capsys):
+    path = os.path.join(SCENES, "sphere_dipole.lua")
+    code, inst = headless.run(path, 100)
+    out = capsys.readouterr().out
+    assert code == 0
+    assert "=== Dipole beside a dielectric sphere ===  (sphere_dipole.lua)" in out
+    assert "Grid 128x128x128 (2.1 M cells" in out and "1 source term(s)" in out
+    assert "[t=   100.0 step     200]" in out
+    assert "probe behind" in out and "flux  radiated" in out and "far field [lambda=16.0 cells" in out
+    # the same scene stepped by the oracle, measured through the same host arithmetic
+    sc = ScriptEngine(echo=False).run_file(path).scene
+    o = oracle.Oracle(sc.grid, "f32")
+    oracle.load_scene(o, sc)
+    o.ntff_configure(sc.far_field["box_min"], sc.far_field["box_max"], sc.far_field["wavelength"],
+                     sc.far_field["averaging"])
+    o.step(200)
+
+    class OracleGrid:
+        def __getattr__(self, k):
+            return getattr(o, k)
+
+        def time(self):
+            return 100.0
+
+        def step_count(self):
+            return 200
+    ref = Instruments(OracleGrid(), sc, out=lambda s: None)
+    ref.measure()
+    assert ref.probes[0]["sample"] == inst.probes[0]["sample"]
+    assert ref.fluxes[0]["inst"] == inst.fluxes[0]["inst"]
+
+
+def test_fed_dipole_sweep_report(capsys):
+    code, inst = headless.run(os.path.join(SCENES, "fed_dipole.lua"), 300, {"length": "17"})
+    out = capsys.readouterr().out
+    assert code == 0
+    assert "Parameters:" in out and "= 17" in out
+    assert "sweep: 600 steps recorded" in out and "sweep feed" in out and "best match" in out
+    ps = inst.sweep_result["ports"][0]
+    assert 20.0 < ps["best_wl"] < 60.0
+
+
+def test_slit_wall_flux_plane(capsys):
+    code, inst = headless.run(os.path.join(SCENES, "slit_wall.lua"), 120)
+    out = capsys.readouterr().out
+    assert code == 0
+    assert "flux  transmitted" in out and "probe slit1" in out and "probe screen" in out
+    assert np.isfinite(inst.fluxes[0]["inst"])

@@ -96,7 +96,7 @@ def test_plain_small_2000_steps():
     steps = 2000
     L = sc.grid.pml_thickness
     ff = sc.far_field
-    name, bmin, bmax = sc.fluxes[0]
+    bmin, bmax = sc.fluxes[0].box_min, sc.fluxes[0].box_max
     planes = []
     for ax in range(3):
         u, v = (1, 2) if ax == 0 else ((0, 2) if ax == 1 else (0, 1))

@@ -1,0 +1,153 @@
+"""Scene scripts through the scene API: the solver inputs a script produces (materials, edge
+overrides, thin-wire terms, sources, ports and monitors) against the same scene built directly
+with the scene builder, plus the API's validation and error messages."""
+import os
+
+import numpy as np
+import pytest
+
+from em_lab_gb300 import abi, configs
+from em_lab_gb300.scene import EnvironmentBuilder, SourceDesc
+from em_lab_gb300.script import ScriptEngine, ScriptError
+
+SCENES = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "em_lab_gb300", "scenes")
+
+
+def run(src, overrides=None):
+    return ScriptEngine(overrides, echo=False).run_source(src, "test.lua")
+
+
+def edge_list(sc):
+    return sorted((e.x, e.y, e.z, e.axis, e.sigma) for e in sc.edges)
+
+
+def wire_list(sc):
+    return sorted((w.x, w.y, w.z, w.component, w.term, w.factor) for w in sc.wires)
+
+
+def src_tuple(s):
+    return (s.center, s.half_extent, s.softness, s.polarization, s.amplitude, s.wavelength, s.phase, s.waveform,
+            s.ramp_periods, s.repeat_periods, s.delay_periods, s.enabled)
+
+
+def test_sphere_dipole_script_equals_plain_small_config():
+    res = ScriptEngine(echo=False).run_file(os.path.join(SCENES, "sphere_dipole.lua"))
+    a, b = res.scene, configs.plain_small()
+    assert a.grid.size == b.grid.size and a.grid.pml_thickness == b.grid.pml_thickness
+    assert a.grid.courant == b.grid.courant
+    assert np.array_equal(a.materials.sigma, b.materials.sigma)
+    assert np.array_equal(a.materials.epsilon_r, b.materials.epsilon_r)
+    assert [src_tuple(s) for s in a.sources] == [src_tuple(s) for s in b.sources]
+    assert [p[1] for p in a.probes] == [p[1] for p in b.probes]
+    assert (a.fluxes[0].box_min, a.fluxes[0].box_max) == (b.fluxes[0].box_min, b.fluxes[0].box_max)
+    for k in ("box_min", "box_max", "wavelength", "averaging"):
+        assert tuple(np.atleast_1d(a.far_field[k])) == tuple(np.atleast_1d(b.far_field[k])), k
+
+
+def test_fed_dipole_script_equals_builder():
+    res = ScriptEngine({"length": "21"}, echo=False).run_file(os.path.join(SCENES, "fed_dipole.lua"))
+    a = res.scene
+    grid = abi.GridConfig((96, 96, 112), courant=0.5, pml_thickness=12)
+    b = EnvironmentBuilder("ref", grid, wavelength=32.0)
+    wave = SourceDesc(wavelength=32.0, waveform=abi.WAVE_PULSE, ramp_periods=float(np.float32(0.4)))
+    b.thin_dipole(wave, (48.0, 48.0, 56.0), 2, 21, radius=float(np.float32(0.08)), name="feed")
+    b = b.build()
+    assert edge_list(a) == edge_list(b)
+    assert wire_list(a) == wire_list(b)
+    assert [src_tuple(s) for s in a.sources] == [src_tuple(s) for s in b.sources]
+    assert [(p.texel, p.axis, p.edges, p.name) for p in a.ports] == [(p.texel, p.axis, p.edges, p.name) for p in b.ports]
+    assert a.sweep == {"wavelength_min": 20.0, "wavelength_max": 60.0, "points": 64, "log": ""}
+    assert [p.value for p in res.params] == [21.0, 0.08]
+
+
+def test_geometry_primitives_voxelise_like_the_builder():
+    res = run("""
+        scene { size = {48, 40, 36}, pml = 4, wavelength = 20 }
+        box { min = {10, 10, 10}, max = {20, 18, 16}, material = { name = "d", epsilon_r = 3 } }
+        sphere { center = {30, 20, 20}, radius = {5, 4, 3}, material = "fr4" }
+        cylinder { center = {24, 30, 18}, axis = "x", radius = 3, length = 12, thickness = 1, material = "pec" }
+        box { center = {36, 12, 24}, size = 6, rotate = {0, 0, 45}, material = "glass" }
+        shape { min = {4, 4, 4}, max = {12, 12, 12}, inside = function(x, y, z) return x + y < 16 end, material = "water" }
+    """)
+    sc = res.scene
+    mats = sc.materials
+    assert mats.epsilon_r[12, 12, 12] == np.float32(3.0)            # inside the first box
+    assert mats.epsilon_r[9, 12, 12] == 1.0                           # just outside (z = 9)
+    assert mats.epsilon_r[20, 20, 30] == np.float32(4.4)              # ellipsoid centre, fr4
+    assert mats.sigma[18, 30, 24] == 0.0                              # hollow tube inside
+    assert mats.sigma[18, 30 + 2, 24] == np.float32(1e7)              # tube wall (pec)
+    assert mats.epsilon_r[24, 12, 36] == np.float32(6.3)              # rotated cube centre
+    assert mats.epsilon_r[5, 5, 5] == np.float32(78.0) and mats.epsilon_r[5, 11, 11] == 1.0  # predicate shape
+
+
+def test_wall_slits_and_plane_wave():
+    res = ScriptEngine({"spacing": "16"}, echo=False).run_file(os.path.join(SCENES, "slit_wall.lua"))
+    sc = res.scene
+    s = sc.materials.sigma
+    # [z, y, x]: slits of width 6 centred at y = 48 -+ 8 in the wall at x = 48..49; metal elsewhere
+    assert s[32, 40, 48] == 0.0 and s[32, 56, 49] == 0.0
+    assert s[32, 48, 48] > 1e6 and s[32, 36, 48] > 1e6 and s[32, 40, 50] == 0.0
+    assert len(sc.sources) == 2                                   # one-way sheet: two quarter-wave-spaced sheets
+    assert sc.sources[1].center[0] - sc.sources[0].center[0] == pytest.approx(4.0)
+    assert sc.sources[1].delay_periods == pytest.approx(0.25)
+    assert [f.kind for f in sc.fluxes] == ["plane"] and sc.fluxes[0].rect_min == (10, 10)
+
+
+def test_array_and_cage():
+    res = run("""
+        scene { size = {96, 96, 64}, pml = 8, wavelength = 24 }
+        array { elements = {2, 3}, spacing = 12, length = 11, steer = {10, 0}, taper = "hann", name = "ant" }
+        cage { min = {10, 10, 10}, max = {30, 30, 30}, spacing = 5, bar = 1, material = "pec" }
+    """)
+    sc = res.scene
+    assert len(sc.ports) == 6 and sc.ports[0].name == "ant[0,0]"
+    assert len({s.phase for s in sc.sources}) == 2                 # progressive phase along the steered axis
+    assert sc.materials.sigma[10, 10, 10] > 0 and sc.materials.sigma[12, 12, 10] == 0
+
+
+@pytest.mark.parametrize("src,msg", [
+    ("box { min = {1, 1, 1}, max = {2, 2, 2}, material = 'unobtainium' }", "unknown material 'unobtainium'"),
+    ("box { min = {1, 1, 1} }", "missing required vector 'max'"),
+    ("probe { position = 'here' }", "'position' must be a 3-vector"),
+    ("box { min = {1, 1, 1}, max = {2, 2, 2} } scene { size = 64 }", "scene{} must be the first call"),
+    ("scene { size = 8 }", "size must be at least 16 cells"),
+    ("scene { courant = 0.6 }", "courant must be < 1/sqrt(3)"),
+    ("dipole { length = 4 }", "thin-wire dipole needs length >= 5"),
+    ("wire { from = {1, 1, 1}, to = {2, 2, 1} }", "differ along exactly one axis"),
+    ("radar {}", "radar{}: not supported"),
+    ("local v = vec(1, 2, 3) + 'x'", "arithmetic"),
+])
+def test_errors(src, msg):
+    with pytest.raises(ScriptError, match=msg.replace("(", r"\(").replace(")", r"\)").replace("{", r"\{")
+                       .replace("}", r"\}")):
+        run(src)
+
+
+def test_vector_prelude_and_grid_globals():
+    res = run("""
+        scene { size = {64, 48, 32}, pml = 6, wavelength = 20, cell_size = 0.002 }
+        local a = vec(1, 2, 3)
+        local b = a * 2 + 1 - vec(1)
+        print(tostring(b), b.x, b:length() > 0, a:dot(X), tostring(a:cross(Y)), tostring(a:with('z', 9)))
+        print(tostring(grid.center), grid.nx, grid.pml, grid.wavelength, deg(180), wavelengths(2), mm(4), lerp(1, 3, 0.5))
+        local n = 0
+        for x in range(0, 1, 0.25) do n = n + 1 end
+        print(n, clamp(5, 0, 3), tostring(-a), a == vec(1, 2, 3))
+    """)
+    assert res.output == ["vec(2, 4, 6)\t2\ttrue\t1\tvec(-3, 0, 1)\tvec(1, 2, 9)",
+                          # cell_size is the float32 value, as the reference exposes it
+                          "vec(32, 24, 16)\t64\t6\t20.0\t3.1415926535898\t40.0\t1.9999999050051\t2.0",
+                          "5\t3\tvec(-1, -2, -3)\ttrue"]
+
+
+def test_warnings():
+    res = run("""
+        scene { size = 48, pml = 6 }
+        probe { position = {2, 20, 20} }
+        box { min = {0, 0, 0}, max = {4, 4, 4}, colour = 'red' }
+        monopole { base = {24, 24, 24}, length = 6 }
+    """)
+    w = " | ".join(res.warnings)
+    assert "unknown field 'colour'" in w
+    assert "lies inside the absorbing boundary layer" in w
+    assert "no conductor touches the base of the feed gap" in w
