@@ -185,7 +185,7 @@ def dft_setup(grid, sc):
 
 def kernel_name(kernel: str, tiling: int) -> str:
     if kernel == "fused":
-        return "yee_tma2" if tiling in (0, 64, 128) else "yee_tma"
+        return "yee_tma2" if tiling in (0, 32, 64, 128) else "yee_tma"
     return {"fused_ldg": "yee_fused", "split": "yee_split_b+yee_split_e"}[kernel]
 
 
@@ -298,7 +298,7 @@ def main():
                     help="plain_large: the 512^3 dipole + blocks workload (default); plain_small: 128^3 sphere")
     ap.add_argument("--size", type=int, default=512, help="edge of the plain_large grid")
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
-    ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 64, 128])
+    ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 32, 64, 128])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end leg (default: --steps)")
     args = ap.parse_args()

@@ -182,8 +182,8 @@ YeeArgs yee_args(emlab_grid* g) {
     // tile height and z chunks: enough CTAs for ~4 per SM, but at least 8 planes each (the first
     // plane of a chunk is recomputed)
     const int mode = g->tile_rows == 0 ? 64 : g->tile_rows;  // automatic: 64 x 8 pair tiles
-    const int ty = mode == 16 || mode == 128 ? 16 : 8;
-    const int tx = (mode == 64 || mode == 128) && g->kernel == EMLAB_KERNEL_FUSED ? 64 : 32;
+    const int ty = mode == 16 || mode == 128 ? 16 : (mode == 32 ? 4 : 8);
+    const int tx = (mode == 32 || mode == 64 || mode == 128) && g->kernel == EMLAB_KERNEL_FUSED ? 64 : 32;
     a.tile_rows = g->kernel == EMLAB_KERNEL_FUSED ? mode : ty;
     const long long xy = (long long)((a.nx + tx - 1) / tx) * ((a.ny + ty - 1) / ty);
     const long long want = 152 * 4;
@@ -735,9 +735,10 @@ int emlab_grid_set_kernel(emlab_grid* g, int kernel) {
 
 int emlab_grid_set_tiling(emlab_grid* g, int tile_rows) {
     if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
-    EMLAB_REQUIRE(tile_rows == 0 || tile_rows == 8 || tile_rows == 16 || tile_rows == 64 || tile_rows == 128,
-                  "tiling must be 0 (automatic), 8 or 16 (32-cell rows), 64 or 128 (64 x 8 or 64 x 16 tiles of "
-                  "cell pairs)");
+    EMLAB_REQUIRE(tile_rows == 0 || tile_rows == 8 || tile_rows == 16 || tile_rows == 32 || tile_rows == 64 ||
+                      tile_rows == 128,
+                  "tiling must be 0 (automatic), 8 or 16 (32-cell rows), 32, 64 or 128 (64 x 4, 64 x 8 or 64 x 16 "
+                  "tiles of cell pairs)");
     g->tile_rows = tile_rows;
     if (g->configured) refresh_tma(g);  // the TMA boxes depend on the tile height
     return EMLAB_OK;

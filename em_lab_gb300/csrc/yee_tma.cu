@@ -468,15 +468,16 @@ __device__ __forceinline__ PairItem pair_item(const PairSched& ps, int nz, int i
 // on across item boundaries, so the pipeline never drains inside a launch. The leader takes the
 // next item when its loads reach it and posts the item number in a small shared ring that the
 // other warps read at their item boundary (always at least one barrier later).
-// 64 x 8 tiles: two 288-thread CTAs per SM; 64 x 16 tiles: one 544-thread CTA. Registers are
-// allocated per SM quadrant and 17-18 warps put 5 warps on one quadrant: 96 registers at most.
+// 64 x 4 tiles: four 160-thread CTAs per SM; 64 x 8: two 288-thread CTAs; 64 x 16: one 544-thread
+// CTA. Registers are allocated per SM quadrant and 17-20 warps put 5 warps on one quadrant: 96
+// registers at most.
 template <int TY, typename Idx>
-__global__ void __launch_bounds__(32 * (TY + 1), TY == 8 ? 2 : 1)
+__global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1))
     yee_tma2(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUtensorMap tey,
              const __grid_constant__ CUtensorMap tez, const __grid_constant__ CUtensorMap tbx,
              const __grid_constant__ CUtensorMap tby, const __grid_constant__ CUtensorMap tbz,
              const __grid_constant__ CUtensorMap tcls, YeeArgs a, PairSched ps, unsigned* err) {
-    static_assert(TY == 8 || TY == 16, "register budget assumes 9 or 17 warps per CTA");
+    static_assert(TY == 4 || TY == 8 || TY == 16, "register budget assumes 5, 9 or 17 warps per CTA");
     using Lay = Layout2<TY, Idx>;
     constexpr int S_ = Lay::STAGES;
     extern __shared__ __align__(128) unsigned char smem[];
@@ -774,8 +775,8 @@ bool encode(CUtensorMap* m, CUtensorMapDataType type, int elem, const void* base
 
 // tiling modes: 8, 16 = 32 x TY tiles of single cells (yee_tma); 64, 128 = 64 x 8 and 64 x 16 tiles
 // of cell pairs (yee_tma2)
-int tile_rows(const YeeArgs& a) { return a.tile_rows == 16 || a.tile_rows == 128 ? 16 : 8; }
-bool pair_tiles(const YeeArgs& a) { return a.tile_rows == 64 || a.tile_rows == 128; }
+int tile_rows(const YeeArgs& a) { return a.tile_rows == 16 || a.tile_rows == 128 ? 16 : (a.tile_rows == 32 ? 4 : 8); }
+bool pair_tiles(const YeeArgs& a) { return a.tile_rows == 32 || a.tile_rows == 64 || a.tile_rows == 128; }
 
 template <int TY, typename Idx>
 bool launch_t(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaStream_t s) {
@@ -826,8 +827,8 @@ bool launch_p(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaSt
             cudaFuncSetAttribute(yee_tma2<TY, Idx>, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(yee_tma2<TY, Idx>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 std::min(100, (100 * (TY == 8 ? 2 : 1) * (Lay::SMEM + 1024) + smem_sm - 1) /
-                                                   smem_sm)) != cudaSuccess ||
+                                 std::min(100, (100 * (TY == 4 ? 4 : (TY == 8 ? 2 : 1)) * (Lay::SMEM + 1024) +
+                                                smem_sm - 1) / smem_sm)) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, yee_tma2<TY, Idx>, 32 * (TY + 1), Lay::SMEM) !=
                 cudaSuccess ||
             resident < 1) {
@@ -876,6 +877,9 @@ bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsi
     if (pair_tiles(a) && tile_rows(a) == 16)
         return wide ? launch_p<16, uint32_t>(a, m, gen, err, s, tickets)
                     : launch_p<16, uint16_t>(a, m, gen, err, s, tickets);
+    if (pair_tiles(a) && tile_rows(a) == 4)
+        return wide ? launch_p<4, uint32_t>(a, m, gen, err, s, tickets)
+                    : launch_p<4, uint16_t>(a, m, gen, err, s, tickets);
     if (pair_tiles(a))
         return wide ? launch_p<8, uint32_t>(a, m, gen, err, s, tickets)
                     : launch_p<8, uint16_t>(a, m, gen, err, s, tickets);

@@ -65,8 +65,8 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False):
     m = sc.materials
     grid.upload_materials(m.sigma, m.epsilon_r, sc.edges, sc.wires)
     grid.set_sources(sc.sources)
-    inst = Instruments(grid, sc)
-    for w in res.warnings:
+    inst = Instruments(grid, sc, output_dir=res.output_dir)
+    for w in res.warnings + inst.warnings:
         print(f"  warning: {w}", file=sys.stderr)
     print_header(res, grid, os.path.basename(str(script)))
     if inst.empty():
@@ -101,6 +101,7 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False):
                 inst.print_report()
             print(f"GPU timings: sim {sim_ms:.3f} ms/frame ({spf} steps), render 0.000 ms")
     finite = grid.check_finite()
+    inst.close()
     grid.close()
     return (2 if (inst.unstable or not finite) else 0), inst
 

@@ -12,6 +12,7 @@ themselves run on the device), the far-field direction set and pattern analysis
 from __future__ import annotations
 
 import math
+import os
 import sys
 
 import numpy as np
@@ -72,6 +73,11 @@ def far_field_directions(axis):
     return np.array(dirs, np.float32), cuts
 
 
+def _g(v):
+    """A number as C++ streams print it by default (6 significant digits, %g)."""
+    return "%g" % v
+
+
 def to_dbi(d):
     return float(np.float32(10.0 * math.log10(d))) if d > 1e-12 else -120.0
 
@@ -96,6 +102,7 @@ def analyse_cut(cut, dbi):
                 half[k_dir] = (k - 1 + frac) * step
                 break
     cut["beamwidth"] = 360.0 if (half[0] < 0 or half[1] < 0) else half[0] + half[1]
+    cut["dbi"] = dbi
     cut["front_back"] = dbi[peak] - at(peak + n // 2)
 
 
@@ -126,19 +133,24 @@ def sample_block(block, origin, extent, q, ch):
 class Instruments:
     """Instruments::configure / measure / evaluate / printReport for one scene on one grid."""
 
-    def __init__(self, grid, scene, out=print):
+    def __init__(self, grid, scene, out=print, output_dir=""):
         self.g = grid
         self.sc = scene
         self.out = out
+        self.output_dir = output_dir
+        self.warnings = []
         self.size = tuple(scene.grid.size)
         self.averaging_time = 3.0 * max(scene.wavelength, 2.0)
         self.unstable = False
         self.measure_time, self.measure_step = 0.0, 0
         self.probes = []
-        for name, pos in scene.probes:
+        logs = list(getattr(scene, "probe_logs", [])) + [""] * len(scene.probes)
+        for (name, pos), log in zip(scene.probes, logs):
             p = tuple(min(max(float(v), 0.0), float(n - 1)) for v, n in zip(pos, self.size))
-            self.probes.append({"name": name, "pos": p, "sample": None})
-        self.fluxes = [{"setup": f, "inst": 0.0, "avg": 0.0, "peak": 0.0, "last": -1.0} for f in scene.fluxes]
+            self.probes.append({"name": name, "pos": p, "sample": None,
+                                "log": self.open_log(log, "step,time,Ex,Ey,Ez,Bx,By,Bz,absE,absB,Sx,Sy,Sz")})
+        self.fluxes = [{"setup": f, "inst": 0.0, "avg": 0.0, "peak": 0.0, "last": -1.0,
+                        "log": self.open_log(f.log, "step,time,P,P_avg")} for f in scene.fluxes]
         self.ports = list(scene.ports)
         self.readings = [None] * len(self.ports)
         self.sweep_setup = scene.sweep if self.ports else None
@@ -150,6 +162,34 @@ class Instruments:
         self.configure()
 
     # ------------------------------------------------------------------ set-up
+    def resolve(self, path):
+        if not path:
+            return ""
+        p = path if os.path.isabs(path) or not self.output_dir else os.path.join(self.output_dir, path)
+        d = os.path.dirname(p)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        return p
+
+    def open_log(self, path, header):
+        """Instruments::openLog (Instruments.cpp:19-33): CSV with a header line, relative paths
+        under the scene's output directory."""
+        if not path:
+            return None
+        try:
+            f = open(self.resolve(path), "w")
+        except OSError:
+            self.warnings.append(f"cannot open log file '{path}'")
+            return None
+        f.write(header + "\n")
+        return f
+
+    def close(self):
+        for rec in self.probes + self.fluxes:
+            if rec.get("log"):
+                rec["log"].close()
+                rec["log"] = None
+
     def configure(self):
         g, sc = self.g, self.sc
         t = g.time()
@@ -195,6 +235,11 @@ class Instruments:
                 m = self.sc.materials.get(cell)
                 p["sample"] = {"E": E, "B": B, "S": [float(v) for v in S], "sigma": m.sigma, "eps": m.epsilon_r}
                 finite = finite and all(math.isfinite(v) for v in E + B)
+                if p["log"]:
+                    em = math.sqrt(float(np.float32(np.dot(np.asarray(E, np.float32), np.asarray(E, np.float32)))))
+                    bm = math.sqrt(float(np.float32(np.dot(np.asarray(B, np.float32), np.asarray(B, np.float32)))))
+                    p["log"].write(",".join([str(self.measure_step), _g(self.measure_time)] +
+                                            [_g(v) for v in E + B + [em, bm] + list(p["sample"]["S"])]) + "\n")
         if self.planes:
             sums = g.flux_planes([pl for _, _, pl in self.planes])
             totals = [0.0] * len(self.fluxes)
@@ -210,6 +255,8 @@ class Instruments:
                 f["inst"] = P
                 f["peak"] = max(f["peak"], abs(P))
                 f["last"] = self.measure_time
+                if f["log"]:
+                    f["log"].write(f"{self.measure_step},{_g(self.measure_time)},{_g(P)},{_g(f['avg'])}\n")
         if not finite and not self.unstable:
             self.unstable = True
             print(f"ERROR: non-finite field values detected at step {self.measure_step}", file=sys.stderr)
@@ -255,6 +302,8 @@ class Instruments:
                     analyse_cut(cc, dbi)
                     cuts.append(cc)
                 pat["cuts"] = cuts
+                if self.ff.get("log"):
+                    self.write_pattern_csv(self.resolve(self.ff["log"]), pat)
             self.pattern = pat
         self.evaluate_ports()
 
@@ -309,6 +358,30 @@ class Instruments:
                 ps["band"] = (1.0 / edge(-1), 1.0 / edge(+1))
             res["ports"].append(ps)
         self.sweep_result = res
+        if s.get("log"):
+            self.write_sweep_csv(self.resolve(s["log"]), res)
+
+    def write_sweep_csv(self, path, res):
+        """PortMonitor::writeSweepCsv (Ports.cpp:280-297)."""
+        with open(path, "w") as f:
+            f.write("frequency_Hz,wavelength_cells")
+            for p in self.ports:
+                f.write(f",{p.name}_R_ohm,{p.name}_X_ohm,{p.name}_S11_dB,{p.name}_VSWR")
+            f.write("\n")
+            for i in range(len(res["ports"][0]["points"])):
+                wl = res["ports"][0]["points"][i]["wl"]
+                row = [_g(K_C0 / (wl * float(np.float32(self.sc.cell_size)))), _g(wl)]
+                for ps in res["ports"]:
+                    pt = ps["points"][i]
+                    row += [_g(pt["z"].real), _g(pt["z"].imag), _g(pt["s11"]), _g(pt["vswr"])]
+                f.write(",".join(row) + "\n")
+
+    def write_pattern_csv(self, path, pat):
+        """FarFieldMonitor::writeCsv (FarField.cpp:336-349): angle and the three cuts in dBi."""
+        with open(path, "w") as f:
+            f.write("angle_deg" + "".join(f",{c['name']}_dBi" for c in pat["cuts"]) + "\n")
+            for i, ang in enumerate(pat["cuts"][0]["angles"]):
+                f.write(_g(ang) + "".join("," + _g(c["dbi"][i]) for c in pat["cuts"]) + "\n")
 
     # ------------------------------------------------------------------ report
     def print_ports(self, max_lines):

@@ -349,6 +349,7 @@ class Scene:
     sources: list = field(default_factory=list)    # SourceDesc
     ports: list = field(default_factory=list)      # PortSetup
     probes: list = field(default_factory=list)     # (name, position)
+    probe_logs: list = field(default_factory=list) # CSV path per probe ("" = none)
     fluxes: list = field(default_factory=list)     # FluxSetup
     far_field: dict | None = None                  # box_min, box_max, wavelength, averaging
     sweep: dict | None = None                      # wavelength_min, wavelength_max, points

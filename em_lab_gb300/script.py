@@ -85,6 +85,7 @@ class ScriptResult:
     params: list
     warnings: list
     output: list
+    output_dir: str = ""      # where relative log paths go (ScriptEngine.cpp:2647-2651)
 
 
 def _round_half_away(x: float) -> int:
@@ -1377,9 +1378,9 @@ class ScriptEngine:
         a = Args(self, "probe", ["position", "name", "log"], t)
         self.lock()
         pos = a.req_vec("position")
-        probes = self.env().probes
-        probes.append((a.str("name", f"probe{len(probes) + 1}"), pos))
-        a.str("log", "")
+        sc = self.env()
+        sc.probes.append((a.str("name", f"probe{len(sc.probes) + 1}"), pos))
+        sc.probe_logs.append(a.str("log", ""))
         a.check_unknown()
 
     def api_flux_plane(self, t=None, *r):
@@ -1521,7 +1522,13 @@ class ScriptEngine:
     def run_file(self, path) -> ScriptResult:
         with open(path, "r", encoding="utf-8") as f:
             src = f.read()
-        return self.run_source(src, os.path.basename(str(path)))
+        res = self.run_source(src, os.path.basename(str(path)))
+        base = os.path.dirname(os.path.abspath(str(path)))
+        od = self.settings.output_dir
+        stem = os.path.splitext(os.path.basename(str(path)))[0]
+        res.output_dir = (os.path.join(base, "output", stem) if not od else
+                          (od if os.path.isabs(od) else os.path.join(base, od)))
+        return res
 
 
 def sheet_current_for_field(field_amplitude, wavelength, softness) -> float:

@@ -158,9 +158,9 @@ int emlab_grid_write_components(emlab_grid* g, const float* ex, const float* ey,
                                 const float* by, const float* bz);
 /* Selects the solver kernel (EMLAB_KERNEL_FUSED or EMLAB_KERNEL_SPLIT); results are identical. */
 int emlab_grid_set_kernel(emlab_grid* g, int kernel);
-/* Tile shape of the fused kernels: 8 or 16 (rows of 32 cells per CTA, one cell per thread), 64 or
- * 128 (64 x 8 or 64 x 16 tiles, two cells per thread; TMA kernel only) or 0 for the automatic
- * choice. A tuning knob only: every choice gives bit-identical results. */
+/* Tile shape of the fused kernels: 8 or 16 (rows of 32 cells per CTA, one cell per thread), 32, 64
+ * or 128 (64 x 4, 64 x 8 or 64 x 16 tiles, two cells per thread; TMA kernel only) or 0 for the
+ * automatic choice. A tuning knob only: every choice gives bit-identical results. */
 int emlab_grid_set_tiling(emlab_grid* g, int tile_rows);
 /* The cudaStream_t the grid launches on (for events and for ordering caller work). */
 int emlab_grid_stream(emlab_grid* g, void** stream);

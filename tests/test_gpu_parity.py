@@ -73,7 +73,8 @@ KERNELS = [abi.KERNEL_FUSED, abi.KERNEL_FUSED_LDG, abi.KERNEL_SPLIT]
 @pytest.mark.parametrize("seed,size,pml,rows", [(1, (24, 20, 18), 4, 0), (2, (37, 29, 23), 5, 16),
                                                 (3, (64, 40, 33), 8, 8), (4, (40, 260, 16), 3, 16),
                                                 (5, (131, 45, 29), 6, 64), (6, (63, 17, 20), 4, 64),
-                                                (7, (131, 45, 29), 6, 128), (9, (70, 33, 21), 5, 128)])
+                                                (7, (131, 45, 29), 6, 128), (9, (70, 33, 21), 5, 128),
+                                                (10, (131, 45, 29), 6, 32), (11, (66, 19, 23), 4, 32)])
 def test_random_scene_bit_exact(kernel, seed, size, pml, rows):
     sc = configs.random_scene(size=size, pml=pml, seed=seed)
     steps = 80
@@ -86,7 +87,7 @@ def test_random_scene_bit_exact(kernel, seed, size, pml, rows):
 
 
 @pytest.mark.parametrize("kernel", [abi.KERNEL_FUSED, abi.KERNEL_FUSED_LDG])
-@pytest.mark.parametrize("rows", [8, 16, 64, 128])
+@pytest.mark.parametrize("rows", [8, 16, 32, 64, 128])
 def test_fused_equals_split_and_chunking(kernel, rows):
     sc = configs.random_scene(size=(70, 300, 26), pml=6, seed=11)
     a = run_gpu(sc, 30, kernel, chunks=3, rows=rows)
@@ -94,7 +95,8 @@ def test_fused_equals_split_and_chunking(kernel, rows):
     assert_bitwise(a, b, "fused vs split")
 
 
-@pytest.mark.parametrize("kernel,rows", [(abi.KERNEL_FUSED, 8), (abi.KERNEL_FUSED, 64), (abi.KERNEL_FUSED, 128),
+@pytest.mark.parametrize("kernel,rows", [(abi.KERNEL_FUSED, 8), (abi.KERNEL_FUSED, 32), (abi.KERNEL_FUSED, 64),
+                                         (abi.KERNEL_FUSED, 128),
                                          (abi.KERNEL_FUSED_LDG, 0),
                                          (abi.KERNEL_SPLIT, 0)])
 def test_wide_class_index(kernel, rows):

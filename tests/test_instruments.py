@@ -165,3 +165,20 @@ def test_sample_block_matches_trilinear():
                 w = (f[0] if dx else 1 - f[0]) * (f[1] if dy else 1 - f[1]) * (f[2] if dz else 1 - f[2])
                 want += w * blk[((i0[2] + dz) * 3 + i0[1] + dy) * 3 + i0[0] + dx, 1]
     assert got == pytest.approx(want, rel=1e-5)
+
+
+def test_csv_logs(tmp_path):
+    sc = configs.plain_small()
+    sc.probe_logs = ["probe.csv"]
+    sc.fluxes[0].log = "logs/flux.csv"
+    g = FakeGrid()
+    inst = Instruments(g, sc, out=lambda s: None, output_dir=str(tmp_path))
+    inst.measure()
+    g.t, g.n = 101.0, 202
+    inst.measure()
+    inst.close()
+    probe = (tmp_path / "probe.csv").read_text().splitlines()
+    flux = (tmp_path / "logs" / "flux.csv").read_text().splitlines()
+    assert probe[0] == "step,time,Ex,Ey,Ez,Bx,By,Bz,absE,absB,Sx,Sy,Sz"
+    assert probe[1].startswith("200,100,33.5,63.5,63.5,68,0,0,") and len(probe) == 3
+    assert flux == ["step,time,P,P_avg", "200,100,0,0", "202,101,0,0"]
