@@ -74,7 +74,7 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False):
     spf = steps_per_frame if steps_per_frame is not None else 2
     if sc.view.get("steps_per_frame"):
         spf = sc.view["steps_per_frame"]
-    every_step = bool(inst.ports or inst.ff)
+    every_step = bool(inst.ports or inst.ff or inst.coaxes)
     sim_ms = 0.0
     frame = 0
     while frame < frames:
@@ -89,6 +89,7 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False):
             inst.evaluate_far_field()
             if inst.sweep_setup:
                 inst.evaluate_sweep()
+        inst.poll_coax()  # the reference polls the line monitor once per frame
         frame += 1
         if frame % 100 == 0 and not inst.empty():
             inst.print_report()

@@ -73,6 +73,10 @@ def far_field_directions(axis):
     return np.array(dirs, np.float32), cuts
 
 
+def _round_half_away(x: float) -> int:
+    return int(math.floor(x + 0.5)) if x >= 0 else -int(math.floor(-x + 0.5))
+
+
 def _g(v):
     """A number as C++ streams print it by default (6 significant digits, %g)."""
     return "%g" % v
@@ -159,6 +163,8 @@ class Instruments:
         self.pattern = None
         self.port_start = 0.0
         self.ff_start = 0.0
+        self.coaxes = list(getattr(scene, "coaxes", []))
+        self.coax_readings = [None] * len(self.coaxes)
         self.configure()
 
     # ------------------------------------------------------------------ set-up
@@ -204,13 +210,167 @@ class Instruments:
             self.ff_box = box
             self.ff_start = t
             self.dirs, self.cuts = far_field_directions(self.ff.get("axis", (0.0, 0.0, 1.0)))
+        if self.coaxes:
+            self.configure_coax()
+            self.coax_start = t
         self.planes = []
         for k, f in enumerate(sc.fluxes):
             for sign, axis, index, rmin, rmax in f.planes():
                 self.planes.append((k, sign, abi.FluxPlane(axis, index, rmin, rmax)))
 
     def empty(self):
-        return not (self.probes or self.fluxes or self.ff or self.ports)
+        return not (self.probes or self.fluxes or self.ff or self.ports or self.coaxes)
+
+    # ------------------------------------------------------------------ coax lines (Coax.cpp)
+    def configure_coax(self):
+        """CoaxMonitor::configure (Coax.cpp:80-168): per station k = 1 .. length-1 of each cable, V
+        (E line integral inner -> shield, averaged over the 4 sides), I (B loop round the inner
+        conductor) and Icm (B loop round the whole shield, or the balun sleeve)."""
+        quantities, terms, weights = [], [], []
+        self.coax_layout = []
+
+        def node_lo(c, size):
+            return _round_half_away(float(np.float32(c) - np.float32(0.5) * np.float32(size)))
+
+        def node_hi(c, size):
+            return _round_half_away(float(np.float32(c) + np.float32(0.5) * np.float32(size)))
+        for c in self.coaxes:
+            a, u, v = c.axis, (c.axis + 1) % 3, (c.axis + 2) % 3
+
+            def texel(ia, iu, iv):
+                t = [0, 0, 0]
+                t[a], t[u], t[v] = ia, iu, iv
+                return t
+
+            def add(t, comp, w):
+                terms.append([t[0], t[1], t[2], comp])
+                weights.append(w)
+
+            def loop(ia, u0, u1, v0, v1, w):
+                for iv in range(v0, v1 + 1):
+                    add(texel(ia, u1, iv), 3 + v, w)
+                    add(texel(ia, u0 - 1, iv), 3 + v, -w)
+                for iu in range(u0, u1 + 1):
+                    add(texel(ia, iu, v1), 3 + u, -w)
+                    add(texel(ia, iu, v0 - 1), 3 + u, w)
+            cu, cv = c.center[u], c.center[v]
+            iu0, iu1, iv0, iv1 = node_lo(cu, c.inner), node_hi(cu, c.inner), node_lo(cv, c.inner), node_hi(cv, c.inner)
+            su0, su1, sv0, sv1 = node_lo(cu, c.outer), node_hi(cu, c.outer), node_lo(cv, c.outer), node_hi(cv, c.outer)
+            shield = c.outer + 2 * c.wall
+            first = len(quantities)
+            for k in range(1, c.length):
+                ia = c.start + c.sign * k
+                f0 = len(terms)
+                w = float(np.float32(1.0) / (np.float32(4.0) * np.float32(c.inner + 1)))
+                for r in range(iv0, iv1 + 1):
+                    for i in range(iu1, su1):
+                        add(texel(ia, i, r), u, w)
+                    for i in range(su0, iu0):
+                        add(texel(ia, i, r), u, -w)
+                for r in range(iu0, iu1 + 1):
+                    for i in range(iv1, sv1):
+                        add(texel(ia, r, i), v, w)
+                    for i in range(sv0, iv0):
+                        add(texel(ia, r, i), v, -w)
+                quantities.append([f0, len(terms) - f0, 0, 0])
+                ib = c.start + k if c.sign > 0 else c.start - k - 1
+                sgn = float(c.sign)
+                f2 = len(terms)
+                loop(ib, iu0, iu1, iv0, iv1, sgn)
+                quantities.append([f2, len(terms) - f2, 1, 0])
+                out = c.sleeve_outer if (c.sleeve_outer > 0 and c.sleeve_start <= k < c.sleeve_end) else shield
+                f2 = len(terms)
+                loop(ib, node_lo(cu, out), node_hi(cu, out), node_lo(cv, out), node_hi(cv, out), sgn)
+                quantities.append([f2, len(terms) - f2, 1, 0])
+            self.coax_layout.append((first, max(c.length - 1, 0)))
+        self.g.lines_configure(quantities, terms, weights, max(self.coaxes[0].wavelength, 2.0), 4.0)
+        self.coax_peak = [0.0] * len(self.coaxes)
+
+    def poll_coax(self):
+        """CoaxMonitor::analyse (Coax.cpp:214-288): two-wave least-squares fit of V(t) and I(t)
+        with the lattice's TEM propagation constant."""
+        if not self.coaxes:
+            return
+        ph, now = self.g.lines_read()
+        dt = self.g.dt()
+        for li, c in enumerate(self.coaxes):
+            first, n = self.coax_layout[li]
+            r = {"valid": False}
+            tV = [k + 1.0 for k in range(n)]
+            tI = [k + 1.5 for k in range(n)]
+            q = [first + 3 * k for k in range(n)]
+            V = [complex(float(ph[i, 2]), float(ph[i, 3])) for i in q]
+            I = [complex(float(ph[i + 1, 2]), float(ph[i + 1, 3])) for i in q]
+            Icm = [complex(float(ph[i + 2, 2]), float(ph[i + 2, 3])) for i in q]
+            vmax = max((abs(float(now[i])) for i in q), default=0.0)
+            self.coax_peak[li] = max(vmax, self.coax_peak[li] * 0.995)
+            w = 2.0 * math.pi / max(c.wavelength, 2.0)
+            s_arg = math.sqrt(float(c.epsilon_r)) * math.sin(0.5 * w * dt) / dt
+            beta = 2.0 * math.asin(min(max(s_arg, -1.0), 1.0))
+            r["beta"] = beta
+            self.coax_readings[li] = r
+            if c.pulsed or n < 8:
+                continue
+            edge = float(c.outer + 2)
+
+            def fit(t, x):
+                m11 = m12 = m22 = r1 = r2 = 0j
+                for k in range(len(t)):
+                    if t[k] < edge or t[k] > c.length - edge:
+                        continue
+                    e = complex(math.cos(-beta * t[k]), math.sin(-beta * t[k]))
+                    f = e.conjugate()
+                    m11 += abs(e) ** 2
+                    m12 += e.conjugate() * f
+                    m22 += abs(f) ** 2
+                    r1 += e.conjugate() * x[k]
+                    r2 += f.conjugate() * x[k]
+                det = m11 * m22 - m12 * m12.conjugate()
+                if abs(det) < 1e-30:
+                    return None
+                return (r1 * m22 - m12 * r2) / det, (m11 * r2 - m12.conjugate() * r1) / det
+            fv, fi = fit(tV, V), fit(tI, I)
+            if fv is None or fi is None or abs(fv[0]) < 1e-20:
+                continue
+            A, B = fv
+            Ai = fi[0]
+            res = tot = 0.0
+            for k in range(n):
+                if tV[k] < edge or tV[k] > c.length - edge:
+                    continue
+                model = (A * complex(math.cos(-beta * tV[k]), math.sin(-beta * tV[k])) +
+                         B * complex(math.cos(beta * tV[k]), math.sin(beta * tV[k])))
+                res += abs(V[k] - model) ** 2
+                tot += abs(model) ** 2
+            gam = B / A * complex(math.cos(2 * beta * c.length), math.sin(2 * beta * c.length))
+            gg = min(abs(gam), 0.999999)
+            z0n, rsn = c.z0_ohm / K_ETA0, c.source_ohm / K_ETA0
+            p_fwd, p_avail = abs(A) ** 2 / (2.0 * z0n), c.drive * c.drive / (8.0 * rsn)
+            i_fwd = abs(A) / z0n
+            cm = max((abs(x) for x in Icm), default=0.0)
+            r.update(valid=True, A=A, B=B, residual=math.sqrt(res / tot) if tot > 0 else 1.0,
+                     z0m=abs(A / Ai) * K_ETA0 if abs(Ai) > 1e-30 else 0.0, gamma=gam,
+                     vswr=(1.0 + gg) / (1.0 - gg), rl=-20.0 * math.log10(gg) if gg > 1e-12 else 200.0,
+                     zend=c.z0_ohm * (1.0 + gam) / (1.0 - gam), fwd=p_fwd / p_avail if p_avail > 0 else 0.0,
+                     cm_db=20.0 * math.log10(cm / i_fwd) if cm > 0 and i_fwd > 0 else -300.0)
+
+    def print_coax(self):
+        """Instruments::printCoax (Instruments.cpp:366-385)."""
+        if not self.coaxes:
+            return
+        periods = max(self.g.time() - self.coax_start, 0.0) / max(self.coaxes[0].wavelength, 2.0)
+        for c, r in zip(self.coaxes, self.coax_readings):
+            self.out(f"    {c.name}: Z0 {c.z0_ohm:.1f} ohm (eps_r {c.epsilon_r:.2f}, velocity factor "
+                     f"{1.0 / math.sqrt(c.epsilon_r):.2f}), {c.termination} end, {periods:.0f} periods")
+            if not r or not r["valid"]:
+                continue
+            g = r["gamma"]
+            self.out(f"      waves: Z0 measured {r['z0m']:.1f} ohm, end Gamma {abs(g):.3f} @ "
+                     f"{math.degrees(math.atan2(g.imag, g.real)):+.0f} deg (RL {r['rl']:.1f} dB), VSWR {r['vswr']:.2f}, "
+                     f"Z_end {r['zend'].real:.1f} {r['zend'].imag:+.1f}j ohm")
+            self.out(f"      forward {100.0 * r['fwd']:.0f}% of available, delivered {100.0 * (1.0 - abs(g) ** 2):.0f}% "
+                     f"of forward; shield outside current {max(r['cm_db'], -200.0):.1f} dB vs line current; fit "
+                     f"residual {r['residual']:.1e}")
 
     # ------------------------------------------------------------------ measurement
     def measure(self):
@@ -464,6 +624,7 @@ class Instruments:
         for f in self.fluxes:
             out(f"    flux  {f['setup'].name:<28s} P={f['inst']:+.4e}  <P>={f['avg']:+.4e}  peak|P|={f['peak']:.4e}")
         self.print_ports(4)
+        self.print_coax()
         if self.ff:
             pat = self.pattern
             settle = max(self.g.time() - self.ff_start, 0.0) / max(self.ff["wavelength"], 1.0)

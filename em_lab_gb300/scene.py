@@ -338,6 +338,33 @@ class FluxSetup:
 
 
 @dataclass
+class CoaxSetup:
+    """CoaxSetup (src/Coax.hpp:25-45): a voxel coaxial cable and what its monitor needs."""
+
+    name: str
+    axis: int = 0
+    sign: int = 1
+    start: int = 0
+    center: tuple = (0.0, 0.0, 0.0)
+    length: int = 0
+    inner: int = 1
+    outer: int = 5
+    wall: int = 1
+    sleeve_start: int = -1
+    sleeve_end: int = -1
+    sleeve_outer: int = 0
+    epsilon_r: float = 1.0
+    z0_ohm: float = 50.0
+    wavelength: float = 16.0
+    cell_size: float = 1e-3
+    termination: str = "load"
+    source_ohm: float = 50.0
+    load_ohm: float = 50.0
+    drive: float = 1.0
+    pulsed: bool = False
+
+
+@dataclass
 class Scene:
     """The solver-facing part of Environment (src/Environment.hpp:165-187)."""
 
@@ -357,6 +384,7 @@ class Scene:
     wavelength: float = 16.0
     description: str = ""
     view: dict = field(default_factory=dict)       # ViewHints used by the headless runner
+    coaxes: list = field(default_factory=list)     # CoaxSetup
 
 
 class EnvironmentBuilder:

@@ -6,8 +6,8 @@ calls into a `scene.Scene`: src/ScriptEngine.cpp (SceneSettings :90-101, Args :2
 plane waves :1526-1590, instruments :1737-1805, far_field :2160-2190, final checks :2420-2520).
 The vector prelude (vec, X/Y/Z, deg, wavelengths, meters, mm, lerp, clamp, range) is provided as
 native functions with the same behaviour. Functions of the reference's API that drive subsystems
-this build does not implement (radar, crpa, emitter, coax, loop, frame) raise a script error
-that names them.
+this build does not implement (radar, crpa, emitter, loop, frame) raise a script error that
+names them.
 """
 from __future__ import annotations
 
@@ -19,7 +19,7 @@ import numpy as np
 
 from . import abi
 from .lua import Interpreter, LuaError, LuaFunction, LuaTable, lua_type, tostr
-from .scene import (K_PERFECT_EDGE_SIGMA, BoxShape, CylinderShape, DifferenceShape, EllipsoidShape,
+from .scene import (K_PERFECT_EDGE_SIGMA, BoxShape, CoaxSetup, CylinderShape, DifferenceShape, EllipsoidShape,
                     EnvironmentBuilder, FluxSetup, LambdaShape, Material, SourceDesc, TransformedShape, WallShape,
                     rotation_from_euler_degrees)
 
@@ -44,7 +44,7 @@ BUILTIN_MATERIALS = {
     "ground_wet": (25.0, None, 0.02, None), "water": (78.0, None, None, 0.1), "seawater": (74.0, None, 4.0, None),
 }
 
-UNSUPPORTED = ("loop", "frame", "radar", "emitter", "crpa", "coax")
+UNSUPPORTED = ("loop", "frame", "radar", "emitter", "crpa")
 
 
 class ScriptError(Exception):
@@ -621,7 +621,7 @@ class ScriptEngine:
         api = {"scene": self.api_scene, "view": self.api_view, "material": self.api_material, "param": self.api_param,
                "box": self.api_box, "sphere": self.api_sphere, "cylinder": self.api_cylinder,
                "wall": self.api_wall, "grating": self.api_grating, "shape": self.api_shape,
-               "cage": self.api_cage, "array": self.api_array,
+               "cage": self.api_cage, "array": self.api_array, "coax": self.api_coax,
                "dipole": self.api_dipole, "monopole": self.api_monopole, "wire": self.api_wire,
                "sheet": self.api_sheet, "sweep": self.api_sweep, "plane_wave": self.api_plane_wave,
                "gaussian_beam": self.api_gaussian_beam, "current_source": self.api_current_source,
@@ -1120,6 +1120,144 @@ class ScriptEngine:
                     self.add_source(e)
         a.check_unknown()
 
+    def api_coax(self, t=None, *r):
+        """coax{} (ScriptEngine.cpp:1964-2152): a square coaxial cable of voxels (shield with end
+        plates, dielectric, 1x1-cell inner conductor), a resistive generator across the first gap
+        cell, a load / open / short / antenna-terminal far end, an optional sleeve balun, and the
+        line monitor's set-up. Returns z0, z0_air, epsilon_r, velocity_factor, wavelength, far_end
+        (and inner_terminal / outer_terminal for termination = "terminals")."""
+        a = Args(self, "coax", ["from", "axis", "length", "inner", "outer", "wall", "z0", "material", "termination",
+                                "load", "terminals", "balun", "balun_length", "balun_gap", "amplitude", "impedance",
+                                "name", "wavelength", "frequency", "phase", "waveform", "ramp", "pulse_width",
+                                "interval", "delay", "enabled"], t)
+        self.lock()
+        wave = SourceDesc()
+        self.read_waveform(a, wave)
+        frm = a.req_vec("from")
+        d = a.opt_direction("axis") or (1.0, 0.0, 0.0)
+        ax = self.wire_axis(a, d)
+        u, v = (ax + 1) % 3, (ax + 2) % 3
+        sg = 1 if d[ax] >= 0 else -1
+        ln = _round_half_away(a.positive("length", 4.0 * wave.wavelength))
+        inner = _round_half_away(a.num("inner", 1.0))
+        outer = _round_half_away(a.num("outer", 5.0))
+        wall = _round_half_away(a.num("wall", 1.0))
+        if inner != 1:
+            a.fail("inner must be 1 cell (the generator drives the inner conductor across a 1x1-cell gap)")
+        if outer < 3 or outer % 2 == 0:
+            a.fail("outer (the inside of the shield, cells) must be odd and >= 3")
+        if wall < 1:
+            a.fail("wall must be >= 1 cell")
+        term = a.str("termination", "load").lower()
+        if term not in ("load", "open", "short", "terminals"):
+            a.fail("termination must be \"load\", \"open\", \"short\" or \"terminals\" (connect an antenna)")
+        if ln < 2 * outer + 12:
+            a.fail(f"length must be at least {2 * outer + 12} cells for this cross-section")
+        name = a.str("name", "cable")
+        g = coax_geometry_factor(inner, outer)
+        z0_air = K_ETA0 / g
+        if a.has("material"):
+            diel = self.read_material(a, "vacuum")
+        else:
+            target = a.positive("z0", 50.0)
+            er = (z0_air / target) * (z0_air / target)
+            if er < 1.0:
+                self.warn(f"coax: {target:.1f} ohm needs a wider shield; with outer = {outer} the air-filled line "
+                          f"is {z0_air:.1f} ohm")
+                er = 1.0
+            diel = Material(0.0, float(max(f32(er), f32(1.0))))
+            if er > 1.0:
+                key = name + " dielectric"
+                self.used_dielectrics[key] = max(self.used_dielectrics.get(key, 0.0), diel.epsilon_r)
+        z0 = z0_air / math.sqrt(max(diel.epsilon_r, 1.0))
+        tdir = a.opt_direction("terminals") or ((0.0, 1.0, 0.0) if ax == 2 else (0.0, 0.0, 1.0))
+        tax = self.wire_axis(a, tdir)
+        if tax == ax:
+            a.fail("terminals must be perpendicular to the cable axis")
+        ts = 1 if tdir[tax] >= 0 else -1
+        start = _round_half_away(frm[ax])
+        centre = [0.0, 0.0, 0.0]
+        centre[ax] = float(start)
+        centre[u] = float(f32(math.floor(frm[u]) + 0.5))
+        centre[v] = float(f32(math.floor(frm[v]) + 0.5))
+        b = self.env_builder()
+
+        def put(t0, t1, size, m):
+            lo, hi = [0.0] * 3, [0.0] * 3
+            lo[ax] = float(start + t0 if sg > 0 else start - t1)
+            hi[ax] = float(start + t1 if sg > 0 else start - t0)
+            for k in (u, v):
+                lo[k] = float(f32(centre[k] - 0.5 * size))
+                hi[k] = float(f32(centre[k] + 0.5 * size))
+            b.box(lo, hi, m)
+        metal = Material(float(f32(4.0 * float(K_PERFECT_EDGE_SIGMA))), 1.0)
+        shield = outer + 2 * wall
+        capped = term != "terminals"
+        c = CoaxSetup(name, ax, sg, start, tuple(centre), ln, inner, outer, wall, epsilon_r=diel.epsilon_r,
+                      z0_ohm=float(f32(z0)), wavelength=wave.wavelength, cell_size=float(f32(self.settings.cell_size)),
+                      termination=term, pulsed=wave.waveform == abi.WAVE_PULSE)
+        if a.boolean("balun", False):
+            bl = _round_half_away(a.positive("balun_length", 0.25 * wave.wavelength))
+            gap = _round_half_away(a.positive("balun_gap", 2.0))
+            sleeve = shield + 2 * (gap + wall)
+            if bl + wall >= ln - 4:
+                a.fail("balun_length is too long for this cable")
+            put(ln - bl - wall, ln, sleeve, metal)
+            put(ln - bl, ln, shield + 2 * gap, Material())
+            c.sleeve_start, c.sleeve_end, c.sleeve_outer = ln - bl - wall, ln, sleeve
+        put(-wall, ln + wall if capped else ln, shield, metal)
+        put(0, ln, outer, diel)
+        inner_end = {"terminals": ln + 3, "short": ln, "load": ln - 1}.get(term, ln - 2)
+        put(1, inner_end, inner, metal)
+        gen_ohm = float(f32(a.positive("impedance", z0)))
+        drive = float(f32(a.num("amplitude", 1.0)))
+        gap_cell = [0, 0, 0]
+        gap_cell[ax] = start if sg > 0 else start - 1
+        gap_cell[u] = int(math.floor(centre[u]))
+        gap_cell[v] = int(math.floor(centre[v]))
+        self.add_feed(wave, gap_cell, ax, float(sg), 4, (True, gen_ohm, drive), name)
+        c.source_ohm, c.drive = gen_ohm, drive
+        c.load_ohm = float(f32(a.positive("load", z0)))
+        if term == "load":
+            cell = list(gap_cell)
+            cell[ax] = start + ln - 1 if sg > 0 else start - ln
+            quiet = SourceDesc(**{k: getattr(wave, k) for k in wave.__dataclass_fields__})
+            quiet.enabled = True
+            self.add_feed(quiet, cell, ax, float(-sg), 4, (True, c.load_ohm, 0.0), name + " load")
+        elif a.has("load"):
+            self.warn("coax: 'load' only applies to termination = \"load\"")
+        inner_node, outer_node = [0.0] * 3, [0.0] * 3
+        if term == "terminals":
+            tu = v if tax == u else u
+            lo, hi = [0.0] * 3, [0.0] * 3
+            lo[ax] = float(start + ln if sg > 0 else start - ln - 3)
+            hi[ax] = float(start + ln + 3 if sg > 0 else start - ln)
+            lo[tu], hi[tu] = centre[tu] - 0.5, centre[tu] + 0.5
+            wall_in = 0.5 * outer
+            wall_out = wall_in + wall
+            lo[tax] = centre[tax] - wall_out if ts > 0 else centre[tax] + wall_in
+            hi[tax] = centre[tax] - wall_in if ts > 0 else centre[tax] + wall_out
+            b.box(lo, hi, metal)
+            inner_node[ax] = outer_node[ax] = float(start + sg * (ln + 2))
+            inner_node[tu] = outer_node[tu] = centre[tu] - 0.5
+            inner_node[tax] = centre[tax] + 0.5 * ts
+            outer_node[tax] = centre[tax] - ts * wall_out
+        self.env().coaxes.append(c)
+        a.check_unknown()
+        out = LuaTable()
+        out.rawset("z0", z0)
+        out.rawset("z0_air", z0_air)
+        out.rawset("epsilon_r", diel.epsilon_r)
+        out.rawset("velocity_factor", 1.0 / math.sqrt(max(diel.epsilon_r, 1.0)))
+        out.rawset("wavelength", wave.wavelength / math.sqrt(max(diel.epsilon_r, 1.0)))
+        end = list(centre)
+        end[ax] = float(start + sg * ln)
+        out.rawset("far_end", self.vec(*end))
+        if term == "terminals":
+            out.rawset("inner_terminal", self.vec(*inner_node))
+            out.rawset("outer_terminal", self.vec(*outer_node))
+        return out
+
     # -- antennas (ScriptEngine.cpp:1077-1460)
     def add_thin_wire(self, node, axis, i0, i1, radius, gap=None):
         if i1 <= i0:
@@ -1529,6 +1667,48 @@ class ScriptEngine:
         res.output_dir = (os.path.join(base, "output", stem) if not od else
                           (od if os.path.isabs(od) else os.path.join(base, od)))
         return res
+
+
+def coax_geometry_factor(inner: int, outer: int) -> float:
+    """CoaxMonitor::geometryFactor (Coax.cpp:43-78): Laplace's equation on the lattice nodes of
+    the square cross-section (inner conductor at 1, shield at 0) by SOR in the same sweep order;
+    G = sum over the transverse edges of (delta phi)^2, so Z0 = eta0 / (sqrt(eps_r) G)."""
+    n = outer + 1
+    lo = (outer - inner) // 2
+    hi = lo + inner
+    phi = [0.0] * (n * n)
+    fixed = [False] * (n * n)
+    for j in range(n):
+        for i in range(n):
+            k = j * n + i
+            if i == 0 or j == 0 or i == n - 1 or j == n - 1:
+                fixed[k] = True
+            if lo <= i <= hi and lo <= j <= hi:
+                fixed[k] = True
+                phi[k] = 1.0
+    omega = 2.0 / (1.0 + math.sin(math.pi / n))
+    for _ in range(20000):
+        change = 0.0
+        for j in range(1, n - 1):
+            for i in range(1, n - 1):
+                k = j * n + i
+                if fixed[k]:
+                    continue
+                target = 0.25 * (((phi[k - 1] + phi[k + 1]) + phi[k - n]) + phi[k + n])
+                d = omega * (target - phi[k])
+                phi[k] += d
+                change = max(change, abs(d))
+        if change < 1e-13:
+            break
+    g = 0.0
+    for j in range(n):
+        for i in range(n):
+            k = j * n + i
+            if i + 1 < n:
+                g += (phi[k + 1] - phi[k]) * (phi[k + 1] - phi[k])
+            if j + 1 < n:
+                g += (phi[k + n] - phi[k]) * (phi[k + n] - phi[k])
+    return g
 
 
 def sheet_current_for_field(field_amplitude, wavelength, softness) -> float:

@@ -62,3 +62,14 @@ def test_slit_wall_flux_plane(capsys):
     assert code == 0
     assert "flux  transmitted" in out and "probe slit1" in out and "probe screen" in out
     assert np.isfinite(inst.fluxes[0]["inst"])
+
+
+def test_coax_matched_line_measures_z0(capsys):
+    code, inst = headless.run(os.path.join(SCENES, "coax_load.lua"), 200)
+    out = capsys.readouterr().out
+    assert code == 0
+    assert "cable: Z0 50.0 ohm" in out and "waves: Z0 measured" in out
+    r = inst.coax_readings[0]
+    assert r["valid"]
+    assert abs(r["z0m"] - 50.0) < 2.5            # the line's own V+/I+ against the lattice Z0
+    assert abs(r["gamma"]) < 0.1                 # matched resistive load at the far end

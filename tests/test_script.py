@@ -151,3 +151,36 @@ def test_warnings():
     assert "unknown field 'colour'" in w
     assert "lies inside the absorbing boundary layer" in w
     assert "no conductor touches the base of the feed gap" in w
+
+
+def test_coax_builder_and_monitor_layout():
+    from em_lab_gb300.instruments import Instruments
+    from em_lab_gb300.script import coax_geometry_factor
+    assert coax_geometry_factor(1, 5) == pytest.approx(4.8, abs=1e-12)   # square lattice coax, 5-cell shield
+    res = ScriptEngine(echo=False).run_file(os.path.join(SCENES, "coax_load.lua"))
+    sc = res.scene
+    c = sc.coaxes[0]
+    assert c.z0_ohm == pytest.approx(50.0, rel=1e-6) and c.epsilon_r == pytest.approx((376.730313668 / 4.8 / 50) ** 2, rel=1e-6)
+    assert len(sc.ports) == 2 and [p.name for p in sc.ports] == ["cable", "cable load"]
+    assert res.output[0].startswith("coax: Z0 50.00 ohm")
+    m = sc.materials
+    assert m.sigma[20, 20, 20 + 60] > 1e5 and m.epsilon_r[20, 21, 20 + 60] == np.float32(c.epsilon_r)  # inner / dielectric
+
+    class Grid:
+        def time(self):
+            return 0.0
+
+        def dt(self):
+            return 0.5
+
+        def lines_configure(self, q, t, w, wl, avg):
+            self.q, self.t, self.w = q, t, w
+
+        def ports_configure(self, *a, **k):
+            pass
+    g = Grid()
+    Instruments(g, sc, out=lambda s: None)
+    assert len(g.q) == 3 * (c.length - 1)
+    kinds = [q[2] for q in g.q[:3]]
+    assert kinds == [0, 1, 1]
+    assert g.q[0][1] == 4 * 2 * 2 and g.q[1][1] == 8     # V: 4 sides x 2 node rows x 2 cells; I: 8 B terms
