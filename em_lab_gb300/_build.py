@@ -28,7 +28,7 @@ HOST_FLAGS = "-fPIC,-fopenmp,-ffp-contract=off,-O2"
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", HOST_FLAGS,
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
 
-SOURCES = ["yee.cu", "yee_tma.cu", "monitors.cu", "capi.cu", "noalloc.cu", "dft_tc.cu", "setup.cpp"]
+SOURCES = ["yee.cu", "yee_tma.cu", "monitors.cu", "capi.cu", "noalloc.cu", "dft_tc.cu", "render.cu", "setup.cpp"]
 HEADERS = ["emlab_math.h", "emlab_internal.h", "setup.h", "yee_common.cuh"]
 
 
@@ -78,7 +78,8 @@ def build_library(verbose: bool = False, force: bool = False) -> Path:
 
 def build_oracle(verbose: bool = False, force: bool = False) -> Path:
     ORACLE_LIB.parent.mkdir(parents=True, exist_ok=True)
-    deps = [ORACLE_SRC, ROOT / "oracle" / "oracle_impl.h", CSRC / "emlab_math.h", ROOT / "include" / "emlab.h"]
+    deps = [ORACLE_SRC, ROOT / "oracle" / "oracle_impl.h", ROOT / "oracle" / "oracle_render.h", CSRC / "emlab_math.h",
+            ROOT / "include" / "emlab.h"]
     if force or _stale(ORACLE_LIB, deps):
         cc = os.environ.get("CC", "gcc")
         _run([cc, "-O2", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-std=c11",

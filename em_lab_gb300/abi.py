@@ -70,6 +70,15 @@ class FluxPlane(C.Structure):
     _fields_ = [("axis", C.c_int), ("index", C.c_int), ("rect_min", C.c_int * 2), ("rect_max", C.c_int * 2)]
 
 
+class RenderParams(C.Structure):
+    """emlab_render_params: camera and look of one rendered frame."""
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("inv_view_proj", C.c_float * 16),
+                ("cam_pos", C.c_float * 3), ("vol_min", C.c_float * 3), ("vol_size", C.c_float * 3),
+                ("clip_min", C.c_float * 3), ("clip_max", C.c_float * 3), ("step_voxels", C.c_float),
+                ("gain_e", C.c_float), ("gain_b", C.c_float), ("density", C.c_float), ("emission", C.c_float),
+                ("material_opacity", C.c_float), ("exposure", C.c_float), ("mode", C.c_int), ("signed_axis", C.c_int)]
+
+
 class GridState(C.Structure):
     _fields_ = [("time", C.c_double), ("dt", C.c_float), ("step_count", C.c_uint64), ("nx", C.c_int),
                 ("ny", C.c_int), ("nz", C.c_int), ("device_bytes", C.c_uint64), ("source_cells", C.c_int),

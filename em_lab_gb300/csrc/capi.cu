@@ -1104,6 +1104,36 @@ int emlab_probe_gather(emlab_grid* g, const int* origins, int n_probes, float* o
     return EMLAB_OK;
 }
 
+int emlab_render(emlab_grid* g, const emlab_render_params* params, unsigned char* rgba) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(params && rgba, "null render argument");
+    EMLAB_REQUIRE(params->width > 0 && params->height > 0 && params->width <= 16384 && params->height <= 16384,
+                  "render size must be 1..16384 pixels per side");
+    EMLAB_REQUIRE(std::isfinite(params->step_voxels), "render step must be finite");
+    // the host-side clamps of VolumeRenderer::render (src/VolumeRenderer.cpp:100, 111)
+    emlab_render_params q = *params;
+    q.step_voxels = std::clamp(q.step_voxels, 0.1f, 4.0f);
+    q.signed_axis = std::clamp(q.signed_axis, 0, 2);
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    const size_t cells = (size_t)g->cfg.nx * g->cfg.ny * g->cfg.nz;
+    const size_t pixels = (size_t)q.width * q.height;
+    DevBuf<float> d_sigma, d_eps;
+    DevBuf<unsigned char> d_img;
+    const bool mats = g->cell_sigma.size() == cells && g->cell_eps.size() == cells;
+    if (mats) {
+        EMLAB_CUDA(d_sigma.alloc(cells));
+        EMLAB_CUDA(d_eps.alloc(cells));
+        EMLAB_CUDA(cudaMemcpyAsync(d_sigma.p, g->cell_sigma.data(), cells * 4, cudaMemcpyHostToDevice, g->stream));
+        EMLAB_CUDA(cudaMemcpyAsync(d_eps.p, g->cell_eps.data(), cells * 4, cudaMemcpyHostToDevice, g->stream));
+    }
+    EMLAB_CUDA(d_img.alloc(pixels * 4));
+    launch_raymarch(monitor_args(g), mats ? d_sigma.p : nullptr, mats ? d_eps.p : nullptr, q, d_img.p, g->stream);
+    ++g_launches;
+    if (int rc = check_launch()) return rc;
+    EMLAB_CUDA(cudaMemcpyAsync(rgba, d_img.p, pixels * 4, cudaMemcpyDeviceToHost, g->stream));
+    return emlab_grid_synchronize(g, 0);
+}
+
 int emlab_flux_planes(emlab_grid* g, const emlab_flux_plane* planes, int n_planes, double* out) {
     if (int rc = require_grid(g)) return rc;
     EMLAB_REQUIRE(planes && out && n_planes >= 0, "bad flux arguments");

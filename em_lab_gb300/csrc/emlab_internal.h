@@ -15,6 +15,7 @@
 
 #include <vector>
 
+#include "emlab.h"
 #include "emlab_math.h"
 
 namespace emlab {
@@ -107,6 +108,8 @@ void launch_dft_sample(const MonitorArgs& m, const int* box, int points, float* 
 void launch_dft_fold(const float* blk, int T, int points, int nf, const float2* W, const double* omega, long long n0,
                      double dt, double* X, cudaStream_t s);
 void launch_dft_to_phasor(const double* X, int points, int f, double scale, float* ph, cudaStream_t s);
+void launch_raymarch(const MonitorArgs& m, const float* sigma, const float* eps, const emlab_render_params& p,
+                     unsigned char* img, cudaStream_t s);
 // tensor-core fold (dft_tc.cu): MMA N for nf frequencies, host twiddle tables (hi, lo) in the
 // kernel's shared-memory layout, and the launcher (false if nf is too large or set-up failed)
 int dft_tc_mma_n(int nf);

@@ -79,6 +79,7 @@ def load_library() -> C.CDLL:
         "emlab_probe_gather": ([P, ip, I, fp], I),
         "emlab_flux_planes": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
+        "emlab_render": ([P, C.POINTER(abi.RenderParams), C.POINTER(C.c_ubyte)], I),
         "emlab_lines_configure": ([P, ip, I, ip, fp, I, F, F], I),
         "emlab_lines_read": ([P, fp, fp], I),
         "emlab_debug_expf": ([fp, fp, SZ], I),
@@ -398,6 +399,12 @@ class SimulationGrid:
         out = np.zeros(max(1, n), np.float64)
         _check(self._lib.emlab_flux_planes_noalloc(self._h, arr, n, out.ctypes.data_as(C.POINTER(C.c_double))))
         return out[:n]
+
+    def render(self, params: abi.RenderParams) -> np.ndarray:
+        """Ray-marched RGBA8 image of the current fields, (height, width, 4), rows bottom-up."""
+        out = np.zeros((params.height, params.width, 4), np.uint8)
+        _check(self._lib.emlab_render(self._h, C.byref(params), out.ctypes.data_as(C.POINTER(C.c_ubyte))))
+        return out
 
     def lines_configure(self, quantities, terms, weights, wavelength, averaging_periods=4.0):
         q = np.ascontiguousarray(np.asarray(quantities, np.int32).reshape(-1, 4))

@@ -7,7 +7,9 @@ Follows the unattended `--frames` mode of the reference application (src/Main.cp
 need every step run on the device inside the step), measures probes and fluxes every second frame,
 evaluates the far field, port readings and sweep every 50th frame, prints the instrument report
 every 100th frame and once more after the last frame. Exit code 2 = non-finite fields, 3 = script
-error. There is no window and no renderer: the render timing is reported as 0.
+error. There is no window: with --screenshot the last frame's volume pass is ray-marched on the GPU
+(render.py, csrc/render.cu) at --width x --height and saved as a BMP (Main.cpp:814-829, 1122-1128);
+the render timing is that pass, else 0.
 """
 from __future__ import annotations
 
@@ -49,7 +51,30 @@ def print_header(res, grid, script_name):
             print(f"  {'':<8s} {p.label:<24s} = {_value_string(p)}")
 
 
-def run(script, frames, overrides=None, steps_per_frame=None, quiet=False):
+def view_settings(sc):
+    """The scene's view{} hints with the signed-mode axis defaulting to the first source's dominant
+    polarization component (Main.cpp:542-569)."""
+    v = dict(sc.view)
+    if "component" not in v and sc.sources:
+        px, py, pz = (abs(float(c)) for c in sc.sources[0].polarization)
+        v["component"] = 0 if (px >= py and px >= pz) else (1 if py >= pz else 2)
+    return v
+
+
+def screenshot(grid, sc, path, width, height):
+    """Ray-marches the current fields at width x height and writes a BMP; returns the render ms."""
+    from .render import render_params, write_bmp
+    params = render_params(grid.size(), view_settings(sc), width, height)
+    t0 = time.perf_counter()
+    img = grid.render(params)
+    ms = (time.perf_counter() - t0) * 1e3
+    write_bmp(path, img)
+    print(f"Saved screenshot {path}")
+    return ms
+
+
+def run(script, frames, overrides=None, steps_per_frame=None, quiet=False, screenshot_path=None,
+        width=1920, height=1080):
     """Runs `script` for `frames` frames; returns (exit code, Instruments)."""
     from . import SimulationGrid
     from .instruments import NO_INSTRUMENTS_HINT, Instruments
@@ -100,7 +125,10 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False):
                 inst.evaluate_sweep()
             if not inst.empty():
                 inst.print_report()
-            print(f"GPU timings: sim {sim_ms:.3f} ms/frame ({spf} steps), render 0.000 ms")
+            render_ms = 0.0
+            if screenshot_path:
+                render_ms = screenshot(grid, sc, screenshot_path, width, height)
+            print(f"GPU timings: sim {sim_ms:.3f} ms/frame ({spf} steps), render {render_ms:.3f} ms")
     finite = grid.check_finite()
     inst.close()
     grid.close()
@@ -113,6 +141,9 @@ def main(argv=None):
     ap.add_argument("--set", action="append", default=[], metavar="NAME=VALUE", help="override a script param{}")
     ap.add_argument("--frames", type=int, default=100, help="run this many frames, then exit")
     ap.add_argument("--steps", type=int, default=2, help="simulation steps per frame (the scene's view{} wins)")
+    ap.add_argument("--width", type=int, default=1920, help="screenshot width")
+    ap.add_argument("--height", type=int, default=1080, help="screenshot height")
+    ap.add_argument("--screenshot", metavar="FILE.bmp", help="save the last frame of the run")
     a = ap.parse_args(argv)
     overrides = {}
     for kv in a.set:
@@ -121,7 +152,8 @@ def main(argv=None):
             continue
         k, v = kv.split("=", 1)
         overrides[k] = v
-    code, _ = run(a.script, max(a.frames, 1), overrides, min(max(a.steps, 0), 64))
+    code, _ = run(a.script, max(a.frames, 1), overrides, min(max(a.steps, 0), 64), screenshot_path=a.screenshot,
+                  width=max(a.width, 1), height=max(a.height, 1))
     return code
 
 

@@ -241,9 +241,30 @@ class Args:
         for k in list(self.t.hash.keys()):
             if isinstance(k, str):
                 if k not in self.keys:
-                    self.eng.warn(f"{self.what}: unknown field '{k}' ignored")
+                    self.eng.warn(f"{self.what}: unknown field '{k}' ignored{suggestion(k, self.keys)}")
             else:
                 self.eng.warn(f"{self.what}: positional (unnamed) values are ignored; use key = value")
+
+
+def edit_distance(a: str, b: str) -> int:
+    """Levenshtein distance (ScriptEngine.cpp:47-57)."""
+    prev = list(range(len(b) + 1))
+    for i in range(1, len(a) + 1):
+        cur = [i] + [0] * len(b)
+        for j in range(1, len(b) + 1):
+            cur[j] = min(prev[j] + 1, cur[j - 1] + 1, prev[j - 1] + (a[i - 1] != b[j - 1]))
+        prev = cur
+    return prev[len(b)]
+
+
+def suggestion(word: str, candidates) -> str:
+    """' (did you mean 'x'?)' for the closest candidate within edit distance 2 (ScriptEngine.cpp:59-70)."""
+    best, best_d = "", 3
+    for c in candidates:
+        d = edit_distance(word.lower(), c.lower())
+        if d < best_d:
+            best_d, best = d, c
+    return f" (did you mean '{best}'?)" if best else ""
 
 
 def _parse_axis(s: str):
@@ -342,7 +363,8 @@ class ScriptEngine:
         elif type(v) is str:
             name = v.lower()
             if name not in self.materials:
-                a.fail(f"unknown material '{v}'. Define it with material{{ name = \"{v}\", epsilon_r = ..., ... }}")
+                a.fail(f"unknown material '{v}'{suggestion(v, list(self.materials))}. "
+                       f"Define it with material{{ name = \"{v}\", epsilon_r = ..., ... }}")
             spec = self.materials[name]
         elif type(v) is LuaTable:
             m = Args(self, "material (inline)", ["epsilon_r", "sigma", "conductivity", "loss_tangent", "name"], v)
@@ -683,8 +705,37 @@ class ScriptEngine:
     def api_view(self, t=None, *r):
         a = Args(self, "view", ["mode", "component", "gain", "gain_e", "gain_b", "exposure", "density", "step",
                                 "steps_per_frame", "distance", "yaw", "pitch", "target", "overlay", "metal_opacity"], t)
+        v = self.view
+        m = a.opt_str("mode")
+        if m is not None:
+            modes = ["fields", "e", "b", "poynting", "signed"]
+            if m.lower() not in modes:
+                a.fail("mode must be one of \"fields\", \"e\", \"b\", \"poynting\", \"signed\""
+                       + suggestion(m, modes))
+            v["mode"] = modes.index(m.lower())
+        if a.has("component"):
+            v["component"] = a.axis("component", 2)
+        g = a.opt_num("gain")
+        if g is not None:
+            v["gain_e"] = v["gain_b"] = float(g)
+        for key, name in (("gain_e", "gain_e"), ("gain_b", "gain_b"), ("exposure", "exposure"),
+                          ("density", "density"), ("step", "step")):
+            x = a.opt_num(key)
+            if x is not None:
+                v[name] = float(x)
+        x = a.opt_num("metal_opacity")
+        if x is not None:
+            v["metal_opacity"] = min(max(float(x), 0.0), 1.0)
         if a.has("steps_per_frame"):
-            self.view["steps_per_frame"] = min(max(a.integer("steps_per_frame", 2), 1), 64)
+            v["steps_per_frame"] = min(max(a.integer("steps_per_frame", 2), 1), 64)
+        v["distance"] = float(a.num("distance", v.get("distance", 3.0)))
+        v["yaw"] = float(a.num("yaw", v.get("yaw", -55.0)))
+        v["pitch"] = float(a.num("pitch", v.get("pitch", 30.0)))
+        t = a.opt_vec("target")
+        if t is not None:
+            v["target"] = tuple(float(c) for c in t)
+        if a.has("overlay"):
+            v["overlay"] = a.boolean("overlay", True)
         a.check_unknown()
 
     def api_material(self, t=None, *r):

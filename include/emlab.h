@@ -229,6 +229,25 @@ int emlab_ntff_dft_read(emlab_grid* g, double* out);
  * (the amplitude of a steady tone): out[2d] = |N_perp - r x L|^2, out[1] = radiated power. */
 int emlab_ntff_dft_evaluate(emlab_grid* g, int f, const float* directions, int n_dirs, float* out);
 
+/* ---- volume rendering: VolumeRenderer (src/VolumeRenderer.cpp:66-118, shaders/raymarch.frag) */
+/* Camera and look of one rendered frame. inv_view_proj: inverse of projection * view, column-
+ * major (glm layout); world space is the lattice mapped to [-1, 1] along the longest axis
+ * (VolumeRenderer::latticeToWorld). mode: 0 E + B, 1 E, 2 B, 3 |E x B|, 4 signed E component. */
+typedef struct emlab_render_params {
+    int width, height;
+    float inv_view_proj[16];
+    float cam_pos[3];
+    float vol_min[3], vol_size[3];     /* world box of the whole grid */
+    float clip_min[3], clip_max[3];    /* world box actually marched (cutaway) */
+    float step_voxels, gain_e, gain_b, density, emission, material_opacity, exposure;
+    int mode, signed_axis;
+} emlab_render_params;
+/* Ray-marches the current fields into rgba (width * height * 4 bytes, rows bottom-up as
+ * glReadPixels returns them); the cell sigma / eps_r of the uploaded MaterialVolume are drawn as
+ * metal / dielectric surfaces. The headless replacement of the reference's on-screen renderer and
+ * of --screenshot. */
+int emlab_render(emlab_grid* g, const emlab_render_params* params, unsigned char* rgba);
+
 /* ---- probes and flux: FieldAnalyzer (src/FieldAnalyzer.hpp:73-130) ----------------------- */
 /* probe_gather.comp (FieldAnalyzer.cpp:274-303): origins are 4 ints per probe (xyz used); out
  * receives 54 texels (27 E, then 27 B, 4 floats each) per probe. */

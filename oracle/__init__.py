@@ -319,3 +319,24 @@ def load_scene(target, scene):
     m = scene.materials
     target.upload_materials(m.sigma, m.epsilon_r, scene.edges, scene.wires)
     target.set_sources(scene.sources)
+
+
+def render(e_rgba, b_rgba, params: abi.RenderParams, ref: bool = False) -> np.ndarray:
+    """The volume pass (raymarch.frag) on the CPU: the restatement (oracle_render.h) or, with
+    ref=True, the reference's own shader compiled through the GLSL shim (oracle/_ref). e_rgba and
+    b_rgba are (nz, ny, nx, 4) float32 textures; returns (height, width, 4) uint8, bottom row first."""
+    e = np.ascontiguousarray(e_rgba, np.float32)
+    b = np.ascontiguousarray(b_rgba, np.float32)
+    assert e.shape == b.shape and e.ndim == 4 and e.shape[3] == 4
+    nz, ny, nx = e.shape[:3]
+    lib = load_ref() if ref else load()
+    fn = lib.oracle_render_ref if ref else lib.oracle_render
+    fp = C.POINTER(C.c_float)
+    fn.argtypes = [fp, fp, C.c_int, C.c_int, C.c_int, C.POINTER(abi.RenderParams), C.POINTER(C.c_ubyte)]
+    fn.restype = C.c_int
+    out = np.zeros((params.height, params.width, 4), np.uint8)
+    rc = fn(e.ctypes.data_as(fp), b.ctypes.data_as(fp), nx, ny, nz, C.byref(params),
+            out.ctypes.data_as(C.POINTER(C.c_ubyte)))
+    if rc != 0:
+        raise ValueError("oracle render: bad arguments")
+    return out

@@ -2,8 +2,8 @@
 
 Reads the shader files where they lie in the reference tree (default /root/reference/shaders, or
 $EMLAB_REFERENCE/shaders), rewrites the GLSL-only syntax mechanically (resource declarations ->
-globals, `out` parameters -> references, swizzles -> calls, float literals -> float suffix,
-array constructors -> brace lists) into oracle/_ref/*.hpp, and builds oracle/_ref/libemlab_ref.so
+globals, fragment inputs/outputs -> per-thread globals, `out` parameters -> references, swizzles
+-> calls, `.a` -> `.w`, float literals -> float suffix, array constructors -> brace lists) into oracle/_ref/*.hpp, and builds oracle/_ref/libemlab_ref.so
 from oracle/ref_driver.cpp, which runs every dispatch of SimulationGrid::step and the monitors over
 the CPU with those shader bodies and the GLSL semantics of oracle/glsl_shim.hpp. Nothing under
 oracle/_ref is committed. Without the reference tree the recipe does nothing.
@@ -24,7 +24,7 @@ LIB = OUT / "libemlab_ref.so"
 SHADERS = ["common.glsl", "field_sampling.glsl", "ntff_common.glsl", "update_B.comp", "update_E.comp",
            "apply_sources.comp", "clear_fields.comp", "port_accumulate.comp", "probe_gather.comp",
            "poynting_flux.comp", "ntff_accumulate.comp", "ntff_pattern.comp", "ntff_reduce.comp",
-           "line_accumulate.comp"]
+           "line_accumulate.comp", "raymarch.frag"]
 
 
 def reference_shaders() -> Path | None:
@@ -64,6 +64,7 @@ def transform(text: str) -> str:
         s = re.sub(r'#include\s+"([\w.]+)"', r'#include "\1.hpp"', s)
         if re.match(r"\s*layout\s*\(\s*local_size", s):
             continue
+        s = re.sub(r"layout\s*\(\s*location[^)]*\)\s*(?:in|out)\s+(\w+)\s+(\w+)\s*;", r"thread_local \1 \2;", s)
         s = re.sub(r"layout\s*\(\s*std430[^)]*\)\s*(?:(?:readonly|writeonly|restrict)\s+)*buffer\s+\w+\s*\{\s*(\w+)\s+"
                    r"(\w+)\s*\[\s*\]\s*;\s*\}\s*;", r"\1* \2 = nullptr;", s)
         s = re.sub(r"layout\s*\([^)]*\)\s*uniform\s+(?:restrict\s+)?(\w+)\s+(\w+)\s*;", r"\1 \2;", s)
@@ -71,7 +72,8 @@ def transform(text: str) -> str:
         s = re.sub(r"^(\s*)shared\s+", r"\1thread_local ", s)
         s = re.sub(r"\bout\s+(\w+)\s+(\w+)", r"\1& \2", s)
         code, sep, comment = s.partition("//")
-        code = re.sub(r"\.(xyz|xy|zw)\b(?!\s*\()", r".\1()", code)
+        code = re.sub(r"\.(xyz|xy|zw|rgb)\b(?!\s*\()", r".\1()", code)
+        code = re.sub(r"\.a\b(?!\s*\()", ".w", code)
         code = _FLOAT.sub(lambda m: m.group(1) + "f", code)
         lines.append(code + sep + comment)
     return _array_ctor("\n".join(lines)) + "\n"
@@ -83,6 +85,7 @@ def build(force: bool = False, verbose: bool = False) -> Path | None:
         return None
     OUT.mkdir(parents=True, exist_ok=True)
     deps = [HERE / "ref_driver.cpp", HERE / "glsl_shim.hpp", HERE / "emlab_oracle.c", HERE / "oracle_impl.h",
+            HERE / "oracle_render.h",
             HERE.parent / "em_lab_gb300" / "csrc" / "emlab_math.h", Path(__file__)]
     changed = force or not LIB.exists()
     for name in SHADERS:

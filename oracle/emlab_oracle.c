@@ -13,6 +13,8 @@
  * -ffp-contract=off so that no multiply-add is fused; OpenMP parallelises the cell loops (each
  * cell's result does not depend on the thread count).
  *
+ * oracle_render.h restates the volume pass of the screenshot path (shaders/raymarch.frag).
+ *
  * Pinning: oracle/build_ref.py compiles the reference's own shader files (from the reference tree)
  * as C++ through a GLSL shim into oracle/_ref; tests/test_oracle_ref.py checks this restatement
  * against them bit for bit, and tests/golden/ holds fixtures produced by that build.
@@ -269,3 +271,6 @@ double oracle_signal(const emlab_source* s, double tAbs) {
 #undef R
 #undef OR_DOUBLE
 #undef NAME
+
+/* the volume pass of the screenshot path (shaders/raymarch.frag) */
+#include "oracle_render.h"

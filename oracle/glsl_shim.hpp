@@ -66,11 +66,15 @@ struct vec4 {
     explicit vec4(float s) : x(s), y(s), z(s), w(s) {}
     vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
     vec4(const vec3& v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
+    vec4(const vec2& v, float c, float d) : x(v.x), y(v.y), z(c), w(d) {}
     float& operator[](int i) & { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
     float operator[](int i) const& { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
     Swz3 xyz() & { return Swz3{&x, &y, &z}; }
     vec3 xyz() const& { return vec3(x, y, z); }
     vec3 xyz() && { return vec3(x, y, z); }
+    Swz3 rgb() & { return Swz3{&x, &y, &z}; }
+    vec3 rgb() const& { return vec3(x, y, z); }
+    vec3 rgb() && { return vec3(x, y, z); }
     Swz2 xy() & { return Swz2{&x, &y}; }
     vec2 xy() const& { return vec2(x, y); }
     vec2 xy() && { return vec2(x, y); }
@@ -134,6 +138,8 @@ inline vec3 operator-(const vec3& a) { return vec3(-a.x, -a.y, -a.z); }
 inline vec3& operator+=(vec3& a, const vec3& b) { a = a + b; return a; }
 inline vec3& operator-=(vec3& a, const vec3& b) { a = a - b; return a; }
 inline vec3& operator*=(vec3& a, const vec3& b) { a = a * b; return a; }
+inline vec3& operator*=(vec3& a, float s) { a = a * s; return a; }
+inline vec3& operator+=(vec3& a, float s) { a = a + s; return a; }
 
 #define GLSL_V4_OP(OP)                                                                                    \
     inline vec4 operator OP(const vec4& a, const vec4& b) {                                               \
@@ -196,6 +202,22 @@ inline bool all(const bvec3& b) { return b.x && b.y && b.z; }
 inline vec2 unpackHalf2x16(uint v) {
     return vec2(emlab_half_to_float((uint16_t)(v & 0xffffu)), emlab_half_to_float((uint16_t)(v >> 16)));
 }
+// fragment-stage built-ins used by raymarch.frag
+inline float clamp(float v, float lo, float hi) { return min(max(v, lo), hi); }
+inline float dot(const vec2& a, const vec2& b) { return a.x * b.x + a.y * b.y; }
+inline float length(const vec3& v) { return sqrtf(dot(v, v)); }
+inline vec3 normalize(const vec3& v) {
+    const float l = length(v);
+    return vec3(v.x / l, v.y / l, v.z / l);
+}
+inline float fract(float x) { return x - floorf(x); }
+inline float smoothstep(float e0, float e1, float x) {
+    const float t = clamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
+    return t * t * (3.0f - 2.0f * t);
+}
+inline vec3 mix(const vec3& x, const vec3& y, float a) { return x * (1.0f - a) + y * a; }
+inline float pow(float x, float y) { return powf(x, y); }
+inline vec3 pow(const vec3& x, const vec3& y) { return vec3(powf(x.x, y.x), powf(x.y, y.y), powf(x.z, y.z)); }
 // Workgroup barrier: ref_driver.cpp runs a workgroup's invocations as fibers and installs the hook
 // that suspends the calling invocation until all of them have arrived.
 extern thread_local void (*g_barrier_hook)();
@@ -235,10 +257,41 @@ inline void imageStore(const image3D& t, const ivec3& p, const vec4& v) {
     q[0] = v.x, q[1] = v.y, q[2] = v.z, q[3] = v.w;
 }
 
+// texture(sampler3D, uvw) with a linear filter and clamp-to-edge: the eight texels around
+// uvw * size - 0.5, weights multiplied x, y, z, accumulated z-, y-, x-major.
+inline vec4 texture(const sampler3D& t, const vec3& uvw) {
+    const float px = uvw.x * (float)t.size.x - 0.5f, py = uvw.y * (float)t.size.y - 0.5f,
+                pz = uvw.z * (float)t.size.z - 0.5f;
+    const float fx = floorf(px), fy = floorf(py), fz = floorf(pz);
+    const float ax = px - fx, ay = py - fy, az = pz - fz;
+    const int ix = (int)fx, iy = (int)fy, iz = (int)fz;
+    vec4 r(0.0f);
+    for (int dz = 0; dz <= 1; ++dz)
+        for (int dy = 0; dy <= 1; ++dy)
+            for (int dx = 0; dx <= 1; ++dx) {
+                const float w = (dx ? ax : 1.0f - ax) * (dy ? ay : 1.0f - ay) * (dz ? az : 1.0f - az);
+                const ivec3 p(clamp(ix + dx, 0, t.size.x - 1), clamp(iy + dy, 0, t.size.y - 1),
+                              clamp(iz + dz, 0, t.size.z - 1));
+                r += w * texelFetch(t, p, 0);
+            }
+    return r;
+}
+
+struct mat4 {
+    vec4 c[4];  // columns
+};
+inline vec4 operator*(const mat4& m, const vec4& v) {
+    return vec4(m.c[0].x * v.x + m.c[1].x * v.y + m.c[2].x * v.z + m.c[3].x * v.w,
+                m.c[0].y * v.x + m.c[1].y * v.y + m.c[2].y * v.z + m.c[3].y * v.w,
+                m.c[0].z * v.x + m.c[1].z * v.y + m.c[2].z * v.z + m.c[3].z * v.w,
+                m.c[0].w * v.x + m.c[1].w * v.y + m.c[2].w * v.z + m.c[3].w * v.w);
+}
+
 // ---- invocation ids (per OpenMP thread) -----------------------------------------------------------
 extern thread_local uvec3 gl_GlobalInvocationID;
 extern thread_local uvec3 gl_WorkGroupID;
 extern thread_local uint gl_LocalInvocationIndex;
 extern thread_local uvec3 gl_NumWorkGroups;
+extern thread_local vec4 gl_FragCoord;
 
 }  // namespace glsl

@@ -68,6 +68,10 @@ namespace sh_ntff_red {
 namespace sh_lines {
 #include "line_accumulate.comp.hpp"
 }
+thread_local vec4 gl_FragCoord;
+namespace sh_raymarch {
+#include "raymarch.frag.hpp"
+}
 }  // namespace glsl
 
 using namespace glsl;
@@ -623,6 +627,49 @@ void oracle_flux_planes_ref(void* h, const emlab_flux_plane* planes, int n, doub
         for (float f : partials) sum += (double)f;
         out[pi] = sum;
     }
+}
+
+// The volume pass (raymarch.frag) over the reference's two RGBA32F textures, one fragment per pixel
+// centre of a width x height target (bottom row first), uniforms as VolumeRenderer::render sets
+// them (src/VolumeRenderer.cpp:96-112), the RGBA8 target's unorm conversion rounding to nearest.
+int oracle_render_ref(const float* e_rgba, const float* b_rgba, int nx, int ny, int nz, const emlab_render_params* p,
+                      unsigned char* rgba) {
+    namespace S = sh_raymarch;
+    if (!e_rgba || !b_rgba || !p || !rgba || nx <= 0 || ny <= 0 || nz <= 0 || p->width <= 0 || p->height <= 0 ||
+        !std::isfinite(p->step_voxels))
+        return -1;
+    for (int c = 0; c < 4; ++c)
+        S::uInvViewProj.c[c] = vec4(p->inv_view_proj[4 * c], p->inv_view_proj[4 * c + 1], p->inv_view_proj[4 * c + 2],
+                                    p->inv_view_proj[4 * c + 3]);
+    S::uEField = sampler3D{e_rgba, ivec3(nx, ny, nz)};
+    S::uBField = sampler3D{b_rgba, ivec3(nx, ny, nz)};
+    S::uCamPos = vec3(p->cam_pos[0], p->cam_pos[1], p->cam_pos[2]);
+    S::uVolMin = vec3(p->vol_min[0], p->vol_min[1], p->vol_min[2]);
+    S::uVolSize = vec3(p->vol_size[0], p->vol_size[1], p->vol_size[2]);
+    S::uClipMin = vec3(p->clip_min[0], p->clip_min[1], p->clip_min[2]);
+    S::uClipMax = vec3(p->clip_max[0], p->clip_max[1], p->clip_max[2]);
+    S::uGridSize = vec3((float)nx, (float)ny, (float)nz);
+    S::uStepVoxels = std::clamp(p->step_voxels, 0.1f, 4.0f);
+    S::uGainE = p->gain_e;
+    S::uGainB = p->gain_b;
+    S::uDensity = p->density;
+    S::uEmission = p->emission;
+    S::uMaterialOpacity = p->material_opacity;
+    S::uExposure = p->exposure;
+    S::uMode = p->mode;
+    S::uSignedAxis = std::clamp(p->signed_axis, 0, 2);
+    const int w = p->width, h = p->height;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const float fx = (float)x + 0.5f, fy = (float)y + 0.5f;
+            gl_FragCoord = vec4(fx, fy, 0.5f, 1.0f);
+            S::vNdc = vec2(fx / (float)w * 2.0f - 1.0f, fy / (float)h * 2.0f - 1.0f);
+            S::main();
+            unsigned char* o = rgba + 4 * ((size_t)y * w + x);
+            for (int k = 0; k < 4; ++k) o[k] = (unsigned char)lrintf(std::clamp(S::oColor[k], 0.0f, 1.0f) * 255.0f);
+        }
+    return 0;
 }
 
 }  // extern "C"

@@ -7,7 +7,9 @@ against it where the reference tree is absent.
 Each fixture is a seeded scene from em_lab_gb300.configs.random_scene stepped N times by the
 reference shaders (emlab_expf as exp): the six field components, the port series and phasors, the
 far-field phasors, the coax-line phasors, probe blocks, flux sums and the far-field pattern of 64
-directions.
+directions. raymarch.npz holds frames of the reference's volume pass (shaders/raymarch.frag through
+the same shim) over the textures of a seeded scene: the render parameters as raw bytes and the
+RGB of each frame.
 """
 import hashlib
 import os
@@ -74,9 +76,56 @@ def run(o, sc, steps):
     return out
 
 
+RENDER_SCENE = dict(size=(20, 16, 14), pml=3, seed=4)
+RENDER_STEPS = 40
+
+
+def render_textures():
+    """E and B textures (rgb = field, alpha = cell sigma / eps_r) of the render fixture's scene."""
+    sc = configs.random_scene(**RENDER_SCENE)
+    o = oracle.Oracle(sc.grid, "f32")
+    oracle.load_scene(o, sc)
+    o.step(RENDER_STEPS)
+    f = o.read_components()
+    e = np.stack([f[0], f[1], f[2], sc.materials.sigma], axis=-1).astype(np.float32)
+    b = np.stack([f[3], f[4], f[5], sc.materials.epsilon_r], axis=-1).astype(np.float32)
+    return e, b
+
+
+def render_views(size, gain):
+    """(name, view hints, width, height): every mode, a cutaway, a close and a far camera."""
+    v = []
+    for mode in range(5):
+        v.append((f"mode{mode}", {"mode": mode, "gain": gain, "component": 1, "metal_opacity": 0.7}, 48, 32))
+    v.append(("inside", {"mode": 0, "gain": gain, "distance": 0.3, "yaw": 20.0, "pitch": -10.0, "step": 0.3}, 40, 24))
+    v.append(("far", {"mode": 0, "gain": gain * 4, "distance": 9.0, "pitch": 75.0, "exposure": 3.0}, 33, 21))
+    return v
+
+
+def make_render_golden():
+    from em_lab_gb300 import render
+    e, b = render_textures()
+    size = (e.shape[2], e.shape[1], e.shape[0])
+    gain = float(1.0 / (0.25 * np.abs(e[..., :3]).max()))
+    out = {}
+    for name, view, w, h in render_views(size, gain):
+        p = render.render_params(size, view, w, h)
+        if name == "mode3":  # cutaway: the upper half of x
+            p.clip_min[0] = p.vol_min[0] + 0.5 * p.vol_size[0]
+        img = oracle.render(e, b, p, ref=True)
+        out[f"{name}_params"] = np.frombuffer(bytes(p), np.uint8)
+        out[f"{name}_rgb"] = img[..., :3]
+    out["steps"] = np.array(RENDER_STEPS)
+    np.savez_compressed(os.path.join(OUT, "raymarch.npz"), **out)
+    print("raymarch written")
+
+
 def main():
     if not oracle.ref_available():
         sys.exit("oracle/_ref is not built: run python oracle/build_ref.py (needs the reference tree)")
+    if "--render-only" in sys.argv:
+        make_render_golden()
+        return
     for name, kw, steps, full in CASES:
         sc = configs.random_scene(**kw)
         o = oracle.Oracle(sc.grid, "ref")
@@ -89,6 +138,7 @@ def main():
                 out[f"mid{c}"] = f[f.shape[0] // 2]
         np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
         print(name, "written")
+    make_render_golden()
 
 
 if __name__ == "__main__":

@@ -73,3 +73,19 @@ def test_coax_matched_line_measures_z0(capsys):
     assert r["valid"]
     assert abs(r["z0m"] - 50.0) < 2.5            # the line's own V+/I+ against the lattice Z0
     assert abs(r["gamma"]) < 0.1                 # matched resistive load at the far end
+
+
+def test_screenshot_of_last_frame(tmp_path, capsys):
+    """--screenshot: the last frame ray-marched on the GPU and saved as a 24-bit BMP."""
+    shot = tmp_path / "frame.bmp"
+    code = headless.main(["--script", os.path.join(SCENES, "sphere_dipole.lua"), "--frames", "30",
+                          "--screenshot", str(shot), "--width", "161", "--height", "90"])
+    out = capsys.readouterr().out
+    assert code == 0 and f"Saved screenshot {shot}" in out
+    data = shot.read_bytes()
+    row = (161 * 3 + 3) & ~3
+    assert data[:2] == b"BM" and len(data) == 54 + 90 * row
+    pix = np.frombuffer(data[54:], np.uint8).reshape(90, row)[:, :161 * 3].reshape(90, 161, 3)
+    # the dipole's field glows over the dark background: some pixels are far brighter than the corner
+    assert int(pix.max()) >= int(pix[0, 0].max()) + 30
+    assert "render 0.000 ms" not in out

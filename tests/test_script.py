@@ -2,6 +2,7 @@
 overrides, thin-wire terms, sources, ports and monitors) against the same scene built directly
 with the scene builder, plus the API's validation and error messages."""
 import os
+import re
 
 import numpy as np
 import pytest
@@ -115,11 +116,13 @@ def test_array_and_cage():
     ("dipole { length = 4 }", "thin-wire dipole needs length >= 5"),
     ("wire { from = {1, 1, 1}, to = {2, 2, 1} }", "differ along exactly one axis"),
     ("radar {}", "radar{}: not supported"),
+    ("view { mode = 'poyntng' }", "mode must be one of \"fields\", \"e\", \"b\", \"poynting\", \"signed\" "
+                                  "(did you mean 'poynting'?)"),
+    ("box { min = {1, 1, 1}, max = {2, 2, 2}, material = 'coper' }", "unknown material 'coper' (did you mean 'copper'?)"),
     ("local v = vec(1, 2, 3) + 'x'", "arithmetic"),
 ])
 def test_errors(src, msg):
-    with pytest.raises(ScriptError, match=msg.replace("(", r"\(").replace(")", r"\)").replace("{", r"\{")
-                       .replace("}", r"\}")):
+    with pytest.raises(ScriptError, match=re.escape(msg)):
         run(src)
 
 
@@ -151,6 +154,22 @@ def test_warnings():
     assert "unknown field 'colour'" in w
     assert "lies inside the absorbing boundary layer" in w
     assert "no conductor touches the base of the feed gap" in w
+
+
+def test_view_hints():
+    res = run("""
+        scene { size = 48 }
+        view { mode = "Signed", component = "y", gain = 3, gain_b = 5, exposure = 2, density = 0.5, step = 0.4,
+               metal_opacity = 1.7, steps_per_frame = 300, distance = 2, yaw = 10, target = {1, 2, 3}, overlay = false }
+        view { pitch = 45 }
+    """)
+    v = res.scene.view
+    assert v["mode"] == 4 and v["component"] == 1
+    assert (v["gain_e"], v["gain_b"], v["exposure"], v["density"], v["step"]) == (3.0, 5.0, 2.0, 0.5, 0.4)
+    assert v["metal_opacity"] == 1.0 and v["steps_per_frame"] == 64
+    assert (v["distance"], v["yaw"], v["pitch"], v["target"], v["overlay"]) == (2.0, 10.0, 45.0, (1.0, 2.0, 3.0), False)
+    res = run("scene { size = 48 } view { colour = 1 }")
+    assert "view: unknown field 'colour' ignored" in " | ".join(res.warnings)
 
 
 def test_coax_builder_and_monitor_layout():
