@@ -288,14 +288,85 @@ def run_reference(args):
     return 0
 
 
+def run_batched(args):
+    """--workload batched: the batched antenna sweep (256 seeded scenes, cube edges 48-160, 8-cell
+    absorber, thin-wire dipole or monopole over ground with a 50-ohm Gaussian-pulse feed, one random
+    dielectric sphere or box), every scene run to -60 dB port ring-down and its 128-point Z(f) sweep
+    evaluated. value = sweeps per hour of the batched path (scene stacks, one launch per pass for all
+    scenes of a cross-section); beside it the same scenes one grid at a time."""
+    import torch
+    from em_lab_gb300 import batch, configs, launch_count
+
+    rank, world, local = _rank_env()
+    if world > 1 and rank != 0:
+        return 0  # one GPU per run in this mode
+    torch.cuda.set_device(local)
+    n = args.scenes
+    t0 = time.perf_counter()
+    scenes = configs.batched_scenes(n, seed=args.seed)
+    build_s = time.perf_counter() - t0
+    # warm-up: a few chunks of a small batch (kernel loading, allocator)
+    warm = batch.BatchRunner([configs.batched_scene(args.seed + 1, i) for i in range(4)], max_steps=64 * args.warmup)
+    warm.run()
+    for gr in warm.groups:
+        gr.stack.close()
+    l0 = launch_count()
+    runner = batch.BatchRunner(scenes, chunk=64)
+    with ClockSampler(local) as clk:
+        results = runner.run()
+    launches = launch_count() - l0
+    done = sum(r.done for r in results)
+    steps = [r.steps for r in results]
+    scene_cells = [int(np.prod(sc.grid.size)) for sc in scenes]
+    useful = float(sum(c * st for c, st in zip(scene_cells, steps)))
+    value = done / runner.wall_s * 3600.0
+    single = None
+    if not args.no_single:
+        ts = []
+        sample = scenes if args.single_all else scenes[:: max(1, n // 32)]
+        for sc in sample:
+            tm = {}
+            batch.run_single(sc, chunk=64, timing=tm)
+            ts.append(tm)
+        run_s = sum(t["run_s"] for t in ts)
+        cells_single = sum(int(np.prod(sc.grid.size)) * t["steps"] for sc, t in zip(sample, ts))
+        single = {"scenes": len(sample), "sweeps_per_hour": len(sample) / run_s * 3600.0,
+                  "mcells_per_s": cells_single / run_s / 1e6, "setup_s_per_scene": sum(t["setup_s"] for t in ts) / len(ts),
+                  "note": "the same scenes, one SimulationGrid each, same ring-down rule; stepping + sweep timed, set-up excluded"}
+    line = {
+        "metric": "Z(f) sweeps/hr (batched, run to -60 dB port ring-down)", "value": value, "unit": "sweeps/hr",
+        "n_gpus": 1, "steps": int(max(steps)), "warmup": args.warmup, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batched antenna sweep: {n} seeded scenes (seed {args.seed}), cube edges 48-160 cells, "
+                               "8-cell absorber, thin-wire dipole or monopole over ground, 50-ohm Gaussian-pulse feed, "
+                               "one random dielectric sphere or box, 128-point Z(f) sweep per scene",
+                   "groups": len(runner.groups), "chunk_steps": 64, "l2": "inputs larger than L2 (stack state > 129 MB)"},
+        "scenes_done": done, "scenes_rung_down": sum(r.rung_down for r in results), "scene_steps": {"min": int(min(steps)), "median": int(np.median(steps)), "max": int(max(steps))},
+        "mcells_per_s": useful / runner.wall_s / 1e6,
+        "setup_s": {"scene_build": build_s, "stack_upload": runner.setup_s},
+        "single_grid": single,
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    for gr in runner.groups:
+        gr.stack.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="plain_large", choices=["plain_large", "plain_small"],
-                    help="plain_large: the 512^3 dipole + blocks workload (default); plain_small: 128^3 sphere")
+    ap.add_argument("--workload", default="plain_large", choices=["plain_large", "plain_small", "batched"],
+                    help="plain_large: the 512^3 dipole + blocks workload (default); plain_small: 128^3 sphere; "
+                         "batched: 256 antenna scenes to port ring-down (sweeps/hr)")
+    ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
+    ap.add_argument("--seed", type=int, default=2024, help="batched: scene seed")
+    ap.add_argument("--no-single", action="store_true", help="batched: skip the one-grid-per-scene comparison")
+    ap.add_argument("--single-all", action="store_true", help="batched: compare on every scene, not a sample")
     ap.add_argument("--size", type=int, default=512, help="edge of the plain_large grid")
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
     ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 32, 64, 128])
@@ -305,6 +376,8 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     args.warmup = max(args.warmup, 3)
+    if args.workload == "batched":
+        return run_batched(args)
 
     import torch
     rank, world, local = _rank_env()

@@ -1,0 +1,242 @@
+"""Batched antenna sweeps: many independent scenes stepped together until their ports ring down.
+
+Scenes are grouped by cross-section (nx, ny) and each group becomes one `SceneStack`: a single grid
+whose every solver launch covers all of its scenes (csrc/stack.cu). Each group runs on its own CUDA
+stream, so the groups' launches overlap on the device. Every `chunk` steps the port series of the
+chunk is read back; a scene is done when its port voltage has stayed below `ringdown_db` (-60 dB)
+of its peak for two periods of its design wavelength. A finished scene's impedance sweep Z(f) is
+evaluated on the host from its whole series (Ports.cpp:187-278: the FP64 DFT of V and I with the
+half-step phase correction of I, Z = -V/I * eta0), and the scene is dropped from its stack by
+compaction once a quarter of the stack has finished.
+
+The single-scene reference path steps one SimulationGrid per scene (src/SimulationGrid.cpp:368-433);
+`run_single` does that with this library, for comparison and as the judge of the batched results.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from .grid import SceneStack, SimulationGrid
+from .scene import K_ETA0
+
+DB_RINGDOWN = -60.0
+
+
+@dataclass
+class SceneResult:
+    index: int
+    steps: int = 0
+    series: list = field(default_factory=list)  # chunks of (steps, 2) float32: V, I of the scene's port
+    done: bool = False
+    rung_down: bool = False  # False when done at the step cap
+    wall_s: float = 0.0
+    sweep: dict | None = None
+
+
+def sweep_sums(series: np.ndarray, lambda_min: float, lambda_max: float, points: int, dt: float) -> np.ndarray:
+    """(points, 4): Re V(f), Im V(f), Re I(f), Im I(f) of one port series (Ports.cpp:187-238; the
+    library's sweep_kernel computes the same sums on the device). I is shifted by half a step."""
+    nu_lo = 1.0 / max(lambda_max, lambda_min)
+    nu_hi = 1.0 / min(lambda_max, lambda_min)
+    nu = nu_lo + (nu_hi - nu_lo) * np.arange(points) / (points - 1)
+    w = 2.0 * math.pi * nu
+    k = np.arange(series.shape[0], dtype=np.float64)
+    ph = -np.outer(w * dt, k)
+    c, s = np.cos(ph), np.sin(ph)
+    V = series[:, 0].astype(np.float64)
+    I = series[:, 1].astype(np.float64)
+    out = np.empty((points, 4))
+    out[:, 0], out[:, 1] = c @ V, s @ V
+    ic, is_ = c @ I, s @ I
+    ch, sh = np.cos(w * 0.5 * dt), np.sin(w * 0.5 * dt)
+    out[:, 2] = ic * ch - is_ * sh
+    out[:, 3] = ic * sh + is_ * ch
+    return out
+
+
+def impedance(sums: np.ndarray, lambda_min: float, lambda_max: float, z0: float = 50.0):
+    """Z(f) (ohm), S11 (dB) and the best-match wavelength from sweep sums (Ports.cpp:240-278)."""
+    pts = sums.shape[0]
+    nu_lo = 1.0 / max(lambda_max, lambda_min)
+    nu_hi = 1.0 / min(lambda_max, lambda_min)
+    nu = nu_lo + (nu_hi - nu_lo) * np.arange(pts) / (pts - 1)
+    sv = sums[:, 0] + 1j * sums[:, 1]
+    si = sums[:, 2] + 1j * sums[:, 3]
+    z = np.where(np.abs(si) > 1e-30, -sv / np.where(np.abs(si) > 1e-30, si, 1.0) * K_ETA0, 0.0)
+    g = np.abs((z - z0) / (z + z0))
+    s11 = np.where(g > 1e-12, 20.0 * np.log10(np.maximum(g, 1e-300)), -200.0)
+    return {"nu": nu, "z": z, "s11": s11, "best_wl": float(1.0 / nu[int(np.argmin(s11))])}
+
+
+def scene_sweep(sc, series: np.ndarray, dt: float):
+    sw = sc.sweep
+    sums = sweep_sums(series, sw["wavelength_min"], sw["wavelength_max"], int(sw["points"]), dt)
+    z0 = float(sc.ports[0].impedance_ohm) if sc.ports else 50.0
+    return impedance(sums, sw["wavelength_min"], sw["wavelength_max"], z0)
+
+
+class RingDown:
+    """-60 dB watch on one port voltage: peak |V| so far and the last step at which |V| exceeded the
+    threshold fraction of it; done once `window` quiet steps follow and at least `min_steps` ran."""
+
+    def __init__(self, window: int, min_steps: int, db: float = DB_RINGDOWN, max_steps: int = 1 << 62):
+        self.window, self.min_steps, self.max_steps = int(window), int(min_steps), int(max_steps)
+        self.ratio = 10.0 ** (db / 20.0)
+        self.peak = 0.0
+        self.last_loud = 0
+        self.steps = 0
+
+    def feed(self, v: np.ndarray) -> bool:
+        a = np.abs(np.asarray(v, np.float64))
+        for k in range(a.size):  # the peak grows while the pulse passes: compare against the running peak
+            if a[k] > self.peak:
+                self.peak = float(a[k])
+            if a[k] > self.ratio * self.peak:
+                self.last_loud = self.steps + k
+        self.steps += a.size
+        return self.done()
+
+    def rung_down(self) -> bool:
+        return self.peak > 0.0 and self.steps >= self.min_steps and self.steps - 1 - self.last_loud >= self.window
+
+    def done(self) -> bool:
+        return self.rung_down() or self.steps >= self.max_steps
+
+
+MAX_PERIODS = 120  # a scene that has not rung down after this many design periods stops there (flagged)
+
+
+def _watch(sc, dt: float) -> RingDown:
+    period = sc.wavelength / dt  # steps per period of the design wavelength
+    return RingDown(window=int(math.ceil(2.0 * period)), min_steps=int(math.ceil(4.0 * period)),
+                    max_steps=int(math.ceil(MAX_PERIODS * period)))
+
+
+class _Group:
+    def __init__(self, scenes, indices, chunk):
+        self.indices = list(indices)  # scene indices into the batch, in stack order
+        self.scenes = [scenes[i] for i in indices]
+        first = self.scenes[0]
+        self.stack = SceneStack(first.grid, [sc.grid.size[2] for sc in self.scenes])
+        for k, sc in enumerate(self.scenes):
+            m = sc.materials
+            self.stack.upload_scene_materials(k, m.sigma, m.epsilon_r, sc.edges, sc.wires)
+        self.stack.set_scene_sources([sc.sources for sc in self.scenes])
+        self.stack.commit()
+        self.chunk = chunk
+        self.attach_ports()
+
+    def attach_ports(self):
+        z0, _ = self.stack.layout()
+        ports = []
+        for k, sc in enumerate(self.scenes):
+            p = sc.ports[0]
+            ports.append(abi.Port(int(p.texel[0]), int(p.texel[1]), int(p.texel[2]) + z0[k], int(p.axis),
+                                  int(p.edges), 1 if p.sign >= 0 else -1))
+        self.stack.ports_configure(ports, self.scenes[0].wavelength, 4.0, False, self.chunk)
+
+    def compact(self, keep):
+        self.stack.compact(keep)
+        self.indices = [i for i, k in zip(self.indices, keep) if k]
+        self.scenes = [s for s, k in zip(self.scenes, keep) if k]
+        self.attach_ports()
+
+
+class BatchRunner:
+    """Steps `scenes` (each with one feed port) to port ring-down in stacks grouped by cross-section."""
+
+    def __init__(self, scenes, chunk: int = 64, max_steps: int = 200_000, compact_fraction: float = 0.25):
+        for sc in scenes:
+            if not sc.ports:
+                raise ValueError(f"{sc.name}: a batched scene needs a feed port")
+        self.scenes = list(scenes)
+        self.chunk = int(chunk)
+        self.max_steps = int(max_steps)
+        self.compact_fraction = float(compact_fraction)
+        groups = {}
+        for i, sc in enumerate(self.scenes):
+            key = (sc.grid.size[0], sc.grid.size[1], sc.grid.pml_thickness, float(sc.grid.courant),
+                   float(sc.grid.pml_sigma_max), float(sc.grid.pml_grading))
+            groups.setdefault(key, []).append(i)
+        t0 = time.perf_counter()
+        self.groups = [_Group(self.scenes, idx, self.chunk) for _, idx in sorted(groups.items(), key=lambda kv: kv[0])]
+        self.setup_s = time.perf_counter() - t0
+        self.results = [SceneResult(i) for i in range(len(self.scenes))]
+        self.watch = [_watch(sc, float(sc.grid.courant)) for sc in self.scenes]
+        self.cell_steps = 0
+        self.steps = 0
+
+    def run(self, on_done=None):
+        t0 = time.perf_counter()
+        active = [g for g in self.groups]
+        while active and self.steps < self.max_steps:
+            for g in active:  # enqueue the chunk on every group's stream, then collect
+                g.stack.step(self.chunk)
+            for g in active:
+                nx, ny, nz = g.stack.size()
+                z0, nzs = g.stack.layout()
+                self.cell_steps += nx * ny * sum(nzs) * self.chunk
+                ser = g.stack.ports_take_series(self.chunk)
+                for k, i in enumerate(g.indices):
+                    r = self.results[i]
+                    if r.done:
+                        continue
+                    r.series.append(ser[:, k].copy())
+                    r.steps += ser.shape[0]
+                    if self.watch[i].feed(ser[:, k, 0]):
+                        r.done = True
+                        r.rung_down = self.watch[i].rung_down()
+                        r.wall_s = time.perf_counter() - t0
+                        sc = self.scenes[i]
+                        r.sweep = scene_sweep(sc, np.concatenate(r.series), float(sc.grid.courant))
+                        if on_done:
+                            on_done(i, r)
+            self.steps += self.chunk
+            still = []
+            for g in active:
+                keep = [not self.results[i].done for i in g.indices]
+                if not any(keep):
+                    g.stack.close()
+                    continue
+                if keep.count(False) >= max(1, int(self.compact_fraction * len(keep))):
+                    g.compact(keep)
+                still.append(g)
+            active = still
+        self.wall_s = time.perf_counter() - t0
+        return self.results
+
+
+def run_single(sc, chunk: int = 64, max_steps: int = 200_000, timing: dict | None = None):
+    """One scene on its own SimulationGrid to the same ring-down rule: (series (steps, 2), sweep).
+    `timing`, if given, receives the set-up and the stepping wall-clock seconds and the steps."""
+    t0 = time.perf_counter()
+    g = SimulationGrid(sc.grid)
+    m = sc.materials
+    g.upload_materials(m.sigma, m.epsilon_r, sc.edges, sc.wires)
+    g.set_sources(sc.sources)
+    g.ports_configure([sc.ports[0].to_c()], sc.wavelength, 4.0, False, chunk)
+    g.synchronize()
+    t1 = time.perf_counter()
+    dt = float(sc.grid.courant)
+    watch = _watch(sc, dt)
+    parts = []
+    steps = 0
+    while steps < max_steps:
+        g.step(chunk)
+        ser = g.ports_take_series(chunk)
+        parts.append(ser[:, 0].copy())
+        steps += ser.shape[0]
+        if watch.feed(ser[:, 0, 0]):
+            break
+    series = np.concatenate(parts)
+    sweep = scene_sweep(sc, series, dt)
+    t2 = time.perf_counter()
+    g.close()
+    if timing is not None:
+        timing.update(setup_s=t1 - t0, run_s=t2 - t1, steps=steps)
+    return series, sweep

@@ -131,3 +131,62 @@ def fibonacci_directions(n: int) -> np.ndarray:
     phi = np.arccos(1 - 2 * i / n)
     th = math.pi * (1 + 5 ** 0.5) * i
     return np.stack([np.cos(th) * np.sin(phi), np.sin(th) * np.sin(phi), np.cos(phi)], 1).astype(np.float32)
+
+
+BATCH_EDGES = tuple(range(48, 161, 16))
+
+
+def batched_scene(seed: int, index: int, pml: int = 8):
+    """One scene of the batched antenna sweep: a cube of edge 48, 64, ..., 160 cells (uniform) with an
+    8-cell absorber; a thin-wire z dipole at the centre or a monopole over a PEC ground plate (50/50),
+    length uniform in [0.3, 0.7] lambda, wire radius uniform in [0.02, 0.2] cell, fed by a 50-ohm
+    resistive voltage source with a Gaussian pulse (0.4 periods: about 0.3-1.7 f0); one dielectric
+    sphere or box (eps_r uniform in [1, 10], sigma log-uniform in [1e-4, 1e-1] S/m) beside it.
+    lambda = 0.6 (edge - 2 pml) cells. Port sweep 0.3-1.7 f0 at 128 points. Seeded by (seed, index)."""
+    rng = np.random.default_rng([int(seed), int(index)])
+    n = int(rng.choice(BATCH_EDGES))
+    grid = abi.GridConfig((n, n, n), courant=0.5, pml_thickness=pml, pml_sigma_max=1.6, pml_grading=3.0)
+    wl = float(f32(0.6 * (n - 2 * pml)))
+    b = EnvironmentBuilder(f"batch{seed}_{index}", grid, wavelength=wl)
+    monopole = bool(rng.random() < 0.5)
+    length = float(f32(rng.uniform(0.3, 0.7) * wl))
+    radius = float(f32(rng.uniform(0.02, 0.2)))
+    wave = SourceDesc(wavelength=wl, waveform=abi.WAVE_PULSE, ramp_periods=0.4)
+    c = n * 0.5
+    lo, hi = pml + 3, n - pml - 3
+    if monopole:
+        zg = pml + 4  # ground plate: one metal layer below the surface plane zg
+        b.box((float(lo), float(lo), float(zg - 1)), (float(hi), float(hi), float(zg)), Material(1.0e7, 1.0))
+        node = [int(math.floor(c + 0.5)), int(math.floor(c + 0.5)), zg]
+        rod = max(1, int(math.floor(length + 0.5)) - 1)
+        b.add_thin_wire(node, 2, zg, zg + 1 + rod, radius, zg)
+        b.add_feed(wave, node, 2, 1.0, 1, 50.0, 1.0, True, "monopole")
+        ant_lo, ant_hi = zg, zg + 1 + rod
+    else:
+        b.thin_dipole(wave, (c, c, c), 2, length, radius=radius, impedance_ohm=50.0, drive=1.0, name="dipole")
+        arm = EnvironmentBuilder.dipole_arm(length)
+        ant_lo, ant_hi = int(math.floor(c)) - arm, int(math.floor(c)) + 1 + arm
+    # the obstacle: beside the antenna (at least 3 cells of clearance from its axis)
+    eps = float(rng.uniform(1.0, 10.0))
+    m = resolve_material(eps, 1.0e-3, wl, conductivity=float(10.0 ** rng.uniform(-4.0, -1.0)))
+    if rng.random() < 0.5:
+        r = float(rng.uniform(2.0, max(2.5, n / 10.0)))
+        off = float(rng.uniform(r + 3.0, max(r + 3.5, hi - c - r)))
+        ang = float(rng.uniform(0.0, 2.0 * math.pi))
+        zc = float(rng.uniform(max(lo + r, ant_lo - 2.0), min(hi - r, ant_hi + 2.0)))
+        b.sphere((c + off * math.cos(ang), c + off * math.sin(ang), zc), r, m)
+    else:
+        e = rng.integers(3, max(4, n // 5) + 1, size=3)
+        side = 1 if rng.random() < 0.5 else -1
+        x0 = c + side * 3.0 if side > 0 else c - 3.0 - float(e[0])
+        y0 = float(rng.uniform(lo, max(lo + 1.0, hi - e[1])))
+        z0 = float(rng.uniform(lo, max(lo + 1.0, hi - e[2])))
+        b.box((x0, y0, z0), (x0 + float(e[0]), y0 + float(e[1]), z0 + float(e[2])), m)
+    b.scene.sweep = {"wavelength_min": wl / 1.7, "wavelength_max": wl / 0.3, "points": 128}
+    sc = b.build()
+    sc.description = f"{'monopole' if monopole else 'dipole'} L={length:.2f} a={radius:.3f} eps={eps:.2f}"
+    return sc
+
+
+def batched_scenes(count: int = 256, seed: int = 2024):
+    return [batched_scene(seed, i) for i in range(count)]

@@ -17,8 +17,7 @@
 #include <vector>
 
 #include "../../include/emlab.h"
-#include "emlab_internal.h"
-#include "setup.h"
+#include "grid_state.h"
 
 using namespace emlab;
 
@@ -27,133 +26,12 @@ namespace {
 thread_local std::string g_last_error;
 std::atomic<uint64_t> g_launches{0};
 
-int fail(int code, const std::string& msg) {
+}  // namespace
+
+int emlab::fail(int code, const std::string& msg) {
     g_last_error = msg;
     return code;
 }
-
-#define EMLAB_CUDA(call)                                                                                      \
-    do {                                                                                                      \
-        cudaError_t e_ = (call);                                                                              \
-        if (e_ != cudaSuccess)                                                                                \
-            return fail(e_ == cudaErrorMemoryAllocation ? EMLAB_ERR_OOM : EMLAB_ERR_CUDA,                     \
-                        std::string(#call) + ": " + cudaGetErrorString(e_));                                  \
-    } while (0)
-
-#define EMLAB_REQUIRE(cond, msg) \
-    do {                         \
-        if (!(cond)) return fail(EMLAB_ERR_INVALID, msg); \
-    } while (0)
-
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    ~DevBuf() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    cudaError_t alloc(size_t count) {
-        release();
-        if (count == 0) return cudaSuccess;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-        if (e == cudaSuccess) n = count;
-        else p = nullptr;
-        return e;
-    }
-};
-
-constexpr int kChunk = 1024;  // sub-steps whose host-side scalars are uploaded together
-
-}  // namespace
-
-struct emlab_grid {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    emlab_grid_config cfg{};
-    bool configured = false;
-    int pitch = 0;
-    long long plane = 0;
-    long long padded = 0;  // floats per component array
-    DevBuf<float> fields;  // 12 component arrays: generation 0 (Ex..Bz), generation 1
-    int cur = 0;
-    int kernel = EMLAB_KERNEL_FUSED;
-    int tile_rows = 0;  // 0: automatic
-    // materials
-    DevBuf<uint8_t> cls;
-    bool wide = false;
-    DevBuf<float4> tabE, tabM, tabW;
-    uint32_t classes = 0, wire_start = 0;
-    DevBuf<float> pml;
-    int pml_stride = 0;
-    DevBuf<uint8_t> pml_cls;
-    DevBuf<float2> pml_coef;
-    int pml_K = 0;
-    TmaMaps* tma = nullptr;
-    DevBuf<unsigned> d_err;  // set by a solver kernel whose bounded on-device wait ran out
-    DevBuf<unsigned long long> d_work;  // ticket counter of the persistent Yee kernel (never reset)
-    unsigned long long work_base = 0;   // tickets consumed by the launches issued so far
-    std::vector<float> cell_sigma, cell_eps;  // alpha channels of the textures (read-back only)
-    // sources
-    std::vector<emlab_source> desc;
-    std::vector<float> packed;
-    DevBuf<float4> d_src;
-    DevBuf<int4> d_cells;
-    DevBuf<int> d_lists;
-    int nsrc = 0, ncells = 0;
-    // per-chunk scalars: signals[k][nsrc], port rot[k], ntff rot[k], line rot[k], blends
-    DevBuf<uint8_t> d_stage;
-    uint8_t* h_stage[2] = {nullptr, nullptr};
-    cudaEvent_t stage_done[2] = {nullptr, nullptr};
-    size_t stage_bytes = 0;
-    int stage_slot = 0;
-    uint64_t step = 0;
-    // ports
-    int nports = 0;
-    DevBuf<int4> d_ports;
-    DevBuf<float> d_port_ph, d_series;
-    size_t series_cap = 0, recorded = 0;
-    bool recording = false;
-    float port_wl = 16.0f, port_avg = 4.0f;
-    // ntff
-    bool ntff_on = false;
-    int box[13] = {};
-    int points = 0;
-    DevBuf<int> d_box;
-    DevBuf<float> d_ntff;
-    float ntff_wl = 16.0f, ntff_avg = 4.0f;
-    // lines
-    int nq = 0;
-    DevBuf<int4> d_q, d_terms;
-    DevBuf<float> d_weights, d_line_ph, d_line_now;
-    float line_wl = 16.0f, line_avg = 4.0f;
-    // multi-frequency far-field DFT
-    bool dft_on = false;
-    int dft_box[13] = {};
-    int dft_points = 0, dft_nf = 0, dft_t = 0;
-    long long dft_n0 = 0;
-    uint64_t dft_samples = 0;
-    std::vector<double> dft_omega;
-    DevBuf<int> d_dft_box;
-    DevBuf<float2> d_dft_w;
-    DevBuf<double> d_dft_omega, d_dft_x;
-    DevBuf<float> d_dft_blk;
-    DevBuf<float> d_dft_bhi, d_dft_blo;  // tensor-core twiddles (split hi/lo, MMA operand layout)
-    int dft_engine = EMLAB_DFT_TENSOR;
-    // scratch
-    DevBuf<unsigned> d_flag;
-    // solver-pass timing: event pairs recorded around each Yee launch, read back lazily
-    bool timing = false;
-    std::vector<cudaEvent_t> ev_start, ev_stop;
-    size_t ev_used = 0;
-    double timed_ms = 0.0;
-    uint64_t timed_launches = 0;
-
-    float* comp(int gen, int c) { return fields.p + (size_t)(gen * 6 + c) * padded; }
-    long long cells() const { return (long long)cfg.nx * cfg.ny * cfg.nz; }
-};
 
 namespace {
 
@@ -176,6 +54,7 @@ YeeArgs yee_args(emlab_grid* g) {
     a.pml_stride = g->pml_stride;
     a.pml_cls = g->pml_cls.p;
     a.pml_coef = g->pml_coef.p;
+    a.pml_z = g->pml_z.p;
     a.pml_K = g->pml_K;
     a.L = g->cfg.pml_thickness;
     a.dt = g->cfg.courant;
@@ -211,7 +90,9 @@ int check_launch() {
     return EMLAB_OK;
 }
 
-int upload_class_table(emlab_grid* g, const ClassTable& t) {
+}  // namespace
+
+int emlab::upload_class_table(emlab_grid* g, const ClassTable& t) {
     const long long ncls = (long long)t.cls.size();
     g->wide = t.classes > 65536u;
     EMLAB_CUDA(g->cls.alloc((size_t)ncls * (g->wide ? 4 : 2)));
@@ -236,7 +117,7 @@ int upload_class_table(emlab_grid* g, const ClassTable& t) {
 }
 
 // Tensor maps of both field generations and the class index (the TMA kernel's inputs).
-void refresh_tma(emlab_grid* g) {
+void emlab::refresh_tma(emlab_grid* g) {
     if (!g->tma) g->tma = tma_maps_create();
     const int cur = g->cur;
     for (int gen = 0; gen < 2; ++gen) {
@@ -246,11 +127,83 @@ void refresh_tma(emlab_grid* g) {
     g->cur = cur;
 }
 
-int clear_fields(emlab_grid* g) {
+int emlab::clear_fields(emlab_grid* g) {
     EMLAB_CUDA(cudaMemsetAsync(g->fields.p, 0, g->fields.n * sizeof(float), g->stream));
     g->cur = 0;
     return EMLAB_OK;
 }
+
+// Absorber tables of the configured size (common.glsl:23-43). In a stack, the z entries are each
+// scene's own tables at its planes; separator planes lie outside every layer.
+int emlab::upload_pml(emlab_grid* g) {
+    const emlab_grid_config& c = g->cfg;
+    const int S = std::max(c.nx, std::max(c.ny, c.nz));
+    g->pml_stride = S;
+    std::vector<float> pt = pml_tables(c, S);
+    std::vector<uint8_t> pcls;
+    std::vector<float> coef;
+    pml_class_tables(c, S, pcls, coef, g->pml_K);
+    std::vector<uint8_t> pz((size_t)c.nz, 0);
+    const int L = c.pml_thickness;
+    if (g->stack.scenes() == 0) {
+        for (int z = 0; z < c.nz; ++z) pz[(size_t)z] = (z < L || z >= c.nz - (L + 1)) ? 1 : 0;
+    } else {
+        for (int z = 0; z < c.nz; ++z) {  // separators: no absorber
+            pt[(size_t)2 * S + z] = 0.0f, pt[(size_t)5 * S + z] = 0.0f;
+            pcls[(size_t)2 * S + z] = 0, pcls[(size_t)5 * S + z] = 0;
+        }
+        for (int i = 0; i < g->stack.scenes(); ++i) {
+            emlab_grid_config ci = c;
+            ci.nz = g->stack.nz[i];
+            const int Si = std::max(ci.nx, std::max(ci.ny, ci.nz));
+            const std::vector<float> ti = pml_tables(ci, Si);
+            std::vector<uint8_t> ci_cls;
+            std::vector<float> ci_coef;
+            int Ki = 0;
+            pml_class_tables(ci, Si, ci_cls, ci_coef, Ki);
+            for (int z = 0; z < ci.nz; ++z) {
+                const size_t zz = (size_t)g->stack.z0[i] + z;
+                pt[2 * (size_t)S + zz] = ti[2 * (size_t)Si + z];
+                pt[5 * (size_t)S + zz] = ti[5 * (size_t)Si + z];
+                pcls[2 * (size_t)S + zz] = ci_cls[2 * (size_t)Si + z];
+                pcls[5 * (size_t)S + zz] = ci_cls[5 * (size_t)Si + z];
+                pz[zz] = (z < L || z >= ci.nz - (L + 1)) ? 1 : 0;
+            }
+        }
+    }
+    EMLAB_CUDA(g->pml.alloc(pt.size()));
+    EMLAB_CUDA(cudaMemcpy(g->pml.p, pt.data(), pt.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->pml_cls.alloc(pcls.size()));
+    EMLAB_CUDA(cudaMemcpy(g->pml_cls.p, pcls.data(), pcls.size(), cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->pml_coef.alloc(coef.size() / 2));
+    EMLAB_CUDA(cudaMemcpy(g->pml_coef.p, coef.data(), coef.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->pml_z.alloc(pz.size()));
+    EMLAB_CUDA(cudaMemcpy(g->pml_z.p, pz.data(), pz.size(), cudaMemcpyHostToDevice));
+    return EMLAB_OK;
+}
+
+// Packed sources and their per-cell lists on the device (zoff: empty for a single scene).
+int emlab::upload_sources(emlab_grid* g, const std::vector<float>& packed, const std::vector<int32_t>& cells,
+                          const std::vector<int32_t>& lists, const std::vector<int32_t>& zoff) {
+    g->ncells = (int)(cells.size() / 4) - 1;
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));  // buffers may be in use by queued steps
+    EMLAB_CUDA(g->d_src.alloc(std::max<size_t>(1, packed.size() / 4)));
+    if (!packed.empty())
+        EMLAB_CUDA(cudaMemcpy(g->d_src.p, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_cells.alloc(cells.size() / 4));
+    EMLAB_CUDA(cudaMemcpy(g->d_cells.p, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_lists.alloc(std::max<size_t>(1, lists.size())));
+    if (!lists.empty())
+        EMLAB_CUDA(cudaMemcpy(g->d_lists.p, lists.data(), lists.size() * 4, cudaMemcpyHostToDevice));
+    g->d_zoff.release();
+    if (!zoff.empty()) {
+        EMLAB_CUDA(g->d_zoff.alloc(zoff.size()));
+        EMLAB_CUDA(cudaMemcpy(g->d_zoff.p, zoff.data(), zoff.size() * 4, cudaMemcpyHostToDevice));
+    }
+    return EMLAB_OK;
+}
+
+namespace {
 
 void rotation(double w, double tE, double dt, float4& r) {
     const double tH = tE - 0.5 * dt;
@@ -322,13 +275,22 @@ int dft_fold(emlab_grid* g) {
     return EMLAB_OK;
 }
 
-int require_grid(const emlab_grid* g) {
+}  // namespace
+
+int emlab::reset_monitors(emlab_grid* g) {
+    int rc = emlab_ports_configure(g, nullptr, 0, 16.0f, 4.0f, 0, 0);
+    int zero[3] = {0, 0, 0};
+    if (!rc) rc = emlab_ntff_configure(g, zero, zero, 0.0f, 4.0f, nullptr);
+    if (!rc) rc = emlab_lines_configure(g, nullptr, 0, nullptr, nullptr, 0, 16.0f, 4.0f);
+    if (!rc) rc = emlab_ntff_dft_configure(g, zero, zero, nullptr, 0, nullptr);
+    return rc;
+}
+
+int emlab::require_grid(const emlab_grid* g) {
     if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
     if (!g->configured) return fail(EMLAB_ERR_INVALID, "grid is not configured");
     return EMLAB_OK;
 }
-
-}  // namespace
 
 namespace emlab {
 int grid_view(emlab_grid* g, MonitorArgs* m, cudaStream_t* stream, int* device) {
@@ -407,19 +369,8 @@ int emlab_grid_configure(emlab_grid* g, const emlab_grid_config* req) {
     }
     g->cfg = c;
     g->pitch = pitch, g->plane = plane, g->padded = padded;
-    g->pml_stride = std::max(c.nx, std::max(c.ny, c.nz));
-    const std::vector<float> pt = pml_tables(c, g->pml_stride);
-    EMLAB_CUDA(g->pml.alloc(pt.size()));
-    EMLAB_CUDA(cudaMemcpy(g->pml.p, pt.data(), pt.size() * 4, cudaMemcpyHostToDevice));
-    {
-        std::vector<uint8_t> pcls;
-        std::vector<float> coef;
-        pml_class_tables(c, g->pml_stride, pcls, coef, g->pml_K);
-        EMLAB_CUDA(g->pml_cls.alloc(pcls.size()));
-        EMLAB_CUDA(cudaMemcpy(g->pml_cls.p, pcls.data(), pcls.size(), cudaMemcpyHostToDevice));
-        EMLAB_CUDA(g->pml_coef.alloc(coef.size() / 2));
-        EMLAB_CUDA(cudaMemcpy(g->pml_coef.p, coef.data(), coef.size() * 4, cudaMemcpyHostToDevice));
-    }
+    g->stack = StackLayout();  // a single scene
+    if (int rc = upload_pml(g)) return rc;
     // vacuum materials: class 0 everywhere (SimulationGrid.cpp:185-192)
     const long long n = g->cells();
     try {
@@ -455,11 +406,7 @@ int emlab_grid_configure(emlab_grid* g, const emlab_grid_config* req) {
         rc = emlab_grid_set_sources(g, d.data(), d.size());
         if (rc) return rc;
     }
-    emlab_ports_configure(g, nullptr, 0, 16.0f, 4.0f, 0, 0);
-    int zero[3] = {0, 0, 0};
-    emlab_ntff_configure(g, zero, zero, 0.0f, 4.0f, nullptr);
-    emlab_lines_configure(g, nullptr, 0, nullptr, nullptr, 0, 16.0f, 4.0f);
-    emlab_ntff_dft_configure(g, zero, zero, nullptr, 0, nullptr);
+    if (int rc2 = reset_monitors(g)) return rc2;
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
     return EMLAB_OK;
 }
@@ -475,6 +422,7 @@ int emlab_grid_upload_materials(emlab_grid* g, const float* sigma, const float* 
                                 const emlab_edge_override* edges, size_t n_edges, const emlab_wire_term* wires,
                                 size_t n_wires) {
     if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(g->stack.scenes() == 0, "a stack of scenes takes materials per scene (emlab_stack_upload_materials)");
     if (nx != g->cfg.nx || ny != g->cfg.ny || nz != g->cfg.nz)
         return fail(EMLAB_ERR_INVALID, "SimulationGrid: material volume size does not match the grid");
     EMLAB_REQUIRE(sigma && eps_r, "null material array");
@@ -498,6 +446,7 @@ int emlab_grid_upload_materials(emlab_grid* g, const float* sigma, const float* 
 int emlab_grid_set_sources(emlab_grid* g, const emlab_source* sources, size_t n) {
     if (int rc = require_grid(g)) return rc;
     EMLAB_REQUIRE(sources || n == 0, "null source array");
+    EMLAB_REQUIRE(g->stack.scenes() == 0, "a stack of scenes takes sources per scene (emlab_stack_set_sources)");
     EMLAB_CUDA(cudaSetDevice(g->device));
     std::vector<emlab_source> desc;
     std::vector<float> packed;
@@ -507,16 +456,7 @@ int emlab_grid_set_sources(emlab_grid* g, const emlab_source* sources, size_t n)
     std::vector<int32_t> cells, lists;
     const int dims[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
     source_lists(packed, g->nsrc, dims, cells, lists);
-    g->ncells = (int)(cells.size() / 4) - 1;
-    EMLAB_CUDA(cudaStreamSynchronize(g->stream));  // buffers may be in use by queued steps
-    EMLAB_CUDA(g->d_src.alloc(std::max<size_t>(1, packed.size() / 4)));
-    if (!packed.empty())
-        EMLAB_CUDA(cudaMemcpy(g->d_src.p, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice));
-    EMLAB_CUDA(g->d_cells.alloc(cells.size() / 4));
-    EMLAB_CUDA(cudaMemcpy(g->d_cells.p, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice));
-    EMLAB_CUDA(g->d_lists.alloc(lists.size()));
-    EMLAB_CUDA(cudaMemcpy(g->d_lists.p, lists.data(), lists.size() * 4, cudaMemcpyHostToDevice));
-    return EMLAB_OK;
+    return upload_sources(g, packed, cells, lists, {});
 }
 
 int emlab_grid_reset_fields(emlab_grid* g) {
@@ -531,6 +471,7 @@ int emlab_grid_step(emlab_grid* g, int count) {
     if (int rc = require_grid(g)) return rc;
     if (count <= 0) return EMLAB_OK;
     EMLAB_CUDA(cudaSetDevice(g->device));
+    if (int rc = stack_commit(g)) return rc;
     const double dt = (double)g->cfg.courant;
     const int nsrc = g->nsrc;
     for (int base = 0; base < count; base += kChunk) {
@@ -594,7 +535,7 @@ int emlab_grid_step(emlab_grid* g, int count) {
             if (g->timing) EMLAB_CUDA(cudaEventRecord(ev1, g->stream));
             if (g->ncells > 0) {
                 SourceArgs sa{};
-                sa.cells = g->d_cells.p, sa.lists = g->d_lists.p, sa.src = g->d_src.p;
+                sa.cells = g->d_cells.p, sa.zoff = g->d_zoff.p, sa.lists = g->d_lists.p, sa.src = g->d_src.p;
                 sa.signals = d_sig, sa.nsrc = nsrc, sa.ncells = g->ncells;
                 launch_sources(a, sa, k, g->wide, g->stream);
                 g_launches += 1;
@@ -829,6 +770,17 @@ int emlab_ports_read_series(emlab_grid* g, float* out, size_t max_steps, size_t*
     const size_t s = std::min(max_steps, g->recorded);
     EMLAB_CUDA(cudaMemcpyAsync(out, g->d_series.p, s * g->nports * 8, cudaMemcpyDeviceToHost, g->stream));
     return emlab_grid_synchronize(g, 0);
+}
+
+int emlab_ports_take_series(emlab_grid* g, float* out, size_t max_steps, size_t* steps) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(out || max_steps == 0, "null output");
+    const size_t s = std::min(max_steps, g->recorded);
+    if (steps) *steps = s;
+    if (s) EMLAB_CUDA(cudaMemcpyAsync(out, g->d_series.p, s * g->nports * 8, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    g->recorded = 0;  // the next step records from the start of the buffer again
+    return EMLAB_OK;
 }
 
 int emlab_ports_sweep_sums(emlab_grid* g, double lambda_min, double lambda_max, int points, double* out,

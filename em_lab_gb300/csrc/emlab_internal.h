@@ -44,6 +44,8 @@ struct YeeArgs {
     int pml_stride;
     const unsigned char* pml_cls;  // [6][pml_stride]: depth class of each position (same order)
     const float2* pml_coef;        // [K][K][K]: (e^{-x}, dt phi(x)), x = dt ((V_i + V_j) + V_k)
+    const unsigned char* pml_z;    // [nz]: 1 where the plane lies in the absorber along z (common.glsl:40-43;
+                                   // per scene in a stack of scenes)
     int pml_K;
     int L;
     float dt;
@@ -54,7 +56,8 @@ struct YeeArgs {
 };
 
 struct SourceArgs {
-    const int4* cells;       // xyz = cell, w = first list entry; entry n is the sentinel
+    const int4* cells;       // xyz = cell (scene coordinates), w = first list entry; entry n is the sentinel
+    const int* zoff;         // per cell: first plane of its scene in a stack of scenes (null: 0)
     const int* lists;
     const float4* src;       // 4 float4 per source: center, halfExtent, polAmp, softness
     const float* signals;    // [step][nsrc]

@@ -1,0 +1,172 @@
+// grid_state.h - the state behind an emlab_grid handle, shared by the C-ABI translation units
+// (capi.cu: single grids and monitors; stack.cu: stacks of independent scenes).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "emlab_internal.h"
+#include "setup.h"
+
+namespace emlab {
+
+// Records msg as the calling thread's last error and returns code.
+int fail(int code, const std::string& msg);
+
+#define EMLAB_CUDA(call)                                                                                      \
+    do {                                                                                                      \
+        cudaError_t e_ = (call);                                                                              \
+        if (e_ != cudaSuccess)                                                                                \
+            return fail(e_ == cudaErrorMemoryAllocation ? EMLAB_ERR_OOM : EMLAB_ERR_CUDA,                     \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                                  \
+    } while (0)
+
+#define EMLAB_REQUIRE(cond, msg) \
+    do {                         \
+        if (!(cond)) return fail(EMLAB_ERR_INVALID, msg); \
+    } while (0)
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        release();
+        if (count == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        else p = nullptr;
+        return e;
+    }
+};
+
+constexpr int kChunk = 1024;  // sub-steps whose host-side scalars are uploaded together
+
+// A stack of independent scenes of equal nx x ny along z: scene i occupies planes z0[i] ..
+// z0[i] + nz[i] - 1, and one separator plane of a frozen class (never changes from zero) lies
+// between consecutive scenes.
+struct StackLayout {
+    std::vector<int> z0, nz;
+    std::vector<ClassTable> tabs;                    // per-scene class tables until they are merged
+    std::vector<bool> has_tab;
+    std::vector<std::vector<emlab_source>> sources;  // per-scene sources (scene coordinates)
+    bool dirty = false;                              // per-scene tables not merged yet
+    int scenes() const { return (int)z0.size(); }
+};
+
+}  // namespace emlab
+
+struct emlab_grid {
+    template <typename T>
+    using DevBuf = emlab::DevBuf<T>;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    emlab_grid_config cfg{};
+    bool configured = false;
+    int pitch = 0;
+    long long plane = 0;
+    long long padded = 0;  // floats per component array
+    DevBuf<float> fields;  // 12 component arrays: generation 0 (Ex..Bz), generation 1
+    int cur = 0;
+    int kernel = EMLAB_KERNEL_FUSED;
+    int tile_rows = 0;  // 0: automatic
+    // materials
+    DevBuf<uint8_t> cls;
+    bool wide = false;
+    DevBuf<float4> tabE, tabM, tabW;
+    uint32_t classes = 0, wire_start = 0;
+    DevBuf<float> pml;
+    int pml_stride = 0;
+    DevBuf<uint8_t> pml_cls;
+    DevBuf<float2> pml_coef;
+    DevBuf<uint8_t> pml_z;  // per plane: inside the absorber along z
+    int pml_K = 0;
+    emlab::TmaMaps* tma = nullptr;
+    DevBuf<unsigned> d_err;  // set by a solver kernel whose bounded on-device wait ran out
+    DevBuf<unsigned long long> d_work;  // ticket counter of the persistent Yee kernel (never reset)
+    unsigned long long work_base = 0;   // tickets consumed by the launches issued so far
+    std::vector<float> cell_sigma, cell_eps;  // alpha channels of the textures (read-back only)
+    // sources
+    std::vector<emlab_source> desc;
+    std::vector<float> packed;
+    DevBuf<float4> d_src;
+    DevBuf<int4> d_cells;
+    DevBuf<int> d_lists;
+    DevBuf<int> d_zoff;  // stacks: per source cell, the first plane of its scene
+    int nsrc = 0, ncells = 0;
+    // stack of scenes (empty: a single scene)
+    emlab::StackLayout stack;
+    uint32_t stack_sep = 0;  // class of the separator planes
+    // per-chunk scalars: signals[k][nsrc], port rot[k], ntff rot[k], line rot[k], blends
+    DevBuf<uint8_t> d_stage;
+    uint8_t* h_stage[2] = {nullptr, nullptr};
+    cudaEvent_t stage_done[2] = {nullptr, nullptr};
+    size_t stage_bytes = 0;
+    int stage_slot = 0;
+    uint64_t step = 0;
+    // ports
+    int nports = 0;
+    DevBuf<int4> d_ports;
+    DevBuf<float> d_port_ph, d_series;
+    size_t series_cap = 0, recorded = 0;
+    bool recording = false;
+    float port_wl = 16.0f, port_avg = 4.0f;
+    // ntff
+    bool ntff_on = false;
+    int box[13] = {};
+    int points = 0;
+    DevBuf<int> d_box;
+    DevBuf<float> d_ntff;
+    float ntff_wl = 16.0f, ntff_avg = 4.0f;
+    // lines
+    int nq = 0;
+    DevBuf<int4> d_q, d_terms;
+    DevBuf<float> d_weights, d_line_ph, d_line_now;
+    float line_wl = 16.0f, line_avg = 4.0f;
+    // multi-frequency far-field DFT
+    bool dft_on = false;
+    int dft_box[13] = {};
+    int dft_points = 0, dft_nf = 0, dft_t = 0;
+    long long dft_n0 = 0;
+    uint64_t dft_samples = 0;
+    std::vector<double> dft_omega;
+    DevBuf<int> d_dft_box;
+    DevBuf<float2> d_dft_w;
+    DevBuf<double> d_dft_omega, d_dft_x;
+    DevBuf<float> d_dft_blk;
+    DevBuf<float> d_dft_bhi, d_dft_blo;  // tensor-core twiddles (split hi/lo, MMA operand layout)
+    int dft_engine = EMLAB_DFT_TENSOR;
+    // scratch
+    DevBuf<unsigned> d_flag;
+    // solver-pass timing: event pairs recorded around each Yee launch, read back lazily
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_start, ev_stop;
+    size_t ev_used = 0;
+    double timed_ms = 0.0;
+    uint64_t timed_launches = 0;
+
+    float* comp(int gen, int c) { return fields.p + (size_t)(gen * 6 + c) * padded; }
+    long long cells() const { return (long long)cfg.nx * cfg.ny * cfg.nz; }
+};
+
+namespace emlab {
+// helpers of capi.cu used by stack.cu
+int require_grid(const emlab_grid* g);
+int upload_class_table(emlab_grid* g, const ClassTable& t);
+int upload_pml(emlab_grid* g);
+void refresh_tma(emlab_grid* g);
+int clear_fields(emlab_grid* g);
+int reset_monitors(emlab_grid* g);
+int upload_sources(emlab_grid* g, const std::vector<float>& packed, const std::vector<int32_t>& cells,
+                   const std::vector<int32_t>& lists, const std::vector<int32_t>& zoff);
+// stack.cu: merges per-scene materials uploaded since the last step
+int stack_commit(emlab_grid* g);
+}  // namespace emlab

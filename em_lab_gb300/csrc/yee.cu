@@ -186,7 +186,8 @@ __global__ void __launch_bounds__(64) apply_sources(YeeArgs a, SourceArgs sa, in
         jz = jz + (pa.z * as) * wz;
     }
     if (jx == 0.0f && jy == 0.0f && jz == 0.0f) return;
-    const int x = entry.x, y = entry.y, z = entry.z;
+    // the footprint above is evaluated in scene coordinates; memory and absorber in grid planes
+    const int x = entry.x, y = entry.y, z = entry.z + (sa.zoff ? sa.zoff[id] : 0);
     const long long i = (long long)z * a.plane + (long long)y * a.pitch + x;
     const unsigned c = load_class<Idx>(a, i);
     float cbx, cby, cbz;

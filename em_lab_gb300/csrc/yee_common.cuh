@@ -14,8 +14,8 @@
 namespace emlab {
 
 __device__ __forceinline__ bool in_pml(const YeeArgs& a, int x, int y, int z) {
-    // common.glsl:40-43
-    return x < a.L || y < a.L || z < a.L || x >= a.nx - (a.L + 1) || y >= a.ny - (a.L + 1) || z >= a.nz - (a.L + 1);
+    // common.glsl:40-43 (the z test is a per-plane table: a stack of scenes has one layer per scene face)
+    return x < a.L || y < a.L || x >= a.nx - (a.L + 1) || y >= a.ny - (a.L + 1) || __ldg(a.pml_z + z) != 0;
 }
 
 template <typename Idx>

@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY <= 8 ? 3 : 1)
         const unsigned char* st1 = smem + ((rel + 1) % S_) * Lay::STAGE;
         const bool emit = z >= zs;
         const int buf = rel & 1;
-        const bool pz = z < L || z >= a.nz - (L + 1);
+        const bool pz = __ldg(a.pml_z + z) != 0;
         const int iz = __ldg(pcls + 2 * PS + z), hz = __ldg(pcls + 5 * PS + z);
         const float* Es = reinterpret_cast<const float*>(st + Lay::E_OFF);
         const float* E1 = reinterpret_cast<const float*>(st1 + Lay::E_OFF);
@@ -615,7 +615,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1)
             const unsigned char* st1 = smem + ((k + 1) % S_) * Lay::STAGE;
             const bool emit = z >= zs;
             float* sb = sB + (iter & 1) * 3 * SBC - 2;  // indexed by box element
-            const bool pz = z < L || z >= a.nz - (L + 1);
+            const bool pz = __ldg(a.pml_z + z) != 0;
             const int zn = min(z + 1, a.nz - 1);
             const int iz_n = __ldg(pcls + 2 * PS + zn), hz_n = __ldg(pcls + 5 * PS + zn);
             const float* Es = reinterpret_cast<const float*>(st + Lay::E_OFF);

@@ -80,6 +80,14 @@ def load_library() -> C.CDLL:
         "emlab_flux_planes": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_render": ([P, C.POINTER(abi.RenderParams), C.POINTER(C.c_ubyte)], I),
+        "emlab_ports_take_series": ([P, fp, SZ, C.POINTER(SZ)], I),
+        "emlab_stack_configure": ([P, C.POINTER(abi.GridConfig), ip, I], I),
+        "emlab_stack_info": ([P, ip, ip, ip], I),
+        "emlab_stack_upload_materials": ([P, I, fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ,
+                                          C.POINTER(abi.WireTerm), SZ], I),
+        "emlab_stack_commit": ([P], I),
+        "emlab_stack_set_sources": ([P, C.POINTER(abi.Source), ip, SZ], I),
+        "emlab_stack_compact": ([P, C.POINTER(C.c_ubyte)], I),
         "emlab_lines_configure": ([P, ip, I, ip, fp, I, F, F], I),
         "emlab_lines_read": ([P, fp, fp], I),
         "emlab_debug_expf": ([fp, fp, SZ], I),
@@ -314,6 +322,15 @@ class SimulationGrid:
         _check(self._lib.emlab_ports_read_series(self._h, _fptr(out), steps.value, C.byref(steps)))
         return out[: steps.value, :n]
 
+    def ports_take_series(self, max_steps: int) -> np.ndarray:
+        """The steps recorded since the last take (at most max_steps), (steps, ports, 2); recording
+        restarts at the start of the buffer."""
+        n = getattr(self, "_nports", 0)
+        out = np.zeros((max(1, int(max_steps)), max(1, n), 2), np.float32)
+        steps = C.c_size_t()
+        _check(self._lib.emlab_ports_take_series(self._h, _fptr(out), int(max_steps), C.byref(steps)))
+        return out[: steps.value, :n]
+
     def ports_sweep_sums(self, lambda_min, lambda_max, points):
         n = getattr(self, "_nports", 0)
         out = np.zeros((n, points, 4), np.float64)
@@ -423,3 +440,63 @@ class SimulationGrid:
         return ph[:n], now[:n]
 
 
+
+
+class SceneStack(SimulationGrid):
+    """Independent scenes of equal nx x ny stepped as one grid (emlab_stack_*): scene i occupies
+    planes z0[i] .. z0[i] + nz[i] - 1 with a frozen separator plane between scenes, and evolves bit for
+    bit as it would on a SimulationGrid of its own. Materials and sources are given per scene in the
+    scene's own coordinates; ports are attached in stack planes (scene z + z0)."""
+
+    def __init__(self, config: abi.GridConfig, scene_nz):
+        super().__init__(None)
+        cfg = abi.GridConfig()
+        C.memmove(C.byref(cfg), C.byref(config), C.sizeof(cfg))
+        nz = (C.c_int * len(scene_nz))(*[int(v) for v in scene_nz])
+        _check(self._lib.emlab_stack_configure(self._h, C.byref(cfg), nz, len(scene_nz)))
+
+    def layout(self):
+        """(z0, nz) lists of the scenes now in the stack."""
+        n = C.c_int()
+        _check(self._lib.emlab_stack_info(self._h, C.byref(n), None, None))
+        z0 = (C.c_int * max(1, n.value))()
+        nz = (C.c_int * max(1, n.value))()
+        _check(self._lib.emlab_stack_info(self._h, C.byref(n), z0, nz))
+        return list(z0[: n.value]), list(nz[: n.value])
+
+    def scenes(self) -> int:
+        return len(self.layout()[0])
+
+    def upload_scene_materials(self, scene: int, sigma, eps_r, edges=(), wires=()):
+        nz_s, ny, nx = np.asarray(sigma).shape
+        s = _f32(sigma)
+        e = _f32(eps_r, s.size)
+        ea, ne = abi.array_of(abi.EdgeOverride, edges)
+        wa, nw = abi.array_of(abi.WireTerm, wires)
+        _check(self._lib.emlab_stack_upload_materials(self._h, int(scene), _fptr(s), _fptr(e), nx, ny, nz_s, ea, ne,
+                                                      wa, nw))
+
+    def commit(self):
+        _check(self._lib.emlab_stack_commit(self._h))
+
+    def set_scene_sources(self, per_scene):
+        """per_scene[i]: the sources of scene i (scene coordinates)."""
+        flat, owner = [], []
+        for i, srcs in enumerate(per_scene):
+            for sdesc in srcs:
+                flat.append(sdesc.to_c() if hasattr(sdesc, "to_c") else sdesc)
+                owner.append(i)
+        arr, n = abi.array_of(abi.Source, flat)
+        own = (C.c_int * max(1, n))(*owner)
+        _check(self._lib.emlab_stack_set_sources(self._h, arr, own, n))
+
+    def compact(self, keep):
+        k = (C.c_ubyte * len(keep))(*[1 if v else 0 for v in keep])
+        _check(self._lib.emlab_stack_compact(self._h, k))
+        self._nports = 0
+
+    def scene_components(self, scene: int, comps=None):
+        """The six components of one scene, each (nz_i, ny, nx)."""
+        z0, nz = self.layout()
+        comps = self.read_components() if comps is None else comps
+        return [c[z0[scene]: z0[scene] + nz[scene]] for c in comps]

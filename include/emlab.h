@@ -185,6 +185,9 @@ int emlab_ports_read_phasors(emlab_grid* g, float* out);
 /* Recorded (V, I) pairs, [step][port], recordedSteps() x ports x 2 floats (PortMonitor::readSeries,
  * src/Ports.cpp:138-143). *steps receives recordedSteps(); out may be NULL to query it. */
 int emlab_ports_read_series(emlab_grid* g, float* out, size_t max_steps, size_t* steps);
+/* Copies the recorded steps (at most max_steps) like emlab_ports_read_series, then restarts the
+ * recording at the start of the buffer: chunked read-back of long runs (a ring-down watch). */
+int emlab_ports_take_series(emlab_grid* g, float* out, size_t max_steps, size_t* steps);
 /* Running DFT of the recorded series at `points` frequencies evenly spaced in 1/lambda between
  * 1/lambda_max and 1/lambda_min, in FP64 on the device (the sums of PortMonitor::evaluateSweep,
  * src/Ports.cpp:215-242, I corrected by e^{i w dt/2}): out[(port * points + f) * 4 + {0..3}] =
@@ -247,6 +250,32 @@ typedef struct emlab_render_params {
  * metal / dielectric surfaces. The headless replacement of the reference's on-screen renderer and
  * of --screenshot. */
 int emlab_render(emlab_grid* g, const emlab_render_params* params, unsigned char* rgba);
+
+/* ---- stacks of independent scenes (batched sweeps; no reference counterpart: the reference steps
+ * one SimulationGrid per scene, src/SimulationGrid.cpp:149-199, 368-433) ----
+ * Scenes of equal nx x ny and equal solver settings lie one after another along z in one grid,
+ * scene i at planes z0[i] .. z0[i] + nz[i] - 1, one frozen separator plane between scenes; every
+ * step launch covers all of them, and each scene evolves bit for bit as it would alone. */
+/* Configures g as a stack: cfg gives nx, ny and the solver settings (cfg->nz is ignored), scene_nz
+ * the depth of each scene (each clamped as SimulationGrid::configure clamps). Fields cleared, every
+ * scene vacuum, no sources, monitors detached. */
+int emlab_stack_configure(emlab_grid* g, const emlab_grid_config* cfg, const int* scene_nz, int n_scenes);
+/* Layout: number of scenes, first plane and depth of each (arrays of n_scenes entries, or NULL). */
+int emlab_stack_info(const emlab_grid* g, int* n_scenes, int* z0, int* nz);
+/* uploadMaterials for one scene, in the scene's own coordinates (nz = the scene's depth). Clears the
+ * fields of the stack and its step count. The merged class table is built at the next step or
+ * emlab_stack_commit. */
+int emlab_stack_upload_materials(emlab_grid* g, int scene, const float* sigma, const float* eps_r, int nx, int ny,
+                                 int nz, const emlab_edge_override* edges, size_t n_edges,
+                                 const emlab_wire_term* wires, size_t n_wires);
+int emlab_stack_commit(emlab_grid* g);
+/* setSources per scene: sources[k] (scene coordinates) belongs to scene scene_of[k]; each scene's
+ * sources are filtered and capped as setSources does for one grid. */
+int emlab_stack_set_sources(emlab_grid* g, const emlab_source* sources, const int* scene_of, size_t n);
+/* Drops the scenes whose keep[i] is 0: the others' fields, materials and sources move to a shorter
+ * stack (device copies; step count kept). Monitors are detached: ports are re-attached by the
+ * caller at the scenes' new planes (emlab_stack_info). */
+int emlab_stack_compact(emlab_grid* g, const unsigned char* keep);
 
 /* ---- probes and flux: FieldAnalyzer (src/FieldAnalyzer.hpp:73-130) ----------------------- */
 /* probe_gather.comp (FieldAnalyzer.cpp:274-303): origins are 4 ints per probe (xyz used); out
