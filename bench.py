@@ -308,8 +308,7 @@ def run_batched(args):
     # warm-up: a few chunks of a small batch (kernel loading, allocator)
     warm = batch.BatchRunner([configs.batched_scene(args.seed + 1, i) for i in range(4)], max_steps=64 * args.warmup)
     warm.run()
-    for gr in warm.groups:
-        gr.stack.close()
+    warm.close()
     l0 = launch_count()
     runner = batch.BatchRunner(scenes, chunk=64)
     with ClockSampler(local) as clk:
@@ -349,8 +348,7 @@ def run_batched(args):
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
-    for gr in runner.groups:
-        gr.stack.close()
+    runner.close()
     return 0
 
 

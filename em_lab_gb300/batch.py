@@ -93,11 +93,13 @@ class RingDown:
 
     def feed(self, v: np.ndarray) -> bool:
         a = np.abs(np.asarray(v, np.float64))
-        for k in range(a.size):  # the peak grows while the pulse passes: compare against the running peak
-            if a[k] > self.peak:
-                self.peak = float(a[k])
-            if a[k] > self.ratio * self.peak:
-                self.last_loud = self.steps + k
+        if a.size:
+            # the peak grows while the pulse passes: each sample is compared with the running peak
+            peak = np.maximum.accumulate(np.maximum(a, self.peak))
+            loud = np.nonzero(a > self.ratio * peak)[0]
+            if loud.size:
+                self.last_loud = self.steps + int(loud[-1])
+            self.peak = float(peak[-1])
         self.steps += a.size
         return self.done()
 
@@ -129,6 +131,7 @@ class _Group:
         self.stack.set_scene_sources([sc.sources for sc in self.scenes])
         self.stack.commit()
         self.chunk = chunk
+        self.stack.set_graph(chunk)  # each chunk replays one captured graph of its launches
         self.attach_ports()
 
     def attach_ports(self):
@@ -171,44 +174,68 @@ class BatchRunner:
         self.cell_steps = 0
         self.steps = 0
 
-    def run(self, on_done=None):
-        t0 = time.perf_counter()
-        active = [g for g in self.groups]
-        while active and self.steps < self.max_steps:
-            for g in active:  # enqueue the chunk on every group's stream, then collect
-                g.stack.step(self.chunk)
-            for g in active:
-                nx, ny, nz = g.stack.size()
-                z0, nzs = g.stack.layout()
-                self.cell_steps += nx * ny * sum(nzs) * self.chunk
-                ser = g.stack.ports_take_series(self.chunk)
-                for k, i in enumerate(g.indices):
-                    r = self.results[i]
-                    if r.done:
-                        continue
-                    r.series.append(ser[:, k].copy())
-                    r.steps += ser.shape[0]
-                    if self.watch[i].feed(ser[:, k, 0]):
-                        r.done = True
-                        r.rung_down = self.watch[i].rung_down()
-                        r.wall_s = time.perf_counter() - t0
-                        sc = self.scenes[i]
-                        r.sweep = scene_sweep(sc, np.concatenate(r.series), float(sc.grid.courant))
-                        if on_done:
-                            on_done(i, r)
-            self.steps += self.chunk
-            still = []
-            for g in active:
-                keep = [not self.results[i].done for i in g.indices]
-                if not any(keep):
-                    g.stack.close()
+    def _run_group(self, g, t0, on_done, lock):
+        """One stack's loop (its own host thread and CUDA stream): step a chunk, read the chunk's port
+        series back, watch every scene, evaluate the finished ones, compact. The library releases the
+        interpreter lock inside its calls, so the stacks' chunks overlap on the device."""
+        steps = 0
+        while g.indices and steps < self.max_steps:
+            g.stack.step(self.chunk)
+            ser = g.stack.ports_take_series(self.chunk)
+            nx, ny, _ = g.stack.size()
+            cells = nx * ny * sum(g.stack.layout()[1]) * ser.shape[0]
+            finished = []
+            for k, i in enumerate(g.indices):
+                r = self.results[i]
+                if r.done:
                     continue
-                if keep.count(False) >= max(1, int(self.compact_fraction * len(keep))):
-                    g.compact(keep)
-                still.append(g)
-            active = still
+                r.series.append(ser[:, k].copy())
+                r.steps += ser.shape[0]
+                if self.watch[i].feed(ser[:, k, 0]):
+                    r.done = True
+                    r.rung_down = self.watch[i].rung_down()
+                    r.wall_s = time.perf_counter() - t0
+                    sc = self.scenes[i]
+                    r.sweep = scene_sweep(sc, np.concatenate(r.series), float(sc.grid.courant))
+                    finished.append(i)
+            with lock:
+                self.cell_steps += cells
+                if on_done:
+                    for i in finished:
+                        on_done(i, self.results[i])
+            steps += self.chunk
+            keep = [not self.results[i].done for i in g.indices]
+            if not any(keep):
+                g.indices = []
+            elif keep.count(False) >= max(1, int(self.compact_fraction * len(keep))):
+                g.compact(keep)
+        with lock:
+            self.steps = max(self.steps, steps)
+
+    def run(self, on_done=None):
+        import threading
+        t0 = time.perf_counter()
+        lock = threading.Lock()
+        errors = []
+
+        def body(g):
+            try:
+                self._run_group(g, t0, on_done, lock)
+            except BaseException as e:  # re-raised on the calling thread
+                errors.append(e)
+        threads = [threading.Thread(target=body, args=(g,)) for g in self.groups]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
         self.wall_s = time.perf_counter() - t0
+        if errors:
+            raise errors[0]
         return self.results
+
+    def close(self):
+        for g in self.groups:
+            g.stack.close()
 
 
 def run_single(sc, chunk: int = 64, max_steps: int = 200_000, timing: dict | None = None):
@@ -220,6 +247,7 @@ def run_single(sc, chunk: int = 64, max_steps: int = 200_000, timing: dict | Non
     g.upload_materials(m.sigma, m.epsilon_r, sc.edges, sc.wires)
     g.set_sources(sc.sources)
     g.ports_configure([sc.ports[0].to_c()], sc.wavelength, 4.0, False, chunk)
+    g.set_graph(chunk)
     g.synchronize()
     t1 = time.perf_counter()
     dt = float(sc.grid.courant)

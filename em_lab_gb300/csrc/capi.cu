@@ -92,7 +92,14 @@ int check_launch() {
 
 }  // namespace
 
+void emlab::invalidate_graphs(emlab_grid* g) {
+    for (auto& row : g->graph_exec)
+        for (auto& e : row)
+            if (e) cudaGraphExecDestroy(e), e = nullptr;
+}
+
 int emlab::upload_class_table(emlab_grid* g, const ClassTable& t) {
+    invalidate_graphs(g);
     const long long ncls = (long long)t.cls.size();
     g->wide = t.classes > 65536u;
     EMLAB_CUDA(g->cls.alloc((size_t)ncls * (g->wide ? 4 : 2)));
@@ -118,6 +125,7 @@ int emlab::upload_class_table(emlab_grid* g, const ClassTable& t) {
 
 // Tensor maps of both field generations and the class index (the TMA kernel's inputs).
 void emlab::refresh_tma(emlab_grid* g) {
+    invalidate_graphs(g);
     if (!g->tma) g->tma = tma_maps_create();
     const int cur = g->cur;
     for (int gen = 0; gen < 2; ++gen) {
@@ -136,6 +144,7 @@ int emlab::clear_fields(emlab_grid* g) {
 // Absorber tables of the configured size (common.glsl:23-43). In a stack, the z entries are each
 // scene's own tables at its planes; separator planes lie outside every layer.
 int emlab::upload_pml(emlab_grid* g) {
+    invalidate_graphs(g);
     const emlab_grid_config& c = g->cfg;
     const int S = std::max(c.nx, std::max(c.ny, c.nz));
     g->pml_stride = S;
@@ -185,6 +194,7 @@ int emlab::upload_pml(emlab_grid* g) {
 // Packed sources and their per-cell lists on the device (zoff: empty for a single scene).
 int emlab::upload_sources(emlab_grid* g, const std::vector<float>& packed, const std::vector<int32_t>& cells,
                           const std::vector<int32_t>& lists, const std::vector<int32_t>& zoff) {
+    invalidate_graphs(g);
     g->ncells = (int)(cells.size() / 4) - 1;
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));  // buffers may be in use by queued steps
     EMLAB_CUDA(g->d_src.alloc(std::max<size_t>(1, packed.size() / 4)));
@@ -217,6 +227,7 @@ float blend_of(float avg, float wl, double dt) {
 
 int ensure_stage(emlab_grid* g, size_t bytes) {
     if (bytes <= g->stage_bytes) return EMLAB_OK;
+    invalidate_graphs(g);
     for (int s = 0; s < 2; ++s) {
         if (g->stage_done[s]) cudaEventSynchronize(g->stage_done[s]);
         if (g->h_stage[s]) cudaFreeHost(g->h_stage[s]);
@@ -286,6 +297,64 @@ int emlab::reset_monitors(emlab_grid* g) {
     return rc;
 }
 
+// The launches of one sub-step k of a staged chunk: the Yee pass (advancing the field generation),
+// the sources on the new generation, then the per-step monitors. In a graph capture (graph = true)
+// the persistent kernel's ticket counter is reset before the launch and its base is 0. Returns the
+// number of kernel launches.
+namespace {
+uint64_t enqueue_step(emlab_grid* g, int k, bool graph, const float* d_sig, const float4* d_prot,
+                      const float4* d_nrot, const float4* d_lrot, const float* d_bl, long long rec, cudaEvent_t ev0,
+                      cudaEvent_t ev1) {
+    uint64_t launched = 0;
+    YeeArgs a = yee_args(g);
+    if (ev0) cudaEventRecord(ev0, g->stream);
+    if (g->kernel == EMLAB_KERNEL_SPLIT) {
+        launch_yee_split(a, g->wide, g->stream);
+        launched += 2;
+    } else {
+        unsigned long long tickets = 0;
+        bool tma = false;
+        if (g->kernel == EMLAB_KERNEL_FUSED) {
+            if (graph) {
+                cudaMemsetAsync(g->d_work.p, 0, 8, g->stream);
+                a.work_base = 0;
+            }
+            tma = launch_yee_tma(a, g->tma, g->cur, g->wide, g->d_err.p, g->stream, &tickets);
+        }
+        if (graph) g->graph_tickets = tickets;
+        else g->work_base += tickets;
+        if (!tma) launch_yee_fused(a, g->wide, g->stream);
+        launched += 1;
+        g->cur ^= 1;
+        a = yee_args(g);  // sources act on the new generation
+    }
+    if (ev1) cudaEventRecord(ev1, g->stream);
+    if (g->ncells > 0) {
+        SourceArgs sa{};
+        sa.cells = g->d_cells.p, sa.zoff = g->d_zoff.p, sa.lists = g->d_lists.p, sa.src = g->d_src.p;
+        sa.signals = d_sig, sa.nsrc = g->nsrc, sa.ncells = g->ncells;
+        launch_sources(a, sa, k, g->wide, g->stream);
+        launched += 1;
+    }
+    if (!graph) ++g->step;
+    const MonitorArgs mon = monitor_args(g);
+    if (g->ntff_on) {
+        launch_ntff(mon, g->d_box.p, g->points, g->d_ntff.p, d_nrot + k, d_bl + 1, 0, g->stream);
+        launched += 1;
+    }
+    if (g->nports) {
+        launch_ports(mon, g->d_ports.p, g->nports, g->d_port_ph.p, g->d_series.p, rec, d_prot + k, d_bl, 0, g->stream);
+        launched += 1;
+    }
+    if (g->nq) {
+        launch_lines(mon, g->d_q.p, g->nq, g->d_terms.p, g->d_weights.p, g->d_line_ph.p, g->d_line_now.p, d_lrot + k,
+                     d_bl + 2, 0, g->stream);
+        launched += 1;
+    }
+    return launched;
+}
+}  // namespace
+
 int emlab::require_grid(const emlab_grid* g) {
     if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
     if (!g->configured) return fail(EMLAB_ERR_INVALID, "grid is not configured");
@@ -344,6 +413,7 @@ int emlab_grid_destroy(emlab_grid* g) {
     }
     for (size_t i = 0; i < g->ev_start.size(); ++i) cudaEventDestroy(g->ev_start[i]), cudaEventDestroy(g->ev_stop[i]);
     if (g->tma) tma_maps_destroy(g->tma);
+    invalidate_graphs(g);
     cudaStream_t s = g->stream;
     delete g;
     if (s) cudaStreamDestroy(s);
@@ -504,69 +574,79 @@ int emlab_grid_step(emlab_grid* g, int count) {
         blends[1] = blend_of(g->ntff_avg, g->ntff_wl, dt);
         blends[2] = blend_of(g->line_avg, g->line_wl, dt);
         uint8_t* d = g->d_stage.p;
-        EMLAB_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g->stream));
-        EMLAB_CUDA(cudaEventRecord(g->stage_done[slot], g->stream));
         const float* d_sig = reinterpret_cast<const float*>(d);
         const float4* d_prot = reinterpret_cast<const float4*>(d + sig_bytes);
         const float4* d_nrot = d_prot + m;
         const float4* d_lrot = d_nrot + m;
         const float* d_bl = reinterpret_cast<const float*>(d_lrot + m);
+        // A chunk of exactly graph_chunk steps replays a captured graph of the same launches (the
+        // staging copy included); the per-step host work is then one graph launch per chunk. Port
+        // recording restarts at row 0 every chunk, so the caller takes the series after each chunk.
+        const bool graph = g->graph_chunk > 0 && m == g->graph_chunk && (m % 2) == 0 && !g->timing && !g->dft_on &&
+                           (!g->nports || !g->recording || (g->recorded == 0 && g->series_cap >= (size_t)m));
+        if (graph && g->graph_warm) {
+            cudaGraphExec_t& ex = g->graph_exec[slot][g->cur];
+            if (!ex) {
+                const int cur0 = g->cur;
+                const unsigned long long base0 = g->work_base;
+                uint64_t launched = 0;
+                EMLAB_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+                cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g->stream);
+                for (int k = 0; k < m; ++k)
+                    launched += enqueue_step(g, k, true, d_sig, d_prot, d_nrot, d_lrot, d_bl,
+                                             g->nports && g->recording ? k : -1, nullptr, nullptr);
+                cudaGraph_t graph_def = nullptr;
+                const cudaError_t ce = cudaStreamEndCapture(g->stream, &graph_def);
+                g->cur = cur0, g->work_base = base0;
+                cudaError_t ie = ce;
+                if (ce == cudaSuccess) ie = cudaGraphInstantiate(&ex, graph_def, 0);
+                if (graph_def) cudaGraphDestroy(graph_def);
+                cudaGetLastError();
+                if (ie != cudaSuccess) {
+                    ex = nullptr;
+                    return fail(EMLAB_ERR_CUDA, std::string("step graph capture: ") + cudaGetErrorString(ie));
+                }
+                g->graph_launches = launched;
+            }
+            EMLAB_CUDA(cudaGraphLaunch(ex, g->stream));
+            EMLAB_CUDA(cudaEventRecord(g->stage_done[slot], g->stream));
+            g->step += (uint64_t)m;
+            if (g->nports && g->recording) g->recorded = (size_t)m;
+            if (g->kernel != EMLAB_KERNEL_SPLIT && g->graph_tickets) g->work_base = g->graph_tickets;
+            g_launches += g->graph_launches;
+            if (int rc = check_launch()) return rc;
+            continue;
+        }
+        if (graph) g->graph_warm = true;  // one ordinary chunk first: the launchers' one-time set-up
+        EMLAB_CUDA(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, g->stream));
+        EMLAB_CUDA(cudaEventRecord(g->stage_done[slot], g->stream));
         // monitor kernels get this sub-step's rotation and their blend by pointer (index 0)
         for (int k = 0; k < m; ++k) {
-            YeeArgs a = yee_args(g);
+            long long rec = -1;
+            if (g->nports && g->recording && g->recorded < g->series_cap) rec = (long long)g->recorded++;
             cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-            if (g->timing) {
+            if (g->timing)
                 if (int rc = timing_pair(g, &ev0, &ev1)) return rc;
-                EMLAB_CUDA(cudaEventRecord(ev0, g->stream));
-            }
-            if (g->kernel == EMLAB_KERNEL_SPLIT) {
-                launch_yee_split(a, g->wide, g->stream);
-                g_launches += 2;
-            } else {
-                unsigned long long tickets = 0;
-                const bool tma = g->kernel == EMLAB_KERNEL_FUSED &&
-                                 launch_yee_tma(a, g->tma, g->cur, g->wide, g->d_err.p, g->stream, &tickets);
-                g->work_base += tickets;
-                if (!tma) launch_yee_fused(a, g->wide, g->stream);
-                g_launches += 1;
-                g->cur ^= 1;
-                a = yee_args(g);  // sources act on the new generation
-            }
-            if (g->timing) EMLAB_CUDA(cudaEventRecord(ev1, g->stream));
-            if (g->ncells > 0) {
-                SourceArgs sa{};
-                sa.cells = g->d_cells.p, sa.zoff = g->d_zoff.p, sa.lists = g->d_lists.p, sa.src = g->d_src.p;
-                sa.signals = d_sig, sa.nsrc = nsrc, sa.ncells = g->ncells;
-                launch_sources(a, sa, k, g->wide, g->stream);
-                g_launches += 1;
-            }
-            ++g->step;
-            const MonitorArgs mon = monitor_args(g);
-            if (g->ntff_on) {
-                launch_ntff(mon, g->d_box.p, g->points, g->d_ntff.p, d_nrot + k, d_bl + 1, 0, g->stream);
-                g_launches += 1;
-            }
-            if (g->nports) {
-                long long rec = -1;
-                if (g->recording && g->recorded < g->series_cap) rec = (long long)g->recorded++;
-                launch_ports(mon, g->d_ports.p, g->nports, g->d_port_ph.p, g->d_series.p, rec, d_prot + k, d_bl, 0,
-                             g->stream);
-                g_launches += 1;
-            }
-            if (g->nq) {
-                launch_lines(mon, g->d_q.p, g->nq, g->d_terms.p, g->d_weights.p, g->d_line_ph.p, g->d_line_now.p,
-                             d_lrot + k, d_bl + 2, 0, g->stream);
-                g_launches += 1;
-            }
+            g_launches += enqueue_step(g, k, false, d_sig, d_prot, d_nrot, d_lrot, d_bl, rec, ev0, ev1);
             if (g->dft_on) {
                 if (g->dft_t == 0) g->dft_n0 = (long long)g->step;  // time index of the block's first sample
-                launch_dft_sample(mon, g->d_dft_box.p, g->dft_points, g->d_dft_blk.p, g->dft_t, g->stream);
+                launch_dft_sample(monitor_args(g), g->d_dft_box.p, g->dft_points, g->d_dft_blk.p, g->dft_t, g->stream);
                 g_launches += 1;
                 if (++g->dft_t == kDftBlock) dft_fold(g);
             }
             if (int rc = check_launch()) return rc;
         }
     }
+    return EMLAB_OK;
+}
+
+int emlab_grid_set_graph(emlab_grid* g, int chunk) {
+    if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
+    EMLAB_REQUIRE(chunk == 0 || (chunk >= 2 && chunk <= kChunk && chunk % 2 == 0),
+                  "graph chunk must be 0 (off) or an even number of steps up to 1024");
+    invalidate_graphs(g);
+    g->graph_chunk = chunk;
+    g->graph_warm = false;
     return EMLAB_OK;
 }
 
@@ -726,6 +806,7 @@ int emlab_grid_check_finite(emlab_grid* g) {
 int emlab_ports_configure(emlab_grid* g, const emlab_port* ports, size_t n, float wavelength, float averaging_periods,
                           int sweep, size_t record_steps) {
     if (int rc = require_grid(g)) return rc;
+    invalidate_graphs(g);
     EMLAB_REQUIRE(ports || n == 0, "null port array");
     EMLAB_CUDA(cudaSetDevice(g->device));
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
@@ -820,6 +901,7 @@ int emlab_ntff_configure(emlab_grid* g, const int box_min[3], const int box_max[
     if (int rc = require_grid(g)) return rc;
     EMLAB_CUDA(cudaSetDevice(g->device));
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    invalidate_graphs(g);
     g->ntff_on = false;
     g->d_ntff.release();
     if (!(wavelength > 0.0f)) return EMLAB_OK;
@@ -905,6 +987,7 @@ int emlab_ntff_dft_configure(emlab_grid* g, const int box_min[3], const int box_
     if (int rc = require_grid(g)) return rc;
     EMLAB_CUDA(cudaSetDevice(g->device));
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    invalidate_graphs(g);
     g->dft_on = false;
     g->d_dft_x.release(), g->d_dft_blk.release();
     if (n_freq <= 0) return EMLAB_OK;
@@ -1134,6 +1217,7 @@ int emlab_lines_configure(emlab_grid* g, const int* quantities, int n_quantities
     if (int rc = require_grid(g)) return rc;
     EMLAB_CUDA(cudaSetDevice(g->device));
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    invalidate_graphs(g);
     g->nq = 0;
     g->d_q.release(), g->d_terms.release(), g->d_weights.release(), g->d_line_ph.release(), g->d_line_now.release();
     if (n_quantities <= 0) return EMLAB_OK;

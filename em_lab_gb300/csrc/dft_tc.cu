@@ -18,6 +18,7 @@
 // applies the FP32 rotation by the block phase (cos, sin of w_f t0 evaluated in FP64 per CTA) and
 // the FP64 accumulation. Every mbarrier wait is bounded; on expiry the CTA records an error,
 // releases its tensor memory and leaves.
+#include <mutex>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -271,6 +272,8 @@ bool launch_dft_fold_tc(const float* blk, int T, int points, int nf, const float
     if (n > 256) return false;
     const TcLayout lay = tc_layout(n, nf);
     static int max_set = 0, sms = 0, smem_sm = 0;
+    static std::mutex setup;
+    std::lock_guard<std::mutex> lk(setup);
     if (lay.smem > max_set) {
         int dev = 0;
         if (cudaFuncSetAttribute(dft_fold_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, lay.smem) !=

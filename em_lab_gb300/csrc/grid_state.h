@@ -146,6 +146,12 @@ struct emlab_grid {
     int dft_engine = EMLAB_DFT_TENSOR;
     // scratch
     DevBuf<unsigned> d_flag;
+    // CUDA graphs of `graph_chunk` steps, one per (staging slot, field generation at the chunk start)
+    int graph_chunk = 0;  // 0: launches are issued one by one
+    bool graph_warm = false;
+    cudaGraphExec_t graph_exec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    unsigned long long graph_tickets = 0;  // work tickets the last solver launch of a chunk consumes
+    uint64_t graph_launches = 0;           // kernel launches in one chunk graph
     // solver-pass timing: event pairs recorded around each Yee launch, read back lazily
     bool timing = false;
     std::vector<cudaEvent_t> ev_start, ev_stop;
@@ -165,6 +171,8 @@ int upload_pml(emlab_grid* g);
 void refresh_tma(emlab_grid* g);
 int clear_fields(emlab_grid* g);
 int reset_monitors(emlab_grid* g);
+// drops the captured step graphs (any change of a buffer, a monitor or a launch setting)
+void invalidate_graphs(emlab_grid* g);
 int upload_sources(emlab_grid* g, const std::vector<float>& packed, const std::vector<int32_t>& cells,
                    const std::vector<int32_t>& lists, const std::vector<int32_t>& zoff);
 // stack.cu: merges per-scene materials uploaded since the last step

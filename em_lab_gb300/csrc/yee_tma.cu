@@ -17,6 +17,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "yee_common.cuh"
 
@@ -746,19 +747,19 @@ using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, voi
                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 EncodeFn encode_fn() {
-    static EncodeFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static const EncodeFn fn = [] {  // initialised once, thread-safe
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeFn>(p);
-    }
+            return reinterpret_cast<EncodeFn>(p);
+        return (EncodeFn) nullptr;
+    }();
     return fn;
 }
+
+std::mutex g_launch_setup;  // the launchers' one-time attribute set-up (grids may step from several threads)
 
 bool encode(CUtensorMap* m, CUtensorMapDataType type, int elem, const void* base, const YeeArgs& a, int box_w,
             int box_h) {
@@ -782,11 +783,14 @@ template <int TY, typename Idx>
 bool launch_t(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaStream_t s) {
     using Lay = Layout<TY, Idx>;
     static bool configured = false;
-    if (!configured) {
-        if (cudaFuncSetAttribute(yee_tma<TY, Idx>, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM) !=
-            cudaSuccess)
-            return false;
-        configured = true;
+    {
+        std::lock_guard<std::mutex> lk(g_launch_setup);
+        if (!configured) {
+            if (cudaFuncSetAttribute(yee_tma<TY, Idx>, cudaFuncAttributeMaxDynamicSharedMemorySize, Lay::SMEM) !=
+                cudaSuccess)
+                return false;
+            configured = true;
+        }
     }
     const dim3 grid((a.nx + 31) / 32, (a.ny + TY - 1) / TY, (a.nz + a.zchunk - 1) / a.zchunk);
     yee_tma<TY, Idx><<<grid, dim3(32, TY + 1), Lay::SMEM, s>>>(m->e[gen][0], m->e[gen][1], m->e[gen][2], m->b[gen][0],
@@ -816,6 +820,7 @@ bool launch_p(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaSt
               unsigned long long* tickets) {
     using Lay = Layout2<TY, Idx>;
     static int resident = 0, sms = 0;  // per process: one device model
+    std::unique_lock<std::mutex> lk(g_launch_setup);
     if (!resident) {
         int dev = 0, smem_sm = 0;
         // shared-memory carveout for exactly the CTAs wanted per SM (two 64 x 8 or one 64 x 16): the
@@ -836,6 +841,7 @@ bool launch_p(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaSt
             return false;
         }
     }
+    lk.unlock();
     PairSched ps = pair_schedule(a, TY, resident * sms);
     const int grid = std::min(ps.items, resident * sms);
     ps.work = a.work, ps.base = a.work_base;

@@ -81,6 +81,7 @@ def load_library() -> C.CDLL:
         "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_render": ([P, C.POINTER(abi.RenderParams), C.POINTER(C.c_ubyte)], I),
         "emlab_ports_take_series": ([P, fp, SZ, C.POINTER(SZ)], I),
+        "emlab_grid_set_graph": ([P, I], I),
         "emlab_stack_configure": ([P, C.POINTER(abi.GridConfig), ip, I], I),
         "emlab_stack_info": ([P, ip, ip, ip], I),
         "emlab_stack_upload_materials": ([P, I, fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ,
@@ -258,6 +259,10 @@ class SimulationGrid:
     def set_tiling(self, tile_rows: int):
         """Tile height of the fused kernels (8, 16, or 0 = automatic); results do not depend on it."""
         _check(self._lib.emlab_grid_set_tiling(self._h, int(tile_rows)))
+
+    def set_graph(self, chunk: int):
+        """Replay chunks of exactly `chunk` steps as captured CUDA graphs (0: off); same results."""
+        _check(self._lib.emlab_grid_set_graph(self._h, int(chunk)))
 
     def stream_handle(self) -> int:
         p = C.c_void_p()

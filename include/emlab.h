@@ -119,6 +119,7 @@ int emlab_version(void);
 /* Kernels this library has launched since load (graph launches count their kernel nodes). */
 uint64_t emlab_launch_count(void);
 
+
 /* ---- solver: SimulationGrid (src/SimulationGrid.hpp:155-216) ------------------------------ */
 /* SimulationGrid::SimulationGrid (src/SimulationGrid.cpp:135-147): binds the current CUDA device
  * and creates the handle's stream. */
@@ -169,6 +170,13 @@ int emlab_grid_stream(emlab_grid* g, void** stream);
  * device time in ms and the number of timed launches since the last reset (reset = 1 clears). */
 int emlab_grid_set_timing(emlab_grid* g, int enabled);
 int emlab_grid_kernel_time(emlab_grid* g, double* ms, uint64_t* launches, int reset);
+/* Chunks of exactly `chunk` steps (even, <= 1024; 0 = off) replay a captured CUDA graph of their
+ * launches instead of issuing them one by one (no reference counterpart: the reference issues one
+ * dispatch per pass per sub-step, src/SimulationGrid.cpp:368-433). Results are identical. Chunks
+ * with the multi-frequency far-field DFT attached, or with solver timing on, run without a graph;
+ * with port recording on, a chunk uses its graph when the caller has taken the series
+ * (emlab_ports_take_series) since the last chunk. */
+int emlab_grid_set_graph(emlab_grid* g, int chunk);
 /* Non-finite check over E and B on the device (Instruments::applyMeasurement's stability check,
  * src/Instruments.cpp:271-275): EMLAB_ERR_NONFINITE if any component is NaN or infinite. */
 int emlab_grid_check_finite(emlab_grid* g);

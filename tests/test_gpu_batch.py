@@ -141,3 +141,52 @@ def test_batch_runner_equals_single_runs():
         np.testing.assert_array_equal(got, series)
         np.testing.assert_array_equal(r.sweep["z"], sweep["z"])
         assert abs(r.sweep["s11"]).max() < 200.0
+
+
+@pytest.mark.parametrize("chunk", [16, 64])
+def test_graph_chunks_equal_launch_by_launch(chunk):
+    """Captured step graphs give the same fields, port series, port/far-field/line phasors."""
+    sc = configs.random_scene(size=(40, 36, 30), pml=5, seed=21)
+    out = []
+    for graph in (False, True):
+        g = SimulationGrid(sc.grid)
+        oracle.load_scene(g, sc)
+        if graph:
+            g.set_graph(chunk)
+        ports = [p.to_c() for p in sc.ports] or [abi.Port(20, 18, 15, 2, 1, 1)]
+        g.ports_configure(ports, 12.0, 4.0, False, chunk)
+        g.ntff_configure((9, 9, 9), (30, 26, 20), 12.0)
+        g.lines_configure([[0, 2, 0, 0]], [[20, 18, 15, 2], [20, 18, 16, 2]], [1.0, 0.5], 12.0)
+        series = []
+        for _ in range(3):
+            g.step(chunk)
+            series.append(g.ports_take_series(chunk))
+        g.step(5)  # a partial chunk: launch by launch
+        g.step(chunk)
+        series.append(g.ports_take_series(chunk + 5))
+        out.append((g.read_components(), np.concatenate(series), g.ports_phasors(), g.ntff_phasors(),
+                    g.lines_read()[0], g.step_count()))
+        g.close()
+    (c0, s0, p0, n0, l0, k0), (c1, s1, p1, n1, l1, k1) = out
+    assert k0 == k1 == 4 * chunk + 5
+    for a, b in zip(c0, c1):
+        np.testing.assert_array_equal(a, b)
+    for a, b in ((s0, s1), (p0, p1), (n0, n1), (l0, l1)):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_graph_chunks_on_a_stack_after_compaction():
+    scenes = scenes_xy(24, 20, (18, 22, 19), (31, 32, 33), pml=4)
+    st = stack_of(scenes)
+    st.set_graph(8)
+    st.step(8)
+    st.step(8)
+    st.compact([True, False, True])
+    st.step(8)
+    st.step(8)
+    comps = st.read_components()
+    for k, sc in zip(range(2), (scenes[0], scenes[2])):
+        ref = oracle_run(sc, 32)
+        for c, (a, b) in enumerate(zip(st.scene_components(k, comps), ref)):
+            np.testing.assert_array_equal(a, b, err_msg=f"scene {k} component {c}")
+    st.close()
