@@ -352,19 +352,54 @@ def run_batched(args):
     return 0
 
 
+def run_learned(args):
+    """--workload learned: the learned ring-down extrapolator (BASELINE config 4 shapes). Training
+    runs of the batched generator's scenes (seed --seed) to -60 dB ring-down, training on the GPU
+    with this library's kernels, then on held-out scenes (seed --seed + 1): sweeps/hr of the plain
+    solver to ring-down (the judge) against the learned path (early window + inference), and the
+    |dZ| and S11 error of the network and of the early window's truncated DFT."""
+    import torch
+    from em_lab_gb300 import extrap, launch_count
+
+    rank, world, local = _rank_env()
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    l0 = launch_count()
+    with ClockSampler(local) as clk:
+        out, _ = extrap.experiment(args.seed, args.train_scenes, args.seed + 1, args.scenes, epochs=args.epochs,
+                                   log=lambda m: print(m, file=sys.stderr))
+    line = {
+        "metric": "Z(f) sweeps/hr learned vs plain (held-out scenes)", "value": out["sweeps_per_hour"]["learned"],
+        "unit": "sweeps/hr", "n_gpus": 1, "steps": None, "warmup": args.warmup, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 GEMMs, fp32 accumulation",
+        "data": "synthetic (runs generated by the batched solver)",
+        "config": {"workload": f"learned ring-down extrapolator: {args.train_scenes} training scenes (seed {args.seed}), "
+                               f"{args.scenes} held-out scenes (seed {args.seed + 1}), early window "
+                               f"{extrap.PERIODS_IN:g} design periods, {args.epochs} epochs"},
+        "plain_sweeps_per_hour": out["sweeps_per_hour"]["plain"], "speedup": out["speedup"], "wall": out["wall"],
+        "accuracy": out["eval"], "training": out["training"], "train_runs": out["train_runs"], "steps_median": out["steps"],
+        "gpu_launches": int(launch_count() - l0), "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="plain_large", choices=["plain_large", "plain_small", "batched"],
+    ap.add_argument("--workload", default="plain_large", choices=["plain_large", "plain_small", "batched", "learned"],
                     help="plain_large: the 512^3 dipole + blocks workload (default); plain_small: 128^3 sphere; "
                          "batched: 256 antenna scenes to port ring-down (sweeps/hr)")
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
     ap.add_argument("--seed", type=int, default=2024, help="batched: scene seed")
     ap.add_argument("--no-single", action="store_true", help="batched: skip the one-grid-per-scene comparison")
     ap.add_argument("--single-all", action="store_true", help="batched: compare on every scene, not a sample")
+    ap.add_argument("--train-scenes", type=int, default=4096, help="learned: training scenes")
+    ap.add_argument("--epochs", type=int, default=60, help="learned: training epochs")
     ap.add_argument("--size", type=int, default=512, help="edge of the plain_large grid")
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
     ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 32, 64, 128])
@@ -376,6 +411,8 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "learned":
+        return run_learned(args)
 
     import torch
     rank, world, local = _rank_env()

@@ -153,7 +153,10 @@ class _Group:
 class BatchRunner:
     """Steps `scenes` (each with one feed port) to port ring-down in stacks grouped by cross-section."""
 
-    def __init__(self, scenes, chunk: int = 64, max_steps: int = 200_000, compact_fraction: float = 0.25):
+    def __init__(self, scenes, chunk: int = 64, max_steps: int = 200_000, compact_fraction: float = 0.25,
+                 stop_steps=None):
+        """stop_steps: per scene, stop after this many steps without waiting for the ring-down (the
+        early window of a learned extrapolation); None: run every scene to ring-down."""
         for sc in scenes:
             if not sc.ports:
                 raise ValueError(f"{sc.name}: a batched scene needs a feed port")
@@ -170,7 +173,10 @@ class BatchRunner:
         self.groups = [_Group(self.scenes, idx, self.chunk) for _, idx in sorted(groups.items(), key=lambda kv: kv[0])]
         self.setup_s = time.perf_counter() - t0
         self.results = [SceneResult(i) for i in range(len(self.scenes))]
-        self.watch = [_watch(sc, float(sc.grid.courant)) for sc in self.scenes]
+        if stop_steps is None:
+            self.watch = [_watch(sc, float(sc.grid.courant)) for sc in self.scenes]
+        else:
+            self.watch = [RingDown(window=1 << 40, min_steps=int(n), max_steps=int(n)) for n in stop_steps]
         self.cell_steps = 0
         self.steps = 0
 

@@ -136,7 +136,7 @@ def fibonacci_directions(n: int) -> np.ndarray:
 BATCH_EDGES = tuple(range(48, 161, 16))
 
 
-def batched_scene(seed: int, index: int, pml: int = 8):
+def batched_scene(seed: int, index: int, pml: int = 8, edges=BATCH_EDGES):
     """One scene of the batched antenna sweep: a cube of edge 48, 64, ..., 160 cells (uniform) with an
     8-cell absorber; a thin-wire z dipole at the centre or a monopole over a PEC ground plate (50/50),
     length uniform in [0.3, 0.7] lambda, wire radius uniform in [0.02, 0.2] cell, fed by a 50-ohm
@@ -144,7 +144,7 @@ def batched_scene(seed: int, index: int, pml: int = 8):
     sphere or box (eps_r uniform in [1, 10], sigma log-uniform in [1e-4, 1e-1] S/m) beside it.
     lambda = 0.6 (edge - 2 pml) cells. Port sweep 0.3-1.7 f0 at 128 points. Seeded by (seed, index)."""
     rng = np.random.default_rng([int(seed), int(index)])
-    n = int(rng.choice(BATCH_EDGES))
+    n = int(rng.choice(edges))
     grid = abi.GridConfig((n, n, n), courant=0.5, pml_thickness=pml, pml_sigma_max=1.6, pml_grading=3.0)
     wl = float(f32(0.6 * (n - 2 * pml)))
     b = EnvironmentBuilder(f"batch{seed}_{index}", grid, wavelength=wl)
@@ -188,5 +188,5 @@ def batched_scene(seed: int, index: int, pml: int = 8):
     return sc
 
 
-def batched_scenes(count: int = 256, seed: int = 2024):
-    return [batched_scene(seed, i) for i in range(count)]
+def batched_scenes(count: int = 256, seed: int = 2024, edges=BATCH_EDGES):
+    return [batched_scene(seed, i, edges=edges) for i in range(count)]

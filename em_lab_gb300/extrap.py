@@ -1,0 +1,432 @@
+"""Learned ring-down extrapolator: predicts a scene's converged port impedance Z(f) from the first few
+periods of its port V(t), I(t), so an antenna sweep can stop each scene early.
+
+Network (every layer a GEMM on the tcgen05 tensor cores with BF16 operands and FP32 accumulation,
+csrc/learn.cu; FP32 master weights and Adam):
+  encoder  conv1d 2 -> 32 channels (kernel 8, stride 4, pad 2, ReLU): 256 samples -> 64 positions
+           conv1d 32 -> 64 channels (kernel 8, stride 4, pad 2, ReLU): 64 -> 16 positions
+  head     [1024 encoder features | 256 truncated-DFT features] -> 256 -> 256 -> 256 -> 256 (ReLU)
+           -> 256 outputs: Re, Im of Z(f) / 100 ohm at the 128 sweep frequencies.
+Inputs (host, from the early window of `PERIODS_IN` design periods): V and I resampled to 256
+points in units of the period (I scaled by eta0 / 100, both by the window's peak), and the "method
+without the network": Z_trunc(f) = -V(f) / I(f) * eta0 from the DFT of the early window alone.
+Targets: Z(f) of the whole series run to -60 dB ring-down (the plain solver is the judge).
+PyTorch only allocates the device buffers and moves the batches; every forward and backward
+operation is a kernel of this library.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import time
+
+import numpy as np
+
+from .batch import K_ETA0, sweep_sums
+from .grid import _check, load_library
+
+T_IN = 256             # resampled early-window samples per channel
+PERIODS_IN = 4.0       # early window, design periods
+NF = 128               # sweep frequencies
+Z_SCALE = 100.0        # ohm per output unit
+Z_CLIP = 10.0          # feature / target clip (units of Z_SCALE)
+I_SCALE = K_ETA0 / 100.0
+
+CONV = [  # (name, c_in, c_out, kernel, stride, pad, L_in, L_out)
+    ("conv1", 2, 32, 8, 4, 2, 256, 64),
+    ("conv2", 32, 64, 8, 4, 2, 64, 16),
+]
+ENC = CONV[-1][2] * CONV[-1][7]  # 1024 encoder features
+HEAD = [("fc1", ENC + 2 * NF, 256, True), ("fc2", 256, 256, True), ("fc3", 256, 256, True),
+        ("fc4", 256, 256, True), ("out", 256, 2 * NF, False)]
+
+
+def layer_shapes():
+    """(name, fan_out, fan_in) of every weight matrix; conv weights are (c_out, kernel * c_in)."""
+    s = [(n, co, k * ci) for n, ci, co, k, *_ in CONV]
+    s += [(n, o, i) for n, i, o, _ in HEAD]
+    return s
+
+
+def init_params(seed: int = 0):
+    """He-initialised FP32 weights and zero biases: {name: (W (out, in), b (out,))}."""
+    rng = np.random.default_rng(seed)
+    p = {}
+    for name, o, i in layer_shapes():
+        scale = math.sqrt(2.0 / i) if name != "out" else math.sqrt(1.0 / i)
+        p[name] = (rng.standard_normal((o, i)).astype(np.float32) * np.float32(scale), np.zeros(o, np.float32))
+    return p
+
+
+# ---- features ------------------------------------------------------------------------------------
+def early_steps(sc) -> int:
+    return int(math.ceil(PERIODS_IN * sc.wavelength / float(sc.grid.courant)))
+
+
+def truncated_z(sc, series_early):
+    """The method without the network: Z(f) from the DFT of the early window alone."""
+    from .batch import impedance
+    sw = sc.sweep
+    sums = sweep_sums(series_early, sw["wavelength_min"], sw["wavelength_max"], NF, float(sc.grid.courant))
+    return impedance(sums, sw["wavelength_min"], sw["wavelength_max"], float(sc.ports[0].impedance_ohm))["z"]
+
+
+def features(sc, series):
+    """(x (T_IN, 2) float32 position-major, zt (2 NF,) float32, Z_trunc complex (NF,)) from the first
+    early_steps(sc) rows of a scene's (V, I) series."""
+    n = early_steps(sc)
+    ser = np.asarray(series[:n], np.float64)
+    if ser.shape[0] < n:
+        raise ValueError("series shorter than the early window")
+    t = np.arange(T_IN) * (n / T_IN)
+    k = np.arange(n)
+    v = np.interp(t, k, ser[:, 0])
+    i = np.interp(t, k, ser[:, 1]) * I_SCALE
+    peak = max(np.abs(v).max(), np.abs(i).max(), 1e-30)
+    x = np.stack([v / peak, i / peak], axis=1).astype(np.float32)
+    zt = truncated_z(sc, ser.astype(np.float32))
+    zf = np.concatenate([np.clip(zt.real / Z_SCALE, -Z_CLIP, Z_CLIP), np.clip(zt.imag / Z_SCALE, -Z_CLIP, Z_CLIP)])
+    return x, zf.astype(np.float32), zt
+
+
+def target(z_conv):
+    return np.concatenate([np.clip(z_conv.real / Z_SCALE, -Z_CLIP, Z_CLIP),
+                           np.clip(z_conv.imag / Z_SCALE, -Z_CLIP, Z_CLIP)]).astype(np.float32)
+
+
+def to_z(y):
+    y = np.asarray(y, np.float64)
+    return (y[..., :NF] + 1j * y[..., NF:]) * Z_SCALE
+
+
+# ---- device network --------------------------------------------------------------------------------
+class Net:
+    """The extrapolator on the GPU: FP32 master weights, BF16 copies, Adam state, activations for a
+    batch of up to `batch` rows. forward() / backward() / step() launch this library's kernels."""
+
+    def __init__(self, params, batch: int = 256, device: str = "cuda"):
+        import torch
+        self.torch = torch
+        self.lib = _nn_lib()
+        self.B = int(batch)
+        self.dev = device
+        f32, bf16 = torch.float32, torch.bfloat16
+        self.W, self.Wb, self.b, self.mW, self.vW, self.mb, self.vb, self.gW, self.gb = {}, {}, {}, {}, {}, {}, {}, {}, {}
+        for name, o, i in layer_shapes():
+            w, b = params[name]
+            self.W[name] = torch.from_numpy(np.ascontiguousarray(w)).to(device)
+            self.Wb[name] = torch.empty((o, i), dtype=bf16, device=device)
+            self.b[name] = torch.from_numpy(np.ascontiguousarray(b)).to(device)
+            for d, shape in ((self.mW, (o, i)), (self.vW, (o, i)), (self.gW, (o, i)), (self.mb, (o,)),
+                             (self.vb, (o,)), (self.gb, (o,))):
+                d[name] = torch.zeros(shape, dtype=f32, device=device)
+            self._conv(self.W[name], self.Wb[name])
+        B = self.B
+        z = lambda *s, dt=f32: torch.zeros(s, dtype=dt, device=device)  # noqa: E731
+        self.x0 = z(B, T_IN, 2, dt=bf16)
+        self.cols1 = z(B * 64, 16, dt=bf16)
+        self.z1 = z(B * 64, 32)
+        self.a1 = z(B * 64, 32, dt=bf16)
+        self.cols2 = z(B * 16, 256, dt=bf16)
+        self.z2 = z(B * 16, 64)
+        self.X0 = z(B, ENC + 2 * NF, dt=bf16)
+        self.zh = {n: z(B, o) for n, i, o, _ in HEAD}
+        self.ah = {n: z(B, o, dt=bf16) for n, i, o, r in HEAD if r}
+        self.y = self.zh["out"]
+        self.t = z(B, 2 * NF)
+        self.dy = z(B, 2 * NF)
+        self.dz = {n: z(B, o) for n, i, o, _ in HEAD}
+        self.dzb = {n: z(B, o, dt=bf16) for n, i, o, _ in HEAD}
+        self.dx = {n: z(B, i) for n, i, o, _ in HEAD}
+        self.dz2 = z(B * 16, 64)
+        self.dz2b = z(B * 16, 64, dt=bf16)
+        self.dcols2 = z(B * 16, 256)
+        self.da1 = z(B * 64, 32)
+        self.dz1 = z(B * 64, 32)
+        self.dz1b = z(B * 64, 32, dt=bf16)
+        self.loss = z(1)
+        self.t_step = 0
+        self.n = 0
+
+    # -- helpers
+    @property
+    def stream(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def _p(self, t):
+        return C.c_void_p(t.data_ptr())
+
+    def _fp(self, t):
+        return C.cast(C.c_void_p(t.data_ptr()), C.POINTER(C.c_float))
+
+    def _conv(self, src, dst_bf, ldo=None, cols=None, off=0):
+        n = src.numel()
+        cols = cols or (src.shape[-1] if src.dim() > 1 else n)
+        _check(self.lib.emlab_nn_to_bf16(self._fp(src), n, self._p(dst_bf), ldo or cols, cols, off, self.stream))
+
+    def _gemm(self, M, N, K, A, sam, sak, B, sbn, sbk, Cc, ldc):
+        _check(self.lib.emlab_nn_gemm(M, N, K, self._p(A), sam, sak, self._p(B), sbn, sbk, self._fp(Cc), ldc,
+                                      self.stream))
+
+    def _bias_act(self, z, bias, M, N, relu, out, ldo, off, bias_n):
+        _check(self.lib.emlab_nn_bias_act(self._fp(z), self._fp(bias), M, N, bias_n, 1 if relu else 0,
+                                          self._p(out) if out is not None else None, ldo, off, self.stream))
+
+    def load(self, x, zt, t=None):
+        """A batch: x (n, T_IN, 2), zt (n, 2 NF), targets t (n, 2 NF) (float32 host arrays)."""
+        torch = self.torch
+        n = x.shape[0]
+        assert n <= self.B
+        self.n = n
+        xs = torch.zeros((self.B, T_IN, 2), dtype=torch.float32, device=self.dev)
+        xs[:n] = torch.from_numpy(np.ascontiguousarray(x, np.float32)).to(self.dev)
+        zs = torch.zeros((self.B, 2 * NF), dtype=torch.float32, device=self.dev)
+        zs[:n] = torch.from_numpy(np.ascontiguousarray(zt, np.float32)).to(self.dev)
+        self._conv(xs.view(self.B * T_IN, 2), self.x0.view(self.B * T_IN, 2))
+        self._conv(zs, self.X0, ldo=ENC + 2 * NF, cols=2 * NF, off=ENC)
+        self.t.zero_()
+        if t is not None:
+            self.t[:n] = torch.from_numpy(np.ascontiguousarray(t, np.float32)).to(self.dev)
+
+    # -- forward / backward
+    def forward(self):
+        B, lib, s = self.B, self.lib, self.stream
+        c1, c2 = CONV
+        _check(lib.emlab_nn_im2col(self._p(self.x0), B, c1[6], c1[1], c1[3], c1[4], c1[5], c1[7], self._p(self.cols1), s))
+        self._gemm(B * 64, 32, 16, self.cols1, 16, 1, self.Wb["conv1"], 16, 1, self.z1, 32)
+        self._bias_act(self.z1, self.b["conv1"], B * 64, 32, True, self.a1, 32, 0, 32)
+        _check(lib.emlab_nn_im2col(self._p(self.a1), B, c2[6], c2[1], c2[3], c2[4], c2[5], c2[7], self._p(self.cols2), s))
+        self._gemm(B * 16, 64, 256, self.cols2, 256, 1, self.Wb["conv2"], 256, 1, self.z2, 64)
+        # rows (b, l) of z2 are the encoder features of sample b at columns l * 64 + c
+        self._bias_act(self.z2, self.b["conv2"], B, ENC, True, self.X0, ENC + 2 * NF, 0, 64)
+        x = self.X0
+        for name, i, o, relu in HEAD:
+            self._gemm(B, o, i, x, i, 1, self.Wb[name], i, 1, self.zh[name], o)
+            out = self.ah.get(name)
+            self._bias_act(self.zh[name], self.b[name], B, o, relu, out, o, 0, o)
+            x = out
+        return self.y
+
+    def backward(self):
+        """MSE gradients of every weight and bias (loss over the loaded rows; padding rows carry zero
+        targets and zero outputs' gradient is masked by the row count)."""
+        B, lib, s = self.B, self.lib, self.stream
+        n = self.n
+        self.loss.zero_()
+        # only the loaded rows contribute: gradient rows beyond n are zero
+        self.dy.zero_()
+        _check(lib.emlab_nn_mse(self._fp(self.y), self._fp(self.t), n * 2 * NF, self._fp(self.dy),
+                                self._fp(self.loss), s))
+        up = self.dy
+        ins = {"fc1": self.X0}
+        for k in range(1, len(HEAD)):
+            ins[HEAD[k][0]] = self.ah[HEAD[k - 1][0]]
+        for name, i, o, relu in reversed(HEAD):
+            dz, dzb = self.dz[name], self.dzb[name]
+            _check(lib.emlab_nn_act_grad(self._fp(up), o, 0, self._fp(self.zh[name]), B, o, 1 if relu else 0,
+                                         self._fp(dz), self._p(dzb), s))
+            self._gemm(o, i, B, dzb, 1, o, ins[name], 1, i, self.gW[name], i)
+            _check(lib.emlab_nn_col_sum(self._fp(dz), B, o, self._fp(self.gb[name]), s))
+            self._gemm(B, i, o, dzb, o, 1, self.Wb[name], 1, i, self.dx[name], i)
+            up = self.dx[name]
+        c1, c2 = CONV
+        # conv2: dz2 over rows (b, l) x 64 channels = the encoder part of d(X0)
+        _check(lib.emlab_nn_act_grad(self._fp(up), ENC + 2 * NF, 0, self._fp(self.z2), B, ENC, 1, self._fp(self.dz2),
+                                     self._p(self.dz2b), s))
+        self._gemm(64, 256, B * 16, self.dz2b, 1, 64, self.cols2, 1, 256, self.gW["conv2"], 256)
+        _check(lib.emlab_nn_col_sum(self._fp(self.dz2), B * 16, 64, self._fp(self.gb["conv2"]), s))
+        self._gemm(B * 16, 256, 64, self.dz2b, 64, 1, self.Wb["conv2"], 1, 256, self.dcols2, 256)
+        _check(lib.emlab_nn_col2im(self._fp(self.dcols2), B, c2[6], c2[1], c2[3], c2[4], c2[5], c2[7],
+                                   self._fp(self.da1), s))
+        _check(lib.emlab_nn_act_grad(self._fp(self.da1), 32, 0, self._fp(self.z1), B * 64, 32, 1, self._fp(self.dz1),
+                                     self._p(self.dz1b), s))
+        self._gemm(32, 16, B * 64, self.dz1b, 1, 32, self.cols1, 1, 16, self.gW["conv1"], 16)
+        _check(lib.emlab_nn_col_sum(self._fp(self.dz1), B * 64, 32, self._fp(self.gb["conv1"]), s))
+
+    def step(self, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        self.t_step += 1
+        for name, o, i in layer_shapes():
+            _check(self.lib.emlab_nn_adam(self._fp(self.W[name]), self._fp(self.mW[name]), self._fp(self.vW[name]),
+                                          self._fp(self.gW[name]), o * i, lr, b1, b2, eps, self.t_step,
+                                          self._p(self.Wb[name]), self.stream))
+            _check(self.lib.emlab_nn_adam(self._fp(self.b[name]), self._fp(self.mb[name]), self._fp(self.vb[name]),
+                                          self._fp(self.gb[name]), o, lr, b1, b2, eps, self.t_step, None,
+                                          self.stream))
+
+    def status(self):
+        _check(self.lib.emlab_nn_status(self.stream))
+
+    def predict(self, x, zt):
+        out = []
+        for s in range(0, x.shape[0], self.B):
+            self.load(x[s:s + self.B], zt[s:s + self.B])
+            self.forward()
+            out.append(self.y[: self.n].cpu().numpy())
+        self.status()
+        return np.concatenate(out) if out else np.zeros((0, 2 * NF), np.float32)
+
+    def params(self):
+        return {n: (self.W[n].cpu().numpy(), self.b[n].cpu().numpy()) for n, _, _ in layer_shapes()}
+
+    def grads(self):
+        return {n: (self.gW[n].cpu().numpy(), self.gb[n].cpu().numpy()) for n, _, _ in layer_shapes()}
+
+
+def _nn_lib():
+    lib = load_library()
+    if getattr(lib, "_nn_ready", False):
+        return lib
+    P, I, L, F = C.c_void_p, C.c_int, C.c_longlong, C.c_float
+    fp = C.POINTER(C.c_float)
+    sig = {
+        "emlab_nn_gemm": [I, I, I, P, L, L, P, L, L, fp, L, P],
+        "emlab_nn_status": [P],
+        "emlab_nn_bias_act": [fp, fp, I, I, I, I, P, L, I, P],
+        "emlab_nn_act_grad": [fp, L, I, fp, I, I, I, fp, P, P],
+        "emlab_nn_col_sum": [fp, I, I, fp, P],
+        "emlab_nn_im2col": [P, I, I, I, I, I, I, I, P, P],
+        "emlab_nn_col2im": [fp, I, I, I, I, I, I, I, fp, P],
+        "emlab_nn_mse": [fp, fp, L, fp, fp, P],
+        "emlab_nn_adam": [fp, fp, fp, fp, L, F, F, F, F, I, P, P],
+        "emlab_nn_to_bf16": [fp, L, P, L, I, I, P],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes, fn.restype = args, I
+    lib._nn_ready = True
+    return lib
+
+
+# ---- data, training, evaluation --------------------------------------------------------------------
+def dataset(scenes, results):
+    """(x, zt, t, z_trunc, z_conv) arrays of the scenes that rang down and ran past the early window."""
+    xs, zts, ts, ztr, zc = [], [], [], [], []
+    for sc, r in zip(scenes, results):
+        if not (r.done and r.rung_down and r.sweep is not None):
+            continue
+        ser = np.concatenate(r.series)
+        if ser.shape[0] < early_steps(sc):
+            continue
+        x, zf, ztrunc = features(sc, ser)
+        xs.append(x), zts.append(zf), ts.append(target(r.sweep["z"])), ztr.append(ztrunc), zc.append(r.sweep["z"])
+    if not xs:
+        return None
+    return (np.stack(xs), np.stack(zts), np.stack(ts), np.stack(ztr), np.stack(zc))
+
+
+def train(x, zt, t, epochs=40, batch=256, lr=1e-3, seed=0, log=None):
+    """Adam on the MSE of Z(f) / 100 ohm with a cosine learning-rate decay; returns (Net, per-epoch
+    mean losses)."""
+    net = Net(init_params(seed), batch=batch)
+    rng = np.random.default_rng(seed)
+    n = x.shape[0]
+    losses = []
+    for ep in range(epochs):
+        order = rng.permutation(n)
+        tot, cnt = 0.0, 0
+        lr_ep = lr * 0.5 * (1.0 + math.cos(math.pi * ep / max(epochs, 1)))
+        for s in range(0, n, batch):
+            idx = order[s:s + batch]
+            net.load(x[idx], zt[idx], t[idx])
+            net.forward()
+            net.backward()
+            net.step(lr=lr_ep)
+            tot += float(net.loss.item()) * len(idx)
+            cnt += len(idx)
+        net.status()
+        losses.append(tot / max(cnt, 1))
+        if log:
+            log(f"epoch {ep}: loss {losses[-1]:.5f}")
+    return net, losses
+
+
+def rel_error(z_pred, z_ref):
+    """|Z_pred - Z_ref| / |Z_ref| per frequency."""
+    return np.abs(z_pred - z_ref) / np.maximum(np.abs(z_ref), 1e-9)
+
+
+def s11_db(z, z0=50.0):
+    g = np.abs((z - z0) / (z + z0))
+    return 20.0 * np.log10(np.maximum(g, 1e-10))
+
+
+def summary(z_pred, z_ref):
+    """Per-scene median |dZ| / |Z| over the band, and |S11| dB error, summarised over scenes."""
+    rel = np.median(rel_error(z_pred, z_ref), axis=1)
+    ds11 = np.median(np.abs(s11_db(z_pred) - s11_db(z_ref)), axis=1)
+    return {"dz_median": float(np.median(rel)), "dz_p90": float(np.percentile(rel, 90)),
+            "within_2pct": float(np.mean(rel <= 0.02)), "s11_db_median": float(np.median(ds11)),
+            "s11_db_p90": float(np.percentile(ds11, 90)), "scenes": int(rel.size)}
+
+
+def run_scenes(scenes, early: bool):
+    """Steps scenes in stacks: to ring-down (early False) or for their early window only; returns
+    (results, wall seconds of the run, stack set-up excluded)."""
+    from .batch import BatchRunner
+    stop = [early_steps(sc) for sc in scenes] if early else None
+    r = BatchRunner(scenes, chunk=64, stop_steps=stop)
+    res = r.run()
+    r.close()
+    return res, r.wall_s
+
+
+WAVE = 512  # scenes stepped together at most (device memory: about 50 GB of stacks per wave)
+
+
+def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=1e-3, seed=0, edges=None, log=None):
+    """Generates training runs with the batched solver (every scene to -60 dB ring-down, in waves of
+    WAVE scenes), trains the extrapolator, and on held-out scenes compares (a) the plain solver run
+    to ring-down, the judge, (b) the early window's truncated DFT (the method without the network)
+    and (c) the network's prediction from the same early window. Sweeps/hr of (a) and (c) are
+    wall-clock figures of stepping, read-back, features and inference (stack set-up excluded)."""
+    from . import configs
+    edges = edges or configs.BATCH_EDGES
+    out = {}
+    t0 = time.perf_counter()
+    rows = [[], [], []]
+    tr_wall = 0.0
+    for w0 in range(0, n_train, WAVE):
+        scenes = [configs.batched_scene(train_seed, i, edges=edges) for i in range(w0, min(n_train, w0 + WAVE))]
+        res, wall = run_scenes(scenes, early=False)
+        tr_wall += wall
+        d = dataset(scenes, res)
+        if d is not None:
+            for k in range(3):
+                rows[k].append(d[k])
+        if log:
+            log(f"training runs {w0 + len(scenes)}/{n_train}: {wall:.1f} s")
+    x, zt, t = (np.concatenate(r) for r in rows)
+    out["train_runs"] = {"scenes": n_train, "usable": int(x.shape[0]), "wall_s": tr_wall}
+    t1 = time.perf_counter()
+    net, losses = train(x, zt, t, epochs=epochs, batch=batch, lr=lr, seed=seed, log=log)
+    out["training"] = {"epochs": epochs, "samples": int(x.shape[0]), "loss_first": losses[0], "loss_last": losses[-1],
+                       "wall_s": time.perf_counter() - t1}
+    eval_scenes = [configs.batched_scene(eval_seed, i, edges=edges) for i in range(n_eval)]
+    # (a) the judge: plain runs of the held-out scenes to ring-down
+    ev_res, plain_wall = run_scenes(eval_scenes, early=False)
+    # (b, c) the early window only, then features and inference
+    early_res, early_wall = run_scenes(eval_scenes, early=True)
+    t2 = time.perf_counter()
+    xs, zts, ztr, keep = [], [], [], []
+    for k, (sc, r) in enumerate(zip(eval_scenes, early_res)):
+        ser = np.concatenate(r.series)
+        if ser.shape[0] < early_steps(sc):
+            continue
+        xe, ze, zr = features(sc, ser)
+        xs.append(xe), zts.append(ze), ztr.append(zr), keep.append(k)
+    y = net.predict(np.stack(xs), np.stack(zts))
+    infer_wall = time.perf_counter() - t2
+    learned_wall = early_wall + infer_wall
+    z_pred = to_z(y)
+    z_trunc = np.stack(ztr)
+    ok = [j for j, k in enumerate(keep) if ev_res[k].rung_down]
+    z_conv = np.stack([ev_res[keep[j]].sweep["z"] for j in ok])
+    out["eval"] = {"scenes": n_eval, "judged": len(ok),
+                   "network": summary(z_pred[ok], z_conv), "truncated_dft": summary(z_trunc[ok], z_conv)}
+    out["sweeps_per_hour"] = {"plain": n_eval / plain_wall * 3600.0, "learned": n_eval / learned_wall * 3600.0}
+    out["speedup"] = plain_wall / learned_wall
+    out["wall"] = {"plain_s": plain_wall, "early_s": early_wall, "features_inference_s": infer_wall}
+    out["steps"] = {"plain_median": float(np.median([r.steps for r in ev_res])),
+                    "early_median": float(np.median([early_steps(sc) for sc in eval_scenes]))}
+    out["wall_s"] = time.perf_counter() - t0
+    return out, net.params()

@@ -1,0 +1,84 @@
+"""The learned extrapolator's host side: the CPU restatement's backward formulas against finite
+differences, its BF16 rounding, and the early-window features."""
+import math
+
+import numpy as np
+import pytest
+
+from em_lab_gb300 import batch, configs, extrap
+from oracle import extrap_ref as R
+
+
+def small_params(seed=1):
+    p = extrap.init_params(seed)
+    return {k: (w.astype(np.float64), b.astype(np.float64) + 0.01) for k, (w, b) in p.items()}
+
+
+def test_bf16_rounding_is_nearest_even():
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -9, -2.5, 1e-30, 3.14159265], np.float32)
+    r = R.bf16(x)
+    assert r[0] == 1.0 and r[1] == 1.0  # a tie rounds to the even mantissa
+    assert r[2] == np.float32(1.0 + 2 ** -7)  # above the tie: up
+    assert r[3] == -2.5
+    assert r[5] == np.float32(3.140625)
+    assert np.all(R.bf16(r) == r)
+
+
+def test_backward_matches_finite_differences():
+    rng = np.random.default_rng(0)
+    p = small_params()
+    B, n = 3, 3
+    x = rng.standard_normal((B, extrap.T_IN, 2))
+    zt = rng.standard_normal((B, 2 * extrap.NF)) * 0.5
+    t = rng.standard_normal((B, 2 * extrap.NF)) * 0.5
+    y, cache = R.forward(p, x, zt, exact=True)
+    g = R.backward(p, cache, t, n, exact=True)
+    for name in ("conv1", "conv2", "fc1", "fc3", "out"):
+        w, b = p[name]
+        for _ in range(3):
+            i, j = rng.integers(0, w.shape[0]), rng.integers(0, w.shape[1])
+            h = 1e-6
+            wp, wm = w.copy(), w.copy()
+            wp[i, j] += h
+            wm[i, j] -= h
+            lp = R.loss({**p, name: (wp, b)}, x, zt, t, n)
+            lm = R.loss({**p, name: (wm, b)}, x, zt, t, n)
+            fd = (lp - lm) / (2 * h)
+            assert g[name][0][i, j] == pytest.approx(fd, rel=1e-4, abs=1e-9), (name, i, j)
+        k = rng.integers(0, b.shape[0])
+        bp, bm = b.copy(), b.copy()
+        bp[k] += 1e-6
+        bm[k] -= 1e-6
+        fd = (R.loss({**p, name: (w, bp)}, x, zt, t, n) - R.loss({**p, name: (w, bm)}, x, zt, t, n)) / 2e-6
+        assert g[name][1][k] == pytest.approx(fd, rel=1e-4, abs=1e-9), (name, "bias", k)
+
+
+def test_layer_shapes_follow_the_spec():
+    shapes = {n: (o, i) for n, o, i in extrap.layer_shapes()}
+    assert shapes["conv1"] == (32, 16) and shapes["conv2"] == (64, 256)
+    assert shapes["fc1"] == (256, 1024 + 256) and shapes["fc4"] == (256, 256) and shapes["out"] == (256, 256)
+    hidden = [n for n, i, o, r in extrap.HEAD if r]
+    assert len(hidden) == 4  # a 4-layer MLP head of width 256
+
+
+def test_features_are_scale_invariant_and_match_the_sweep():
+    sc = configs.batched_scene(4, 0)
+    n = extrap.early_steps(sc)
+    assert n == math.ceil(extrap.PERIODS_IN * sc.wavelength / 0.5)
+    k = np.arange(n + 50)
+    v = np.sin(k * 0.07) * np.exp(-k / 300.0)
+    i = 0.1 * np.cos(k * 0.07 + 0.3) * np.exp(-k / 300.0)
+    ser = np.stack([v, i], axis=1).astype(np.float32)
+    x1, z1, zt1 = extrap.features(sc, ser)
+    x2, z2, zt2 = extrap.features(sc, ser * np.float32(8.0))
+    np.testing.assert_allclose(x1, x2, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(zt1, zt2, rtol=1e-5)
+    assert x1.shape == (extrap.T_IN, 2) and z1.shape == (2 * extrap.NF,)
+    assert np.abs(x1).max() == pytest.approx(1.0, rel=1e-6)
+    # Z_trunc is the sweep of the early window alone
+    sw = sc.sweep
+    ref = batch.impedance(batch.sweep_sums(ser[:n], sw["wavelength_min"], sw["wavelength_max"], 128, 0.5),
+                          sw["wavelength_min"], sw["wavelength_max"], 50.0)["z"]
+    np.testing.assert_allclose(zt1, ref, rtol=1e-9)
+    np.testing.assert_allclose(extrap.to_z(extrap.target(ref)), np.clip(ref.real, -1000, 1000) +
+                               1j * np.clip(ref.imag, -1000, 1000), rtol=1e-5)
