@@ -365,6 +365,7 @@ def run_learned(args):
     if world > 1 and rank != 0:
         return 0
     torch.cuda.set_device(local)
+    extrap.PERIODS_IN = float(args.periods)
     l0 = launch_count()
     with ClockSampler(local) as clk:
         out, _ = extrap.experiment(args.seed, args.train_scenes, args.seed + 1, args.scenes, epochs=args.epochs,
@@ -399,7 +400,8 @@ def main():
     ap.add_argument("--no-single", action="store_true", help="batched: skip the one-grid-per-scene comparison")
     ap.add_argument("--single-all", action="store_true", help="batched: compare on every scene, not a sample")
     ap.add_argument("--train-scenes", type=int, default=4096, help="learned: training scenes")
-    ap.add_argument("--epochs", type=int, default=60, help="learned: training epochs")
+    ap.add_argument("--epochs", type=int, default=300, help="learned: training epochs")
+    ap.add_argument("--periods", type=float, default=4.0, help="learned: early window, design periods")
     ap.add_argument("--size", type=int, default=512, help="edge of the plain_large grid")
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
     ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 32, 64, 128])
