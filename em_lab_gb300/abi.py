@@ -79,6 +79,14 @@ class RenderParams(C.Structure):
                 ("material_opacity", C.c_float), ("exposure", C.c_float), ("mode", C.c_int), ("signed_axis", C.c_int)]
 
 
+class RadarGeometry(C.Structure):
+    """emlab_radar_geometry: the back-projection image grid and array frame."""
+    _fields_ = [("tx", C.c_float * 3), ("axes", C.c_float * 9), ("interior_min", C.c_float * 3),
+                ("interior_max", C.c_float * 3), ("omega", C.c_double), ("dt", C.c_double), ("sample_dt", C.c_double),
+                ("r0", C.c_float), ("dr", C.c_float), ("az0", C.c_float), ("daz", C.c_float), ("el0", C.c_float),
+                ("del_", C.c_float), ("nr", C.c_int), ("naz", C.c_int), ("nel", C.c_int)]
+
+
 class GridState(C.Structure):
     _fields_ = [("time", C.c_double), ("dt", C.c_float), ("step_count", C.c_uint64), ("nx", C.c_int),
                 ("ny", C.c_int), ("nz", C.c_int), ("device_bytes", C.c_uint64), ("source_cells", C.c_int),

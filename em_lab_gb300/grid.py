@@ -81,6 +81,7 @@ def load_library() -> C.CDLL:
         "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_render": ([P, C.POINTER(abi.RenderParams), C.POINTER(C.c_ubyte)], I),
         "emlab_ports_take_series": ([P, fp, SZ, C.POINTER(SZ)], I),
+        "emlab_radar_backproject": ([C.POINTER(abi.RadarGeometry), fp, I, I, fp, dp, fp, dp, I, dp], I),
         "emlab_grid_set_graph": ([P, I], I),
         "emlab_stack_configure": ([P, C.POINTER(abi.GridConfig), ip, I], I),
         "emlab_stack_info": ([P, ip, ip, ip], I),
@@ -326,6 +327,12 @@ class SimulationGrid:
         out = np.zeros((max(1, steps.value), max(1, n), 2), np.float32)
         _check(self._lib.emlab_ports_read_series(self._h, _fptr(out), steps.value, C.byref(steps)))
         return out[: steps.value, :n]
+
+    def ports_recorded(self) -> int:
+        """Steps recorded so far (PortMonitor::recordedSteps)."""
+        steps = C.c_size_t()
+        _check(self._lib.emlab_ports_read_series(self._h, None, 0, C.byref(steps)))
+        return int(steps.value)
 
     def ports_take_series(self, max_steps: int) -> np.ndarray:
         """The steps recorded since the last take (at most max_steps), (steps, ports, 2); recording

@@ -87,8 +87,10 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False, scree
         return 3, None
     sc = res.scene
     grid = SimulationGrid(sc.grid)
-    m = sc.materials
-    grid.upload_materials(m.sigma, m.epsilon_r, sc.edges, sc.wires)
+    # a radar first records the scene without its targets (Main.cpp:472-507)
+    first = res.background if (getattr(sc, "radar", None) is not None and res.background is not None) else sc
+    m = first.materials
+    grid.upload_materials(m.sigma, m.epsilon_r, first.edges, first.wires)
     grid.set_sources(sc.sources)
     inst = Instruments(grid, sc, output_dir=res.output_dir)
     for w in res.warnings + inst.warnings:
@@ -108,6 +110,12 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False, scree
             grid.step(spf)
         grid.synchronize(600000)
         sim_ms = (time.perf_counter() - t0) * 1e3
+        if inst.radar is not None:  # swap in the targets once the calibration pass is recorded (Main.cpp:1079-1088)
+            inst.radar.update()
+            if inst.radar.calibration_complete():
+                grid.upload_materials(sc.materials.sigma, sc.materials.epsilon_r, sc.edges, sc.wires)
+                grid.reset_fields()
+                inst.radar.begin_measurement()
         if frame % 2 == 0 or spf == 0:
             inst.measure()
         if every_step and frame % 50 == 49:

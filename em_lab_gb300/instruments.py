@@ -165,6 +165,7 @@ class Instruments:
         self.ff_start = 0.0
         self.coaxes = list(getattr(scene, "coaxes", []))
         self.coax_readings = [None] * len(self.coaxes)
+        self.radar = None
         self.configure()
 
     # ------------------------------------------------------------------ set-up
@@ -202,8 +203,20 @@ class Instruments:
         if self.ports:
             avg = self.ff["averaging"] if self.ff else 4.0
             self.port_wavelength = max(self.ports[0].wavelength, 2.0)
-            g.ports_configure([p.to_c() for p in self.ports], self.port_wavelength, avg,
-                              sweep=self.sweep_setup is not None)
+            radar = getattr(sc, "radar", None)
+            if radar is not None:
+                # the radar records every element (and its reference channels) on the port monitor;
+                # the elements' readings are its first channels (Instruments.cpp:81-95)
+                from .radar import RadarMonitor
+                rs = dict(radar)
+                rs["log_path"] = self.resolve(rs.get("log", ""))
+                self.radar = RadarMonitor(g, rs, self.ports, sc.sources, self.ports[0].wavelength, sc.cell_size,
+                                          getattr(sc, "targets", []), self.warnings)
+                if self.radar.phase == "off":
+                    self.radar = None
+            if self.radar is None:
+                g.ports_configure([p.to_c() for p in self.ports], self.port_wavelength, avg,
+                                  sweep=self.sweep_setup is not None)
             self.port_start = t
         if self.ff:
             box = g.ntff_configure(self.ff["box_min"], self.ff["box_max"], self.ff["wavelength"], self.ff["averaging"])
@@ -552,7 +565,7 @@ class Instruments:
         periods = max(self.g.time() - self.port_start, 0.0) / self.port_wavelength
         accepted = sum(r["accepted"] for r in rd if r)
         available = sum(r["available"] for r in rd if r)
-        cw_lines = 0 if self.sweep_setup else max_lines
+        cw_lines = 0 if (self.sweep_setup or self.radar) else max_lines
         if periods < 12.0 and cw_lines > 0:
             out(f"    ports: averaging ({periods:.0f} of ~12 periods), impedances still settling")
         for i, p in enumerate(self.ports[:cw_lines]):
@@ -624,6 +637,8 @@ class Instruments:
         for f in self.fluxes:
             out(f"    flux  {f['setup'].name:<28s} P={f['inst']:+.4e}  <P>={f['avg']:+.4e}  peak|P|={f['peak']:.4e}")
         self.print_ports(4)
+        if self.radar:
+            self.radar.report(out)
         self.print_coax()
         if self.ff:
             pat = self.pattern

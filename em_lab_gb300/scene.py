@@ -385,6 +385,8 @@ class Scene:
     description: str = ""
     view: dict = field(default_factory=dict)       # ViewHints used by the headless runner
     coaxes: list = field(default_factory=list)     # CoaxSetup
+    radar: dict | None = None                      # RadarSetup (radar{})
+    targets: list = field(default_factory=list)    # TargetInfo of target = true objects
 
 
 class EnvironmentBuilder:

@@ -44,7 +44,7 @@ BUILTIN_MATERIALS = {
     "ground_wet": (25.0, None, 0.02, None), "water": (78.0, None, None, 0.1), "seawater": (74.0, None, 4.0, None),
 }
 
-UNSUPPORTED = ("loop", "frame", "radar", "emitter", "crpa")
+UNSUPPORTED = ("loop", "frame", "emitter", "crpa")
 
 
 class ScriptError(Exception):
@@ -86,6 +86,7 @@ class ScriptResult:
     warnings: list
     output: list
     output_dir: str = ""      # where relative log paths go (ScriptEngine.cpp:2647-2651)
+    background: object = None  # radar scenes: the scene without its targets (the calibration run)
 
 
 def _round_half_away(x: float) -> int:
@@ -277,7 +278,10 @@ def _parse_axis(s: str):
 class ScriptEngine:
     """One scene-script run (ScriptEngine::run / runOnce, ScriptEngine.cpp:2560-2654)."""
 
-    def __init__(self, overrides=None, echo=True):
+    def __init__(self, overrides=None, echo=True, with_targets=True):
+        self.with_targets = with_targets  # False: the radar's calibration run leaves out target = true objects
+        self.targets = []
+        self.radar = None
         self.overrides = dict(overrides or {})
         self.output = []
         self.echo = echo
@@ -405,6 +409,33 @@ class ScriptEngine:
         sz = np.abs(np.asarray(a.req_vec("size"), f32))
         return c - f32(0.5) * sz, c + f32(0.5) * sz
 
+    def target_info(self, shape, name):
+        """targetInfo (ScriptEngine.cpp:798-827): a radar target's bounds and the centres of its
+        cells, subsampled to about 200 000 points."""
+        lo_b, hi_b = shape.bounds()
+        n = np.asarray(self.settings.size)
+        lo = np.clip(np.floor(np.asarray(lo_b, np.float64)).astype(int), 0, n - 1)
+        hi = np.clip(np.ceil(np.asarray(hi_b, np.float64)).astype(int), 0, n - 1)
+        span = (hi - lo + 1).astype(np.float32)
+        stride = max(1, int(math.ceil(float(np.cbrt(f32(span[0] * span[1] * span[2]) / f32(200000.0))))))
+        zz, yy, xx = np.meshgrid(np.arange(lo[2], hi[2] + 1, stride), np.arange(lo[1], hi[1] + 1, stride),
+                                 np.arange(lo[0], hi[0] + 1, stride), indexing="ij")
+        px, py, pz = (xx + f32(0.5)).astype(f32), (yy + f32(0.5)).astype(f32), (zz + f32(0.5)).astype(f32)
+        inside = np.asarray(shape.contains(px, py, pz), bool)
+        pts = np.stack([px[inside], py[inside], pz[inside]], axis=1).astype(f32)
+        if pts.size:
+            mn, mx = pts.min(axis=0) - f32(0.5), pts.max(axis=0) + f32(0.5)
+        else:
+            mn, mx = np.asarray(lo_b, f32), np.asarray(hi_b, f32)
+        return {"name": name, "min": tuple(float(v) for v in mn), "max": tuple(float(v) for v in mx), "points": pts}
+
+    def take_target(self, a, shape) -> bool:
+        """target = true: record the target; True when the object is left out (calibration run)."""
+        if a.boolean("target", False):
+            self.targets.append(self.target_info(shape, a.str("name", a.what)))
+            return not self.with_targets
+        return False
+
     def fill_shape(self, a, local, center, m):
         r = a.opt_vec("rotate")
         if r is not None and math.sqrt(sum(v * v for v in r)) != 0.0:
@@ -412,6 +443,8 @@ class ScriptEngine:
         else:
             rot = np.eye(3, dtype=f32)
         shape = TransformedShape(local, center, rot)
+        if self.take_target(a, shape):
+            return 0
         n = self.env_builder().fill(shape, m)
         if n == 0:
             self.warn(f"{a.what}: shape is empty or lies completely outside the grid")
@@ -640,7 +673,7 @@ class ScriptEngine:
         G.rawset("grid", grid)
         self.grid = grid
 
-        api = {"scene": self.api_scene, "view": self.api_view, "material": self.api_material, "param": self.api_param,
+        api = {"radar": self.api_radar, "scene": self.api_scene, "view": self.api_view, "material": self.api_material, "param": self.api_param,
                "box": self.api_box, "sphere": self.api_sphere, "cylinder": self.api_cylinder,
                "wall": self.api_wall, "grating": self.api_grating, "shape": self.api_shape,
                "cage": self.api_cage, "array": self.api_array, "coax": self.api_coax,
@@ -656,6 +689,55 @@ class ScriptEngine:
                 raise LuaError(f"{_n}{{}}: not supported by this build (it drives a subsystem outside the FDTD "
                                f"time-stepping path)")
             I.register(name, unsupported)
+
+    # -- radar (ScriptEngine.cpp:1804-1848)
+    def api_radar(self, t=None, *r):
+        a = Args(self, "radar", ["range", "fov", "noise", "threshold", "dynamic_range", "reference", "phase_center",
+                                 "tx", "taper", "log", "name"], t)
+        self.lock()
+        rs = {"range_min": 0.0, "range_max": 0.0, "fov_az": 40.0, "fov_el": 40.0, "noise_db": -300.0,
+              "threshold_db": 13.0, "dynamic_range_db": 25.0, "reference": 0.0, "taper": 1,
+              "phase_center": (0.0, 0.0, 0.0), "tx": None, "log": ""}
+        rg = a.opt_vec2("range")
+        if rg is not None:
+            if not (rg[0] >= 0.0) or not (rg[1] > rg[0]):
+                a.fail("range = {min, max} needs 0 <= min < max (cells)")
+            rs["range_min"], rs["range_max"] = float(f32(rg[0])), float(f32(rg[1]))
+        if a.has("fov"):
+            v = a.raw("fov")
+            if type(v) in (int, float):
+                rs["fov_az"] = rs["fov_el"] = float(f32(a.opt_num("fov")))
+            else:
+                f2 = a.opt_vec2("fov")
+                if f2 is not None:
+                    rs["fov_az"], rs["fov_el"] = float(f32(f2[0])), float(f32(f2[1]))
+            if not (0.0 < rs["fov_az"] <= 80.0 and 0.0 < rs["fov_el"] <= 80.0):
+                a.fail("fov = half-angle in degrees (0..80), or {azimuth, elevation}")
+        nz = a.opt_num("noise")
+        if nz is not None:
+            if nz > 0.0:
+                a.fail("noise is in dB relative to the transmit pulse at a port, so it must be negative (e.g. -70)")
+            rs["noise_db"] = float(f32(nz))
+        rs["threshold_db"] = float(f32(a.num("threshold", 13.0)))
+        rs["dynamic_range_db"] = float(f32(a.positive("dynamic_range", 25.0)))
+        rs["reference"] = float(f32(a.num("reference", 0.0)))
+        rs["phase_center"] = tuple(float(v) for v in a.vec("phase_center", (0.0, 0.0, 0.0)))
+        tx = a.opt_vec("tx")
+        rs["tx"] = tuple(float(v) for v in tx) if tx is not None else None
+        taper = a.str("taper", "hamming").lower()
+        if taper in ("uniform", "none"):
+            rs["taper"] = 0
+        elif taper == "hamming":
+            rs["taper"] = 1
+        elif taper in ("hann", "hanning"):
+            rs["taper"] = 2
+        else:
+            a.fail(f"taper must be \"uniform\", \"hamming\" or \"hann\" (got \"{taper}\")")
+        rs["log"] = a.str("log", "")
+        if self.radar is not None:
+            self.warn("radar: only one radar per scene; replacing the previous one")
+        self.radar = rs
+        a.check_unknown()
 
     # -- scene / view / material / param (ScriptEngine.cpp:605-842)
     def api_scene(self, t=None, *r):
@@ -815,7 +897,6 @@ class ScriptEngine:
                 a.fail("thickness must be > 0")
             hi = np.maximum(h - f32(th), f32(0.0))
             local = DifferenceShape(local, BoxShape(-hi, hi))
-        a.boolean("target", False)
         self.fill_shape(a, local, c, m)
         a.check_unknown()
 
@@ -834,7 +915,6 @@ class ScriptEngine:
             ri = rad - f32(th)
             if np.all(ri > 0):
                 local = DifferenceShape(local, EllipsoidShape((0, 0, 0), ri))
-        a.boolean("target", False)
         self.fill_shape(a, local, c, m)
         a.check_unknown()
 
@@ -858,7 +938,6 @@ class ScriptEngine:
             wall = rad - inner
             inner_half = f32(0.5) * ln - wall if capped else f32(0.5) * ln + f32(1.0)
             local = DifferenceShape(local, CylinderShape((0, 0, 0), axis, inner, max(inner_half, f32(0.0))))
-        a.boolean("target", False)
         self.fill_shape(a, local, c, m)
         a.check_unknown()
 
@@ -974,8 +1053,11 @@ class ScriptEngine:
                 v = res[0] if res else None
                 out[k] = v is not None and v is not False
             return out
-        a.boolean("target", False)
-        if self.env_builder().fill(LambdaShape(mn, mx, inside), m) == 0:
+        shape = LambdaShape(mn, mx, inside)
+        if self.take_target(a, shape):
+            a.check_unknown()
+            return
+        if self.env_builder().fill(shape, m) == 0:
             self.warn(f"{a.what}: shape is empty or lies completely outside the grid")
         a.check_unknown()
 
@@ -1701,6 +1783,8 @@ class ScriptEngine:
             sc.view = dict(self.view)
             sc.cell_size = self.settings.cell_size
             sc.wavelength = self.settings.wavelength
+            sc.radar = self.radar
+            sc.targets = list(self.targets)
             self.final_checks(sc)
         except LuaError as e:
             raise ScriptError(str(e)) from None
@@ -1712,6 +1796,14 @@ class ScriptEngine:
         with open(path, "r", encoding="utf-8") as f:
             src = f.read()
         res = self.run_source(src, os.path.basename(str(path)))
+        if self.radar is not None and self.with_targets:
+            # the radar's calibration scene: everything except the targets (ScriptEngine.cpp:2581-2592)
+            bg = ScriptEngine(self.overrides, echo=False, with_targets=False).run_source(src, os.path.basename(str(path)))
+            res.background = bg.scene
+            if not self.targets:
+                res.warnings.append("radar: no object is marked target = true, so the calibration (which removes "
+                                    "the targets) sees the same scene and every echo cancels; mark what the radar "
+                                    "should detect with target = true")
         base = os.path.dirname(os.path.abspath(str(path)))
         od = self.settings.output_dir
         stem = os.path.splitext(os.path.basename(str(path)))[0]

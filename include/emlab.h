@@ -259,6 +259,26 @@ typedef struct emlab_render_params {
  * of --screenshot. */
 int emlab_render(emlab_grid* g, const emlab_render_params* params, unsigned char* rgba);
 
+/* ---- radar imaging: RadarMonitor::computeImage back-projection (src/Radar.cpp:606-646) ---- */
+/* Image grid and array geometry: transmit phase centre, axes (azimuth, elevation, boresight as
+ * three rows), the simulated volume inside the absorber, the carrier omega = 2 pi / lambda, the
+ * solver dt and the decimated sample spacing, range bins r0 + i dr, azimuth and elevation bins in
+ * degrees. */
+typedef struct emlab_radar_geometry {
+    float tx[3];
+    float axes[9];
+    float interior_min[3], interior_max[3];
+    double omega, dt, sample_dt;
+    float r0, dr, az0, daz, el0, del;
+    int nr, naz, nel;
+} emlab_radar_geometry;
+/* power[(ir * nel + ie) * naz + ia] = |sum_i w_i z_i(t_i) e^{j omega t_i}|^2 (-1 outside the volume);
+ * z: M decimated complex baseband samples of C elements ([m][i] as float pairs); elem_pos (C x 3),
+ * weights (C); tx_pos (ntx x 3) and tx_amp (ntx): the transmitting elements. Host arrays. */
+int emlab_radar_backproject(const emlab_radar_geometry* geo, const float* z, int M, int C, const float* elem_pos,
+                            const double* weights, const float* tx_pos, const double* tx_amp, int ntx,
+                            double* power);
+
 /* ---- stacks of independent scenes (batched sweeps; no reference counterpart: the reference steps
  * one SimulationGrid per scene, src/SimulationGrid.cpp:149-199, 368-433) ----
  * Scenes of equal nx x ny and equal solver settings lie one after another along z in one grid,

@@ -115,7 +115,8 @@ def test_array_and_cage():
     ("scene { courant = 0.6 }", "courant must be < 1/sqrt(3)"),
     ("dipole { length = 4 }", "thin-wire dipole needs length >= 5"),
     ("wire { from = {1, 1, 1}, to = {2, 2, 1} }", "differ along exactly one axis"),
-    ("radar {}", "radar{}: not supported"),
+    ("loop {}", "loop{}: not supported"),
+    ("radar { taper = 'kaiser' }", "taper must be \"uniform\", \"hamming\" or \"hann\""),
     ("view { mode = 'poyntng' }", "mode must be one of \"fields\", \"e\", \"b\", \"poynting\", \"signed\" "
                                   "(did you mean 'poynting'?)"),
     ("box { min = {1, 1, 1}, max = {2, 2, 2}, material = 'coper' }", "unknown material 'coper' (did you mean 'copper'?)"),
