@@ -105,6 +105,8 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False, scree
     sim_ms = 0.0
     frame = 0
     while frame < frames:
+        if inst.crpa is not None:  # switches the sources between its passes (Main.cpp:1067)
+            inst.crpa.update()
         t0 = time.perf_counter()
         if spf > 0:
             grid.step(spf)

@@ -166,6 +166,7 @@ class Instruments:
         self.coaxes = list(getattr(scene, "coaxes", []))
         self.coax_readings = [None] * len(self.coaxes)
         self.radar = None
+        self.crpa = None
         self.configure()
 
     # ------------------------------------------------------------------ set-up
@@ -214,7 +215,18 @@ class Instruments:
                                           getattr(sc, "targets", []), self.warnings)
                 if self.radar.phase == "off":
                     self.radar = None
-            if self.radar is None:
+            crpa = getattr(sc, "crpa", None)
+            if crpa is not None and self.radar is None:
+                # the adaptive array switches the sources between its passes and records every port
+                # (Instruments.cpp:97-110); its first update, before the first step, starts a pass
+                from .crpa import CrpaMonitor
+                cs = dict(crpa)
+                cs["log_path"] = self.resolve(cs.get("log", ""))
+                self.crpa = CrpaMonitor(g, cs, getattr(sc, "emitters", []), sc.sources, self.ports,
+                                        self.ports[0].wavelength, sc.cell_size, self.warnings)
+                if self.crpa.phase == "off":
+                    self.crpa = None
+            if self.radar is None and self.crpa is None:
                 g.ports_configure([p.to_c() for p in self.ports], self.port_wavelength, avg,
                                   sweep=self.sweep_setup is not None)
             self.port_start = t
@@ -565,7 +577,7 @@ class Instruments:
         periods = max(self.g.time() - self.port_start, 0.0) / self.port_wavelength
         accepted = sum(r["accepted"] for r in rd if r)
         available = sum(r["available"] for r in rd if r)
-        cw_lines = 0 if (self.sweep_setup or self.radar) else max_lines
+        cw_lines = 0 if (self.sweep_setup or self.radar or self.crpa) else max_lines
         if periods < 12.0 and cw_lines > 0:
             out(f"    ports: averaging ({periods:.0f} of ~12 periods), impedances still settling")
         for i, p in enumerate(self.ports[:cw_lines]):
@@ -639,6 +651,8 @@ class Instruments:
         self.print_ports(4)
         if self.radar:
             self.radar.report(out)
+        if self.crpa:
+            self.crpa.report(out)
         self.print_coax()
         if self.ff:
             pat = self.pattern

@@ -10,8 +10,8 @@ brought to complex baseband and decimated; back-projection over range x azimuth 
 on the GPU (csrc/radar.cu, emlab_radar_backproject); local maxima above the floor are the
 detections, compared with the targets' true nearest points.
 
-Receiver noise is drawn from NumPy's generator seeded per element like the reference's, but not
-bit-identical to std::mt19937 + std::normal_distribution.
+Receiver noise is the reference's: per element, MT19937 seeded with 20251105 + element and the
+polar-method normal generator (em_lab_gb300/crpa.py restates both).
 """
 from __future__ import annotations
 
@@ -22,6 +22,7 @@ import numpy as np
 
 from . import abi
 from .grid import _check, load_library
+from .crpa import MT19937, Normal
 from .instruments import boresight_frame
 
 f32 = np.float32
@@ -355,8 +356,9 @@ class RadarMonitor:
         for i in range(C):
             buf = np.zeros(F, complex)
             buf[:N] = meas[:N, i].astype(np.float64) - self.cal[:N, i].astype(np.float64)
-            if sigma > 0.0:
-                buf[:N] += sigma * np.random.default_rng(20251105 + i).standard_normal(N)
+            if sigma > 0.0:  # each element's own seeded generator (Radar.cpp:590-596)
+                gauss = Normal(MT19937((20251105 + i) & 0xFFFFFFFF))
+                buf[:N] += sigma * np.array([gauss() for _ in range(N)])
             buf = np.fft.ifft(np.fft.fft(buf) * self.filter)
             z[:, i] = (buf[: M * D: D] * rot).astype(np.complex64)
         return z, D, M

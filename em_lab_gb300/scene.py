@@ -386,6 +386,8 @@ class Scene:
     view: dict = field(default_factory=dict)       # ViewHints used by the headless runner
     coaxes: list = field(default_factory=list)     # CoaxSetup
     radar: dict | None = None                      # RadarSetup (radar{})
+    emitters: list = field(default_factory=list)   # EmitterSetup (emitter{})
+    crpa: dict | None = None                       # CrpaSetup (crpa{})
     targets: list = field(default_factory=list)    # TargetInfo of target = true objects
 
 

@@ -44,7 +44,8 @@ BUILTIN_MATERIALS = {
     "ground_wet": (25.0, None, 0.02, None), "water": (78.0, None, None, 0.1), "seawater": (74.0, None, 4.0, None),
 }
 
-UNSUPPORTED = ("loop", "frame", "emitter", "crpa")
+UNSUPPORTED = ("loop", "frame")
+WAVEFORM_KEYS = ["wavelength", "frequency", "phase", "waveform", "ramp", "pulse_width", "interval", "delay", "enabled"]
 
 
 class ScriptError(Exception):
@@ -282,6 +283,8 @@ class ScriptEngine:
         self.with_targets = with_targets  # False: the radar's calibration run leaves out target = true objects
         self.targets = []
         self.radar = None
+        self.emitters = []
+        self.crpa = None
         self.overrides = dict(overrides or {})
         self.output = []
         self.echo = echo
@@ -673,7 +676,7 @@ class ScriptEngine:
         G.rawset("grid", grid)
         self.grid = grid
 
-        api = {"radar": self.api_radar, "scene": self.api_scene, "view": self.api_view, "material": self.api_material, "param": self.api_param,
+        api = {"radar": self.api_radar, "emitter": self.api_emitter, "crpa": self.api_crpa, "scene": self.api_scene, "view": self.api_view, "material": self.api_material, "param": self.api_param,
                "box": self.api_box, "sphere": self.api_sphere, "cylinder": self.api_cylinder,
                "wall": self.api_wall, "grating": self.api_grating, "shape": self.api_shape,
                "cage": self.api_cage, "array": self.api_array, "coax": self.api_coax,
@@ -737,6 +740,104 @@ class ScriptEngine:
         if self.radar is not None:
             self.warn("radar: only one radar per scene; replacing the previous one")
         self.radar = rs
+        a.check_unknown()
+
+    # -- emitters and the adaptive array (ScriptEngine.cpp:1850-1948)
+    def api_emitter(self, t=None, *r):
+        """A transmitter at a point: one ideal dipole (linear) or two crossed dipoles 90 degrees apart
+        in phase, perpendicular to the line toward `toward` (circular; IEEE handedness)."""
+        a = Args(self, "emitter", ["position", "name", "polarization", "toward", "amplitude"] + WAVEFORM_KEYS, t)
+        self.lock()
+        w = SourceDesc()
+        self.read_waveform(a, w)
+        pos = np.asarray(a.req_vec("position"), f32)
+        name = a.str("name", f"emitter {len(self.emitters) + 1}")
+        if any(e["name"] == name for e in self.emitters):
+            a.fail(f"an emitter named '{name}' already exists")
+        index = len(self.emitters)
+        amp = float(f32(a.num("amplitude", 1.0)))
+
+        def add(direction, extra_phase):
+            s = SourceDesc.dipole(tuple(float(v) for v in pos), tuple(float(v) for v in direction), w.wavelength, amp,
+                                  0.0)
+            for k in ("wavelength", "phase", "waveform", "ramp_periods", "repeat_periods", "delay_periods", "enabled"):
+                setattr(s, k, getattr(w, k))
+            s.phase = float(f32(f32(s.phase) + f32(extra_phase)))
+            s.emitter = index
+            self.add_source(s)
+        pv = a.raw("polarization")
+        pol = pv.lower() if type(pv) is str else "linear"
+        if pol in ("rhcp", "lhcp"):
+            toward = np.asarray(a.vec("toward", tuple(v * 0.5 for v in self.settings.size)), f32)
+            d = toward - pos
+            d = (d / f32(np.sqrt(np.sum(d * d, dtype=f32)))).astype(f32)  # propagation direction
+            ref = np.array([0, 0, 1], f32) if abs(d[2]) < 0.9 else np.array([1, 0, 0], f32)
+            ea = np.cross(d, ref).astype(f32)
+            ea = (ea / f32(np.sqrt(np.sum(ea * ea, dtype=f32)))).astype(f32)
+            eb = np.cross(d, ea).astype(f32)  # (ea, eb, d) right-handed
+            add(ea, f32(math.pi / 2))
+            add(eb, 0.0 if pol == "rhcp" else f32(math.pi))
+        else:
+            direction = a.opt_direction("polarization")
+            if direction is None:
+                a.fail("polarization must be \"rhcp\", \"lhcp\" or a direction vector (linear)")
+            add(direction, 0.0)
+            pol = "linear"
+        self.emitters.append({"name": name, "position": tuple(float(v) for v in pos), "polarization": pol})
+        a.check_unknown()
+
+    def api_crpa(self, t=None, *r):
+        a = Args(self, "crpa", ["satellite", "elements", "jnr", "snr", "steering", "weights", "periods", "north", "log",
+                                "name", "adapt", "snapshot_periods", "snapshot_rate", "noise_seed"], t)
+        self.lock()
+        c = {"satellite": a.str("satellite", ""), "elements": []}
+        if not c["satellite"]:
+            a.fail("needs satellite = <emitter name>")
+        els = a.raw("elements")
+        if type(els) is not LuaTable:
+            a.fail("needs elements = { {x = \"port\", y = \"port\", center = vec(...)}, ... }")
+        n = self.I.length(els)
+        for i in range(1, n + 1):
+            e = self.I.index(els, i)
+            if type(e) is not LuaTable:
+                a.fail(f"elements[{i}] must be a table {{x = ..., y = ..., center = ...}}")
+            px, py, ctr = self.I.index(e, "x"), self.I.index(e, "y"), self.I.index(e, "center")
+            el = {"x": px if type(px) is str else "", "y": py if type(py) is str else "", "center": (0.0, 0.0, 0.0)}
+            if type(ctr) is LuaTable:
+                vals = [self.I.index(ctr, k + 1) for k in range(3)]
+                el["center"] = tuple(float(f32(v)) if type(v) in (int, float) else 0.0 for v in vals)
+            if not el["x"] or not el["y"]:
+                a.fail(f"elements[{i}] needs x and y port names")
+            c["elements"].append(el)
+        if len(c["elements"]) < 2:
+            a.fail("a CRPA needs at least 2 elements")
+        c["jnr_db"] = float(f32(a.num("jnr", 40.0)))
+        c["snr_db"] = float(f32(a.num("snr", -20.0)))
+        steering = a.str("steering", "model").lower()
+        if steering not in ("model", "measured"):
+            a.fail("steering must be \"model\" or \"measured\"")
+        c["measured_steering"] = steering == "measured"
+        weights = a.str("weights", "mvdr").lower()
+        if weights not in ("mvdr", "steering"):
+            a.fail("weights must be \"mvdr\" or \"steering\"")
+        c["mvdr"] = weights == "mvdr"
+        c["pass_periods"] = float(f32(a.positive("periods", 36.0)))
+        adapt = a.str("adapt", "blind").lower()
+        if adapt not in ("blind", "ideal"):
+            a.fail("adapt must be \"blind\" or \"ideal\"")
+        c["blind"] = adapt == "blind"
+        c["snapshot_periods"] = float(f32(_round_half_away(a.positive("snapshot_periods", 40.0))))
+        if c["snapshot_periods"] < 8.0:
+            a.fail("snapshot_periods must be at least 8")
+        c["snapshots_per_period"] = min(max(int(_round_half_away(a.positive("snapshot_rate", 4.0))), 1), 16)
+        c["noise_seed"] = int(max(0.0, a.num("noise_seed", 1.0)))
+        nv = a.opt_vec("north")
+        c["north"] = (0.0, 1.0, 0.0)
+        if nv is not None:
+            v = np.asarray(nv, f32)
+            c["north"] = tuple(float(x) for x in v / f32(np.sqrt(np.sum(v * v, dtype=f32))))
+        c["log"] = a.str("log", "")
+        self.crpa = c
         a.check_unknown()
 
     # -- scene / view / material / param (ScriptEngine.cpp:605-842)
@@ -1785,6 +1886,8 @@ class ScriptEngine:
             sc.wavelength = self.settings.wavelength
             sc.radar = self.radar
             sc.targets = list(self.targets)
+            sc.emitters = list(self.emitters)
+            sc.crpa = self.crpa
             self.final_checks(sc)
         except LuaError as e:
             raise ScriptError(str(e)) from None
