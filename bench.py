@@ -386,13 +386,64 @@ def run_learned(args):
     return 0
 
 
+def run_phased(args):
+    """--workload phased_array: BASELINE config 5 shapes. 16 x 16 dipoles at half-wavelength pitch
+    (lambda 24 cells) a quarter wavelength over a ground sheet under a radome slab (eps_r 3.5, 6
+    cells), 384 x 384 x 256 cells with a 12-cell absorber, 50-ohm feeds with a Taylor taper and
+    true-time-delay steering to 8 seeded directions (8 scenes); the 32-frequency tensor-core
+    far-field DFT every step, then the pattern at 181 x 361 angles and all 32 frequencies.
+    value = cell-steps per second of the stepping (DFT included) over the 8 scenes."""
+    import torch
+    from em_lab_gb300 import launch_count, phased
+
+    rank, world, local = _rank_env()
+    if world > 1 and rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dirs = phased.steering_directions(args.seed, 8)
+    warm = phased.build(0.0, 0.0, elements=4, nxy=128, nz=128)
+    phased.run_scene(warm, 64 * args.warmup, 19, 37, freqs=[16])
+    l0 = launch_count()
+    res = []
+    with ClockSampler(local) as clk:
+        for th, ph in dirs:
+            sc = phased.build(th, ph)
+            r = phased.run_scene(sc, args.array_steps)
+            r.pop("pattern")
+            r["steer"] = (th, ph)
+            r["pointing_error_deg"] = phased.angular_error(r["beam_theta"], r["beam_phi"], th, ph)
+            res.append(r)
+    launches = launch_count() - l0
+    cell_steps = sum(r["cells"] * r["steps"] for r in res)
+    step_s = sum(r["step_s"] for r in res)
+    pat_s = sum(r["pattern_s"] for r in res)
+    line = {
+        "metric": "Yee Mcells/s (phased-array scenes, far-field DFT every step)", "value": cell_steps / step_s / 1e6,
+        "unit": "Mcells/s", "n_gpus": 1, "steps": args.array_steps, "warmup": args.warmup,
+        "ms_per_step": step_s / (len(res) * args.array_steps) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "phased array: 8 scenes of 384x384x256 (12-cell absorber), 16x16 thin-wire dipoles at "
+                               "lambda/2 pitch (lambda 24), ground sheet, radome eps_r 3.5, 50-ohm Taylor-tapered "
+                               "time-delay-steered feeds, 32-frequency far-field DFT, pattern 181x361 x 32 frequencies",
+                   "directions_seed": args.seed, "l2": "inputs larger than L2 (1.8 GB of field state per scene)"},
+        "pattern": {"evaluations": sum(r["pattern_evaluations"] for r in res), "seconds": pat_s,
+                    "huygens_points": res[0]["points"]},
+        "beams": [{"steer": r["steer"], "beam": (r["beam_theta"], r["beam_phi"]),
+                   "error_deg": round(r["pointing_error_deg"], 2)} for r in res],
+        "gpu_launches": int(launches), "clocks": clk.summary(), "finite": all(r["finite"] for r in res),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--workload", default="plain_large", choices=["plain_large", "plain_small", "batched", "learned"],
+    ap.add_argument("--workload", default="plain_large",
+                    choices=["plain_large", "plain_small", "batched", "learned", "phased_array"],
                     help="plain_large: the 512^3 dipole + blocks workload (default); plain_small: 128^3 sphere; "
                          "batched: 256 antenna scenes to port ring-down (sweeps/hr)")
     ap.add_argument("--scenes", type=int, default=256, help="batched: number of scenes")
@@ -402,6 +453,7 @@ def main():
     ap.add_argument("--train-scenes", type=int, default=4096, help="learned: training scenes")
     ap.add_argument("--epochs", type=int, default=300, help="learned: training epochs")
     ap.add_argument("--periods", type=float, default=4.0, help="learned: early window, design periods")
+    ap.add_argument("--array-steps", type=int, default=12000, help="phased_array: steps per scene")
     ap.add_argument("--size", type=int, default=512, help="edge of the plain_large grid")
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
     ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 32, 64, 128])
@@ -415,6 +467,8 @@ def main():
         return run_batched(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "phased_array":
+        return run_phased(args)
 
     import torch
     rank, world, local = _rank_env()
