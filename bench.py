@@ -342,7 +342,9 @@ def run_batched(args):
                    "groups": len(runner.groups), "chunk_steps": 64, "l2": "inputs larger than L2 (stack state > 129 MB)"},
         "scenes_done": done, "scenes_rung_down": sum(r.rung_down for r in results), "scene_steps": {"min": int(min(steps)), "median": int(np.median(steps)), "max": int(max(steps))},
         "mcells_per_s": useful / runner.wall_s / 1e6,
-        "setup_s": {"scene_build": build_s, "stack_upload": runner.setup_s},
+        "setup_s": {"scene_build": build_s, "stack_upload_and_tiling": runner.setup_s},
+        "tiling": {f"{g.scenes[0].grid.size[0]}": min(g.tiling, key=g.tiling.get) if g.tiling else None
+                   for g in runner.groups},
         "single_grid": single,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
@@ -520,8 +522,9 @@ def main():
     # --- end-to-end leg through the C ABI with host buffers ------------------------------------
     # The headless frame loop of the reference (Main.cpp:1074-1099): each frame steps the grid
     # (the host computes the source signals and monitor rotations in FP64 and uploads them), then
-    # reads back the probe neighbourhood and the flux box; the port (V, I) series is read back at
-    # the end. Host<->device copies are inside the timed region.
+    # reads back the probe neighbourhood and the flux box the way FieldAnalyzer does, one frame
+    # late (submit after the steps, collect at the next frame); the port (V, I) series is read
+    # back at the end. Host<->device copies are inside the timed region.
     e2e_steps = args.e2e_steps or args.steps
     frame = 2
     probe, planes, bmin, bmax = frame_reads(sc)
@@ -533,9 +536,12 @@ def main():
     frames = 0
     for _ in range(e2e_steps // frame):
         grid.step(frame)
-        grid.probe_gather(probe)
-        grid.flux_planes(planes)
+        # FieldAnalyzer::submit / collect: this frame's probe and flux box are queued behind its
+        # steps; the previous frame's values are read while the GPU runs on
+        grid.analyzer_collect()
+        grid.analyzer_submit(probe, planes)
         frames += 1
+    grid.analyzer_collect()
     tail = []  # end-of-run reads: port series and sweep, far-field pattern
     if sc.ports:
         wl = sc.ports[0].wavelength

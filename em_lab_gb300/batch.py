@@ -119,8 +119,31 @@ def _watch(sc, dt: float) -> RingDown:
                     max_steps=int(math.ceil(MAX_PERIODS * period)))
 
 
+TILINGS = (64, 32, 128, 8)  # 64 x 8, 64 x 4, 64 x 16 pair tiles; 32 x 8 single-cell tiles
+
+
+def autotune_tiling(grid, modes=TILINGS, steps=4):
+    """Times a few steps of the solver pass under each tiling (CUDA events around the launches) and
+    keeps the fastest; the fields and the step count are reset afterwards, so the run starts as if
+    untouched. Returns {mode: ms per launch} and leaves the best mode set."""
+    times = {}
+    for m in modes:
+        grid.set_tiling(m)
+        grid.step(1)  # first launch of a mode: attribute set-up outside the timing
+        grid.set_timing(True)
+        grid.kernel_time(reset=True)
+        grid.step(steps)
+        ms, n = grid.kernel_time(reset=True)
+        grid.set_timing(False)
+        times[m] = ms / max(n, 1)
+    best = min(times, key=times.get)
+    grid.set_tiling(best)
+    grid.reset_fields()
+    return times
+
+
 class _Group:
-    def __init__(self, scenes, indices, chunk):
+    def __init__(self, scenes, indices, chunk, tune=True):
         self.indices = list(indices)  # scene indices into the batch, in stack order
         self.scenes = [scenes[i] for i in indices]
         first = self.scenes[0]
@@ -130,6 +153,7 @@ class _Group:
             self.stack.upload_scene_materials(k, m.sigma, m.epsilon_r, sc.edges, sc.wires)
         self.stack.set_scene_sources([sc.sources for sc in self.scenes])
         self.stack.commit()
+        self.tiling = autotune_tiling(self.stack) if tune else None
         self.chunk = chunk
         self.stack.set_graph(chunk)  # each chunk replays one captured graph of its launches
         self.attach_ports()
@@ -154,7 +178,7 @@ class BatchRunner:
     """Steps `scenes` (each with one feed port) to port ring-down in stacks grouped by cross-section."""
 
     def __init__(self, scenes, chunk: int = 64, max_steps: int = 200_000, compact_fraction: float = 0.25,
-                 stop_steps=None):
+                 stop_steps=None, tune: bool = True):
         """stop_steps: per scene, stop after this many steps without waiting for the ring-down (the
         early window of a learned extrapolation); None: run every scene to ring-down."""
         for sc in scenes:
@@ -170,7 +194,8 @@ class BatchRunner:
                    float(sc.grid.pml_sigma_max), float(sc.grid.pml_grading))
             groups.setdefault(key, []).append(i)
         t0 = time.perf_counter()
-        self.groups = [_Group(self.scenes, idx, self.chunk) for _, idx in sorted(groups.items(), key=lambda kv: kv[0])]
+        self.groups = [_Group(self.scenes, idx, self.chunk, tune) for _, idx in
+                       sorted(groups.items(), key=lambda kv: kv[0])]
         self.setup_s = time.perf_counter() - t0
         self.results = [SceneResult(i) for i in range(len(self.scenes))]
         if stop_steps is None:

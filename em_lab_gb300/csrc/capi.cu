@@ -414,6 +414,11 @@ int emlab_grid_destroy(emlab_grid* g) {
     for (size_t i = 0; i < g->ev_start.size(); ++i) cudaEventDestroy(g->ev_start[i]), cudaEventDestroy(g->ev_stop[i]);
     if (g->tma) tma_maps_destroy(g->tma);
     invalidate_graphs(g);
+    for (auto& a : g->analyzer) {
+        if (a.h_probe) cudaFreeHost(a.h_probe);
+        if (a.h_part) cudaFreeHost(a.h_part);
+        if (a.done) cudaEventDestroy(a.done);
+    }
     cudaStream_t s = g->stream;
     delete g;
     if (s) cudaStreamDestroy(s);
@@ -1208,6 +1213,104 @@ int emlab_flux_planes(emlab_grid* g, const emlab_flux_plane* planes, int n_plane
         for (size_t k = 0; k < rects[i].groups; ++k) s += (double)part[rects[i].offset + k];
         out[i] = s;
     }
+    return EMLAB_OK;
+}
+
+// ---- FieldAnalyzer::submit / collect (src/FieldAnalyzer.cpp:126-272) ------------------------
+int emlab_analyzer_submit(emlab_grid* g, const int* origins, int n_probes, const emlab_flux_plane* planes,
+                          int n_planes) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(n_probes >= 0 && n_planes >= 0 && (origins || !n_probes) && (planes || !n_planes),
+                  "bad analyzer arguments");
+    AnalyzerSlot& a = g->analyzer[g->analyzer_next];
+    EMLAB_REQUIRE(!a.pending, "two measurements are in flight: collect one first");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    if (!a.done) EMLAB_CUDA(cudaEventCreateWithFlags(&a.done, cudaEventDisableTiming));
+    const int size[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+    a.planes.clear();
+    size_t total = 0;
+    std::vector<int> geo;  // axis, index, m0, m1, r0, r1 per plane with partials
+    for (int i = 0; i < n_planes; ++i) {
+        const emlab_flux_plane& p = planes[i];
+        const int axis = std::clamp(p.axis, 0, 2);
+        const int u = axis == 0 ? 1 : 0, v = axis == 2 ? 1 : 2;
+        const int m0 = std::max(p.rect_min[0], 0), m1 = std::max(p.rect_min[1], 0);
+        const int r0 = std::min(p.rect_max[0], size[u]) - m0, r1 = std::min(p.rect_max[1], size[v]) - m1;
+        size_t groups = 0;
+        if (p.index >= 0 && p.index < size[axis] && r0 > 0 && r1 > 0)
+            groups = (size_t)((r0 + 15) / 16) * ((r1 + 15) / 16);
+        a.planes.emplace_back(total, groups);
+        geo.insert(geo.end(), {axis, p.index, m0, m1, r0, r1});
+        total += groups;
+    }
+    if ((size_t)n_probes > a.probe_cap) {
+        if (a.h_probe) cudaFreeHost(a.h_probe);
+        a.h_probe = nullptr;
+        EMLAB_CUDA(cudaMallocHost(&a.h_probe, (size_t)n_probes * 54 * 16));
+        EMLAB_CUDA(a.d_origins.alloc((size_t)n_probes));
+        EMLAB_CUDA(a.d_probe.alloc((size_t)n_probes * 54));
+        a.probe_cap = (size_t)n_probes;
+    }
+    if (total > a.part_cap) {
+        if (a.h_part) cudaFreeHost(a.h_part);
+        a.h_part = nullptr;
+        EMLAB_CUDA(cudaMallocHost(&a.h_part, total * 4));
+        EMLAB_CUDA(a.d_part.alloc(total));
+        a.part_cap = total;
+    }
+    a.origins.assign(origins, origins + (size_t)n_probes * 4);
+    a.n_probes = n_probes;
+    const MonitorArgs m = monitor_args(g);
+    if (n_probes) {
+        EMLAB_CUDA(cudaMemcpyAsync(a.d_origins.p, a.origins.data(), (size_t)n_probes * 16, cudaMemcpyHostToDevice,
+                                   g->stream));
+        launch_probe_gather(m, a.d_origins.p, n_probes, a.d_probe.p, nullptr, nullptr, g->stream);
+        ++g_launches;
+        EMLAB_CUDA(cudaMemcpyAsync(a.h_probe, a.d_probe.p, (size_t)n_probes * 54 * 16, cudaMemcpyDeviceToHost,
+                                   g->stream));
+    }
+    for (int i = 0; i < n_planes; ++i) {
+        if (!a.planes[(size_t)i].second) continue;
+        const int* q = &geo[(size_t)i * 6];
+        launch_flux_plane(m, q[0], q[1], q[2], q[3], q[4], q[5], a.d_part.p + a.planes[(size_t)i].first, g->stream);
+        ++g_launches;
+    }
+    if (total) EMLAB_CUDA(cudaMemcpyAsync(a.h_part, a.d_part.p, total * 4, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = check_launch()) return rc;
+    EMLAB_CUDA(cudaEventRecord(a.done, g->stream));
+    a.pending = true;
+    g->analyzer_next ^= 1;
+    return EMLAB_OK;
+}
+
+int emlab_analyzer_collect(emlab_grid* g, float* probe_out, double* flux_out, int* ready) {
+    if (int rc = require_grid(g)) return rc;
+    if (ready) *ready = 0;
+    AnalyzerSlot& a = g->analyzer[g->analyzer_oldest];
+    if (!a.pending) return EMLAB_OK;
+    EMLAB_REQUIRE((probe_out || !a.n_probes) && (flux_out || a.planes.empty()), "null analyzer output");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    EMLAB_CUDA(cudaEventSynchronize(a.done));
+    const int nx = g->cfg.nx, ny = g->cfg.ny, nz = g->cfg.nz;
+    for (int id = 0; id < a.n_probes * 54; ++id) {
+        const int probe = id / 54, k = id % 54, t = k % 27;
+        const int* o = a.origins.data() + probe * 4;
+        const int x = std::clamp(o[0] + t % 3, 0, nx - 1), y = std::clamp(o[1] + (t / 3) % 3, 0, ny - 1),
+                  z = std::clamp(o[2] + t / 9, 0, nz - 1);
+        const size_t ci = ((size_t)z * ny + y) * nx + x;
+        const float4 v = a.h_probe[id];
+        float* out = probe_out + (size_t)id * 4;
+        out[0] = v.x, out[1] = v.y, out[2] = v.z;
+        out[3] = k < 27 ? g->cell_sigma[ci] : g->cell_eps[ci];
+    }
+    for (size_t i = 0; i < a.planes.size(); ++i) {
+        double s = 0.0;  // FP64 sum of the FP32 workgroup partials (FieldAnalyzer.cpp:395-399)
+        for (size_t k = 0; k < a.planes[i].second; ++k) s += (double)a.h_part[a.planes[i].first + k];
+        flux_out[i] = s;
+    }
+    a.pending = false;
+    g->analyzer_oldest ^= 1;
+    if (ready) *ready = 1;
     return EMLAB_OK;
 }
 

@@ -50,6 +50,21 @@ struct DevBuf {
 
 constexpr int kChunk = 1024;  // sub-steps whose host-side scalars are uploaded together
 
+// One queued FieldAnalyzer measurement: device outputs, pinned host copies, the event that ends it.
+struct AnalyzerSlot {
+    DevBuf<int4> d_origins;
+    DevBuf<float4> d_probe;
+    DevBuf<float> d_part;
+    float4* h_probe = nullptr;
+    float* h_part = nullptr;
+    size_t probe_cap = 0, part_cap = 0;
+    cudaEvent_t done = nullptr;
+    std::vector<int> origins;                 // 4 ints per probe
+    std::vector<std::pair<size_t, size_t>> planes;  // (first partial, count) per plane
+    int n_probes = 0;
+    bool pending = false;
+};
+
 // A stack of independent scenes of equal nx x ny along z: scene i occupies planes z0[i] ..
 // z0[i] + nz[i] - 1, and one separator plane of a frozen class (never changes from zero) lies
 // between consecutive scenes.
@@ -146,6 +161,9 @@ struct emlab_grid {
     int dft_engine = EMLAB_DFT_TENSOR;
     // scratch
     DevBuf<unsigned> d_flag;
+    // asynchronous FieldAnalyzer read-back: two measurements in flight, collected in order
+    emlab::AnalyzerSlot analyzer[2];
+    int analyzer_next = 0, analyzer_oldest = 0;
     // CUDA graphs of `graph_chunk` steps, one per (staging slot, field generation at the chunk start)
     int graph_chunk = 0;  // 0: launches are issued one by one
     bool graph_warm = false;

@@ -81,6 +81,8 @@ def load_library() -> C.CDLL:
         "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_render": ([P, C.POINTER(abi.RenderParams), C.POINTER(C.c_ubyte)], I),
         "emlab_ports_take_series": ([P, fp, SZ, C.POINTER(SZ)], I),
+        "emlab_analyzer_submit": ([P, ip, I, C.POINTER(abi.FluxPlane), I], I),
+        "emlab_analyzer_collect": ([P, fp, dp, ip], I),
         "emlab_radar_backproject": ([C.POINTER(abi.RadarGeometry), fp, I, I, fp, dp, fp, dp, I, dp], I),
         "emlab_grid_set_graph": ([P, I], I),
         "emlab_stack_configure": ([P, C.POINTER(abi.GridConfig), ip, I], I),
@@ -327,6 +329,30 @@ class SimulationGrid:
         out = np.zeros((max(1, steps.value), max(1, n), 2), np.float32)
         _check(self._lib.emlab_ports_read_series(self._h, _fptr(out), steps.value, C.byref(steps)))
         return out[: steps.value, :n]
+
+    def analyzer_submit(self, origins, planes):
+        """FieldAnalyzer::submit: queue probe gathers and flux planes; returns at once."""
+        o = np.zeros((max(1, len(origins)), 4), np.int32)
+        if len(origins):
+            o[: len(origins), :3] = np.asarray(origins, np.int32)[:, :3]
+        arr, n = abi.array_of(abi.FluxPlane, planes)
+        _check(self._lib.emlab_analyzer_submit(self._h, o.ctypes.data_as(C.POINTER(C.c_int)), len(origins), arr, n))
+        self._analyzer = getattr(self, "_analyzer", []) + [(len(origins), n)]
+
+    def analyzer_collect(self):
+        """FieldAnalyzer::collect: (probe blocks (n, 54, 4), flux sums (m,)) of the oldest queued
+        measurement, or None when nothing is pending."""
+        q = getattr(self, "_analyzer", [])
+        if not q:
+            return None
+        npr, npl = q[0]
+        probe = np.zeros((max(1, npr), 54, 4), np.float32)
+        flux = np.zeros(max(1, npl), np.float64)
+        ready = C.c_int()
+        _check(self._lib.emlab_analyzer_collect(self._h, _fptr(probe), flux.ctypes.data_as(C.POINTER(C.c_double)),
+                                                C.byref(ready)))
+        self._analyzer = q[1:]
+        return probe[:npr], flux[:npl]
 
     def ports_recorded(self) -> int:
         """Steps recorded so far (PortMonitor::recordedSteps)."""

@@ -328,6 +328,14 @@ int emlab_flux_planes(emlab_grid* g, const emlab_flux_plane* planes, int n_plane
 #define EMLAB_FLUX_NOALLOC_MAX_PLANES 64
 #define EMLAB_FLUX_NOALLOC_MAX_PARTIALS 65536
 int emlab_flux_planes_noalloc(emlab_grid* g, const emlab_flux_plane* planes, int n_planes, double* out);
+/* FieldAnalyzer::submit / collect (src/FieldAnalyzer.cpp:126-272): submit queues probe gathers
+ * (as emlab_probe_gather) and flux planes (as emlab_flux_planes) on the grid's stream into buffers
+ * the grid owns (pinned host staging) and returns at once; collect waits for the oldest submitted
+ * measurement and returns it, so a frame loop reads the previous frame's values while the next
+ * steps run. At most two measurements are in flight. *ready = 0 when nothing was pending. */
+int emlab_analyzer_submit(emlab_grid* g, const int* probe_origins, int n_probes, const emlab_flux_plane* planes,
+                          int n_planes);
+int emlab_analyzer_collect(emlab_grid* g, float* probe_out, double* flux_out, int* ready);
 
 /* ---- coax line monitor: line_accumulate.comp (src/Coax.cpp:179-197) ---------------------- */
 /* quantities: 4 ints each (first term, term count, 0 = E integral / 1 = B integral, unused);

@@ -176,3 +176,30 @@ def test_dft_tensor_engine_equals_cuda_cores(nf):
     scale = np.abs(b).max()
     assert scale > 0 and np.all(np.isfinite(a))
     assert np.max(np.abs(a - b)) <= DFT_RTOL * scale
+
+
+def test_analyzer_submit_collect_matches_synchronous_reads():
+    """FieldAnalyzer::submit / collect returns, one frame late, exactly what the synchronous probe
+    gather and flux planes return at the step it was submitted."""
+    import numpy as np
+    from em_lab_gb300 import SimulationGrid, abi, configs
+    import oracle
+    sc = configs.random_scene(size=(40, 36, 30), pml=5, seed=3)
+    g = SimulationGrid(sc.grid)
+    oracle.load_scene(g, sc)
+    origins = [(10, 12, 9), (0, 0, 0), (37, 33, 27)]
+    planes = [abi.FluxPlane(0, 12, (3, 4), (30, 25)), abi.FluxPlane(2, 15, (0, 0), (40, 36))]
+    assert g.analyzer_collect() is None
+    expected = []
+    for frame in range(4):
+        g.step(3)
+        expected.append((g.probe_gather(origins), g.flux_planes(planes)))
+        got = g.analyzer_collect()
+        if frame:
+            np.testing.assert_array_equal(got[0], expected[frame - 1][0])
+            np.testing.assert_array_equal(got[1], expected[frame - 1][1])
+        g.analyzer_submit(origins, planes)
+    got = g.analyzer_collect()
+    np.testing.assert_array_equal(got[0], expected[3][0])
+    np.testing.assert_array_equal(got[1], expected[3][1])
+    g.close()
