@@ -1117,6 +1117,43 @@ int emlab_ntff_dft_evaluate(emlab_grid* g, int f, const float* directions, int n
     return EMLAB_OK;
 }
 
+int emlab_ntff_dft_evaluate_all(emlab_grid* g, const float* directions, int n_dirs, float* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(g->dft_on, "no far-field DFT attached");
+    EMLAB_REQUIRE(directions && out && n_dirs > 0, "bad direction arguments");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    if (int rc = dft_fold(g)) return rc;
+    const uint64_t samples = g->dft_samples;
+    EMLAB_REQUIRE(samples > 0, "no far-field DFT samples yet");
+    const int slices = std::clamp((g->dft_points + 4095) / 4096, 1, 64);
+    const int chunk = 8192;
+    DevBuf<float> ph, d_out;
+    DevBuf<float4> d_dirs, d_part;
+    EMLAB_CUDA(ph.alloc((size_t)g->dft_points * 32));
+    EMLAB_CUDA(d_dirs.alloc((size_t)n_dirs));
+    EMLAB_CUDA(cudaMemcpyAsync(d_dirs.p, directions, (size_t)n_dirs * 16, cudaMemcpyHostToDevice, g->stream));
+    EMLAB_CUDA(d_part.alloc((size_t)chunk * slices * 4));
+    EMLAB_CUDA(d_out.alloc((size_t)g->dft_nf * n_dirs * 2));
+    for (int f = 0; f < g->dft_nf; ++f) {
+        launch_dft_to_phasor(g->d_dft_x.p, g->dft_points, f, 2.0 / (double)samples, ph.p, g->stream);
+        const float k = (float)g->dft_omega[(size_t)f];
+        for (int first = 0; first < n_dirs; first += chunk) {
+            const int count = std::min(chunk, n_dirs - first);
+            launch_ntff_pattern_fast(g->d_dft_box.p, g->dft_points, ph.p, d_dirs.p, first, count, slices, k,
+                                     d_part.p, g->stream);
+            launch_ntff_reduce(d_dirs.p, d_part.p, first, count, slices, d_out.p + (size_t)f * n_dirs * 2, g->stream);
+            g_launches += 2;
+        }
+        g_launches += 1;
+    }
+    if (int rc = check_launch()) return rc;
+    EMLAB_CUDA(cudaMemcpyAsync(out, d_out.p, (size_t)g->dft_nf * n_dirs * 8, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    for (int f = 0; f < g->dft_nf; ++f)  // the radiated power is reported once per frequency (first direction)
+        for (int d = 1; d < n_dirs; ++d) out[((size_t)f * n_dirs + d) * 2 + 1] = 0.0f;
+    return EMLAB_OK;
+}
+
 // ---- probes and flux ----------------------------------------------------------------------
 int emlab_probe_gather(emlab_grid* g, const int* origins, int n_probes, float* out) {
     if (int rc = require_grid(g)) return rc;

@@ -101,6 +101,8 @@ void launch_flux_plane(const MonitorArgs& m, int axis, int index, int rmin0, int
                        float* partials, cudaStream_t s);
 void launch_ntff_pattern(const int* box, int points, const float* phasors, const float4* dirs, int first, int count,
                          int slices, float k, float4* partials, cudaStream_t s);
+void launch_ntff_pattern_fast(const int* box, int points, const float* phasors, const float4* dirs, int first,
+                              int count, int slices, float k, float4* partials, cudaStream_t s);
 void launch_ntff_reduce(const float4* dirs, const float4* partials, int first, int count, int slices, float* out,
                         cudaStream_t s);
 void launch_sweep_sums(const float* series, long long steps, int nports, double nu_lo, double nu_hi, int points,

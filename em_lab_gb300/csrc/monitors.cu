@@ -291,6 +291,116 @@ __global__ void __launch_bounds__(128) ntff_pattern_kernel(const int* box, int p
     }
 }
 
+// sin and cos of psi: Cody-Waite reduction by 2 pi (2 pi split into its nearest float and the
+// remainder), then the hardware approximations on [-pi, pi]. Absolute error about |psi| 2^-24 +
+// 2^-21 (6e-6 at |psi| = 100), for pattern evaluations that do not restate a reference shader.
+__device__ __forceinline__ void sincos_reduced(float psi, float* s, float* c) {
+    const float n = rintf(psi * 0.159154943091895336f);
+    float r = fmaf(-n, 6.28318548202514648f, psi);
+    r = fmaf(-n, -1.74845560007441e-07f, r);
+    __sincosf(r, s, c);
+}
+
+// The same sums as ntff_pattern_kernel for 256 directions per block (two per thread, sharing every
+// staged surface point), with sincos_reduced and explicit multiply-adds: the far-field DFT's
+// pattern over large angle grids.
+__global__ void __launch_bounds__(128) ntff_pattern_fast_kernel(const int* box, int points, const float4* ph,
+                                                                const float4* dirs, int first, int count, int slices,
+                                                                float kw, float4* partials) {
+    __shared__ float4 sPos[128], sJr[128], sJi[128], sMr[128], sMi[128];
+    __shared__ float sP[128];
+    __shared__ int sbox[13];
+    const int lid = threadIdx.x;
+    if (lid < 13) sbox[lid] = box[lid];
+    __syncthreads();
+    const int local0 = blockIdx.x * 256 + lid, local1 = local0 + 128;
+    const int slice = blockIdx.y;
+    const bool in0 = local0 < count, in1 = local1 < count;
+    const float4 r0 = in0 ? dirs[first + local0] : make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+    const float4 r1 = in1 ? dirs[first + local1] : make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+    const bool power = blockIdx.x == 0 && first == 0;
+    const float cx = 0.5f * (float)(sbox[0] + sbox[3]), cy = 0.5f * (float)(sbox[1] + sbox[4]),
+                cz = 0.5f * (float)(sbox[2] + sbox[5]);
+    const int per = (points + slices - 1) / slices;
+    const int f0 = slice * per, last = min(f0 + per, points);
+    float a[2][12];
+#pragma unroll
+    for (int t = 0; t < 2; ++t)
+#pragma unroll
+        for (int j = 0; j < 12; ++j) a[t][j] = 0.0f;
+    float P = 0.0f;
+    const float k0x = kw * r0.x, k0y = kw * r0.y, k0z = kw * r0.z, k1x = kw * r1.x, k1y = kw * r1.y, k1z = kw * r1.z;
+    for (int base = f0; base < last; base += 128) {
+        const int i = base + lid;
+        if (i < last) {
+            int node[3];
+            float n[3], w;
+            ntff_point(sbox, i, node, n, w);
+            const float4* s2 = ph + 8 * (long long)i + 4;
+            const float4 eR = s2[0], eI = s2[1], hR = s2[2], hI = s2[3];
+            sPos[lid] = make_float4((float)node[0] - cx, (float)node[1] - cy, (float)node[2] - cz, 0.0f);
+#define EMLAB_CROSS(A0, A1, A2, B0, B1, B2) \
+    make_float4(A1 * B2 - B1 * A2, A2 * B0 - B2 * A0, A0 * B1 - B0 * A1, 0.0f)
+            const float4 jr = EMLAB_CROSS(n[0], n[1], n[2], hR.x, hR.y, hR.z);
+            const float4 ji = EMLAB_CROSS(n[0], n[1], n[2], hI.x, hI.y, hI.z);
+            const float4 mr = EMLAB_CROSS(n[0], n[1], n[2], eR.x, eR.y, eR.z);
+            const float4 mi = EMLAB_CROSS(n[0], n[1], n[2], eI.x, eI.y, eI.z);
+            sJr[lid] = make_float4(w * jr.x, w * jr.y, w * jr.z, 0.0f);
+            sJi[lid] = make_float4(w * ji.x, w * ji.y, w * ji.z, 0.0f);
+            sMr[lid] = make_float4(-w * mr.x, -w * mr.y, -w * mr.z, 0.0f);
+            sMi[lid] = make_float4(-w * mi.x, -w * mi.y, -w * mi.z, 0.0f);
+            if (power) {
+                const float4 c1 = EMLAB_CROSS(eR.x, eR.y, eR.z, hR.x, hR.y, hR.z);
+                const float4 c2 = EMLAB_CROSS(eI.x, eI.y, eI.z, hI.x, hI.y, hI.z);
+                P = P + w * ((c1.x + c2.x) * n[0] + (c1.y + c2.y) * n[1] + (c1.z + c2.z) * n[2]);
+            }
+#undef EMLAB_CROSS
+        }
+        __syncthreads();
+        const int cnt = min(128, last - base);
+        for (int q = 0; q < cnt; ++q) {
+            const float4 pos = sPos[q];
+            const float4 jr = sJr[q], ji = sJi[q], mr = sMr[q], mi = sMi[q];
+            float sn[2], cs[2];
+            sincos_reduced(fmaf(k0x, pos.x, fmaf(k0y, pos.y, k0z * pos.z)), &sn[0], &cs[0]);
+            sincos_reduced(fmaf(k1x, pos.x, fmaf(k1y, pos.y, k1z * pos.z)), &sn[1], &cs[1]);
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                const float c = cs[t], s = sn[t];
+                a[t][0] = fmaf(jr.x, c, fmaf(-ji.x, s, a[t][0]));
+                a[t][1] = fmaf(jr.y, c, fmaf(-ji.y, s, a[t][1]));
+                a[t][2] = fmaf(jr.z, c, fmaf(-ji.z, s, a[t][2]));
+                a[t][3] = fmaf(jr.x, s, fmaf(ji.x, c, a[t][3]));
+                a[t][4] = fmaf(jr.y, s, fmaf(ji.y, c, a[t][4]));
+                a[t][5] = fmaf(jr.z, s, fmaf(ji.z, c, a[t][5]));
+                a[t][6] = fmaf(mr.x, c, fmaf(-mi.x, s, a[t][6]));
+                a[t][7] = fmaf(mr.y, c, fmaf(-mi.y, s, a[t][7]));
+                a[t][8] = fmaf(mr.z, c, fmaf(-mi.z, s, a[t][8]));
+                a[t][9] = fmaf(mr.x, s, fmaf(mi.x, c, a[t][9]));
+                a[t][10] = fmaf(mr.y, s, fmaf(mi.y, c, a[t][10]));
+                a[t][11] = fmaf(mr.z, s, fmaf(mi.z, c, a[t][11]));
+            }
+        }
+        __syncthreads();
+    }
+    sP[lid] = P;
+    __syncthreads();
+    for (int stride = 64; stride > 0; stride >>= 1) {
+        if (lid < stride) sP[lid] = sP[lid] + sP[lid + stride];
+        __syncthreads();
+    }
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+        const int local = t ? local1 : local0;
+        if (!(t ? in1 : in0)) continue;
+        const long long o = 4ll * ((long long)local * slices + slice);
+        partials[o + 0] = make_float4(a[t][0], a[t][1], a[t][2], (power && lid == 0 && t == 0) ? sP[0] : 0.0f);
+        partials[o + 1] = make_float4(a[t][3], a[t][4], a[t][5], 0.0f);
+        partials[o + 2] = make_float4(a[t][6], a[t][7], a[t][8], 0.0f);
+        partials[o + 3] = make_float4(a[t][9], a[t][10], a[t][11], 0.0f);
+    }
+}
+
 // ntff_reduce.comp:19-39
 __global__ void ntff_reduce_kernel(const float4* dirs, const float4* partials, int first, int count, int slices,
                                    float* out) {
@@ -494,6 +604,13 @@ void launch_ntff_pattern(const int* box, int points, const float* phasors, const
     const dim3 grid((count + 127) / 128, slices);
     ntff_pattern_kernel<<<grid, 128, 0, s>>>(box, points, reinterpret_cast<const float4*>(phasors), dirs, first, count,
                                              slices, k, partials);
+}
+
+void launch_ntff_pattern_fast(const int* box, int points, const float* phasors, const float4* dirs, int first,
+                              int count, int slices, float k, float4* partials, cudaStream_t s) {
+    const dim3 grid((count + 255) / 256, slices);
+    ntff_pattern_fast_kernel<<<grid, 128, 0, s>>>(box, points, reinterpret_cast<const float4*>(phasors), dirs, first,
+                                                  count, slices, k, partials);
 }
 
 void launch_ntff_reduce(const float4* dirs, const float4* partials, int first, int count, int slices, float* out,

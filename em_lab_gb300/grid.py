@@ -76,6 +76,7 @@ def load_library() -> C.CDLL:
         "emlab_ntff_dft_engine": ([P, I], I),
         "emlab_ntff_dft_read": ([P, dp], I),
         "emlab_ntff_dft_evaluate": ([P, I, fp, I, fp], I),
+        "emlab_ntff_dft_evaluate_all": ([P, fp, I, fp], I),
         "emlab_probe_gather": ([P, ip, I, fp], I),
         "emlab_flux_planes": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
@@ -432,6 +433,15 @@ class SimulationGrid:
         d[:, :3] = np.asarray(directions, np.float32)[:, :3]
         out = np.zeros((len(directions), 2), np.float32)
         _check(self._lib.emlab_ntff_dft_evaluate(self._h, int(f), _fptr(d), len(d), _fptr(out)))
+        return out
+
+    def ntff_dft_evaluate_all(self, directions) -> np.ndarray:
+        """(frequencies, directions, 2): the pattern at every configured frequency (fast surface
+        phases; see emlab_ntff_dft_evaluate_all)."""
+        d = np.zeros((len(directions), 4), np.float32)
+        d[:, :3] = np.asarray(directions, np.float32)[:, :3]
+        out = np.zeros((self._dft_nf, len(directions), 2), np.float32)
+        _check(self._lib.emlab_ntff_dft_evaluate_all(self._h, _fptr(d), len(d), _fptr(out)))
         return out
 
     def probe_gather(self, origins) -> np.ndarray:

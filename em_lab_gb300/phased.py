@@ -4,8 +4,9 @@ Taylor-tapered and steered by true time delays, in eight seeded directions; the 
 
 The scene is the script `scenes/phased_array.lua`; each steering direction is one scene on a grid
 of its own (a 384 x 384 x 256 scene fills the GPU by itself), stepped with the far-field DFT
-attached, then evaluated with the pattern kernels (ntff_pattern.comp / ntff_reduce.comp restated,
-csrc/monitors.cu) at every frequency over the full angle grid.
+attached, then evaluated at every frequency over the full angle grid by emlab_ntff_dft_evaluate_all (the
+sums of ntff_pattern.comp / ntff_reduce.comp with range-reduced hardware sin/cos, two directions
+per thread, csrc/monitors.cu).
 """
 from __future__ import annotations
 
@@ -65,14 +66,18 @@ def run_scene(sc, steps: int, n_theta: int = 181, n_phi: int = 361, freqs=None):
     t1 = time.perf_counter()
     dirs, th, ph = angle_grid(n_theta, n_phi)
     f0 = int(np.argmin(np.abs(rel - 1.0)))
-    which = range(DFT_FREQS) if freqs is None else freqs
-    pat0 = None
-    for f in which:
-        out = g.ntff_dft_evaluate(f, dirs)
-        if f == f0:
-            pat0 = out[:, 0].reshape(n_theta, n_phi)
-    if pat0 is None:
-        pat0 = g.ntff_dft_evaluate(f0, dirs)[:, 0].reshape(n_theta, n_phi)
+    if freqs is None:  # every frequency in one call (the fast pattern sums)
+        which = range(DFT_FREQS)
+        pat0 = g.ntff_dft_evaluate_all(dirs)[f0, :, 0].reshape(n_theta, n_phi)
+    else:
+        which = freqs
+        pat0 = None
+        for f in which:
+            out = g.ntff_dft_evaluate(f, dirs)
+            if f == f0:
+                pat0 = out[:, 0].reshape(n_theta, n_phi)
+        if pat0 is None:
+            pat0 = g.ntff_dft_evaluate(f0, dirs)[:, 0].reshape(n_theta, n_phi)
     g.synchronize()
     t2 = time.perf_counter()
     finite = g.check_finite()

@@ -239,6 +239,11 @@ int emlab_ntff_dft_read(emlab_grid* g, double* out);
 /* ntff_pattern.comp + ntff_reduce.comp at frequency index f from the DFT sums scaled by 2/samples
  * (the amplitude of a steady tone): out[2d] = |N_perp - r x L|^2, out[1] = radiated power. */
 int emlab_ntff_dft_evaluate(emlab_grid* g, int f, const float* directions, int n_dirs, float* out);
+/* The pattern at every configured frequency: out[(f * n_dirs + d) * 2] = |N_perp - r x L|^2,
+ * out[f * n_dirs * 2 + 1] = radiated power at f. Same sums as emlab_ntff_dft_evaluate with the
+ * surface phases from a 2-pi range reduction and hardware sin/cos (relative difference about 1e-5),
+ * two directions per thread: for large angle grids. */
+int emlab_ntff_dft_evaluate_all(emlab_grid* g, const float* directions, int n_dirs, float* out);
 
 /* ---- volume rendering: VolumeRenderer (src/VolumeRenderer.cpp:66-118, shaders/raymarch.frag) */
 /* Camera and look of one rendered frame. inv_view_proj: inverse of projection * view, column-

@@ -158,6 +158,35 @@ def test_multifrequency_dft_matches_fp64_oracle(engine):
     assert np.all(np.isfinite(pat)) and pat[0, 1] != 0.0
 
 
+PATTERN_FAST_RTOL = 1e-4  # |fast - parity| / max pattern: 2-pi reduced hardware sin/cos and FMA sums
+
+
+def test_dft_pattern_all_frequencies_matches_parity_kernel():
+    """emlab_ntff_dft_evaluate_all (two directions per thread, range-reduced hardware sin/cos, FMA
+    sums) against emlab_ntff_dft_evaluate (the reference-parity pattern sums) at every frequency,
+    over 1000 directions (more than one 256-direction block and a ragged last block), including
+    the radiated power reported on the first direction only."""
+    sc = configs.random_scene(size=(48, 44, 40), pml=5, seed=23)
+    wls = [6.0, 9.0, 14.0, 30.0]
+    g = SimulationGrid(sc.grid)
+    oracle.load_scene(g, sc)
+    g.ntff_dft_configure((7, 7, 7), (40, 36, 32), wls)
+    g.step(150)
+    dirs = configs.fibonacci_directions(1000)
+    fast = g.ntff_dft_evaluate_all(dirs)
+    assert fast.shape == (len(wls), len(dirs), 2)
+    for f in range(len(wls)):
+        ref = g.ntff_dft_evaluate(f, dirs)
+        scale = ref[:, 0].max()
+        assert scale > 0
+        err = np.max(np.abs(fast[f, :, 0] - ref[:, 0])) / scale
+        print(f"frequency {f}: max |fast - parity| / max pattern = {err:.2e}")
+        assert err <= PATTERN_FAST_RTOL
+        assert fast[f, 0, 1] == pytest.approx(ref[0, 1], rel=1e-5)
+        assert np.all(fast[f, 1:, 1] == 0.0)
+    g.close()
+
+
 @pytest.mark.parametrize("nf", [1, 16, 48, 128])
 def test_dft_tensor_engine_equals_cuda_cores(nf):
     """Tensor-core and CUDA-core folds of the same samples over several blocks and a partial one,
