@@ -885,7 +885,7 @@ int emlab_ports_sweep_sums(emlab_grid* g, double lambda_min, double lambda_max, 
     EMLAB_CUDA(cudaMemcpyAsync(out, d_out.p, d_out.n * 8, cudaMemcpyDeviceToHost, g->stream));
     if (int rc = emlab_grid_synchronize(g, 0)) return rc;
     if (residual) {
-        // ring-down: late-time |V| of port 0 relative to its peak (Ports.cpp:346-353)
+        // ring-down: late-time |V| of port 0 relative to its peak (Ports.cpp:206-213)
         std::vector<float> series(g->recorded * g->nports * 2);
         EMLAB_CUDA(cudaMemcpy(series.data(), g->d_series.p, series.size() * 4, cudaMemcpyDeviceToHost));
         const size_t n = g->recorded, tail = std::max<size_t>(n / 20, 1);
@@ -1187,7 +1187,7 @@ int emlab_render(emlab_grid* g, const emlab_render_params* params, unsigned char
     EMLAB_REQUIRE(params->width > 0 && params->height > 0 && params->width <= 16384 && params->height <= 16384,
                   "render size must be 1..16384 pixels per side");
     EMLAB_REQUIRE(std::isfinite(params->step_voxels), "render step must be finite");
-    // the host-side clamps of VolumeRenderer::render (src/VolumeRenderer.cpp:100, 111)
+    // the host-side clamps of VolumeRenderer::render (src/VolumeRenderer.cpp:102, 110)
     emlab_render_params q = *params;
     q.step_voxels = std::clamp(q.step_voxels, 0.1f, 4.0f);
     q.signed_axis = std::clamp(q.signed_axis, 0, 2);
@@ -1246,7 +1246,7 @@ int emlab_flux_planes(emlab_grid* g, const emlab_flux_plane* planes, int n_plane
     EMLAB_CUDA(cudaMemcpyAsync(part.data(), d_part.p, part.size() * 4, cudaMemcpyDeviceToHost, g->stream));
     if (int rc = emlab_grid_synchronize(g, 0)) return rc;
     for (int i = 0; i < n_planes; ++i) {
-        double s = 0.0;  // FP64 sum of the FP32 workgroup partials (FieldAnalyzer.cpp:395-399)
+        double s = 0.0;  // FP64 sum of the FP32 workgroup partials (FieldAnalyzer.cpp:356-357)
         for (size_t k = 0; k < rects[i].groups; ++k) s += (double)part[rects[i].offset + k];
         out[i] = s;
     }
@@ -1341,7 +1341,7 @@ int emlab_analyzer_collect(emlab_grid* g, float* probe_out, double* flux_out, in
         out[3] = k < 27 ? g->cell_sigma[ci] : g->cell_eps[ci];
     }
     for (size_t i = 0; i < a.planes.size(); ++i) {
-        double s = 0.0;  // FP64 sum of the FP32 workgroup partials (FieldAnalyzer.cpp:395-399)
+        double s = 0.0;  // FP64 sum of the FP32 workgroup partials (FieldAnalyzer::collect, FieldAnalyzer.cpp:264-269)
         for (size_t k = 0; k < a.planes[i].second; ++k) s += (double)a.h_part[a.planes[i].first + k];
         flux_out[i] = s;
     }

@@ -434,7 +434,7 @@ __global__ void ntff_reduce_kernel(const float4* dirs, const float4* partials, i
     out[2 * d + 1] = 0.5f * P;
 }
 
-// PortMonitor::evaluateSweep sums (Ports.cpp:355-372) in FP64: one block per (port, frequency)
+// PortMonitor::evaluateSweep sums (Ports.cpp:215-242) in FP64: one block per (port, frequency)
 __global__ void __launch_bounds__(256) sweep_kernel(const float* series, long long steps, int nports, double nu_lo,
                                                     double nu_hi, int points, double dt, double* out) {
     const int pf = blockIdx.x;

@@ -63,7 +63,7 @@ struct PlaneSums {
 };
 
 // FP64 sum of each plane's FP32 workgroup partials in workgroup order, as FieldAnalyzer::collect
-// does on the host (src/FieldAnalyzer.cpp:395-399).
+// does on the host (src/FieldAnalyzer.cpp:264-269).
 __global__ void flux_sum_kernel(const float* partials, PlaneSums ps, double* sums) {
     const int i = threadIdx.x;
     if (i >= ps.n) return;
@@ -89,7 +89,7 @@ extern "C" int emlab_flux_planes_noalloc(emlab_grid* g, const emlab_flux_plane* 
         return report_error(EMLAB_ERR_INVALID, "emlab_flux_planes_noalloc: more planes than its fixed scratch holds "
                                                "(EMLAB_FLUX_NOALLOC_MAX_PLANES)");
     if (n_planes == 0) return EMLAB_OK;
-    // the rectangle clipping of FieldAnalyzer::dispatchPlane (src/FieldAnalyzer.cpp:230-254)
+    // the rectangle clipping of FieldAnalyzer::dispatchPlane (src/FieldAnalyzer.cpp:100-124)
     const int size[3] = {m.nx, m.ny, m.nz};
     PlaneSums ps{};
     int axis[kMaxPlanes], m0[kMaxPlanes], m1[kMaxPlanes], r0[kMaxPlanes], r1[kMaxPlanes];

@@ -64,7 +64,7 @@ __global__ void backproject_kernel(emlab_radar_geometry geo, const float2* z, in
     Geo g;
     g.tx = ld3(geo.tx), g.ax0 = ld3(geo.axes), g.ax1 = ld3(geo.axes + 3), g.ax2 = ld3(geo.axes + 6);
     g.lo = ld3(geo.interior_min), g.hi = ld3(geo.interior_max);
-    // RadarMonitor::direction (Radar.cpp:61-64)
+    // RadarMonitor::direction (Radar.cpp:69-72)
     const float az = geo.az0 + (float)ia * geo.daz, el = geo.el0 + (float)ie * geo.del;
     const float a = az * 0.01745329251994329577f, e = el * 0.01745329251994329577f;
     const float sa = sinf(a), ca = cosf(a), se = sinf(e), ce = cosf(e);

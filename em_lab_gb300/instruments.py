@@ -380,7 +380,7 @@ class Instruments:
                      cm_db=20.0 * math.log10(cm / i_fwd) if cm > 0 and i_fwd > 0 else -300.0)
 
     def print_coax(self):
-        """Instruments::printCoax (Instruments.cpp:366-385)."""
+        """Instruments::printCoax (Instruments.cpp:393-410)."""
         if not self.coaxes:
             return
         periods = max(self.g.time() - self.coax_start, 0.0) / max(self.coaxes[0].wavelength, 2.0)

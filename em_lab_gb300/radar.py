@@ -220,7 +220,7 @@ class RadarMonitor:
         return self.phase == "calibrating" and self.cal is not None
 
     def update(self):
-        """RadarMonitor::update (Radar.cpp:374-409), with the measurement processed when complete."""
+        """RadarMonitor::update (Radar.cpp:371-408), with the measurement processed when complete."""
         if self.phase == "calibrating" and self.cal is None:
             rec = self.recorded()
             period = max(16, int(self.wl / self.dt))

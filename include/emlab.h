@@ -182,7 +182,7 @@ int emlab_grid_set_graph(emlab_grid* g, int chunk);
 int emlab_grid_check_finite(emlab_grid* g);
 
 /* ---- port monitor: PortMonitor (src/Ports.hpp:84-140) ------------------------------------- */
-/* PortMonitor::configure (src/Ports.cpp:183-215): at most 256 ports; phasors cleared; the (V, I)
+/* PortMonitor::configure (src/Ports.cpp:43-75): at most 256 ports; phasors cleared; the (V, I)
  * series is recorded every step when record_steps > 0 (capacity 2^23 floats, src/Ports.cpp:16)
  * or when sweep != 0 (whole capacity). n = 0 disables the monitor. */
 int emlab_ports_configure(emlab_grid* g, const emlab_port* ports, size_t n, float wavelength, float averaging_periods,
@@ -204,7 +204,7 @@ int emlab_ports_sweep_sums(emlab_grid* g, double lambda_min, double lambda_max, 
                            double* residual);
 
 /* ---- far-field monitor: FarFieldMonitor (src/FarField.hpp:75-133) ------------------------ */
-/* FarFieldMonitor::configure (src/FarField.cpp:259-307): box clamped into [L+1, n-L-2];
+/* FarFieldMonitor::configure (src/FarField.cpp:126-174): box clamped into [L+1, n-L-2];
  * EMLAB_ERR_INVALID if degenerate (< 4 cells on an axis). box_out receives the clamped box.
  * wavelength <= 0 disables the monitor. */
 int emlab_ntff_configure(emlab_grid* g, const int box_min[3], const int box_max[3], float wavelength,
@@ -213,7 +213,7 @@ int emlab_ntff_configure(emlab_grid* g, const int box_min[3], const int box_max[
 int emlab_ntff_point_count(emlab_grid* g, int* points);
 /* PhasorPair per point (ntff_common.glsl:17-28): 32 floats each. */
 int emlab_ntff_read_phasors(emlab_grid* g, float* out);
-/* ntff_pattern.comp + ntff_reduce.comp (FarField.cpp:226-243, 359-376): for each direction
+/* ntff_pattern.comp + ntff_reduce.comp (FarField.cpp:226-243, 294-335): for each direction
  * (4 floats, xyz used) out[2d] = |N_perp - r x L|^2 and out[1] = radiated power P. */
 int emlab_ntff_evaluate(emlab_grid* g, const float* directions, int n_dirs, float* out);
 
@@ -314,7 +314,7 @@ int emlab_stack_compact(emlab_grid* g, const unsigned char* keep);
 /* probe_gather.comp (FieldAnalyzer.cpp:274-303): origins are 4 ints per probe (xyz used); out
  * receives 54 texels (27 E, then 27 B, 4 floats each) per probe. */
 int emlab_probe_gather(emlab_grid* g, const int* origins, int n_probes, float* out);
-/* poynting_flux.comp per plane (FieldAnalyzer.cpp:230-254, 391-400): out[i] = FP64 sum of the
+/* poynting_flux.comp per plane (FieldAnalyzer.cpp:100-124, 317-358): out[i] = FP64 sum of the
  * FP32 16x16-workgroup partial sums of plane i (without the box orientation sign). */
 int emlab_flux_planes(emlab_grid* g, const emlab_flux_plane* planes, int n_planes, double* out);
 

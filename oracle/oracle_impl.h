@@ -430,7 +430,7 @@ static void NAME(dft_accumulate)(NAME(grid) * g) {
     }
 }
 
-/* FarFieldMonitor::accumulate (FarField.cpp:331-350) + ntff_accumulate.comp:30-52 */
+/* FarFieldMonitor::accumulate (FarField.cpp:198-217) + ntff_accumulate.comp:30-52 */
 static void NAME(ntff_accumulate)(NAME(grid) * g) {
     const double w = 6.28318530717958647692 / (double)g->ntff_wavelength;
     const double dt = (double)g->cfg.courant;
@@ -469,7 +469,7 @@ static R NAME(edge_current)(const NAME(grid) * g, int x, int y, int z, int a) {
     return (b0v - buv) - (b0u - bvu);
 }
 
-/* PortMonitor::accumulate (Ports.cpp:253-276) + port_accumulate.comp:52-83 */
+/* PortMonitor::accumulate (Ports.cpp:113-136) + port_accumulate.comp:52-83 */
 static void NAME(ports_accumulate)(NAME(grid) * g) {
     const double w = 6.28318530717958647692 / (double)g->port_wavelength;
     const double dt = (double)g->cfg.courant;
@@ -620,7 +620,7 @@ void NAME(oracle_write_components)(void* h, const R* ex, const R* ey, const R* e
     }
 }
 
-/* PortMonitor::configure (Ports.cpp:183-215) */
+/* PortMonitor::configure (Ports.cpp:43-75) */
 int NAME(oracle_ports_configure)(void* h, const emlab_port* ports, size_t n, float wavelength, float avg, int sweep,
                                  size_t record_steps) {
     NAME(grid)* g = (NAME(grid)*)h;
@@ -656,7 +656,7 @@ size_t NAME(oracle_ports_read_series)(void* h, R* out, size_t max_steps) {
     return g->recorded;
 }
 
-/* PortMonitor::evaluateSweep sums (Ports.cpp:346-372), exact phase per sample */
+/* PortMonitor::evaluateSweep sums (Ports.cpp:215-242), exact phase per sample */
 void NAME(oracle_ports_sweep_sums)(void* h, double lmin, double lmax, int points, double* out, double* residual) {
     NAME(grid)* g = (NAME(grid)*)h;
     const size_t n = g->recorded, np = (size_t)g->nports;
@@ -688,7 +688,7 @@ void NAME(oracle_ports_sweep_sums)(void* h, double lmin, double lmax, int points
         }
 }
 
-/* FarFieldMonitor::configure (FarField.cpp:259-307) */
+/* FarFieldMonitor::configure (FarField.cpp:126-174) */
 int NAME(oracle_ntff_configure)(void* h, const int mn[3], const int mx[3], float wavelength, float avg, int box_out[6]) {
     NAME(grid)* g = (NAME(grid)*)h;
     free(g->ntff);
@@ -879,7 +879,7 @@ void NAME(oracle_probe_gather)(void* h, const int* origins, int n, R* out) {
     }
 }
 
-/* poynting_flux.comp:32-63 per plane, partials added in FP64 (FieldAnalyzer.cpp:395-399) */
+/* poynting_flux.comp:32-63 per plane, partials added in FP64 (FieldAnalyzer.cpp:356-357) */
 void NAME(oracle_flux_planes)(void* h, const emlab_flux_plane* planes, int n, double* out) {
     NAME(grid)* g = (NAME(grid)*)h;
     const int size[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};

@@ -255,7 +255,7 @@ void dispatch_step(RefGrid& g, int k) {
     }
     ++g.step;
     const double dt = (double)g.cfg.courant, tE = (double)g.step * dt;
-    if (g.ntff_on) {  // FarFieldMonitor::accumulate (FarField.cpp:331-350)
+    if (g.ntff_on) {  // FarFieldMonitor::accumulate (FarField.cpp:198-217)
         namespace S = sh_ntff_acc;
         S::uEField = sampler3D{g.E.data(), g.n};
         S::uBField = sampler3D{g.B.data(), g.n};
@@ -267,7 +267,7 @@ void dispatch_step(RefGrid& g, int k) {
         rotation(6.28318530717958647692 / g.ntff_wl, tE, dt, S::uRotation, S::uBlend, g.ntff_avg, g.ntff_wl);
         for_ids(g.points, S::main);
     }
-    if (!g.ports.empty()) {  // PortMonitor::accumulate (Ports.cpp:253-276)
+    if (!g.ports.empty()) {  // PortMonitor::accumulate (Ports.cpp:113-136)
         namespace S = sh_port;
         S::uEField = sampler3D{g.E.data(), g.n};
         S::uBField = sampler3D{g.B.data(), g.n};
@@ -513,7 +513,7 @@ void oracle_ntff_read_phasors_ref(void* h, float* out) {
     std::memcpy(out, g->ntff.data(), (size_t)g->points * 32 * sizeof(float));
 }
 
-// FarFieldMonitor::evaluate (FarField.cpp:354-376, 411-425): chunked pattern + reduce dispatches
+// FarFieldMonitor::evaluate (FarField.cpp:226-243, 278-335): chunked pattern + reduce dispatches
 void oracle_ntff_evaluate_ref(void* h, const float* dirs, int n_dirs, float* out) {
     RefGrid* g = (RefGrid*)h;
     const int slices = std::clamp((g->points + 4095) / 4096, 1, 64);
@@ -595,7 +595,7 @@ void oracle_probe_gather_ref(void* h, const int* origins, int n, float* out) {
         out[i * 4] = blocks[i].x, out[i * 4 + 1] = blocks[i].y, out[i * 4 + 2] = blocks[i].z, out[i * 4 + 3] = blocks[i].w;
 }
 
-// FieldAnalyzer::dispatchPlane + FP64 sum of the partials (FieldAnalyzer.cpp:230-254, 395-399)
+// FieldAnalyzer::dispatchPlane + FP64 sum of the partials (FieldAnalyzer.cpp:100-124, 356-357)
 void oracle_flux_planes_ref(void* h, const emlab_flux_plane* planes, int n, double* out) {
     RefGrid* g = (RefGrid*)h;
     namespace S = sh_flux;
