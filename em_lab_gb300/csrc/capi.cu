@@ -770,6 +770,15 @@ int emlab_grid_set_tiling(emlab_grid* g, int tile_rows) {
     return EMLAB_OK;
 }
 
+int emlab_grid_field_ptr(emlab_grid* g, float** ptrs, int* pitch, long long* plane) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(ptrs && pitch && plane, "null argument");
+    for (int c = 0; c < 6; ++c) ptrs[c] = g->comp(g->cur, c);
+    *pitch = g->pitch;
+    *plane = g->plane;
+    return EMLAB_OK;
+}
+
 int emlab_grid_stream(emlab_grid* g, void** stream) {
     if (!g || !stream) return fail(EMLAB_ERR_INVALID, "null argument");
     *stream = (void*)g->stream;

@@ -60,6 +60,7 @@ def load_library() -> C.CDLL:
         "emlab_grid_set_kernel": ([P, I], I),
         "emlab_grid_set_tiling": ([P, I], I),
         "emlab_grid_stream": ([P, C.POINTER(P)], I),
+        "emlab_grid_field_ptr": ([P, C.POINTER(C.c_void_p), C.POINTER(I), C.POINTER(C.c_longlong)], I),
         "emlab_grid_check_finite": ([P], I),
         "emlab_grid_set_timing": ([P, I], I),
         "emlab_grid_kernel_time": ([P, dp, C.POINTER(C.c_uint64), I], I),
@@ -272,6 +273,33 @@ class SimulationGrid:
         p = C.c_void_p()
         _check(self._lib.emlab_grid_stream(self._h, C.byref(p)))
         return int(p.value or 0)
+
+    def field_pointers(self):
+        """(six device addresses Ex..Bz, row pitch, plane stride) of the current generation
+        (emlab_grid_field_ptr); valid until the next step, reset or configure."""
+        ptrs = (C.c_void_p * 6)()
+        pitch = C.c_int()
+        plane = C.c_longlong()
+        _check(self._lib.emlab_grid_field_ptr(self._h, ptrs, C.byref(pitch), C.byref(plane)))
+        return [int(p or 0) for p in ptrs], int(pitch.value), int(plane.value)
+
+    def field_tensors(self):
+        """Zero-copy torch views (nz, ny, nx) of Ex, Ey, Ez, Bx, By, Bz on the grid's device
+        through __cuda_array_interface__; the grid's queued work is waited for first. Valid until
+        the next step, reset or configure."""
+        import torch
+
+        self.synchronize()
+        ptrs, pitch, plane = self.field_pointers()
+        nx, ny, nz = self.size()
+
+        class _View:
+            def __init__(self, ptr):
+                self.__cuda_array_interface__ = {"shape": (nz, ny, nx), "typestr": "<f4", "data": (ptr, False),
+                                                 "strides": (plane * 4, pitch * 4, 4), "version": 2}
+
+        dev = torch.device("cuda", torch.cuda.current_device())
+        return [torch.as_tensor(_View(p), device=dev) for p in ptrs]
 
     def set_timing(self, enabled: bool):
         _check(self._lib.emlab_grid_set_timing(self._h, 1 if enabled else 0))

@@ -165,6 +165,13 @@ int emlab_grid_set_kernel(emlab_grid* g, int kernel);
 int emlab_grid_set_tiling(emlab_grid* g, int tile_rows);
 /* The cudaStream_t the grid launches on (for events and for ordering caller work). */
 int emlab_grid_stream(emlab_grid* g, void** stream);
+/* Device view of the field state, in place of eFieldTexture() / bFieldTexture()
+ * (src/SimulationGrid.hpp:181-182) for monitors that run on the same GPU: ptrs[0..5] receive the
+ * device arrays of Ex, Ey, Ez, Bx, By, Bz of the generation that holds the state once the work
+ * queued so far has run; the value of cell (x, y, z) is p[z * plane + y * pitch + x]. Valid until
+ * the next emlab_grid_step, reset, configure or destroy (a step writes the other generation).
+ * Order device reads after the grid's work through emlab_grid_stream. */
+int emlab_grid_field_ptr(emlab_grid* g, float** ptrs, int* pitch, long long* plane);
 /* Kernel timing of the solver pass: when enabled, CUDA events bracket every Yee launch (the fused
  * kernel, or the split pair) on the grid's stream; emlab_grid_kernel_time returns the accumulated
  * device time in ms and the number of timed launches since the last reset (reset = 1 clears). */

@@ -119,6 +119,18 @@ public:
     std::uint64_t stepCount() const { return state().step_count; }
     size_t gpuMemoryBytes() const { return (size_t)state().device_bytes; }
     emlab_grid* handle() const noexcept { return m_g; }
+    // In place of eFieldTexture() / bFieldTexture(): device arrays Ex, Ey, Ez, Bx, By, Bz of the
+    // current generation, cell (x, y, z) at [z * plane + y * pitch + x]; valid until the next step.
+    struct FieldView {
+        float* component[6];
+        int pitch;
+        long long plane;
+    };
+    FieldView fieldView() const {
+        FieldView v{};
+        check(emlab_grid_field_ptr(m_g, v.component, &v.pitch, &v.plane));
+        return v;
+    }
 
 private:
     static void check(int rc) {

@@ -140,3 +140,54 @@ def test_zero_thickness_absorber_and_minimum_size():
     g.step(40)
     g.synchronize(60000)
     assert_bitwise(g.read_components(), run_oracle(sc, 40), "tiny grid")
+
+
+def test_full_size_workload_bit_exact():
+    """The 512^3 thin-wire dipole workload (16-cell absorber, 5% random dielectric blocks, 50-ohm
+    feed, 32-bit class index, the persistent scheduler over its full item count) from a seeded
+    random state in every cell: 6 steps on the GPU equal the FP32 oracle bit for bit."""
+    import os
+    avail = 0
+    with open("/proc/meminfo") as f:
+        for line in f:
+            if line.startswith("MemAvailable:"):
+                avail = int(line.split()[1]) * 1024
+    if avail < 40 << 30:
+        pytest.skip(f"needs about 20 GB of host memory for the two full-size states ({avail >> 30} GB free)")
+    sc = configs.plain_large(size=512)
+    nx, ny, nz = sc.grid.size
+    rng = np.random.default_rng(99)
+    comps = [rng.standard_normal((nz, ny, nx), dtype=np.float32) for _ in range(6)]
+    g = SimulationGrid(sc.grid)
+    oracle.load_scene(g, sc)
+    g.write_components(comps)
+    g.step(6)
+    g.synchronize(120000)
+    got = g.read_components()
+    g.close()
+    oracle.set_threads(os.cpu_count() or 1)
+    o = oracle.Oracle(sc.grid, "f32")
+    oracle.load_scene(o, sc)
+    o.write_components(comps)
+    del comps
+    o.step(6)
+    want = o.read_components()
+    o.close()
+    assert_bitwise(got, want, "512^3 workload")
+
+
+def test_field_pointers_are_the_state():
+    """emlab_grid_field_ptr: zero-copy device views of the current generation equal the read-back,
+    and follow the generation across a step."""
+    torch = pytest.importorskip("torch")
+    sc = configs.random_scene(size=(40, 36, 30), pml=4, seed=8)
+    g = SimulationGrid(sc.grid)
+    oracle.load_scene(g, sc)
+    for steps in (7, 1):
+        g.step(steps)
+        views = g.field_tensors()
+        host = g.read_components()
+        for v, h in zip(views, host):
+            assert v.shape == h.shape and v.dtype == torch.float32
+            assert np.array_equal(v.cpu().numpy(), h)
+    g.close()
