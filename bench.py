@@ -367,22 +367,32 @@ def run_learned(args):
     if world > 1 and rank != 0:
         return 0
     torch.cuda.set_device(local)
-    extrap.PERIODS_IN = float(args.periods)
+    periods = [float(v) for v in str(args.periods).split(",") if v.strip()]
     l0 = launch_count()
     with ClockSampler(local) as clk:
         out, _ = extrap.experiment(args.seed, args.train_scenes, args.seed + 1, args.scenes, epochs=args.epochs,
+                                   periods=periods, members=args.members, val_frac=args.val_frac, single=True,
                                    log=lambda m: print(m, file=sys.stderr))
+    w = out["windows"][out["chosen_window"]]
+    windows = {k: {"sweeps_per_hour": v["sweeps_per_hour"], "speedup_vs_batched_plain": v["speedup_vs_batched_plain"],
+                   "speedup_vs_single_plain": v.get("speedup_vs_single_plain"), "eval": v["eval"],
+                   "validation": v.get("validation"), "wall": v["wall"], "early_steps_median": v["early_steps_median"],
+                   "training": v["training"]} for k, v in out["windows"].items()}
     line = {
-        "metric": "Z(f) sweeps/hr learned vs plain (held-out scenes)", "value": out["sweeps_per_hour"]["learned"],
+        "metric": "Z(f) sweeps/hr learned vs plain (held-out scenes)", "value": w["sweeps_per_hour"],
         "unit": "sweeps/hr", "n_gpus": 1, "steps": None, "warmup": args.warmup, "ms_per_step": None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 GEMMs, fp32 accumulation",
         "data": "synthetic (runs generated by the batched solver)",
-        "config": {"workload": f"learned ring-down extrapolator: {args.train_scenes} training scenes (seed {args.seed}), "
-                               f"{args.scenes} held-out scenes (seed {args.seed + 1}), early window "
-                               f"{extrap.PERIODS_IN:g} design periods, {args.epochs} epochs"},
-        "plain_sweeps_per_hour": out["sweeps_per_hour"]["plain"], "speedup": out["speedup"], "wall": out["wall"],
-        "accuracy": out["eval"], "training": out["training"], "train_runs": out["train_runs"], "steps_median": out["steps"],
-        "gpu_launches": int(launch_count() - l0), "clocks": clk.summary(),
+        "config": {"workload": f"learned ring-down extrapolator: {args.train_scenes} training scenes (seed {args.seed}; "
+                               f"{args.val_frac:g} of them held for the fallback threshold), {args.scenes} held-out "
+                               f"scenes (seed {args.seed + 1}), early windows {','.join(f'{p:g}' for p in periods)} "
+                               f"design periods, ensembles of {args.members}, {args.epochs} epochs",
+                   "chosen_window": out["chosen_window"],
+                   "fallback_rule": "p90 over validation scenes of band-median |dZ|/|Z| <= 2 % and of the S11 error "
+                                    "<= 0.5 dB; scenes above the ensemble-spread threshold run the plain solver"},
+        "plain": out["plain"], "speedup_vs_batched_plain": w["speedup_vs_batched_plain"],
+        "speedup_vs_single_plain": w.get("speedup_vs_single_plain"), "accuracy": w["eval"], "windows": windows,
+        "train_runs": out["train_runs"], "gpu_launches": int(launch_count() - l0), "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -452,9 +462,11 @@ def main():
     ap.add_argument("--seed", type=int, default=2024, help="batched: scene seed")
     ap.add_argument("--no-single", action="store_true", help="batched: skip the one-grid-per-scene comparison")
     ap.add_argument("--single-all", action="store_true", help="batched: compare on every scene, not a sample")
-    ap.add_argument("--train-scenes", type=int, default=4096, help="learned: training scenes")
-    ap.add_argument("--epochs", type=int, default=300, help="learned: training epochs")
-    ap.add_argument("--periods", type=float, default=4.0, help="learned: early window, design periods")
+    ap.add_argument("--train-scenes", type=int, default=20000, help="learned: training scenes")
+    ap.add_argument("--epochs", type=int, default=100, help="learned: training epochs")
+    ap.add_argument("--periods", default="2,3,4", help="learned: early windows to try, design periods")
+    ap.add_argument("--members", type=int, default=3, help="learned: networks per ensemble")
+    ap.add_argument("--val-frac", type=float, default=0.1, help="learned: training runs held for the fallback rule")
     ap.add_argument("--array-steps", type=int, default=12000, help="phased_array: steps per scene")
     ap.add_argument("--size", type=int, default=512, help="edge of the plain_large grid")
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])

@@ -298,22 +298,6 @@ def _nn_lib():
 
 
 # ---- data, training, evaluation --------------------------------------------------------------------
-def dataset(scenes, results):
-    """(x, zt, t, z_trunc, z_conv) arrays of the scenes that rang down and ran past the early window."""
-    xs, zts, ts, ztr, zc = [], [], [], [], []
-    for sc, r in zip(scenes, results):
-        if not (r.done and r.rung_down and r.sweep is not None):
-            continue
-        ser = np.concatenate(r.series)
-        if ser.shape[0] < early_steps(sc):
-            continue
-        x, zf, ztrunc = features(sc, ser)
-        xs.append(x), zts.append(zf), ts.append(target(r.sweep["z"])), ztr.append(ztrunc), zc.append(r.sweep["z"])
-    if not xs:
-        return None
-    return (np.stack(xs), np.stack(zts), np.stack(ts), np.stack(ztr), np.stack(zc))
-
-
 def train(x, zt, t, epochs=40, batch=256, lr=1e-3, seed=0, log=None):
     """Adam on the MSE of Z(f) / 100 ohm with a cosine learning-rate decay; returns (Net, per-epoch
     mean losses)."""
@@ -373,60 +357,204 @@ def run_scenes(scenes, early: bool):
 WAVE = 512  # scenes stepped together at most (device memory: about 50 GB of stacks per wave)
 
 
-def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=1e-3, seed=0, edges=None, log=None):
-    """Generates training runs with the batched solver (every scene to -60 dB ring-down, in waves of
-    WAVE scenes), trains the extrapolator, and on held-out scenes compares (a) the plain solver run
-    to ring-down, the judge, (b) the early window's truncated DFT (the method without the network)
-    and (c) the network's prediction from the same early window. Sweeps/hr of (a) and (c) are
-    wall-clock figures of stepping, read-back, features and inference (stack set-up excluded)."""
+def record(sc, r):
+    """What the extrapolator keeps of a run that rang down: the scene quantities features() reads
+    and the whole (V, I) series with its converged Z(f); None for a run that did not ring down."""
+    from types import SimpleNamespace as NS
+    if not (r.done and r.rung_down and r.sweep is not None):
+        return None
+    return NS(wavelength=sc.wavelength, grid=NS(courant=sc.grid.courant), sweep=dict(sc.sweep),
+              cells=int(np.prod(sc.grid.size)),
+              ports=[NS(impedance_ohm=sc.ports[0].impedance_ohm)],
+              series=np.ascontiguousarray(np.concatenate(r.series), np.float32), z=r.sweep["z"])
+
+
+def generate(seed, n, edges, log=None):
+    """Runs scenes 0..n-1 of the generator's `seed` to ring-down with the batched solver, in waves;
+    returns (records of the runs that rang down, wall seconds of stepping)."""
     from . import configs
+    recs, wall = [], 0.0
+    for w0 in range(0, n, WAVE):
+        scenes = [configs.batched_scene(seed, i, edges=edges) for i in range(w0, min(n, w0 + WAVE))]
+        res, w = run_scenes(scenes, early=False)
+        wall += w
+        recs += [q for q in (record(sc, r) for sc, r in zip(scenes, res)) if q is not None]
+        if log:
+            log(f"training runs {w0 + len(scenes)}/{n}: {w:.1f} s")
+    return recs, wall
+
+
+def dataset_of(records):
+    """(x, zt, t, z_trunc, z_conv) of the records whose series covers the current early window."""
+    rows = [[], [], [], [], []]
+    for q in records:
+        if q.series.shape[0] < early_steps(q):
+            continue
+        x, zf, ztrunc = features(q, q.series)
+        for k, v in enumerate((x, zf, target(q.z), ztrunc, q.z)):
+            rows[k].append(v)
+    if not rows[0]:
+        return None
+    return tuple(np.stack(r) for r in rows)
+
+
+def ensemble_predict(nets, x, zt):
+    """(mean Z(f) of the members, per-scene spread = band median of the largest member deviation
+    |Z_m - Z_mean| / |Z_mean|): the spread is the extrapolator's own estimate of its error."""
+    zs = np.stack([to_z(n.predict(x, zt)) for n in nets])
+    zm = zs.mean(axis=0)
+    dev = np.abs(zs - zm[None]).max(axis=0) / np.maximum(np.abs(zm), 1e-9)
+    return zm, np.median(dev, axis=1)
+
+
+def per_scene_errors(z_pred, z_ref):
+    """Per-scene band medians of |dZ| / |Z| and of the |S11| dB error."""
+    return (np.median(rel_error(z_pred, z_ref), axis=1),
+            np.median(np.abs(s11_db(z_pred) - s11_db(z_ref)), axis=1))
+
+
+def select_threshold(spread, dz, ds11, dz_p90=0.02, s11_p90=0.5):
+    """The largest spread threshold whose accepted scenes keep the p90 over ALL scenes of |dZ| at or
+    below dz_p90 and of the S11 error at or below s11_p90, the rest falling back to the plain solver
+    (error 0). Chosen on validation runs; -inf (every scene falls back) when no threshold qualifies."""
+    best = -np.inf
+    for tau in np.unique(spread):
+        acc = spread <= tau
+        if (np.percentile(np.where(acc, dz, 0.0), 90) <= dz_p90 and
+                np.percentile(np.where(acc, ds11, 0.0), 90) <= s11_p90):
+            best = float(tau)
+    return best
+
+
+def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=1e-3, seed=0, edges=None, log=None,
+               periods=None, members=1, val_frac=0.0, single=False):
+    """Generates training runs with the batched solver (every scene to -60 dB ring-down, in waves of
+    WAVE scenes) and, for each early window in `periods` (design periods; default PERIODS_IN),
+    trains `members` networks on them and evaluates on held-out scenes against the judge, the plain
+    solver run to ring-down:
+      (a) the plain solver: batched stacks (and with `single`, one SimulationGrid per scene, the
+          reference's way) — sweeps/hr and the converged Z(f);
+      (b) the early window's truncated DFT (the method without the network);
+      (c) the network's prediction (the ensemble mean) from the same early window;
+      (d) with members > 1 and val_frac > 0, the learned path with its fallback: scenes whose
+          ensemble spread exceeds a threshold chosen on a validation split of the training runs
+          (p90 |dZ| <= 2 % and p90 S11 error <= 0.5 dB over all validation scenes) continue with
+          the plain solver, and their Z(f) is the plain solver's.
+    Sweeps/hr are wall-clock figures of stepping, read-back, features and inference (stack set-up
+    excluded). Returns (result dict, parameters of the first member of the last window)."""
+    from . import batch, configs
+    global PERIODS_IN
     edges = edges or configs.BATCH_EDGES
+    periods = list(periods) if periods else [PERIODS_IN]
     out = {}
     t0 = time.perf_counter()
-    rows = [[], [], []]
-    tr_wall = 0.0
-    for w0 in range(0, n_train, WAVE):
-        scenes = [configs.batched_scene(train_seed, i, edges=edges) for i in range(w0, min(n_train, w0 + WAVE))]
-        res, wall = run_scenes(scenes, early=False)
-        tr_wall += wall
-        d = dataset(scenes, res)
-        if d is not None:
-            for k in range(3):
-                rows[k].append(d[k])
-        if log:
-            log(f"training runs {w0 + len(scenes)}/{n_train}: {wall:.1f} s")
-    x, zt, t = (np.concatenate(r) for r in rows)
-    out["train_runs"] = {"scenes": n_train, "usable": int(x.shape[0]), "wall_s": tr_wall}
-    t1 = time.perf_counter()
-    net, losses = train(x, zt, t, epochs=epochs, batch=batch, lr=lr, seed=seed, log=log)
-    out["training"] = {"epochs": epochs, "samples": int(x.shape[0]), "loss_first": losses[0], "loss_last": losses[-1],
-                       "wall_s": time.perf_counter() - t1}
+    recs, tr_wall = generate(train_seed, n_train, edges, log)
+    out["train_runs"] = {"scenes": n_train, "usable": len(recs), "wall_s": tr_wall}
+    n_val = int(round(val_frac * len(recs))) if members > 1 else 0
+    val_recs, fit_recs = recs[:n_val], recs[n_val:]
+
     eval_scenes = [configs.batched_scene(eval_seed, i, edges=edges) for i in range(n_eval)]
-    # (a) the judge: plain runs of the held-out scenes to ring-down
     ev_res, plain_wall = run_scenes(eval_scenes, early=False)
-    # (b, c) the early window only, then features and inference
-    early_res, early_wall = run_scenes(eval_scenes, early=True)
-    t2 = time.perf_counter()
-    xs, zts, ztr, keep = [], [], [], []
-    for k, (sc, r) in enumerate(zip(eval_scenes, early_res)):
-        ser = np.concatenate(r.series)
-        if ser.shape[0] < early_steps(sc):
-            continue
-        xe, ze, zr = features(sc, ser)
-        xs.append(xe), zts.append(ze), ztr.append(zr), keep.append(k)
-    y = net.predict(np.stack(xs), np.stack(zts))
-    infer_wall = time.perf_counter() - t2
-    learned_wall = early_wall + infer_wall
-    z_pred = to_z(y)
-    z_trunc = np.stack(ztr)
-    ok = [j for j, k in enumerate(keep) if ev_res[k].rung_down]
-    z_conv = np.stack([ev_res[keep[j]].sweep["z"] for j in ok])
-    out["eval"] = {"scenes": n_eval, "judged": len(ok),
-                   "network": summary(z_pred[ok], z_conv), "truncated_dft": summary(z_trunc[ok], z_conv)}
-    out["sweeps_per_hour"] = {"plain": n_eval / plain_wall * 3600.0, "learned": n_eval / learned_wall * 3600.0}
-    out["speedup"] = plain_wall / learned_wall
-    out["wall"] = {"plain_s": plain_wall, "early_s": early_wall, "features_inference_s": infer_wall}
-    out["steps"] = {"plain_median": float(np.median([r.steps for r in ev_res])),
-                    "early_median": float(np.median([early_steps(sc) for sc in eval_scenes]))}
+    out["plain"] = {"batched_s": plain_wall, "sweeps_per_hour": n_eval / plain_wall * 3600.0,
+                    "steps_median": float(np.median([r.steps for r in ev_res]))}
+    if single:
+        run_s = 0.0
+        for sc in eval_scenes:
+            tm = {}
+            batch.run_single(sc, chunk=64, timing=tm)
+            run_s += tm["run_s"]
+        out["plain"].update(single_s=run_s, single_sweeps_per_hour=n_eval / run_s * 3600.0)
+
+    windows, params = {}, None
+    saved = PERIODS_IN
+    try:
+        for P in periods:
+            PERIODS_IN = float(P)
+            w = {"periods": float(P)}
+            x, zt, t, _, _ = dataset_of(fit_recs)
+            t1 = time.perf_counter()
+            nets, last = [], []
+            for m in range(members):
+                net, losses = train(x, zt, t, epochs=epochs, batch=batch, lr=lr, seed=seed + m, log=log)
+                nets.append(net)
+                last.append(losses[-1])
+            w["training"] = {"epochs": epochs, "samples": int(x.shape[0]), "members": members,
+                             "loss_last": last, "wall_s": time.perf_counter() - t1}
+            params = nets[0].params()
+            tau = None
+            if n_val:
+                vx, vzt, _, _, vz = dataset_of(val_recs)
+                vzm, vspread = ensemble_predict(nets, vx, vzt)
+                vdz, vds = per_scene_errors(vzm, vz)
+                tau = select_threshold(vspread, vdz, vds)
+                # cell-steps of the learned path with fallback relative to the plain runs
+                usable = [q for q in val_recs if q.series.shape[0] >= early_steps(q)]
+                full = np.array([q.cells * q.series.shape[0] for q in usable], np.float64)
+                early = np.array([q.cells * early_steps(q) for q in usable], np.float64)
+                cost = float((early + np.where(vspread > tau, full, 0.0)).sum() / full.sum())
+                w["validation"] = {"scenes": int(vx.shape[0]), "threshold": tau,
+                                   "accepted": float(np.mean(vspread <= tau)), "cell_steps_vs_plain": cost}
+            # the learned path on the held-out scenes: early window, features, inference
+            early_res, early_wall = run_scenes(eval_scenes, early=True)
+            t2 = time.perf_counter()
+            xs, zts, ztr, keep = [], [], [], []
+            for k, (sc, r) in enumerate(zip(eval_scenes, early_res)):
+                ser = np.concatenate(r.series)
+                if ser.shape[0] < early_steps(sc):
+                    continue
+                xe, ze, zr = features(sc, ser)
+                xs.append(xe), zts.append(ze), ztr.append(zr), keep.append(k)
+            z_pred, spread = ensemble_predict(nets, np.stack(xs), np.stack(zts))
+            infer_wall = time.perf_counter() - t2
+            fb_wall, fallback, fb_z = 0.0, [], {}
+            if tau is not None:
+                fallback = [keep[j] for j in range(len(keep)) if spread[j] > tau]
+                fallback += [k for k in range(n_eval) if k not in keep]
+                if fallback:
+                    fb_res, fb_wall = run_scenes([eval_scenes[k] for k in fallback], early=False)
+                    fb_z = {k: r.sweep["z"] for k, r in zip(fallback, fb_res) if r.sweep is not None}
+            learned_wall = early_wall + infer_wall + fb_wall
+            z_trunc = np.stack(ztr)
+            ok = [j for j, k in enumerate(keep) if ev_res[k].rung_down]
+            z_conv = np.stack([ev_res[keep[j]].sweep["z"] for j in ok])
+            w["eval"] = {"scenes": n_eval, "judged": len(ok), "network": summary(z_pred[ok], z_conv),
+                         "truncated_dft": summary(z_trunc[ok], z_conv)}
+            if tau is not None:
+                z_hyb = z_pred.copy()
+                for j, k in enumerate(keep):
+                    if k in fb_z:
+                        z_hyb[j] = fb_z[k]
+                w["eval"]["with_fallback"] = summary(z_hyb[ok], z_conv)
+                w["eval"]["fallback_scenes"] = len(fallback)
+            w["wall"] = {"early_s": early_wall, "features_inference_s": infer_wall, "fallback_s": fb_wall}
+            w["sweeps_per_hour"] = n_eval / learned_wall * 3600.0
+            w["speedup_vs_batched_plain"] = plain_wall / learned_wall
+            if single:
+                w["speedup_vs_single_plain"] = out["plain"]["single_s"] / learned_wall
+            w["early_steps_median"] = float(np.median([early_steps(sc) for sc in eval_scenes]))
+            windows[f"{P:g}"] = w
+            if log:
+                log(f"window {P:g} periods: {json_safe(w)}")
+    finally:
+        PERIODS_IN = saved
+    out["windows"] = windows
+    # the chosen window's figures at the top level: the lowest validation cost with a fallback,
+    # otherwise the first window
+    costs = {k: w["validation"]["cell_steps_vs_plain"] for k, w in windows.items() if "validation" in w}
+    chosen = min(costs, key=costs.get) if costs else f"{periods[0]:g}"
+    out["chosen_window"] = chosen
+    w0 = windows[chosen]
+    out["eval"] = w0["eval"]
+    out["training"] = w0["training"]
+    out["sweeps_per_hour"] = {"plain": out["plain"]["sweeps_per_hour"], "learned": w0["sweeps_per_hour"]}
+    out["speedup"] = w0["speedup_vs_batched_plain"]
+    out["wall"] = dict(w0["wall"], plain_s=plain_wall)
+    out["steps"] = {"plain_median": out["plain"]["steps_median"], "early_median": w0["early_steps_median"]}
     out["wall_s"] = time.perf_counter() - t0
-    return out, net.params()
+    return out, params
+
+
+def json_safe(d):
+    """A compact one-line rendering of a result dict for the log."""
+    import json
+    return json.dumps(d, default=float)[:600]

@@ -82,3 +82,53 @@ def test_features_are_scale_invariant_and_match_the_sweep():
     np.testing.assert_allclose(zt1, ref, rtol=1e-9)
     np.testing.assert_allclose(extrap.to_z(extrap.target(ref)), np.clip(ref.real, -1000, 1000) +
                                1j * np.clip(ref.imag, -1000, 1000), rtol=1e-5)
+
+
+def test_record_keeps_what_features_read():
+    """A run's record (no material arrays) gives the same features as the scene itself, and runs
+    that did not ring down are dropped."""
+    from types import SimpleNamespace as NS
+    sc = configs.batched_scene(4, 1)
+    n = extrap.early_steps(sc)
+    k = np.arange(n + 200)
+    ser = np.stack([np.sin(k * 0.05), 0.02 * np.cos(k * 0.05)], axis=1).astype(np.float32)
+    z = np.full(extrap.NF, 50.0 + 10.0j)
+    done = NS(done=True, rung_down=True, sweep={"z": z}, series=[ser[:100], ser[100:]])
+    q = extrap.record(sc, done)
+    assert q is not None and q.series.shape == ser.shape
+    for a, b in zip(extrap.features(q, q.series), extrap.features(sc, ser)):
+        np.testing.assert_array_equal(a, b)
+    assert extrap.record(sc, NS(done=True, rung_down=False, sweep={"z": z}, series=[ser])) is None
+    x, zt, t, ztr, zc = extrap.dataset_of([q, q])
+    assert x.shape == (2, extrap.T_IN, 2) and t.shape == (2, 2 * extrap.NF) and np.array_equal(zc[0], z)
+    short = extrap.record(sc, NS(done=True, rung_down=True, sweep={"z": z}, series=[ser[: n - 1]]))
+    assert extrap.dataset_of([short]) is None
+
+
+def test_ensemble_spread_and_fallback_threshold():
+    """Spread = band median of the largest member deviation from the mean; the threshold is the
+    largest that keeps the p90 (over all scenes, fallback scenes counting 0) of |dZ| <= 2 % and of
+    the S11 error <= 0.5 dB."""
+    from types import SimpleNamespace as NS
+    rng = np.random.default_rng(3)
+    y = rng.standard_normal((5, 2 * extrap.NF)).astype(np.float32) * 0.3 + 1.0
+    nets = [NS(predict=lambda x, zt, d=d: y * np.float32(1.0 + d)) for d in (-0.01, 0.0, 0.01)]
+    zm, spread = extrap.ensemble_predict(nets, None, None)
+    np.testing.assert_allclose(zm, extrap.to_z(y), rtol=1e-6)
+    np.testing.assert_allclose(spread, 0.01, rtol=1e-3)
+    # 20 scenes: errors grow with spread; scenes 14.. exceed 2 %
+    spread = np.linspace(0.001, 0.02, 20)
+    dz = spread * 1.5
+    ds11 = np.full(20, 0.1)
+    tau = extrap.select_threshold(spread, dz, ds11)
+    acc = spread <= tau
+    assert np.percentile(np.where(acc, dz, 0.0), 90) <= 0.02
+    nxt = spread[spread > tau]
+    if nxt.size:  # the next threshold up would break the bound
+        acc2 = spread <= nxt.min()
+        assert np.percentile(np.where(acc2, dz, 0.0), 90) > 0.02
+    # every accepted scene 25x over: the interpolated p90 of 20 values lies between the 18th and
+    # 19th largest, so only the lowest-spread scene can be accepted; of 5 values, none
+    assert extrap.select_threshold(spread, np.full(20, 0.5), ds11) == spread[0]
+    assert extrap.select_threshold(spread[:5], np.full(5, 0.5), ds11[:5]) == -np.inf
+    assert extrap.select_threshold(spread, dz * 0.0, ds11) == spread.max()

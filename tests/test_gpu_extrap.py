@@ -94,3 +94,19 @@ def test_trained_network_beats_the_truncated_dft_on_held_out_scenes():
     assert net["dz_median"] < 0.7 * trunc["dz_median"]
     assert net["s11_db_median"] < trunc["s11_db_median"]
     assert out["speedup"] > 1.0
+
+
+def test_ensemble_with_plain_fallback_on_two_windows():
+    """The learned path with its fallback: ensembles of two networks per early window (2 and 4
+    design periods), a spread threshold from a validation split, the rejected scenes re-run by the
+    plain solver (their Z(f) is then the judge's own), and the single-grid plain arm."""
+    out, _ = extrap.experiment(303, 384, 404, 32, epochs=60, edges=(48, 64), periods=(2, 4), members=2,
+                               val_frac=0.25, single=True)
+    assert set(out["windows"]) == {"2", "4"} and out["chosen_window"] in out["windows"]
+    assert out["plain"]["single_sweeps_per_hour"] > 0
+    for w in out["windows"].values():
+        v = w["validation"]
+        assert 0.0 <= v["accepted"] <= 1.0 and 0.0 < v["cell_steps_vs_plain"] <= 1.0 + 1e-9
+        hyb, net = w["eval"]["with_fallback"], w["eval"]["network"]
+        assert hyb["dz_median"] <= net["dz_median"] + 1e-12 or w["eval"]["fallback_scenes"] == 0
+        assert w["sweeps_per_hour"] > 0 and w["speedup_vs_single_plain"] > 0
