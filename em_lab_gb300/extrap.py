@@ -442,7 +442,7 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
           the plain solver, and their Z(f) is the plain solver's.
     Sweeps/hr are wall-clock figures of stepping, read-back, features and inference (stack set-up
     excluded). Returns (result dict, parameters of the first member of the last window)."""
-    from . import batch, configs
+    from . import batch as batch_solver, configs
     global PERIODS_IN
     edges = edges or configs.BATCH_EDGES
     periods = list(periods) if periods else [PERIODS_IN]
@@ -461,7 +461,7 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
         run_s = 0.0
         for sc in eval_scenes:
             tm = {}
-            batch.run_single(sc, chunk=64, timing=tm)
+            batch_solver.run_single(sc, chunk=64, timing=tm)
             run_s += tm["run_s"]
         out["plain"].update(single_s=run_s, single_sweeps_per_hour=n_eval / run_s * 3600.0)
 
