@@ -373,13 +373,29 @@ def run_learned(args):
         out, _ = extrap.experiment(args.seed, args.train_scenes, args.seed + 1, args.scenes, epochs=args.epochs,
                                    periods=periods, members=args.members, val_frac=args.val_frac, single=True,
                                    log=lambda m: print(m, file=sys.stderr))
-    w = out["windows"][out["chosen_window"]]
     windows = {k: {"sweeps_per_hour": v["sweeps_per_hour"], "speedup_vs_batched_plain": v["speedup_vs_batched_plain"],
-                   "speedup_vs_single_plain": v.get("speedup_vs_single_plain"), "eval": v["eval"],
-                   "validation": v.get("validation"), "wall": v["wall"], "early_steps_median": v["early_steps_median"],
-                   "training": v["training"]} for k, v in out["windows"].items()}
+                   "speedup_vs_single_plain": v.get("speedup_vs_single_plain"), "network_only": v["network_only"],
+                   "eval": v["eval"], "validation": v.get("validation"), "wall": v["wall"],
+                   "early_steps_median": v["early_steps_median"], "training": v["training"]}
+               for k, v in out["windows"].items()}
+    # headline: the network alone at the shortest window meeting the medians on validation runs;
+    # beside it the strict operating point (p90 bound with the plain-solver fallback)
+    strict = out["windows"][out["chosen_window"]]
+    net_key = out["chosen_window_network_only"]
+    if net_key is not None:
+        head = dict(out["windows"][net_key]["network_only"], window=net_key, accuracy=out["windows"][net_key]["eval"]["network"],
+                    criterion="median over scenes of band-median |dZ|/|Z| <= 2 % and S11 error <= 0.5 dB "
+                              "(checked on validation runs)")
+    else:
+        head = {"sweeps_per_hour": strict["sweeps_per_hour"], "window": out["chosen_window"]}
+    strict_line = {"window": out["chosen_window"], "sweeps_per_hour": strict["sweeps_per_hour"],
+                   "speedup_vs_batched_plain": strict["speedup_vs_batched_plain"],
+                   "speedup_vs_single_plain": strict.get("speedup_vs_single_plain"),
+                   "accuracy": strict["eval"].get("with_fallback"), "fallback_scenes": strict["eval"].get("fallback_scenes"),
+                   "criterion": "p90 over scenes of band-median |dZ|/|Z| <= 2 % and of the S11 error <= 0.5 dB on "
+                                "validation runs; scenes above the ensemble-spread threshold run the plain solver"}
     line = {
-        "metric": "Z(f) sweeps/hr learned vs plain (held-out scenes)", "value": w["sweeps_per_hour"],
+        "metric": "Z(f) sweeps/hr learned vs plain (held-out scenes)", "value": head["sweeps_per_hour"],
         "unit": "sweeps/hr", "n_gpus": 1, "steps": None, "warmup": args.warmup, "ms_per_step": None,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 GEMMs, fp32 accumulation",
         "data": "synthetic (runs generated by the batched solver)",
@@ -387,11 +403,8 @@ def run_learned(args):
                                f"{args.val_frac:g} of them held for the fallback threshold), {args.scenes} held-out "
                                f"scenes (seed {args.seed + 1}), early windows {','.join(f'{p:g}' for p in periods)} "
                                f"design periods, ensembles of {args.members}, {args.epochs} epochs",
-                   "chosen_window": out["chosen_window"],
-                   "fallback_rule": "p90 over validation scenes of band-median |dZ|/|Z| <= 2 % and of the S11 error "
-                                    "<= 0.5 dB; scenes above the ensemble-spread threshold run the plain solver"},
-        "plain": out["plain"], "speedup_vs_batched_plain": w["speedup_vs_batched_plain"],
-        "speedup_vs_single_plain": w.get("speedup_vs_single_plain"), "accuracy": w["eval"], "windows": windows,
+                   "plain_judge": "batched stacks and one SimulationGrid per scene, each run to -60 dB ring-down"},
+        "headline": head, "strict": strict_line, "plain": out["plain"], "windows": windows,
         "train_runs": out["train_runs"], "gpu_launches": int(launch_count() - l0), "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -464,7 +477,7 @@ def main():
     ap.add_argument("--single-all", action="store_true", help="batched: compare on every scene, not a sample")
     ap.add_argument("--train-scenes", type=int, default=20000, help="learned: training scenes")
     ap.add_argument("--epochs", type=int, default=100, help="learned: training epochs")
-    ap.add_argument("--periods", default="2,3,4", help="learned: early windows to try, design periods")
+    ap.add_argument("--periods", default="1.5,2,3,4", help="learned: early windows to try, design periods")
     ap.add_argument("--members", type=int, default=3, help="learned: networks per ensemble")
     ap.add_argument("--val-frac", type=float, default=0.1, help="learned: training runs held for the fallback rule")
     ap.add_argument("--array-steps", type=int, default=12000, help="phased_array: steps per scene")

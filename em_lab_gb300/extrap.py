@@ -493,7 +493,9 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
                 early = np.array([q.cells * early_steps(q) for q in usable], np.float64)
                 cost = float((early + np.where(vspread > tau, full, 0.0)).sum() / full.sum())
                 w["validation"] = {"scenes": int(vx.shape[0]), "threshold": tau,
-                                   "accepted": float(np.mean(vspread <= tau)), "cell_steps_vs_plain": cost}
+                                   "accepted": float(np.mean(vspread <= tau)), "cell_steps_vs_plain": cost,
+                                   "network_dz_median": float(np.median(vdz)),
+                                   "network_s11_db_median": float(np.median(vds))}
             # the learned path on the held-out scenes: early window, features, inference
             early_res, early_wall = run_scenes(eval_scenes, early=True)
             t2 = time.perf_counter()
@@ -527,6 +529,11 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
                 w["eval"]["with_fallback"] = summary(z_hyb[ok], z_conv)
                 w["eval"]["fallback_scenes"] = len(fallback)
             w["wall"] = {"early_s": early_wall, "features_inference_s": infer_wall, "fallback_s": fb_wall}
+            net_wall = early_wall + infer_wall  # every scene stops at the early window
+            w["network_only"] = {"sweeps_per_hour": n_eval / net_wall * 3600.0,
+                                 "speedup_vs_batched_plain": plain_wall / net_wall}
+            if single:
+                w["network_only"]["speedup_vs_single_plain"] = out["plain"]["single_s"] / net_wall
             w["sweeps_per_hour"] = n_eval / learned_wall * 3600.0
             w["speedup_vs_batched_plain"] = plain_wall / learned_wall
             if single:
@@ -543,6 +550,10 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
     costs = {k: w["validation"]["cell_steps_vs_plain"] for k, w in windows.items() if "validation" in w}
     chosen = min(costs, key=costs.get) if costs else f"{periods[0]:g}"
     out["chosen_window"] = chosen
+    # the network alone: the shortest window whose validation medians meet |dZ| <= 2 % and S11 <= 0.5 dB
+    fit = [k for k, w in windows.items() if "validation" in w and w["validation"]["network_dz_median"] <= 0.02
+           and w["validation"]["network_s11_db_median"] <= 0.5]
+    out["chosen_window_network_only"] = min(fit, key=lambda k: windows[k]["periods"]) if fit else None
     w0 = windows[chosen]
     out["eval"] = w0["eval"]
     out["training"] = w0["training"]
