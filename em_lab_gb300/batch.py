@@ -36,6 +36,7 @@ class SceneResult:
     rung_down: bool = False  # False when done at the step cap
     wall_s: float = 0.0
     sweep: dict | None = None
+    accepted: bool = False  # stopped at its decision step (BatchRunner decide): no sweep of its own
 
 
 def sweep_sums(series: np.ndarray, lambda_min: float, lambda_max: float, points: int, dt: float) -> np.ndarray:
@@ -178,9 +179,13 @@ class BatchRunner:
     """Steps `scenes` (each with one feed port) to port ring-down in stacks grouped by cross-section."""
 
     def __init__(self, scenes, chunk: int = 64, max_steps: int = 200_000, compact_fraction: float = 0.25,
-                 stop_steps=None, tune: bool = True):
+                 stop_steps=None, tune: bool = True, decide_at=None, decide=None):
         """stop_steps: per scene, stop after this many steps without waiting for the ring-down (the
-        early window of a learned extrapolation); None: run every scene to ring-down."""
+        early window of a learned extrapolation); None: run every scene to ring-down.
+        decide_at / decide: once scene i has run decide_at[i] steps (at a chunk boundary) without
+        ringing down, decide(indices, series) is called for the scenes of a stack that reached it in
+        the same chunk (under the runner's lock) and returns one flag per scene: True stops the scene
+        there (result.accepted), False lets it run on to ring-down from where it is."""
         for sc in scenes:
             if not sc.ports:
                 raise ValueError(f"{sc.name}: a batched scene needs a feed port")
@@ -198,6 +203,9 @@ class BatchRunner:
                        sorted(groups.items(), key=lambda kv: kv[0])]
         self.setup_s = time.perf_counter() - t0
         self.results = [SceneResult(i) for i in range(len(self.scenes))]
+        self.decide_at = list(decide_at) if decide_at is not None else None
+        self.decide = decide
+        self.decided = [False] * len(self.scenes)
         if stop_steps is None:
             self.watch = [_watch(sc, float(sc.grid.courant)) for sc in self.scenes]
         else:
@@ -229,7 +237,18 @@ class BatchRunner:
                     sc = self.scenes[i]
                     r.sweep = scene_sweep(sc, np.concatenate(r.series), float(sc.grid.courant))
                     finished.append(i)
+            pending = [i for i in g.indices if self.decide_at is not None and not self.results[i].done
+                       and not self.decided[i] and self.results[i].steps >= self.decide_at[i]]
             with lock:
+                if pending:
+                    flags = self.decide(pending, [np.concatenate(self.results[i].series) for i in pending])
+                    for i, stop in zip(pending, flags):
+                        self.decided[i] = True
+                        if stop:
+                            r = self.results[i]
+                            r.done = r.accepted = True
+                            r.wall_s = time.perf_counter() - t0
+                            finished.append(i)
                 self.cell_steps += cells
                 if on_done:
                     for i in finished:

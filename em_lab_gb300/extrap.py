@@ -426,6 +426,37 @@ def select_threshold(spread, dz, ds11, dz_p90=0.02, s11_p90=0.5):
     return best
 
 
+def run_with_fallback(scenes, nets, tau):
+    """The learned path with the plain solver as its fallback, in one batched run: at its early
+    window each scene's ensemble prediction and spread are computed (one batched inference per stack
+    and chunk); a spread within `tau` stops the scene there, otherwise it steps on from where it is
+    to ring-down and its Z(f) is the plain solver's. Returns ({scene: Z(f)}, wall seconds including
+    the inference, number of fallback scenes)."""
+    from .batch import BatchRunner
+    pred = {}
+
+    def decide(idx, series):
+        xs, zts = [], []
+        for i, ser in zip(idx, series):
+            x, zf, _ = features(scenes[i], ser)
+            xs.append(x), zts.append(zf)
+        zm, spread = ensemble_predict(nets, np.stack(xs), np.stack(zts))
+        for i, z in zip(idx, zm):
+            pred[i] = z
+        return [bool(v <= tau) for v in spread]
+
+    r = BatchRunner(scenes, chunk=64, decide_at=[early_steps(sc) for sc in scenes], decide=decide)
+    res = r.run()
+    r.close()
+    z = {}
+    for i, q in enumerate(res):
+        if q.accepted:
+            z[i] = pred[i]
+        elif q.sweep is not None:
+            z[i] = q.sweep["z"]
+    return z, r.wall_s, sum(1 for q in res if not q.accepted)
+
+
 def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=1e-3, seed=0, edges=None, log=None,
                periods=None, members=1, val_frac=0.0, single=False):
     """Generates training runs with the batched solver (every scene to -60 dB ring-down, in waves of
@@ -487,11 +518,12 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
                 vzm, vspread = ensemble_predict(nets, vx, vzt)
                 vdz, vds = per_scene_errors(vzm, vz)
                 tau = select_threshold(vspread, vdz, vds)
-                # cell-steps of the learned path with fallback relative to the plain runs
+                # cell-steps of the learned path with fallback relative to the plain runs (a rejected
+                # scene runs on from its early window)
                 usable = [q for q in val_recs if q.series.shape[0] >= early_steps(q)]
                 full = np.array([q.cells * q.series.shape[0] for q in usable], np.float64)
                 early = np.array([q.cells * early_steps(q) for q in usable], np.float64)
-                cost = float((early + np.where(vspread > tau, full, 0.0)).sum() / full.sum())
+                cost = float(np.where(vspread > tau, full, early).sum() / full.sum())
                 w["validation"] = {"scenes": int(vx.shape[0]), "threshold": tau,
                                    "accepted": float(np.mean(vspread <= tau)), "cell_steps_vs_plain": cost,
                                    "network_dz_median": float(np.median(vdz)),
@@ -508,27 +540,22 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
                 xs.append(xe), zts.append(ze), ztr.append(zr), keep.append(k)
             z_pred, spread = ensemble_predict(nets, np.stack(xs), np.stack(zts))
             infer_wall = time.perf_counter() - t2
-            fb_wall, fallback, fb_z = 0.0, [], {}
+            # the learned path with its fallback, in one run: every scene is stopped at its early
+            # window if the ensemble's spread is within the threshold, else it runs on to ring-down
+            fb_wall, n_fallback, z_hyb_of = 0.0, 0, {}
             if tau is not None:
-                fallback = [keep[j] for j in range(len(keep)) if spread[j] > tau]
-                fallback += [k for k in range(n_eval) if k not in keep]
-                if fallback:
-                    fb_res, fb_wall = run_scenes([eval_scenes[k] for k in fallback], early=False)
-                    fb_z = {k: r.sweep["z"] for k, r in zip(fallback, fb_res) if r.sweep is not None}
-            learned_wall = early_wall + infer_wall + fb_wall
+                z_hyb_of, fb_wall, n_fallback = run_with_fallback(eval_scenes, nets, tau)
+            learned_wall = (early_wall + infer_wall) if tau is None else fb_wall
             z_trunc = np.stack(ztr)
             ok = [j for j, k in enumerate(keep) if ev_res[k].rung_down]
             z_conv = np.stack([ev_res[keep[j]].sweep["z"] for j in ok])
             w["eval"] = {"scenes": n_eval, "judged": len(ok), "network": summary(z_pred[ok], z_conv),
                          "truncated_dft": summary(z_trunc[ok], z_conv)}
             if tau is not None:
-                z_hyb = z_pred.copy()
-                for j, k in enumerate(keep):
-                    if k in fb_z:
-                        z_hyb[j] = fb_z[k]
-                w["eval"]["with_fallback"] = summary(z_hyb[ok], z_conv)
-                w["eval"]["fallback_scenes"] = len(fallback)
-            w["wall"] = {"early_s": early_wall, "features_inference_s": infer_wall, "fallback_s": fb_wall}
+                z_hyb = np.stack([z_hyb_of[keep[j]] for j in ok])
+                w["eval"]["with_fallback"] = summary(z_hyb, z_conv)
+                w["eval"]["fallback_scenes"] = n_fallback
+            w["wall"] = {"early_s": early_wall, "features_inference_s": infer_wall, "with_fallback_s": fb_wall}
             net_wall = early_wall + infer_wall  # every scene stops at the early window
             w["network_only"] = {"sweeps_per_hour": n_eval / net_wall * 3600.0,
                                  "speedup_vs_batched_plain": plain_wall / net_wall}

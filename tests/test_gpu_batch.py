@@ -143,6 +143,38 @@ def test_batch_runner_equals_single_runs():
         assert abs(r.sweep["s11"]).max() < 200.0
 
 
+def test_batch_runner_decision_stops_or_continues():
+    """decide_at / decide: scenes the callback accepts stop at the first chunk boundary at or after
+    their decision step; rejected scenes run on to ring-down with the same series (bit for bit) and
+    Z(f) as a run without any decision."""
+    scs = [configs.batched_scene(9, i) for i in range(60)]
+    pick = [sc for sc in scs if sc.grid.size[0] in (48, 64)][:6]
+    plain = batch.BatchRunner(pick, chunk=64, max_steps=20000)
+    ref = plain.run()
+    plain.close()
+    at = [150 + 10 * i for i in range(len(pick))]
+    seen = []
+
+    def decide(idx, series):
+        for i, ser in zip(idx, series):
+            assert ser.shape[0] >= at[i] and ser.shape[0] - at[i] < 64
+            seen.append(i)
+        return [i % 2 == 0 for i in idx]  # accept the even scenes
+
+    run = batch.BatchRunner(pick, chunk=64, max_steps=20000, decide_at=at, decide=decide)
+    res = run.run()
+    run.close()
+    assert sorted(seen) == [i for i in range(len(pick)) if ref[i].steps > at[i]]
+    for i, (r, q) in enumerate(zip(res, ref)):
+        if i in seen and i % 2 == 0:
+            assert r.accepted and r.sweep is None and r.steps == -(-at[i] // 64) * 64
+            np.testing.assert_array_equal(np.concatenate(r.series), np.concatenate(q.series)[: r.steps])
+        else:
+            assert not r.accepted and r.steps == q.steps
+            np.testing.assert_array_equal(np.concatenate(r.series), np.concatenate(q.series))
+            np.testing.assert_array_equal(r.sweep["z"], q.sweep["z"])
+
+
 @pytest.mark.parametrize("chunk", [16, 64])
 def test_graph_chunks_equal_launch_by_launch(chunk):
     """Captured step graphs give the same fields, port series, port/far-field/line phasors."""

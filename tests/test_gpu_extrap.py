@@ -106,8 +106,7 @@ def test_ensemble_with_plain_fallback_on_two_windows():
     assert out["plain"]["single_sweeps_per_hour"] > 0
     for w in out["windows"].values():
         v = w["validation"]
-        # a rejected scene re-runs from its first step: the cost can exceed the plain runs' alone
-        assert 0.0 <= v["accepted"] <= 1.0 and 0.0 < v["cell_steps_vs_plain"] < 2.0
+        assert 0.0 <= v["accepted"] <= 1.0 and 0.0 < v["cell_steps_vs_plain"] <= 1.0 + 1e-9
         hyb, net = w["eval"]["with_fallback"], w["eval"]["network"]
         assert hyb["dz_median"] <= net["dz_median"] + 1e-12 or w["eval"]["fallback_scenes"] == 0
         assert w["sweeps_per_hour"] > 0 and w["speedup_vs_single_plain"] > 0
