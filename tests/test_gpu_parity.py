@@ -191,3 +191,27 @@ def test_field_pointers_are_the_state():
             assert v.shape == h.shape and v.dtype == torch.float32
             assert np.array_equal(v.cpu().numpy(), h)
     g.close()
+
+
+def test_large_workload_crop_long_run_bit_exact():
+    """The 512^3 workload's scene at 128^3 (16-cell absorber, thin-wire dipole with its 50-ohm
+    feed, random dielectric blocks) for 5000 steps — the pulse launched, reflected and absorbed —
+    with the port monitor recording every step: fields and the (V, I) series bit-identical to the
+    FP32 oracle."""
+    import os
+    sc = configs.plain_large(size=128)
+    steps = 5000
+    port = [sc.ports[0].to_c()]
+    out = []
+    oracle.set_threads(os.cpu_count() or 1)
+    for t in (SimulationGrid(sc.grid), oracle.Oracle(sc.grid, "f32")):
+        oracle.load_scene(t, sc)
+        t.ports_configure(port, sc.wavelength, 4.0, False, steps)
+        t.step(steps)
+        out.append((t.read_components(), np.asarray(t.ports_series())))
+        t.close()
+    (fg, sg), (fo, so) = out
+    assert_bitwise(fg, fo, "128^3 crop, 5000 steps")
+    assert sg.shape == so.shape and sg.shape[0] == steps
+    assert np.array_equal(sg, so)
+    assert np.abs(sg[:, 0, 0]).max() > 0.0
