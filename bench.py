@@ -358,7 +358,7 @@ def run_learned(args):
     """--workload learned: the learned ring-down extrapolator (BASELINE config 4 shapes). Training
     runs of the batched generator's scenes (seed --seed) to -60 dB ring-down, training on the GPU
     with this library's kernels, then on held-out scenes (seed --seed + 1): sweeps/hr of the plain
-    solver to ring-down (the judge) against the learned path (early window + inference), and the
+    solver to ring-down (the reference result) against the learned path (early window + inference), and the
     |dZ| and S11 error of the network and of the early window's truncated DFT."""
     import torch
     from em_lab_gb300 import extrap, launch_count
@@ -403,7 +403,7 @@ def run_learned(args):
                                f"{args.val_frac:g} of them held for the fallback threshold), {args.scenes} held-out "
                                f"scenes (seed {args.seed + 1}), early windows {','.join(f'{p:g}' for p in periods)} "
                                f"design periods, ensembles of {args.members}, {args.epochs} epochs",
-                   "plain_judge": "batched stacks and one SimulationGrid per scene, each run to -60 dB ring-down"},
+                   "plain_reference": "batched stacks and one SimulationGrid per scene, each run to -60 dB ring-down"},
         "headline": head, "strict": strict_line, "plain": out["plain"], "windows": windows,
         "train_runs": out["train_runs"], "gpu_launches": int(launch_count() - l0), "clocks": clk.summary(),
     }

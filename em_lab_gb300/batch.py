@@ -10,7 +10,7 @@ half-step phase correction of I, Z = -V/I * eta0), and the scene is dropped from
 compaction once a quarter of the stack has finished.
 
 The single-scene reference path steps one SimulationGrid per scene (src/SimulationGrid.cpp:368-433);
-`run_single` does that with this library, for comparison and as the judge of the batched results.
+`run_single` does that with this library, for comparison and as the reference result for the batched runs.
 """
 from __future__ import annotations
 

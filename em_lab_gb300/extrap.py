@@ -10,7 +10,7 @@ csrc/learn.cu; FP32 master weights and Adam):
 Inputs (host, from the early window of `PERIODS_IN` design periods): V and I resampled to 256
 points in units of the period (I scaled by eta0 / 100, both by the window's peak), and the "method
 without the network": Z_trunc(f) = -V(f) / I(f) * eta0 from the DFT of the early window alone.
-Targets: Z(f) of the whole series run to -60 dB ring-down (the plain solver is the judge).
+Targets: Z(f) of the whole series run to -60 dB ring-down (the plain solver is the reference result).
 PyTorch only allocates the device buffers and moves the batches; every forward and backward
 operation is a kernel of this library.
 """
@@ -461,7 +461,7 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
                periods=None, members=1, val_frac=0.0, single=False):
     """Generates training runs with the batched solver (every scene to -60 dB ring-down, in waves of
     WAVE scenes) and, for each early window in `periods` (design periods; default PERIODS_IN),
-    trains `members` networks on them and evaluates on held-out scenes against the judge, the plain
+    trains `members` networks on them and evaluates on held-out scenes against the reference result, the plain
     solver run to ring-down:
       (a) the plain solver: batched stacks (and with `single`, one SimulationGrid per scene, the
           reference's way) — sweeps/hr and the converged Z(f);
@@ -549,7 +549,7 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
             z_trunc = np.stack(ztr)
             ok = [j for j, k in enumerate(keep) if ev_res[k].rung_down]
             z_conv = np.stack([ev_res[keep[j]].sweep["z"] for j in ok])
-            w["eval"] = {"scenes": n_eval, "judged": len(ok), "network": summary(z_pred[ok], z_conv),
+            w["eval"] = {"scenes": n_eval, "compared": len(ok), "network": summary(z_pred[ok], z_conv),
                          "truncated_dft": summary(z_trunc[ok], z_conv)}
             if tau is not None:
                 z_hyb = np.stack([z_hyb_of[keep[j]] for j in ok])

@@ -27,10 +27,16 @@ SHADERS = ["common.glsl", "field_sampling.glsl", "ntff_common.glsl", "update_B.c
            "line_accumulate.comp", "raymarch.frag"]
 
 
-def reference_shaders() -> Path | None:
+def reference_root() -> Path | None:
+    """The reference source tree ($EMLAB_REFERENCE, default /root/reference), if present."""
     base = Path(os.environ.get("EMLAB_REFERENCE", "/root/reference"))
-    d = base / "shaders"
-    return d if d.is_dir() else None
+    return base if base.is_dir() else None
+
+
+def reference_shaders() -> Path | None:
+    base = reference_root()
+    d = base / "shaders" if base else None
+    return d if d is not None and d.is_dir() else None
 
 
 _FLOAT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])")

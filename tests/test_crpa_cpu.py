@@ -60,7 +60,9 @@ def test_solver_and_mvdr_null():
 
 
 def test_crpa_scene_script():
-    ref = "/root/reference/scenes/17_crpa_gps.lua"
+    from oracle.build_ref import reference_root
+    root = reference_root()
+    ref = os.path.join(str(root), "scenes", "17_crpa_gps.lua") if root else ""
     if not os.path.exists(ref):
         pytest.skip("reference tree not present")
     sc = ScriptEngine(echo=False).run_file(ref).scene
