@@ -28,6 +28,10 @@ int main() {
         grid.step(10, [&] { ++callbacks; });
         grid.step(30);
         grid.synchronize();
+        // device view of the state (eFieldTexture / bFieldTexture): non-null arrays, row pitch >= nx
+        const SimulationGrid::FieldView view = grid.fieldView();
+        bool view_ok = view.pitch >= grid.size().x && view.plane >= (long long)view.pitch * grid.size().y;
+        for (float* p : view.component) view_ok = view_ok && p != nullptr;
         MaterialVolume wrong({8, 8, 8});
         bool threw = false;
         try {
@@ -35,9 +39,9 @@ int main() {
         } catch (const std::runtime_error&) {
             threw = true;
         }
-        std::printf("steps %llu time %.3f callbacks %d size-mismatch-throws %d\n",
-                    (unsigned long long)grid.stepCount(), grid.time(), callbacks, threw ? 1 : 0);
-        return (grid.stepCount() == 40 && callbacks == 10 && threw) ? 0 : 1;
+        std::printf("steps %llu time %.3f callbacks %d size-mismatch-throws %d field-view %d\n",
+                    (unsigned long long)grid.stepCount(), grid.time(), callbacks, threw ? 1 : 0, view_ok ? 1 : 0);
+        return (grid.stepCount() == 40 && callbacks == 10 && threw && view_ok) ? 0 : 1;
     } catch (const std::runtime_error& e) {
         std::printf("runtime_error: %s\n", e.what());
         return 3;
