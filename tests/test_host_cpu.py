@@ -153,3 +153,30 @@ def test_cpp_facade_compiles_and_reports_missing_device(tmp_path):
         pytest.skip("a CUDA device is present (the GPU test runs the demo)")
     res = subprocess.run([str(exe)], capture_output=True, text=True)
     assert res.returncode == 3 and "no CUDA device" in res.stdout
+
+
+def grid_handle_functions():
+    """Functions of include/emlab.h whose first parameter is the grid handle."""
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "emlab.h")).read(), flags=re.S)
+    return sorted(set(re.findall(r"\b(emlab_\w+)\s*\(\s*(?:const\s+)?emlab_grid\s*\*\s*\w+", text)))
+
+
+def test_null_grid_handle_is_an_invalid_argument():
+    """Every entry point that takes a grid handle rejects a NULL handle with EMLAB_ERR_INVALID and a
+    message, before touching the device or any other argument (no device needed)."""
+    import ctypes as C
+
+    lib = grid.load_library()
+    names = grid_handle_functions()
+    assert len(names) >= 30
+    for name in names:
+        fn = getattr(lib, name)
+        assert fn.argtypes is not None, f"{name} has no ctypes signature"
+        args = [0.0 if t in (C.c_float, C.c_double) else (0 if t in (C.c_int, C.c_size_t, C.c_longlong, C.c_uint64)
+                                                           else None) for t in fn.argtypes[1:]]
+        rc = fn(None, *args)
+        if name == "emlab_grid_destroy":
+            assert rc == abi.EMLAB_OK  # destroying nothing is allowed, as delete of a null pointer
+            continue
+        assert rc == abi.EMLAB_ERR_INVALID, f"{name}: {rc}"
+        assert lib.emlab_last_error(), name
