@@ -49,7 +49,7 @@ def test_two_gloo_replicas():
     import torch.multiprocessing as mp
 
     port = _free_port()
-    mgr = mp.Manager()
+    mgr = mp.get_context("spawn").Manager()  # no fork of this multi-threaded process
     out = mgr.dict()
     mp.spawn(_rank, args=(2, port, out), nprocs=2, join=True)
     v0, m0, e0, c0, s0 = out[0]
