@@ -203,6 +203,7 @@ class BatchRunner:
                        sorted(groups.items(), key=lambda kv: kv[0])]
         self.setup_s = time.perf_counter() - t0
         self.results = [SceneResult(i) for i in range(len(self.scenes))]
+        self.stop_steps = list(stop_steps) if stop_steps is not None else None
         self.decide_at = list(decide_at) if decide_at is not None else None
         self.decide = decide
         self.decided = [False] * len(self.scenes)
@@ -213,14 +214,29 @@ class BatchRunner:
         self.cell_steps = 0
         self.steps = 0
 
+    def _next_chunk(self, g, steps):
+        """Steps of the stack's next chunk: up to the next multiple of the chunk length (a whole
+        chunk replays one captured graph), or fewer when a scene's stop or decision step comes
+        sooner, so an early window ends exactly there and the chunk grid stays where it was."""
+        n = self.chunk - steps % self.chunk
+        for i in g.indices:
+            r = self.results[i]
+            if r.done:
+                continue
+            for marks in (self.stop_steps, None if self.decide_at is None or self.decided[i] else self.decide_at):
+                if marks is not None and marks[i] > r.steps:
+                    n = min(n, marks[i] - r.steps)
+        return n
+
     def _run_group(self, g, t0, on_done, lock):
         """One stack's loop (its own host thread and CUDA stream): step a chunk, read the chunk's port
         series back, watch every scene, evaluate the finished ones, compact. The library releases the
         interpreter lock inside its calls, so the stacks' chunks overlap on the device."""
         steps = 0
         while g.indices and steps < self.max_steps:
-            g.stack.step(self.chunk)
-            ser = g.stack.ports_take_series(self.chunk)
+            n = self._next_chunk(g, steps)
+            g.stack.step(n)
+            ser = g.stack.ports_take_series(n)
             nx, ny, _ = g.stack.size()
             cells = nx * ny * sum(g.stack.layout()[1]) * ser.shape[0]
             finished = []
@@ -230,7 +246,10 @@ class BatchRunner:
                     continue
                 r.series.append(ser[:, k].copy())
                 r.steps += ser.shape[0]
-                if self.watch[i].feed(ser[:, k, 0]):
+                # the ring-down watch concludes only at whole chunks, as in a run without stop or
+                # decision steps; a stop step ends the scene wherever it falls
+                fed = self.watch[i].feed(ser[:, k, 0])
+                if fed and (self.stop_steps is not None or r.steps % self.chunk == 0):
                     r.done = True
                     r.rung_down = self.watch[i].rung_down()
                     r.wall_s = time.perf_counter() - t0
@@ -253,7 +272,7 @@ class BatchRunner:
                 if on_done:
                     for i in finished:
                         on_done(i, self.results[i])
-            steps += self.chunk
+            steps += n
             keep = [not self.results[i].done for i in g.indices]
             if not any(keep):
                 g.indices = []

@@ -144,9 +144,9 @@ def test_batch_runner_equals_single_runs():
 
 
 def test_batch_runner_decision_stops_or_continues():
-    """decide_at / decide: scenes the callback accepts stop at the first chunk boundary at or after
-    their decision step; rejected scenes run on to ring-down with the same series (bit for bit) and
-    Z(f) as a run without any decision."""
+    """decide_at / decide: the stack steps exactly to each decision step (a short chunk), scenes the
+    callback accepts stop there; rejected scenes run on to ring-down with the same series (bit for
+    bit) and Z(f) as a run without any decision."""
     scs = [configs.batched_scene(9, i) for i in range(60)]
     pick = [sc for sc in scs if sc.grid.size[0] in (48, 64)][:6]
     plain = batch.BatchRunner(pick, chunk=64, max_steps=20000)
@@ -157,7 +157,7 @@ def test_batch_runner_decision_stops_or_continues():
 
     def decide(idx, series):
         for i, ser in zip(idx, series):
-            assert ser.shape[0] >= at[i] and ser.shape[0] - at[i] < 64
+            assert ser.shape[0] == at[i]
             seen.append(i)
         return [i % 2 == 0 for i in idx]  # accept the even scenes
 
@@ -167,7 +167,7 @@ def test_batch_runner_decision_stops_or_continues():
     assert sorted(seen) == [i for i in range(len(pick)) if ref[i].steps > at[i]]
     for i, (r, q) in enumerate(zip(res, ref)):
         if i in seen and i % 2 == 0:
-            assert r.accepted and r.sweep is None and r.steps == -(-at[i] // 64) * 64
+            assert r.accepted and r.sweep is None and r.steps == at[i]
             np.testing.assert_array_equal(np.concatenate(r.series), np.concatenate(q.series)[: r.steps])
         else:
             assert not r.accepted and r.steps == q.steps
