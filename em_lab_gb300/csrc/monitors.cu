@@ -110,37 +110,48 @@ __device__ __forceinline__ void ntff_point(const int* box, int index, int node[3
     n[a] = side == 1 ? 1.0f : -1.0f;
 }
 
-// ntff_accumulate.comp:30-52: 32 floats per point (stage1 eRe, eIm, hRe, hIm, stage2 ...)
+// ntff_accumulate.comp:30-52: 32 floats per point (stage1 eRe, eIm, hRe, hIm, stage2 ...). The
+// block's 256 x 128 B of state move between HBM and shared memory as one contiguous chunk
+// (consecutive threads, consecutive float4s), rows padded to 9 float4s against bank conflicts;
+// each thread then updates its own point there. Same arithmetic per point.
 __global__ void __launch_bounds__(256) ntff_kernel(MonitorArgs m, const int* box, int points, float4* ph,
                                                    const float4* rot, const float* blend, int k) {
     __shared__ int sbox[13];
+    __shared__ float4 st[256 * 9];
     if (threadIdx.x < 13) sbox[threadIdx.x] = box[threadIdx.x];
+    const int first = blockIdx.x * blockDim.x;
+    const int count = min((int)blockDim.x, points - first);
+    float4* base = ph + 8 * (long long)first;
+    for (int j = threadIdx.x; j < 8 * count; j += blockDim.x) st[9 * (j >> 3) + (j & 7)] = base[j];
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= points) return;
-    int node[3];
-    float n[3], w;
-    ntff_point(sbox, i, node, n, w);
-    float E[3], Hh[3];
-    e_at_node(m, node[0], node[1], node[2], E[0], E[1], E[2]);
-    b_at_node(m, node[0], node[1], node[2], Hh[0], Hh[1], Hh[2]);
-    const float4 r = rot[k];
-    const float b = blend[k];
-    float4* p = ph + 8 * (long long)i;
-    float4 s1[4] = {p[0], p[1], p[2], p[3]}, s2[4] = {p[4], p[5], p[6], p[7]};
-    const float f[4] = {2.0f * r.x, -2.0f * r.y, 2.0f * r.z, -2.0f * r.w};
-    for (int q = 0; q < 4; ++q) {
-        const float* src = q < 2 ? E : Hh;
-        s1[q].x = s1[q].x + b * (f[q] * src[0] - s1[q].x);
-        s1[q].y = s1[q].y + b * (f[q] * src[1] - s1[q].y);
-        s1[q].z = s1[q].z + b * (f[q] * src[2] - s1[q].z);
+    const int i = first + threadIdx.x;
+    if (i < points) {
+        int node[3];
+        float n[3], w;
+        ntff_point(sbox, i, node, n, w);
+        float E[3], Hh[3];
+        e_at_node(m, node[0], node[1], node[2], E[0], E[1], E[2]);
+        b_at_node(m, node[0], node[1], node[2], Hh[0], Hh[1], Hh[2]);
+        const float4 r = rot[k];
+        const float b = blend[k];
+        float4* p = st + 9 * threadIdx.x;
+        float4 s1[4] = {p[0], p[1], p[2], p[3]}, s2[4] = {p[4], p[5], p[6], p[7]};
+        const float f[4] = {2.0f * r.x, -2.0f * r.y, 2.0f * r.z, -2.0f * r.w};
+        for (int q = 0; q < 4; ++q) {
+            const float* src = q < 2 ? E : Hh;
+            s1[q].x = s1[q].x + b * (f[q] * src[0] - s1[q].x);
+            s1[q].y = s1[q].y + b * (f[q] * src[1] - s1[q].y);
+            s1[q].z = s1[q].z + b * (f[q] * src[2] - s1[q].z);
+        }
+        for (int q = 0; q < 4; ++q) {
+            s2[q].x = s2[q].x + b * (s1[q].x - s2[q].x);
+            s2[q].y = s2[q].y + b * (s1[q].y - s2[q].y);
+            s2[q].z = s2[q].z + b * (s1[q].z - s2[q].z);
+        }
+        for (int q = 0; q < 4; ++q) p[q] = s1[q], p[4 + q] = s2[q];
     }
-    for (int q = 0; q < 4; ++q) {
-        s2[q].x = s2[q].x + b * (s1[q].x - s2[q].x);
-        s2[q].y = s2[q].y + b * (s1[q].y - s2[q].y);
-        s2[q].z = s2[q].z + b * (s1[q].z - s2[q].z);
-    }
-    for (int q = 0; q < 4; ++q) p[q] = s1[q], p[4 + q] = s2[q];
+    __syncthreads();
+    for (int j = threadIdx.x; j < 8 * count; j += blockDim.x) base[j] = st[9 * (j >> 3) + (j & 7)];
 }
 
 // line_accumulate.comp:30-48
