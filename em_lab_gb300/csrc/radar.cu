@@ -121,14 +121,16 @@ extern "C" int emlab_radar_backproject(const emlab_radar_geometry* geo, const fl
         release();
         return report_error(EMLAB_ERR_OOM, "radar: device allocation failed");
     }
-    cudaMemcpy(dz, z, zb, cudaMemcpyHostToDevice);
-    cudaMemcpy(de, elem_pos, (size_t)C * 12, cudaMemcpyHostToDevice);
-    cudaMemcpy(dt, tx_pos, (size_t)ntx * 12, cudaMemcpyHostToDevice);
-    cudaMemcpy(dw, weights, (size_t)C * 8, cudaMemcpyHostToDevice);
-    cudaMemcpy(da, tx_amp, (size_t)ntx * 8, cudaMemcpyHostToDevice);
-    backproject_kernel<<<(unsigned)((total + 127) / 128), 128>>>(*geo, dz, M, C, de, dw, dt, da, ntx, dp);
-    count_launches(1);
-    cudaError_t e = cudaGetLastError();
+    cudaError_t e = cudaMemcpy(dz, z, zb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(de, elem_pos, (size_t)C * 12, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dt, tx_pos, (size_t)ntx * 12, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dw, weights, (size_t)C * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(da, tx_amp, (size_t)ntx * 8, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        backproject_kernel<<<(unsigned)((total + 127) / 128), 128>>>(*geo, dz, M, C, de, dw, dt, da, ntx, dp);
+        count_launches(1);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaMemcpy(power, dp, (size_t)total * 8, cudaMemcpyDeviceToHost);
     release();
     if (e != cudaSuccess) return report_error(EMLAB_ERR_CUDA, cudaGetErrorString(e));
