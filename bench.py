@@ -124,7 +124,7 @@ def workload_text(args, sc, dft_points=None):
             f"feed, 5% seeded random dielectric blocks, port series recorded every step")
     if dft_points is not None:
         text += (f", far-field DFT at {DFT_FREQS} frequencies on a box {DFT_MARGIN} cells inside the absorber "
-                 f"({dft_points} nodes, tensor-core fold every 64 steps)")
+                 f"({dft_points} nodes)")
     return text
 
 
@@ -203,8 +203,9 @@ def read_traffic(key: str):
     return None
 
 
-def cpu_sample(sc, seconds_budget: float = 20.0, max_steps: int = 8):
-    """The FP32 CPU restatement on every host thread, over the full grid, for a few steps."""
+def cpu_sample(sc, seconds_budget: float = 20.0, max_steps: int = 8, dft: bool = False):
+    """The FP32 CPU restatement on every host thread, over the full grid, for a few steps, with the
+    same per-step monitors as the GPU arm (port series; the 32-frequency far-field DFT if `dft`)."""
     import oracle
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
@@ -213,6 +214,8 @@ def cpu_sample(sc, seconds_budget: float = 20.0, max_steps: int = 8):
     oracle.load_scene(o, sc)
     if sc.ports:
         o.ports_configure([p.to_c() for p in sc.ports], sc.ports[0].wavelength, 4.0, sweep=True)
+    if dft:
+        dft_setup(o, sc)
     setup = time.perf_counter() - t0
     cells = float(np.prod(sc.grid.size))
     o.step(1)  # warm-up (first touch of every page)
@@ -226,7 +229,8 @@ def cpu_sample(sc, seconds_budget: float = 20.0, max_steps: int = 8):
     el = time.perf_counter() - t0
     o.close()
     return {"value": cells * steps / el / 1e6, "unit": "Mcells/s", "cores": threads, "kind": "port",
-            "sample": f"{steps} full-grid steps (B, E, sources{', port monitor' if sc.ports else ''}) of the "
+            "sample": f"{steps} full-grid steps (B, E, sources{', port monitor' if sc.ports else ''}"
+                      f"{', 32-frequency far-field DFT' if dft else ''}) of the "
                       f"{'x'.join(str(v) for v in sc.grid.size)} workload after 1 warm-up step "
                       f"(oracle/emlab_oracle.c FP32, OpenMP {threads} threads, set-up {setup:.1f} s excluded)"}
 
@@ -258,6 +262,11 @@ def run_reference(args):
         oracle.load_scene(runner, sc)
     if sc.ports:
         runner.ports_configure([p.to_c() for p in sc.ports], sc.ports[0].wavelength, 4.0, sweep=True)
+    # the same per-step monitors as the GPU arm: the 32-frequency far-field DFT (FP64 sums every
+    # step) runs in the restatement; the reference's own shaders have no multi-frequency monitor
+    dft_points = None
+    if args.workload == "plain_large" and kind == "port":
+        _, dft_points = dft_setup(runner, sc)
     # each bench step is a bounded sample: one full-grid leapfrog step
     for _ in range(max(1, min(args.warmup, 1))):
         runner.step(1)
@@ -272,8 +281,9 @@ def run_reference(args):
             break
     el = time.perf_counter() - t0
     value = cells * done / el / 1e6
+    monitors = (", port monitor" if sc.ports else "") + (", 32-frequency far-field DFT" if dft_points else "")
     sample = (f"{done} of {args.steps} requested full-grid leapfrog steps (B, E, sources"
-              f"{', port monitor' if sc.ports else ''}) of the {'x'.join(str(v) for v in sc.grid.size)} workload "
+              f"{monitors}) of the {'x'.join(str(v) for v in sc.grid.size)} workload "
               f"within a {budget:.0f} s budget, "
               f"{'reference shaders compiled as C++ (oracle/_ref)' if kind == 'reference' else 'CPU restatement oracle/emlab_oracle.c FP32'}, "
               f"{threads} host threads")
@@ -281,7 +291,10 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": el * 1e3 / done, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": workload_text(args, sc), "cells": int(cells)},
+            "config": {"workload": workload_text(args, sc, dft_points) + (
+                "" if dft_points or args.workload != "plain_large" else
+                " (the far-field DFT is omitted: the reference's shaders have no multi-frequency monitor)"),
+                       "cells": int(cells)},
             "cpu_baseline": {"value": value, "unit": "Mcells/s", "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": value, "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -592,7 +605,7 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            cpu = cpu_sample(sc)
+            cpu = cpu_sample(sc, dft=dft_points is not None)
         except Exception as e:  # pragma: no cover - reported, not fatal
             cpu = {"value": None, "unit": "Mcells/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
@@ -615,6 +628,8 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_kind,
+                         "traffic_source": ("DRAM bytes read + written per launch from one ncu capture "
+                                            "(profiles/traffic.txt), not measured in this run") if traffic else None,
                          "kernel": kname, "kernel_ms_per_launch": per_launch_ms,
                          "algorithmic_bytes_per_cell_step": BYTES_PER_CELL_STEP},
             "cpu_baseline": cpu,

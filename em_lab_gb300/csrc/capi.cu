@@ -1292,6 +1292,7 @@ int emlab_analyzer_submit(emlab_grid* g, const int* origins, int n_probes, const
     if ((size_t)n_probes > a.probe_cap) {
         if (a.h_probe) cudaFreeHost(a.h_probe);
         a.h_probe = nullptr;
+        a.probe_cap = 0;  // a failed allocation below leaves the slot empty, not a null buffer of old capacity
         EMLAB_CUDA(cudaMallocHost(&a.h_probe, (size_t)n_probes * 54 * 16));
         EMLAB_CUDA(a.d_origins.alloc((size_t)n_probes));
         EMLAB_CUDA(a.d_probe.alloc((size_t)n_probes * 54));
@@ -1300,6 +1301,7 @@ int emlab_analyzer_submit(emlab_grid* g, const int* origins, int n_probes, const
     if (total > a.part_cap) {
         if (a.h_part) cudaFreeHost(a.h_part);
         a.h_part = nullptr;
+        a.part_cap = 0;
         EMLAB_CUDA(cudaMallocHost(&a.h_part, total * 4));
         EMLAB_CUDA(a.d_part.alloc(total));
         a.part_cap = total;

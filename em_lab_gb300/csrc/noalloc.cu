@@ -1,13 +1,14 @@
 // noalloc.cu - Poynting flux through planes without any memory allocation.
 //
 // emlab_flux_planes allocates its per-workgroup partial sums with cudaMalloc and frees them again
-// on every call. Some callers cannot do that: cudaMalloc and cudaFree synchronise the whole device
-// (a frame loop that measures flux every other frame, like the reference's, would stall the solver
-// on each measurement), they are not allowed while a CUDA stream capture is in progress, and
-// applications that pre-budget all device memory for their scenes do not want a library allocating
-// behind their back. This variant keeps its scratch in fixed file-scope device arrays instead:
-// kMaxPartials workgroup partials (256 KB) and kMaxPlanes FP64 sums, held by every device that
-// loads the library until the process exits.
+// on every call. Some callers cannot accept that: a frame loop that measures flux every other
+// frame, like the reference's, while the solver keeps stepping (cudaFree waits for the whole
+// device, so every measurement would stall the solver), and applications that budget all device
+// memory themselves (an allocation they did not plan for can fail part-way through a run). This
+// variant keeps its scratch in fixed file-scope device arrays instead: kMaxPartials workgroup
+// partials (256 KB) and kMaxPlanes FP64 sums, held by every device that loads the library until
+// the process exits. The first call on a device looks their addresses up; every call shares them,
+// so calls whose kernels overlap on the GPU race. The call returns once the sums are on the host.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -136,14 +136,27 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY <= 8 ? 3 : 1)
     }
     __syncthreads();
     bool failed = false;
+    int issued_hi = zstart - 1;  // leader: last plane whose loads were issued
+    int waited_ok = zstart - 1;  // leader: last plane whose loads were seen complete
+    // on an expired wait: record the error, then give every copy still in flight (the plane that
+    // timed out included) a bounded time to land before the CTA leaves and its shared memory goes
+    auto bail = [&]() {
+        if (leader) {
+            atomicOr(err, 1u);
+            for (int p = waited_ok + 1; p <= issued_hi; ++p)
+                mbar_wait(bars + (p - zstart) % S_, ((p - zstart) / S_) & 1);
+        }
+    };
     if (leader) {
-        for (int p = zstart; p <= zlast && p < zstart + S_; ++p) issue(p);
+        for (int p = zstart; p <= zlast && p < zstart + S_; ++p) issue(p), issued_hi = p;
         // planes zstart and zstart+1 before the first B phase; later planes one iteration ahead,
         // just before the per-plane barrier, which passes the TMA writes on to the other warps
-        failed = !mbar_wait(bars + 0, 0) || !mbar_wait(bars + 1, 0);
+        failed = !mbar_wait(bars + 0, 0);
+        if (!failed) waited_ok = zstart, failed = !mbar_wait(bars + 1, 0);
+        if (!failed) waited_ok = zstart + 1;
     }
     if (__syncthreads_or(failed)) {
-        if (leader) atomicOr(err, 1u);
+        bail();
         return;
     }
 
@@ -275,15 +288,19 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY <= 8 ? 3 : 1)
             }
         }
         // the next iteration's B phase reads plane z+2: the leader waits for it before the barrier
-        if (leader && z + 1 < ze) failed = !mbar_wait(bars + (rel + 2) % S_, ((rel + 2) / S_) & 1);
+        if (leader && z + 1 < ze) {
+            failed = !mbar_wait(bars + (rel + 2) % S_, ((rel + 2) / S_) & 1);
+            if (!failed) waited_ok = z + 2;
+        }
         if (__syncthreads_or(failed)) {
-            if (leader) atomicOr(err, 1u);
+            bail();
             return;
         }
         // every warp is past its reads of plane z-1's stage: refill it with plane z-1+STAGES
         if (leader && z > zstart && z - 1 + S_ <= zlast) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             issue(z - 1 + S_);
+            issued_hi = z - 1 + S_;
         }
         if (emit && own) {
             // update_E.comp:41-64 for the own cell
@@ -540,11 +557,13 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1)
         prod[6] = waited;
         return ok;
     };
-    // on an expired wait: record the error, give the copies still in flight a bounded time to land
+    // on an expired wait: record the error, then give every copy still in flight a bounded time to
+    // land before the CTA leaves and its shared memory goes. prod[6] is the load whose wait ran out
+    // (not complete), prod[5] - 1 the last load issued.
     auto bail = [&]() {
         if (leader) {
             atomicOr(err, 1u);
-            for (int w = prod[6] + 1; w < prod[5]; ++w) mbar_wait(bars + w % S_, (w / S_) & 1);
+            for (int w = prod[6] < 0 ? 0 : prod[6]; w < prod[5]; ++w) mbar_wait(bars + w % S_, (w / S_) & 1);
         }
     };
 

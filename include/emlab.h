@@ -326,17 +326,20 @@ int emlab_probe_gather(emlab_grid* g, const int* origins, int n_probes, float* o
 int emlab_flux_planes(emlab_grid* g, const emlab_flux_plane* planes, int n_planes, double* out);
 
 /* Flux through planes for callers that must not allocate device memory (no counterpart in the
- * reference). emlab_flux_planes allocates and frees its per-workgroup partial sums on every call;
- * cudaMalloc/cudaFree synchronise the whole device (a frame loop that measures flux every other
- * frame would stall the solver each time), are not allowed during a CUDA stream capture, and are
- * unwelcome in applications that budget all device memory themselves. This entry point allocates
- * nothing: its scratch is a fixed file-scope device array of EMLAB_FLUX_NOALLOC_MAX_PARTIALS FP32
- * workgroup partials (256 KB) plus EMLAB_FLUX_NOALLOC_MAX_PLANES FP64 sums, held by every device
- * that loads the library until the process exits. Requests needing more planes or partials fail
- * with EMLAB_ERR_INVALID. The first call on a device looks the scratch up (cudaGetSymbolAddress,
- * with the grid's device current); make that first call before any stream capture. Every call
- * shares the scratch and overwrites all of it that it reads, so calls whose kernels overlap on the
- * GPU (grids on different streams of one device) race. Results equal emlab_flux_planes bit for bit. */
+ * reference). emlab_flux_planes allocates and frees its per-workgroup partial sums on every call.
+ * Two kinds of caller cannot accept that: a frame loop that measures flux every other frame while
+ * the solver runs (cudaFree waits for the whole device, so each measurement would stall the
+ * stepping), and an application that budgets all device memory itself (a library allocation it
+ * did not plan for can fail part-way through a run, or push its own allocations out). This entry
+ * point allocates nothing: its scratch is a fixed file-scope device array of
+ * EMLAB_FLUX_NOALLOC_MAX_PARTIALS FP32 workgroup partials (256 KB) plus
+ * EMLAB_FLUX_NOALLOC_MAX_PLANES FP64 sums, held by every device that loads the library until the
+ * process exits. Requests needing more planes or partials fail with EMLAB_ERR_INVALID. The first
+ * call on a device looks the scratch up (cudaGetSymbolAddress, with the grid's device current);
+ * make that first call before any stream capture. Every call shares the scratch and overwrites all
+ * of it that it reads, so calls whose kernels overlap on the GPU (grids on different streams of one
+ * device) race. The call waits for the grid's stream and copies the sums to `out` before it
+ * returns. Results equal emlab_flux_planes bit for bit. */
 #define EMLAB_FLUX_NOALLOC_MAX_PLANES 64
 #define EMLAB_FLUX_NOALLOC_MAX_PARTIALS 65536
 int emlab_flux_planes_noalloc(emlab_grid* g, const emlab_flux_plane* planes, int n_planes, double* out);

@@ -278,6 +278,10 @@ class Oracle:
         self._dft_nf = len(wl)
         return tuple(out[:3]), tuple(out[3:])
 
+    def ntff_dft_info(self):
+        """(box nodes, samples accumulated) like the device monitor's emlab_ntff_dft_info."""
+        return int(self._fn("oracle_ntff_dft_points")(self._h)), None
+
     def ntff_dft_read(self):
         n = int(self._fn("oracle_ntff_dft_points")(self._h))
         out = np.zeros((self._dft_nf, n, 6, 2), np.float64)

@@ -1,14 +1,16 @@
 """Compiles the reference's own compute shaders as C++ (test infrastructure; the pin of the oracle).
 
-Reads the shader files where they lie in the reference tree (default /root/reference/shaders, or
-$EMLAB_REFERENCE/shaders), rewrites the GLSL-only syntax mechanically (resource declarations ->
+Reads the shader files where they lie in the reference tree (`--reference PATH` or
+$EMLAB_REFERENCE; without either the recipe does nothing), rewrites the GLSL-only syntax mechanically (resource declarations ->
 globals, fragment inputs/outputs -> per-thread globals, `out` parameters -> references, swizzles
 -> calls, `.a` -> `.w`, float literals -> float suffix, array constructors -> brace lists) into oracle/_ref/*.hpp, and builds oracle/_ref/libemlab_ref.so
 from oracle/ref_driver.cpp, which runs every dispatch of SimulationGrid::step and the monitors over
 the CPU with those shader bodies and the GLSL semantics of oracle/glsl_shim.hpp. Nothing under
-oracle/_ref is committed. Without the reference tree the recipe does nothing.
+oracle/_ref is committed. Without the reference tree the recipe does nothing. The tree it built
+from is recorded in oracle/_ref/source_tree.txt, where the tests look for it when
+$EMLAB_REFERENCE is unset.
 
-    python oracle/build_ref.py [--force]
+    python oracle/build_ref.py --reference PATH [--force]
 """
 from __future__ import annotations
 
@@ -27,10 +29,20 @@ SHADERS = ["common.glsl", "field_sampling.glsl", "ntff_common.glsl", "update_B.c
            "line_accumulate.comp", "raymarch.frag"]
 
 
+_TREE_RECORD = OUT / "source_tree.txt"
+_explicit_root: Path | None = None
+
+
 def reference_root() -> Path | None:
-    """The reference source tree ($EMLAB_REFERENCE, default /root/reference), if present."""
-    base = Path(os.environ.get("EMLAB_REFERENCE", "/root/reference"))
-    return base if base.is_dir() else None
+    """The reference source tree: the recipe's `--reference` argument, else $EMLAB_REFERENCE, else the
+    tree the last build recorded in oracle/_ref/source_tree.txt; None when none of them exists."""
+    cands = [_explicit_root, os.environ.get("EMLAB_REFERENCE")]
+    if _TREE_RECORD.exists():
+        cands.append(_TREE_RECORD.read_text().strip())
+    for c in cands:
+        if c and Path(c).is_dir():
+            return Path(c)
+    return None
 
 
 def reference_shaders() -> Path | None:
@@ -100,6 +112,7 @@ def build(force: bool = False, verbose: bool = False) -> Path | None:
         if not dst.exists() or dst.read_text() != text:
             dst.write_text(text)
             changed = True
+    _TREE_RECORD.write_text(str(src.parent) + "\n")
     if not changed and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return LIB
     # the host-side set-up comes from the restatement: link its object into the same library
@@ -119,5 +132,7 @@ def build(force: bool = False, verbose: bool = False) -> Path | None:
 
 
 if __name__ == "__main__":
+    if "--reference" in sys.argv:
+        _explicit_root = Path(sys.argv[sys.argv.index("--reference") + 1])
     lib = build(force="--force" in sys.argv, verbose=True)
     print(lib if lib else "reference tree not found: nothing built")

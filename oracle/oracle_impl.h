@@ -411,6 +411,12 @@ static void NAME(dft_accumulate)(NAME(grid) * g) {
     const double dt = (double)g->cfg.courant;
     const double tE = (double)g->step * dt, tH = tE - 0.5 * dt;
     const int P = g->dft_points, nf = g->dft_nf;
+    /* the phases depend on the frequency only: evaluated once per step (nf <= 128) */
+    double rot[128][4];
+    for (int f = 0; f < nf && f < 128; ++f) {
+        const double w = g->dft_w[f];
+        rot[f][0] = cos(w * tE), rot[f][1] = sin(w * tE), rot[f][2] = cos(w * tH), rot[f][3] = sin(w * tH);
+    }
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < P; ++i) {
         int node[3];
@@ -418,9 +424,8 @@ static void NAME(dft_accumulate)(NAME(grid) * g) {
         R E[3], H[3];
         NAME(e_at_node)(g, node[0], node[1], node[2], E);
         NAME(b_at_node)(g, node[0], node[1], node[2], H);
-        for (int f = 0; f < nf; ++f) {
-            const double w = g->dft_w[f];
-            const double ce = cos(w * tE), se = sin(w * tE), ch = cos(w * tH), sh = sin(w * tH);
+        for (int f = 0; f < nf && f < 128; ++f) {
+            const double ce = rot[f][0], se = rot[f][1], ch = rot[f][2], sh = rot[f][3];
             double* x = g->dft + ((size_t)f * P + (size_t)i) * 12;
             for (int c = 0; c < 3; ++c) {
                 x[2 * c] += (double)E[c] * ce, x[2 * c + 1] -= (double)E[c] * se;
@@ -565,6 +570,7 @@ int NAME(oracle_ntff_dft_configure)(void* h, const int mn[3], const int mx[3], c
     free(g->dft_w), free(g->dft);
     g->dft_w = NULL, g->dft = NULL, g->dft_on = 0;
     if (nf <= 0) return EMLAB_OK;
+    if (nf > 128) return EMLAB_ERR_INVALID; /* as the device monitor: at most 128 frequencies */
     const int n[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
     const int L = g->cfg.pml_thickness;
     for (int a = 0; a < 3; ++a) {

@@ -1,8 +1,8 @@
 """The allocation-free flux entry point (emlab_flux_planes_noalloc) against emlab_flux_planes.
 
-It serves callers that must not allocate device memory while they measure (frame loops that cannot
-afford the device-wide synchronisation of cudaMalloc/cudaFree, code running during a stream
-capture, hosts that own the whole device-memory budget). Its scratch is a fixed device array shared
+It serves callers that must not allocate device memory while they measure: frame loops that cannot
+afford the device-wide wait of cudaFree while the solver steps, and hosts that budget all device
+memory themselves. Its scratch is a fixed device array shared
 by every call, so two calls in a row must each give exactly what the allocating entry point gives
 for the same fields, and requests beyond the fixed limits must be refused. This file is collected
 last so a failure here cannot hide the other tests.
