@@ -1437,6 +1437,25 @@ int emlab_edge_materials(const float* sigma, const float* eps_r, int nx, int ny,
 
 double emlab_source_signal(const emlab_source* source, double t) { return source ? source_signal(*source, t) : 0.0; }
 
+int emlab_source_lists(const emlab_source* sources, size_t n, int nx, int ny, int nz, float* packed, int32_t* cells,
+                       int32_t* lists, int* n_sources, int* n_cells, int* n_lists) {
+    EMLAB_REQUIRE((sources || n == 0) && nx > 0 && ny > 0 && nz > 0 && n_sources && n_cells && n_lists,
+                  "bad source-list arguments");
+    std::vector<emlab_source> desc;
+    std::vector<float> pk;
+    const int nsrc = pack_sources(sources, n, desc, pk);
+    std::vector<int32_t> c, l;
+    const int size[3] = {nx, ny, nz};
+    source_lists(pk, nsrc, size, c, l);
+    *n_sources = nsrc;
+    *n_cells = (int)(c.size() / 4) - 1;  // the sentinel is not a cell
+    *n_lists = (int)l.size();
+    if (packed) std::copy(pk.begin(), pk.end(), packed);
+    if (cells) std::copy(c.begin(), c.end(), cells);
+    if (lists) std::copy(l.begin(), l.end(), lists);
+    return EMLAB_OK;
+}
+
 // ---- self-checks ---------------------------------------------------------------------------
 int emlab_debug_expf(const float* in, float* out, size_t n) {
     if (!in || !out) return fail(EMLAB_ERR_INVALID, "null argument");

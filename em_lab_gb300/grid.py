@@ -100,6 +100,8 @@ def load_library() -> C.CDLL:
         "emlab_edge_materials": ([fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ, C.POINTER(abi.WireTerm), SZ,
                                   fp, fp, fp, fp, C.POINTER(C.c_uint32)], I),
         "emlab_source_signal": ([C.POINTER(abi.Source), D], D),
+        "emlab_source_lists": ([C.POINTER(abi.Source), SZ, I, I, I, fp, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                C.POINTER(I), C.POINTER(I), C.POINTER(I)], I),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -150,6 +152,23 @@ def edge_materials(sigma, eps_r, edges=(), wires=()):
     _check(load_library().emlab_edge_materials(_fptr(s), _fptr(e), nx, ny, nz, ea, ne, wa, nw,
                                                *[_fptr(o) for o in outs], C.byref(classes)))
     return (*outs, int(classes.value))
+
+
+def source_lists(sources, size):
+    """Host-side setSources arithmetic on a grid of `size` cells: (packed (k, 16) float32 source
+    records, cells (m + 1, 4) int32 with the sentinel, lists int32); needs no device."""
+    arr, n = abi.array_of(abi.Source, [s.to_c() if hasattr(s, "to_c") else s for s in sources])
+    nx, ny, nz = (int(v) for v in size)
+    ns, nc, nl = C.c_int(), C.c_int(), C.c_int()
+    lib = load_library()
+    _check(lib.emlab_source_lists(arr, n, nx, ny, nz, None, None, None, C.byref(ns), C.byref(nc), C.byref(nl)))
+    packed = np.zeros((max(ns.value, 1), 16), np.float32)
+    cells = np.zeros((nc.value + 1, 4), np.int32)
+    lists = np.zeros(max(nl.value, 1), np.int32)
+    i32 = C.POINTER(C.c_int32)
+    _check(lib.emlab_source_lists(arr, n, nx, ny, nz, _fptr(packed), cells.ctypes.data_as(i32),
+                                  lists.ctypes.data_as(i32), C.byref(ns), C.byref(nc), C.byref(nl)))
+    return packed[:ns.value], cells, lists[:nl.value]
 
 
 def source_signal(src, t: float) -> float:

@@ -1,6 +1,7 @@
 """Headless runner: a scene script stepped for N frames with the reference's console output.
 
     python -m em_lab_gb300 --script FILE.lua --frames N [--set NAME=VALUE ...] [--steps N]
+    python -m em_lab_gb300 --scene FILE.npz --frames N     (a scene built earlier, see scene_io)
 
 Follows the unattended `--frames` mode of the reference application (src/Main.cpp:40-103 options,
 464-540 scene load and header, 1043-1157 frame loop): each frame steps the grid (the monitors that
@@ -76,8 +77,6 @@ def screenshot(grid, sc, path, width, height):
 def run(script, frames, overrides=None, steps_per_frame=None, quiet=False, screenshot_path=None,
         width=1920, height=1080):
     """Runs `script` for `frames` frames; returns (exit code, Instruments)."""
-    from . import SimulationGrid
-    from .instruments import NO_INSTRUMENTS_HINT, Instruments
     from .script import ScriptError
 
     try:
@@ -85,6 +84,18 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False, scree
     except ScriptError as e:
         print(f"script error: {e}", file=sys.stderr)
         return 3, None
+    return run_result(res, frames, steps_per_frame, screenshot_path=screenshot_path, width=width, height=height,
+                      script_name=os.path.basename(str(script)))
+
+
+def run_result(res, frames, steps_per_frame=None, screenshot_path=None, width=1920, height=1080,
+               script_name="scene", after_frame=None):
+    """Runs an already built scene (a script's ScriptResult, e.g. loaded by scene_io) for `frames`
+    frames exactly as `run` does; returns (exit code, Instruments). `after_frame(frame, inst)` is
+    called after every frame's measurements (for callers that watch the readings)."""
+    from . import SimulationGrid
+    from .instruments import NO_INSTRUMENTS_HINT, Instruments
+
     sc = res.scene
     grid = SimulationGrid(sc.grid)
     # a radar first records the scene without its targets (Main.cpp:472-507)
@@ -95,7 +106,7 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False, scree
     inst = Instruments(grid, sc, output_dir=res.output_dir)
     for w in res.warnings + inst.warnings:
         print(f"  warning: {w}", file=sys.stderr)
-    print_header(res, grid, os.path.basename(str(script)))
+    print_header(res, grid, script_name)
     if inst.empty():
         print(NO_INSTRUMENTS_HINT)
     spf = steps_per_frame if steps_per_frame is not None else 2
@@ -126,6 +137,8 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False, scree
                 inst.evaluate_sweep()
         inst.poll_coax()  # the reference polls the line monitor once per frame
         frame += 1
+        if after_frame is not None:
+            after_frame(frame, inst)
         if frame % 100 == 0 and not inst.empty():
             inst.print_report()
         if frame >= frames:
@@ -147,7 +160,9 @@ def run(script, frames, overrides=None, steps_per_frame=None, quiet=False, scree
 
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m em_lab_gb300", description=__doc__.split("\n\n")[0])
-    ap.add_argument("--script", required=True, help="scene script (.lua)")
+    src = ap.add_mutually_exclusive_group(required=True)
+    src.add_argument("--script", help="scene script (.lua)")
+    src.add_argument("--scene", help="a built scene saved by em_lab_gb300.scene_io (.npz)")
     ap.add_argument("--set", action="append", default=[], metavar="NAME=VALUE", help="override a script param{}")
     ap.add_argument("--frames", type=int, default=100, help="run this many frames, then exit")
     ap.add_argument("--steps", type=int, default=2, help="simulation steps per frame (the scene's view{} wins)")
@@ -162,6 +177,12 @@ def main(argv=None):
             continue
         k, v = kv.split("=", 1)
         overrides[k] = v
+    if a.scene:
+        from . import scene_io
+        res = scene_io.load(a.scene)
+        code, _ = run_result(res, max(a.frames, 1), min(max(a.steps, 0), 64), screenshot_path=a.screenshot,
+                             width=max(a.width, 1), height=max(a.height, 1), script_name=os.path.basename(a.scene))
+        return code
     code, _ = run(a.script, max(a.frames, 1), overrides, min(max(a.steps, 0), 64), screenshot_path=a.screenshot,
                   width=max(a.width, 1), height=max(a.height, 1))
     return code

@@ -372,6 +372,14 @@ int emlab_edge_materials(const float* sigma, const float* eps_r, int nx, int ny,
                          uint32_t* classes);
 /* SourceDesc::signal (src/SimulationGrid.cpp:103-130): the FP64 source waveform at time t. */
 double emlab_source_signal(const emlab_source* source, double t);
+/* The source records and per-cell source lists setSources derives (src/SimulationGrid.cpp:297-349)
+ * on a grid of nx x ny x nz cells: packed receives 16 floats per kept source (centre, half extent,
+ * polarisation | amplitude, softness, as vec4s); cells 4 ints per listed cell (x, y, z, first list
+ * entry) plus the sentinel (0, 0, 0, list length); lists the source index of every (cell, source)
+ * pair. *n_sources, *n_cells (without the sentinel) and *n_lists receive the sizes; any of packed,
+ * cells, lists may be NULL (a first call sizes the arrays). */
+int emlab_source_lists(const emlab_source* sources, size_t n, int nx, int ny, int nz, float* packed, int32_t* cells,
+                       int32_t* lists, int* n_sources, int* n_cells, int* n_lists);
 
 /* ---- self-checks ------------------------------------------------------------------------- */
 /* Evaluates the device emlab_expf on n inputs (bit-exactness check against the host). */

@@ -80,6 +80,61 @@ def load_ref():
     return lib
 
 
+_REF_HOST_PATH = Path(__file__).resolve().parent / "_ref" / "libemlab_ref_host.so"
+_ref_host = None
+
+
+def ref_host_available() -> bool:
+    """True when oracle/_ref/libemlab_ref_host.so (the reference's host set-up and radar C++,
+    built by oracle/build_ref.py) exists."""
+    return _REF_HOST_PATH.exists()
+
+
+def load_ref_host():
+    """The reference's host C++ (oracle/ref_host.cpp over the extracted spans; raises if absent)."""
+    global _ref_host
+    if _ref_host is not None:
+        return _ref_host
+    if not _REF_HOST_PATH.exists():
+        raise FileNotFoundError(f"{_REF_HOST_PATH} is not built (python oracle/build_ref.py --reference PATH)")
+    lib = C.CDLL(str(_REF_HOST_PATH))
+    I, SZ, F, D = C.c_int, C.c_size_t, C.c_float, C.c_double
+    fp, dp, ip = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int)
+    u32p, i32p = C.POINTER(C.c_uint32), C.POINTER(C.c_int32)
+    src = C.POINTER(abi.Source)
+    spec = {
+        "ref_host_signal": ([src, D], D),
+        "ref_host_dipole": ([fp, fp, F, F, F, src], None),
+        "ref_host_plane_wave": ([I, F, fp, F, F, src], None),
+        "ref_host_upload_materials": ([fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ, C.POINTER(abi.WireTerm),
+                                       SZ, u32p, u32p], I),
+        "ref_host_set_sources": ([src, SZ, I, I, I, fp, i32p, i32p, ip, ip], I),
+        "ref_host_radar_backproject": ([C.POINTER(abi.RadarGeometry), F, fp, I, I, fp, dp, fp, dp, I, dp], None),
+    }
+    for name, (args, res) in spec.items():
+        fn = getattr(lib, name)
+        fn.argtypes, fn.restype = args, res
+    _ref_host = lib
+    return lib
+
+
+def ref_host_backproject(g, wavelength, z, elem_pos, weights, tx_pos, tx_amp):
+    """RadarMonitor::computeImage's back-projection compiled from the reference: power (nr, nel, naz)."""
+    lib = load_ref_host()
+    M, C_ = z.shape
+    out = np.zeros((g.nr, g.nel, g.naz))
+    fp, dp = C.POINTER(C.c_float), C.POINTER(C.c_double)
+    zz = np.ascontiguousarray(z, np.complex64).view(np.float32)
+    ep = np.ascontiguousarray(elem_pos, np.float32)
+    w = np.ascontiguousarray(weights, np.float64)
+    tp = np.ascontiguousarray(tx_pos, np.float32)
+    ta = np.ascontiguousarray(tx_amp, np.float64)
+    lib.ref_host_radar_backproject(C.byref(g), float(wavelength), zz.ctypes.data_as(fp), M, C_, ep.ctypes.data_as(fp),
+                                   w.ctypes.data_as(dp), tp.ctypes.data_as(fp), ta.ctypes.data_as(dp), len(ta),
+                                   out.ctypes.data_as(dp))
+    return out
+
+
 def load():
     global _lib
     if _lib is not None:

@@ -97,6 +97,96 @@ def transform(text: str) -> str:
     return _array_ctor("\n".join(lines)) + "\n"
 
 
+def _lines_between(text: str, start: str, end: str, what: str) -> str:
+    """The lines from the first one containing `start` up to (not including) the next one containing
+    `end`. Raises if either anchor is missing, so a changed reference file fails loudly."""
+    lines = text.splitlines()
+    i = next((k for k, l in enumerate(lines) if start in l), None)
+    if i is None:
+        raise RuntimeError(f"build_ref: anchor of {what} not found: {start!r}")
+    j = next((k for k in range(i + 1, len(lines)) if end in lines[k]), None)
+    if j is None:
+        raise RuntimeError(f"build_ref: end anchor of {what} not found: {end!r}")
+    return "\n".join(lines[i:j]) + "\n"
+
+
+def _braced(text: str, start: str, what: str) -> str:
+    """The lines from the first one containing `start` through the line that closes the brace the
+    start line opens (with whatever follows it on that line, e.g. `};`)."""
+    lines = text.splitlines()
+    i = next((k for k, l in enumerate(lines) if start in l), None)
+    if i is None:
+        raise RuntimeError(f"build_ref: anchor of {what} not found: {start!r}")
+    depth, opened = 0, False
+    for k in range(i, len(lines)):
+        code = lines[k].split("//")[0]
+        for ch in code:
+            if ch == "{":
+                depth, opened = depth + 1, True
+            elif ch == "}":
+                depth -= 1
+        if opened and depth == 0:
+            return "\n".join(lines[i:k + 1]) + "\n"
+    raise RuntimeError(f"build_ref: unbalanced braces in {what}")
+
+
+def host_sources(root: Path) -> dict[str, str]:
+    """The pure-CPU spans of the reference's host code that oracle/ref_host.cpp compiles: the set-up
+    types and member functions of SimulationGrid.hpp/.cpp, the host arithmetic of uploadMaterials
+    and setSources up to their first graphics call, and the radar's direction, transmit delay and
+    back-projection loop. Each span is cut at fixed anchors; the text is not otherwise changed
+    (except `RadarMonitor::` -> `RadarCore::`, the wrapper struct that holds the members it reads)."""
+    hpp = (root / "src" / "SimulationGrid.hpp").read_text()
+    cpp = (root / "src" / "SimulationGrid.cpp").read_text()
+    radar = (root / "src" / "Radar.cpp").read_text()
+    return {
+        "ref_types.inc": _lines_between(hpp, "struct GridConfig {", "class SimulationGrid {", "set-up types"),
+        "ref_gpusource.inc": _braced(cpp, "struct GPUSource {", "GPUSource"),
+        "ref_defs.inc": _lines_between(cpp, "MaterialVolume::MaterialVolume(const glm::ivec3& size)",
+                                       "SimulationGrid::SimulationGrid(", "MaterialVolume / SourceDesc members"),
+        "ref_upload_edges.inc": _lines_between(cpp, "const glm::ivec3 s = m_config.size;",
+                                               "glTextureSubImage3D(m_edgeMaterial", "edge materials"),
+        "ref_upload_wires.inc": _lines_between(cpp, "std::vector<glm::vec2> factor(n * 3",
+                                               "glTextureSubImage3D(m_wireCoef", "thin-wire factors"),
+        "ref_sources_pack.inc": _lines_between(cpp, "m_sources.clear();", "if (!packed.empty())", "source packing"),
+        "ref_sources_lists.inc": _lines_between(cpp, "std::vector<std::pair<std::uint32_t, std::uint32_t>> pairs;",
+                                                "// Immutable storage", "source lists"),
+        "ref_radar_members.inc": (_braced(radar, "glm::vec3 RadarMonitor::direction(", "direction") +
+                                  _braced(radar, "double RadarMonitor::txDelay(", "txDelay")
+                                  ).replace("RadarMonitor::", "RadarCore::"),
+        "ref_radar_rows.inc": _braced(radar, "auto rows = [&](int ieBegin, int ieEnd) {", "back-projection rows"),
+    }
+
+
+HOST_LIB = OUT / "libemlab_ref_host.so"
+
+
+def build_host(force: bool = False, verbose: bool = False) -> Path | None:
+    """oracle/_ref/libemlab_ref_host.so from oracle/ref_host.cpp and the extracted spans."""
+    root = reference_root()
+    if root is None or not (root / "src" / "SimulationGrid.cpp").exists():
+        return None
+    OUT.mkdir(parents=True, exist_ok=True)
+    changed = force or not HOST_LIB.exists()
+    for name, text in host_sources(root).items():
+        dst = OUT / name
+        if not dst.exists() or dst.read_text() != text:
+            dst.write_text(text)
+            changed = True
+    deps = [HERE / "ref_host.cpp", HERE / "glm_host.hpp", Path(__file__)]
+    if not changed and all(HOST_LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return HOST_LIB
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+           "-I", str(OUT), "-I", str(HERE), str(HERE / "ref_host.cpp"), "-o", str(HOST_LIB)]
+    if verbose:
+        print(" ".join(cmd))
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        sys.stderr.write(res.stdout + res.stderr)
+        raise RuntimeError("building the reference host code failed")
+    return HOST_LIB
+
+
 def build(force: bool = False, verbose: bool = False) -> Path | None:
     src = reference_shaders()
     if src is None:
@@ -135,4 +225,7 @@ if __name__ == "__main__":
     if "--reference" in sys.argv:
         _explicit_root = Path(sys.argv[sys.argv.index("--reference") + 1])
     lib = build(force="--force" in sys.argv, verbose=True)
+    host = build_host(force="--force" in sys.argv, verbose=True) if lib else None
     print(lib if lib else "reference tree not found: nothing built")
+    if host:
+        print(host)

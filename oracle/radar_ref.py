@@ -66,3 +66,30 @@ def backproject(geo, z, elem_pos, weights, tx_pos, tx_amp):
                     s_ += weights[i] * complex(v) * complex(math.cos(w * t), math.sin(w * t))
                 out[ir, ie, ia] = s_.real * s_.real + s_.imag * s_.imag
     return out
+
+
+def random_case(seed, nr=40):
+    """A seeded back-projection problem: (geometry, wavelength, z (M, C) complex64, element
+    positions, weights, transmit positions, transmit amplitudes). Ranges reach 10 + 2 (nr - 1)
+    cells from the transmit centre, so with the default nr the far bins leave the volume."""
+    from em_lab_gb300 import abi
+    rng = np.random.default_rng(seed)
+    C, M = 9, 60
+    g = abi.RadarGeometry()
+    tx = np.array([20.3, 40.1, 39.7], f32)
+    for k in range(3):
+        g.tx[k] = float(tx[k])
+        g.interior_min[k] = 5.0
+        g.interior_max[k] = 90.0
+    for k, v in enumerate([0, -1, 0, 0, 0, 1, 1, 0, 0]):  # right, up, boresight (+x)
+        g.axes[k] = float(v)
+    wl = 16.0
+    g.omega, g.dt, g.sample_dt = 2 * math.pi / wl, 0.5, 2.0
+    g.r0, g.dr, g.az0, g.daz, g.el0, g.del_ = 10.0, 2.0, -12.0, 3.0, -9.0, 3.0
+    g.nr, g.naz, g.nel = nr, 9, 7
+    z = (rng.standard_normal((M, C)) + 1j * rng.standard_normal((M, C))).astype(np.complex64)
+    ep = (tx + rng.uniform(-6, 6, (C, 3))).astype(f32)
+    w = rng.uniform(0.3, 1.0, C)
+    tp = (tx + rng.uniform(-2, 2, (3, 3))).astype(f32)
+    ta = rng.uniform(0.5, 1.5, 3)
+    return g, wl, z, ep, w, tp, ta

@@ -7,7 +7,8 @@ against it where the reference tree is absent.
 Each fixture is a seeded scene from em_lab_gb300.configs.random_scene stepped N times by the
 reference shaders (emlab_expf as exp): the six field components, the port series and phasors, the
 far-field phasors, the coax-line phasors, probe blocks, flux sums and the far-field pattern of 64
-directions. raymarch.npz holds frames of the reference's volume pass (shaders/raymarch.frag through
+directions. radar_backproject.npz holds the reference's radar back-projection (its C++, compiled
+by oracle/build_ref.py) of a seeded problem. raymarch.npz holds frames of the reference's volume pass (shaders/raymarch.frag through
 the same shim) over the textures of a seeded scene: the render parameters as raw bytes and the
 RGB of each frame.
 """
@@ -120,7 +121,21 @@ def make_render_golden():
     print("raymarch written")
 
 
+def make_radar_golden():
+    """The reference's back-projection (RadarMonitor::computeImage, compiled from the reference by
+    oracle/build_ref.py) on a seeded problem, for the GPU kernel's test on machines without the tree."""
+    from oracle import radar_ref
+    g, wl, z, ep, w, tp, ta = radar_ref.random_case(5)
+    power = oracle.ref_host_backproject(g, wl, z, ep, w, tp, ta)
+    np.savez_compressed(os.path.join(OUT, "radar_backproject.npz"), geometry=np.frombuffer(bytes(g), np.uint8),
+                        wavelength=np.array(wl), z=z, elem_pos=ep, weights=w, tx_pos=tp, tx_amp=ta, power=power)
+    print("radar_backproject written")
+
+
 def main():
+    if "--radar-only" in sys.argv:
+        make_radar_golden()
+        return
     if not oracle.ref_available():
         sys.exit("oracle/_ref is not built: run python oracle/build_ref.py (needs the reference tree)")
     if "--render-only" in sys.argv:
@@ -139,6 +154,8 @@ def main():
         np.savez_compressed(os.path.join(OUT, f"{name}.npz"), **out)
         print(name, "written")
     make_render_golden()
+    if oracle.ref_host_available():
+        make_radar_golden()
 
 
 if __name__ == "__main__":
