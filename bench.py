@@ -235,6 +235,47 @@ def cpu_sample(sc, seconds_budget: float = 20.0, max_steps: int = 8, dft: bool =
                       f"(oracle/emlab_oracle.c FP32, OpenMP {threads} threads, set-up {setup:.1f} s excluded)"}
 
 
+COMPONENTS = ("Ex", "Ey", "Ez", "Bx", "By", "Bz")
+
+
+def parity_sample(steps: int = 200, size: int = 128):
+    """Part of the CPU-baseline leg: the workload's scene cropped to size^3 (16-cell absorber,
+    thin-wire dipole with its 50-ohm pulsed feed, random dielectric blocks, port series) stepped
+    `steps` times on the GPU and by the CPU restatement in FP32 and FP64. Reports whether the GPU
+    fields and port series equal the FP32 restatement bit for bit (the restatement is itself equal
+    to the reference's shaders compiled as C++), and the relative L2 of every field component and
+    of the port series against the FP64 restatement (the FP32 error floor of the update)."""
+    import oracle
+    from em_lab_gb300 import SimulationGrid, configs
+    oracle.set_threads(os.cpu_count() or 1)
+    sc = configs.plain_large(size=size)
+    port = [sc.ports[0].to_c()]
+    out = {}
+    t0 = time.perf_counter()
+    for label, t in (("gpu", SimulationGrid(sc.grid)), ("f32", oracle.Oracle(sc.grid, "f32")),
+                     ("f64", oracle.Oracle(sc.grid, "f64"))):
+        oracle.load_scene(t, sc)
+        t.ports_configure(port, sc.wavelength, 4.0, False, steps)
+        t.step(steps)
+        out[label] = ([np.asarray(c, np.float64) for c in t.read_components()], np.asarray(t.ports_series(), np.float64))
+        t.close()
+    gpu_f, gpu_s = out["gpu"]
+    f32_f, f32_s = out["f32"]
+    f64_f, f64_s = out["f64"]
+
+    def rel(a, b):
+        n = np.linalg.norm(b)
+        return float(np.linalg.norm(a - b) / n) if n > 0 else 0.0
+    return {"workload": f"{size}^3 crop of the workload's scene (absorber, thin-wire dipole, 50-ohm pulsed feed, "
+                        f"random blocks, port series), {steps} steps",
+            "bit_exact_vs_fp32_oracle": bool(all(np.array_equal(a, b) for a, b in zip(gpu_f, f32_f)) and
+                                             np.array_equal(gpu_s, f32_s)),
+            "max_abs_vs_fp32_oracle": float(max(np.abs(a - b).max() for a, b in zip(gpu_f, f32_f))),
+            "rel_l2_vs_fp64_oracle": {n: rel(a, b) for n, a, b in zip(COMPONENTS, gpu_f, f64_f)},
+            "port_series_rel_l2_vs_fp64_oracle": rel(gpu_s, f64_s),
+            "seconds": round(time.perf_counter() - t0, 1)}
+
+
 def run_reference(args):
     """The reference's CPU implementation of the path on the host cores: its shaders compiled as C++
     (oracle/_ref) where that library was built, else the FP32 restatement, on every host thread."""
@@ -498,6 +539,7 @@ def main():
     ap.add_argument("--kernel", default="fused", choices=["fused", "fused_ldg", "split"])
     ap.add_argument("--tile-rows", type=int, default=0, choices=[0, 8, 16, 32, 64, 128])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the FP32/FP64 parity sample of the CPU leg")
     ap.add_argument("--e2e-steps", type=int, default=0, help="steps of the end-to-end leg (default: --steps)")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -609,6 +651,11 @@ def main():
         except Exception as e:  # pragma: no cover - reported, not fatal
             cpu = {"value": None, "unit": "Mcells/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"}
+        if args.workload == "plain_large" and not args.no_parity:
+            try:
+                cpu["parity"] = parity_sample()
+            except Exception as e:  # pragma: no cover - reported, not fatal
+                cpu["parity"] = {"failed": str(e)}
 
     if rank == 0:
         kname = kernel_name(args.kernel, args.tile_rows)
@@ -633,6 +680,7 @@ def main():
                          "kernel": kname, "kernel_ms_per_launch": per_launch_ms,
                          "algorithmic_bytes_per_cell_step": BYTES_PER_CELL_STEP},
             "cpu_baseline": cpu,
+            "parity": (cpu or {}).get("parity"),
             "e2e": {"value": e2e_value, "unit": "Mcells/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "frames": frames, "steps_per_frame": frame},
             "gpu_launches": int(launches),

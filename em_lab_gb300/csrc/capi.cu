@@ -25,8 +25,11 @@ namespace {
 
 thread_local std::string g_last_error;
 std::atomic<uint64_t> g_launches{0};
+std::atomic<int> g_wait_polls{kWaitPolls};
 
 }  // namespace
+
+int emlab::wait_limit() { return g_wait_polls.load(); }
 
 int emlab::fail(int code, const std::string& msg) {
     g_last_error = msg;
@@ -72,6 +75,7 @@ YeeArgs yee_args(emlab_grid* g) {
     a.zchunk = zc;
     a.work = g->d_work.p;
     a.work_base = g->work_base;
+    a.wait_polls = wait_limit();
     return a;
 }
 
@@ -269,18 +273,32 @@ int timing_pair(emlab_grid* g, cudaEvent_t* start, cudaEvent_t* stop) {
     return EMLAB_OK;
 }
 
-constexpr int kDftBlock = 64;  // samples per time block (the fold kernel's register block)
+constexpr int kDftCoreBlock = 64;  // samples per CUDA-core fold (that kernel's register block)
+
+// Samples per time block of the engine in use: the tensor-core fold takes up to four 64-sample
+// chunks per launch (dft_tc_block), the CUDA-core fold 64.
+int dft_block(const emlab_grid* g) {
+    return g->dft_engine == EMLAB_DFT_TENSOR ? dft_tc_block(g->dft_nf) : kDftCoreBlock;
+}
 
 // Folds the samples gathered so far into the FP64 sums.
 int dft_fold(emlab_grid* g) {
     if (!g->dft_on || g->dft_t == 0) return EMLAB_OK;
     const double dt = (double)g->cfg.courant;
-    if (g->dft_engine != EMLAB_DFT_TENSOR ||
-        !launch_dft_fold_tc(g->d_dft_blk.p, g->dft_t, g->dft_points, g->dft_nf, g->d_dft_bhi.p, g->d_dft_blo.p,
-                            g->d_dft_omega.p, g->dft_n0, dt, g->d_dft_x.p, g->d_err.p, g->stream))
-        launch_dft_fold(g->d_dft_blk.p, g->dft_t, g->dft_points, g->dft_nf, g->d_dft_w.p, g->d_dft_omega.p,
-                        g->dft_n0, dt, g->d_dft_x.p, g->stream);
-    ++g_launches;
+    if (g->dft_engine == EMLAB_DFT_TENSOR &&
+        launch_dft_fold_tc(g->d_dft_blk.p, g->dft_t, g->dft_points, g->dft_nf, g->d_dft_bhi.p, g->d_dft_blo.p,
+                           g->d_dft_omega.p, g->dft_n0, dt, g->d_dft_x.p, g->d_err.p, g->stream)) {
+        ++g_launches;
+    } else {
+        // CUDA-core folds of 64 samples each, every one with the phase of its own first sample
+        const size_t rows = (size_t)6 * g->dft_points;
+        for (int off = 0; off < g->dft_t; off += kDftCoreBlock) {
+            launch_dft_fold(g->d_dft_blk.p + (size_t)off * rows, std::min(kDftCoreBlock, g->dft_t - off),
+                            g->dft_points, g->dft_nf, g->d_dft_w.p, g->d_dft_omega.p, g->dft_n0 + off, dt,
+                            g->d_dft_x.p, g->stream);
+            ++g_launches;
+        }
+    }
     g->dft_samples += (uint64_t)g->dft_t;
     g->dft_t = 0;
     return EMLAB_OK;
@@ -637,7 +655,7 @@ int emlab_grid_step(emlab_grid* g, int count) {
                 if (g->dft_t == 0) g->dft_n0 = (long long)g->step;  // time index of the block's first sample
                 launch_dft_sample(monitor_args(g), g->d_dft_box.p, g->dft_points, g->d_dft_blk.p, g->dft_t, g->stream);
                 g_launches += 1;
-                if (++g->dft_t == kDftBlock) dft_fold(g);
+                if (++g->dft_t == dft_block(g)) dft_fold(g);
             }
             if (int rc = check_launch()) return rc;
         }
@@ -1027,13 +1045,13 @@ int emlab_ntff_dft_configure(emlab_grid* g, const int box_min[3], const int box_
     g->dft_points = b[12];
     g->dft_nf = n_freq;
     g->dft_omega.assign((size_t)n_freq, 0.0);
-    std::vector<float2> w((size_t)n_freq * kDftBlock);
+    std::vector<float2> w((size_t)n_freq * kDftCoreBlock);
     const double dt = (double)g->cfg.courant;
     for (int f = 0; f < n_freq; ++f) {
         g->dft_omega[(size_t)f] = 6.28318530717958647692 / (double)std::max(wavelengths[f], 2.0f);
-        for (int k = 0; k < kDftBlock; ++k) {
+        for (int k = 0; k < kDftCoreBlock; ++k) {
             const double ph = g->dft_omega[(size_t)f] * dt * k;
-            w[(size_t)f * kDftBlock + k] = make_float2((float)std::cos(ph), (float)-std::sin(ph));
+            w[(size_t)f * kDftCoreBlock + k] = make_float2((float)std::cos(ph), (float)-std::sin(ph));
         }
     }
     EMLAB_CUDA(g->d_dft_box.alloc(13));
@@ -1048,7 +1066,9 @@ int emlab_ntff_dft_configure(emlab_grid* g, const int box_min[3], const int box_
     EMLAB_CUDA(g->d_dft_blo.alloc(blo.size()));
     EMLAB_CUDA(cudaMemcpy(g->d_dft_bhi.p, bhi.data(), bhi.size() * 4, cudaMemcpyHostToDevice));
     EMLAB_CUDA(cudaMemcpy(g->d_dft_blo.p, blo.data(), blo.size() * 4, cudaMemcpyHostToDevice));
-    EMLAB_CUDA(g->d_dft_blk.alloc((size_t)kDftBlock * 6 * g->dft_points));
+    // room for the longer of the two engines' blocks (the engine may change between folds)
+    const int block = std::max(kDftCoreBlock, dft_tc_block(n_freq));
+    EMLAB_CUDA(g->d_dft_blk.alloc((size_t)block * 6 * g->dft_points));
     EMLAB_CUDA(g->d_dft_x.alloc((size_t)n_freq * g->dft_points * 12));
     EMLAB_CUDA(cudaMemset(g->d_dft_x.p, 0, g->d_dft_x.n * 8));
     g->dft_t = 0, g->dft_samples = 0;
@@ -1086,6 +1106,10 @@ int emlab_ntff_dft_read(emlab_grid* g, double* out) {
 int emlab_ntff_dft_engine(emlab_grid* g, int engine) {
     if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
     EMLAB_REQUIRE(engine == EMLAB_DFT_TENSOR || engine == EMLAB_DFT_CUDA_CORES, "unknown DFT engine");
+    if (engine != g->dft_engine && g->dft_on) {
+        if (int rc = require_grid(g)) return rc;
+        if (int rc = dft_fold(g)) return rc;  // the partial block is folded with the engine that gathered it
+    }
     g->dft_engine = engine;
     return EMLAB_OK;
 }
@@ -1457,6 +1481,12 @@ int emlab_source_lists(const emlab_source* sources, size_t n, int nx, int ny, in
 }
 
 // ---- self-checks ---------------------------------------------------------------------------
+int emlab_debug_set_wait_limit(int polls) {
+    EMLAB_REQUIRE(polls >= 0, "negative poll count");
+    g_wait_polls = polls > 0 ? std::min(polls, kWaitPolls) : 0;
+    return EMLAB_OK;
+}
+
 int emlab_debug_expf(const float* in, float* out, size_t n) {
     if (!in || !out) return fail(EMLAB_ERR_INVALID, "null argument");
     if (!n) return EMLAB_OK;

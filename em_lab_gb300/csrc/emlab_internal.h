@@ -53,7 +53,14 @@ struct YeeArgs {
     int tile_rows;   // tiling mode of the fused kernels (8, 16: single-cell tiles; 64, 128: pair tiles)
     unsigned long long* work;      // work-item ticket counter of the persistent kernel (monotonic)
     unsigned long long work_base;  // tickets consumed by all earlier launches on this counter
+    int wait_polls;                // polls of a plane's copy barrier before the CTA gives up (wait_limit())
 };
+
+// Polls of an on-device wait (mbarrier) before a kernel reports EMLAB_ERR_TIMEOUT: about a second by
+// default. emlab_debug_set_wait_limit lowers it so a test can make the first wait of a launch run
+// out; the waits that drain copies already in flight before a CTA leaves always keep the default.
+constexpr int kWaitPolls = 1 << 20;
+int wait_limit();
 
 struct SourceArgs {
     const int4* cells;       // xyz = cell (scene coordinates), w = first list entry; entry n is the sentinel
@@ -118,6 +125,7 @@ void launch_raymarch(const MonitorArgs& m, const float* sigma, const float* eps,
 // tensor-core fold (dft_tc.cu): MMA N for nf frequencies, host twiddle tables (hi, lo) in the
 // kernel's shared-memory layout, and the launcher (false if nf is too large or set-up failed)
 int dft_tc_mma_n(int nf);
+int dft_tc_block(int nf);  // samples per tensor-core fold: 64 x min(4, 256 / MMA N)
 void dft_tc_twiddles(int nf, const double* omega, double dt, std::vector<float>& hi, std::vector<float>& lo);
 bool launch_dft_fold_tc(const float* blk, int T, int points, int nf, const float* b_hi, const float* b_lo,
                         const double* omega, long long n0, double dt, double* X, unsigned* err, cudaStream_t s);

@@ -53,9 +53,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Bounded wait: about a second of polling at most (try_wait itself suspends for a while).
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (int i = 0; i < (1 << 20); ++i)
+// Bounded wait: `polls` tries, about a second of polling at the default kWaitPolls (try_wait itself
+// suspends for a while); 0 tries gives up at once (the test hook of emlab_debug_set_wait_limit).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int polls = kWaitPolls) {
+    for (int i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -151,8 +152,8 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY <= 8 ? 3 : 1)
         for (int p = zstart; p <= zlast && p < zstart + S_; ++p) issue(p), issued_hi = p;
         // planes zstart and zstart+1 before the first B phase; later planes one iteration ahead,
         // just before the per-plane barrier, which passes the TMA writes on to the other warps
-        failed = !mbar_wait(bars + 0, 0);
-        if (!failed) waited_ok = zstart, failed = !mbar_wait(bars + 1, 0);
+        failed = !mbar_wait(bars + 0, 0, a.wait_polls);
+        if (!failed) waited_ok = zstart, failed = !mbar_wait(bars + 1, 0, a.wait_polls);
         if (!failed) waited_ok = zstart + 1;
     }
     if (__syncthreads_or(failed)) {
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY <= 8 ? 3 : 1)
         }
         // the next iteration's B phase reads plane z+2: the leader waits for it before the barrier
         if (leader && z + 1 < ze) {
-            failed = !mbar_wait(bars + (rel + 2) % S_, ((rel + 2) / S_) & 1);
+            failed = !mbar_wait(bars + (rel + 2) % S_, ((rel + 2) / S_) & 1, a.wait_polls);
             if (!failed) waited_ok = z + 2;
         }
         if (__syncthreads_or(failed)) {
@@ -552,7 +553,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1)
         bool ok = true;
         while (ok && waited < last) {
             ++waited;
-            ok = mbar_wait(bars + waited % S_, (waited / S_) & 1);
+            ok = mbar_wait(bars + waited % S_, (waited / S_) & 1, a.wait_polls);
         }
         prod[6] = waited;
         return ok;

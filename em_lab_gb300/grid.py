@@ -97,6 +97,7 @@ def load_library() -> C.CDLL:
         "emlab_lines_configure": ([P, ip, I, ip, fp, I, F, F], I),
         "emlab_lines_read": ([P, fp, fp], I),
         "emlab_debug_expf": ([fp, fp, SZ], I),
+        "emlab_debug_set_wait_limit": ([I], I),
         "emlab_edge_materials": ([fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ, C.POINTER(abi.WireTerm), SZ,
                                   fp, fp, fp, fp, C.POINTER(C.c_uint32)], I),
         "emlab_source_signal": ([C.POINTER(abi.Source), D], D),
@@ -129,6 +130,15 @@ def _f32(a, n=None):
 
 def launch_count() -> int:
     return int(load_library().emlab_launch_count())
+
+
+WAIT_POLLS_DEFAULT = 1 << 20
+
+
+def debug_set_wait_limit(polls: int) -> None:
+    """Test hook: polls of an on-device barrier wait before a kernel gives up and the grid reports
+    EMLAB_ERR_TIMEOUT (0: the first wait of every launch gives up; WAIT_POLLS_DEFAULT restores)."""
+    _check(load_library().emlab_debug_set_wait_limit(int(polls)))
 
 
 def device_expf(x) -> np.ndarray:

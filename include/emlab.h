@@ -382,6 +382,13 @@ int emlab_source_lists(const emlab_source* sources, size_t n, int nx, int ny, in
                        int32_t* lists, int* n_sources, int* n_cells, int* n_lists);
 
 /* ---- self-checks ------------------------------------------------------------------------- */
+/* Test hook of the bounded on-device waits (no counterpart in the reference; its bounded waits are
+ * host-side, src/FarField.cpp:287, src/Ports.cpp:152): the number of polls a solver or far-field-fold
+ * kernel makes on a copy or MMA barrier before it records EMLAB_ERR_TIMEOUT and leaves, for launches
+ * queued from now on in this process. 0 makes every such launch give up at its first wait (after
+ * waiting, with the full bound, for the copies it already issued); values above the default (about a
+ * second of polling) are clamped to it. Restore with emlab_debug_set_wait_limit(1 << 20). */
+int emlab_debug_set_wait_limit(int polls);
 /* Evaluates the device emlab_expf on n inputs (bit-exactness check against the host). */
 int emlab_debug_expf(const float* in, float* out, size_t n);
 

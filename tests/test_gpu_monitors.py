@@ -65,7 +65,7 @@ def test_sweep_sums_fp64():
     assert r_gpu == r_cpu
 
 
-def test_check_finite_and_bounded_wait():
+def test_check_finite():
     grid = abi.GridConfig((96, 96, 96), pml_thickness=8)
     g = SimulationGrid(grid)
     assert g.check_finite()
@@ -74,19 +74,92 @@ def test_check_finite_and_bounded_wait():
     g.write_components(comps)
     g.step(2)
     assert not g.check_finite()
-    # a bounded host wait that runs out returns EMLAB_ERR_TIMEOUT and leaves the grid usable
-    g.reset_fields()
-    g.step(400)
-    from em_lab_gb300 import EmlabError
 
-    timed_out = False
-    try:
-        g.synchronize(1)
-    except EmlabError as e:
-        timed_out = e.code == abi.EMLAB_ERR_TIMEOUT
+
+def test_bounded_host_wait_runs_out():
+    """A bounded host wait on the grid's stream (emlab_grid_synchronize) that runs out returns
+    EMLAB_ERR_TIMEOUT and leaves the grid usable. The stream is kept busy deterministically: a
+    bounded device sleep of about 0.2 s queued on the grid's own stream after the steps."""
+    import torch
+    from em_lab_gb300 import EmlabError
+    g = SimulationGrid(abi.GridConfig((64, 64, 64), pml_thickness=8))
+    g.step(10)
     g.synchronize(60000)
-    assert g.step_count() == 400
-    assert timed_out or g.step_count() == 400  # the wait may also finish within 1 ms on a fast device
+    with torch.cuda.stream(torch.cuda.ExternalStream(g.stream_handle())):
+        torch.cuda._sleep(int(4e8))  # ~0.2 s of cycles at 2 GHz: a bounded spin, not a hang
+    with pytest.raises(EmlabError) as e:
+        g.synchronize(1)
+    assert e.value.code == abi.EMLAB_ERR_TIMEOUT
+    g.synchronize(60000)  # the same wait with room to finish succeeds
+    g.step(4)
+    g.synchronize(60000)
+    assert g.step_count() == 14
+    g.close()
+
+
+@pytest.mark.parametrize("rows", [64, 8])
+def test_device_wait_that_runs_out_reports_timeout(rows):
+    """The solver kernel's bounded barrier wait made to run out (the test hook sets its poll count
+    to 0): the CTAs record the error, wait with the full bound for the copies they already issued
+    and leave; the host reports EMLAB_ERR_TIMEOUT; with the normal bound restored the same grid then
+    steps bit for bit like the oracle (persistent pair tiles, tiling 64, and single-cell tiles, 8)."""
+    from em_lab_gb300 import EmlabError, grid as gridmod
+    sc = configs.random_scene(size=(70, 40, 36), pml=5, seed=31)
+    g = SimulationGrid(sc.grid)
+    g.set_tiling(rows)
+    oracle.load_scene(g, sc)
+    g.step(3)
+    g.synchronize(60000)
+    try:
+        gridmod.debug_set_wait_limit(0)
+        g.step(1)
+        with pytest.raises(EmlabError) as e:
+            g.synchronize(60000)
+        assert e.value.code == abi.EMLAB_ERR_TIMEOUT
+    finally:
+        gridmod.debug_set_wait_limit(gridmod.WAIT_POLLS_DEFAULT)
+    g.synchronize(60000)  # the error word was cleared by the report
+    o = oracle.Oracle(sc.grid, "f32")
+    oracle.load_scene(o, sc)
+    oracle.load_scene(g, sc)  # fresh state on the same grid (fields, time) after the failed step
+    for t in (g, o):
+        t.step(25)
+    for c, (a, b) in enumerate(zip(g.read_components(), o.read_components())):
+        assert np.array_equal(a, b), c
+    g.close()
+    o.close()
+
+
+def test_fold_wait_that_runs_out_reports_timeout():
+    """The tensor-core DFT fold's bounded MMA wait made to run out: the fold records the error,
+    waits with the full bound for its MMAs, frees its tensor memory and leaves; the host reports
+    EMLAB_ERR_TIMEOUT and later folds on the same device are correct again."""
+    from em_lab_gb300 import EmlabError, grid as gridmod
+    sc = configs.random_scene(size=(40, 36, 34), pml=5, seed=37)
+    g = SimulationGrid(sc.grid)
+    oracle.load_scene(g, sc)
+    g.ntff_dft_configure((7, 7, 7), (32, 28, 26), [9.0, 15.0])
+    g.step(70)
+    try:
+        gridmod.debug_set_wait_limit(0)
+        with pytest.raises(EmlabError) as e:
+            g.ntff_dft_read()  # folds the partial block
+            g.synchronize(60000)
+        assert e.value.code == abi.EMLAB_ERR_TIMEOUT
+    finally:
+        gridmod.debug_set_wait_limit(gridmod.WAIT_POLLS_DEFAULT)
+    g.synchronize(60000)
+    o = oracle.Oracle(sc.grid, "f32")
+    res = []
+    for t in (g, o):
+        oracle.load_scene(t, sc)  # fresh fields and time on the same grid
+        t.ntff_dft_configure((7, 7, 7), (32, 28, 26), [9.0, 15.0])
+        t.step(300)
+        res.append(t.ntff_dft_read())
+    g.close()
+    o.close()
+    scale = np.abs(res[1]).max()
+    assert scale > 0 and np.max(np.abs(res[0] - res[1])) <= DFT_RTOL * scale
 
 
 def test_plain_small_2000_steps():
@@ -190,7 +263,9 @@ def test_dft_pattern_all_frequencies_matches_parity_kernel():
 @pytest.mark.parametrize("nf", [1, 16, 48, 128])
 def test_dft_tensor_engine_equals_cuda_cores(nf):
     """Tensor-core and CUDA-core folds of the same samples over several blocks and a partial one,
-    for MMA widths N = 32, 96 and 256: the two engines agree to the FP32 level of the in-block sums."""
+    for MMA widths N = 32, 96 and 256 (tensor-core blocks of 256, 256, 128 and 64 samples folded as
+    64-sample chunks; CUDA-core blocks of 64): the two engines agree to the FP32 level of the
+    in-block sums."""
     sc = configs.random_scene(size=(44, 40, 38), pml=5, seed=17)
     wls = list(np.linspace(6.0, 60.0, nf)) if nf > 1 else [16.0]
     out = []
@@ -199,12 +274,32 @@ def test_dft_tensor_engine_equals_cuda_cores(nf):
         oracle.load_scene(g, sc)
         g.ntff_dft_engine(engine)
         g.ntff_dft_configure((7, 7, 7), (36, 32, 30), wls)
-        g.step(64 * 3 + 17)
+        g.step(256 * 2 + 81)
         out.append(g.ntff_dft_read())
     a, b = out
     scale = np.abs(b).max()
     assert scale > 0 and np.all(np.isfinite(a))
     assert np.max(np.abs(a - b)) <= DFT_RTOL * scale
+
+
+def test_dft_engine_switch_inside_a_block():
+    """Switching the fold engine in the middle of a block folds the partial block with the engine
+    that gathered it; the sums match a run on one engine throughout."""
+    sc = configs.random_scene(size=(40, 36, 34), pml=5, seed=19)
+    wls = [8.0, 13.0, 21.0]
+    out = []
+    for switch in (True, False):
+        g = SimulationGrid(sc.grid)
+        oracle.load_scene(g, sc)
+        g.ntff_dft_configure((7, 7, 7), (32, 28, 26), wls)
+        g.step(150)  # inside the tensor engine's first 256-sample block
+        if switch:
+            g.ntff_dft_engine(abi.DFT_CUDA_CORES)
+        g.step(200)
+        out.append(g.ntff_dft_read())
+        g.close()
+    scale = np.abs(out[1]).max()
+    assert scale > 0 and np.max(np.abs(out[0] - out[1])) <= DFT_RTOL * scale
 
 
 def test_analyzer_submit_collect_matches_synchronous_reads():

@@ -1,0 +1,142 @@
+"""The reference's bundled scenes, run headless on the GPU from their saved builds
+(tests/golden/scenes/, written by make_scenes.py from the scripts), with the results the reference
+quotes for them checked at the digits it quotes.
+
+Quoted results (the reference states neither the frame count nor the frame at which each reading
+was taken; the runs below go past the settling of every reading, and where a reading still
+oscillates with the frame at which it is sampled the tolerance covers that oscillation, as noted):
+  - scenes/validation/hertzian_dipole.lua:5-6 — measured D = 1.87 dBi, HPBW 87.5 deg at 16 cells/lambda;
+    docs/UNITS.md:135-141 — far field P_rad = 0.34876, flux box <P> = 0.355;
+  - docs/UNITS.md:149 (scene 04_dipole.lua) — port Z = 64.3 -21.1j ohm, P_acc 8.937e-01 of
+    9.418e-01 available;
+  - scenes/validation/dipole_impedance.lua:4-9 — measured Z at lengths 7, 15, 19 (default), 21:
+    5.9 -j812, 32.6 -j222, 62.9 -j37, 87.1 +j54 ohm;
+  - scenes/validation/coax_line.lua:8-9 — Z0 50.0 ohm; load Gamma 0.057; open |Gamma| 0.999;
+    short 1.000 @ 180 deg; 100 ohm Gamma 0.338, Z 94 -j22 ohm;
+  - src/Main.cpp:1145-1157 — exit code 0 for a finished run, 2 when the fields turn non-finite.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from em_lab_gb300 import headless, scene_io
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "scenes")
+TABLE = json.load(open(os.path.join(HERE, "digests.json")))
+
+
+def load(name, tmp_path):
+    res = scene_io.load(os.path.join(HERE, name + ".npz"))
+    res.output_dir = str(tmp_path)  # CSV logs the scripts ask for go to the test's directory
+    return res
+
+
+@pytest.mark.parametrize("name", sorted(TABLE))
+def test_every_bundled_scene_runs_headless(name, tmp_path, capsys):
+    """Every bundled scene (and the quoted validation settings) runs 120 frames in the headless
+    --frames mode with finite fields and exit code 0, and prints the reference's report."""
+    res = load(name, tmp_path)
+    code, inst = headless.run_result(res, 120, script_name=name)
+    out = capsys.readouterr().out
+    assert code == 0, out[-3000:]
+    assert f"=== {res.scene.name} ===" in out and "GPU timings: sim" in out
+
+
+def run_watch(name, frames, tmp_path, every=50):
+    """Runs a saved scene and returns the readings sampled every `every` frames."""
+    res = load(name, tmp_path)
+    rec = []
+
+    def cb(frame, inst):
+        if frame % every:
+            return
+        r = {"frame": frame}
+        if inst.fluxes:
+            r["flux_avg"] = inst.fluxes[0]["avg"]
+        if inst.pattern and inst.pattern.get("valid"):
+            p = inst.pattern
+            r["P_rad"], r["dbi"] = p["P"], p["max_dbi"]
+            r["hpbw"] = {c["name"]: c["beamwidth"] for c in p["cuts"]}
+        if inst.ports:
+            inst.evaluate_ports()
+            rd = inst.readings[0]
+            if rd and rd["valid"]:
+                r["z"], r["acc"], r["avail"] = rd["z"], rd["accepted"], rd["available"]
+        if inst.coaxes and inst.coax_readings[0] and inst.coax_readings[0]["valid"]:
+            c = inst.coax_readings[0]
+            r["gamma"], r["z0m"], r["zend"] = c["gamma"], c["z0m"], c["zend"]
+        rec.append(r)
+    code, _ = headless.run_result(res, frames, after_frame=cb, script_name=name)
+    assert code == 0
+    return rec
+
+
+def settled(rec, key, last=8):
+    """The last `last` samples of a reading (after settling)."""
+    vals = [r[key] for r in rec if key in r][-last:]
+    assert len(vals) == last, key
+    return vals
+
+
+def test_hertzian_dipole_directivity_power_and_flux(tmp_path):
+    rec = run_watch("hertzian_dipole", 1600, tmp_path)
+    for d in settled(rec, "dbi"):
+        assert round(d, 2) == pytest.approx(1.87, abs=0.005 + 1e-9)  # quoted 1.87 dBi
+    for h in settled(rec, "hpbw"):
+        assert h["xy"] >= 359.0                                      # omni in azimuth
+        assert abs(h["xz"] - 87.5) < 0.06 and abs(h["yz"] - 87.5) < 0.06  # quoted 87.5 deg
+    # P_rad alternates between two values with the 100-frame report phase (0.34866 and 0.34885 here);
+    # the quoted 0.34876 lies between them
+    p = settled(rec, "P_rad")
+    assert min(p) <= 0.34876 <= max(p) and max(p) - min(p) < 3e-4
+    # the flux box's running <P> alternates likewise (0.3549 / 0.3586); quoted 0.355
+    f = settled(rec, "flux_avg")
+    assert min(abs(v - 0.355) for v in f) < 5e-4 and max(abs(v - 0.355) for v in f) < 5e-3
+
+
+def test_dipole_04_port_impedance_and_power(tmp_path):
+    rec = run_watch("04_dipole", 3000, tmp_path)
+    for z, acc, avail in zip(settled(rec, "z"), settled(rec, "acc"), settled(rec, "avail")):
+        assert abs(z.real - 64.3) < 0.1 and abs(z.imag - (-21.1)) < 0.15  # quoted 64.3 -21.1j ohm
+        assert round(avail, 4) == 0.9418                                  # quoted 9.418e-01 available
+        assert abs(acc - 0.8937) < 8e-3                                   # quoted 8.937e-01 accepted
+    # the settled accepted power alternates with the report phase (0.8936 / 0.8877): one phase
+    # rounds to the quoted four digits within one unit
+    assert min(abs(a - 0.8937) for a in settled(rec, "acc")) <= 1e-4
+
+
+@pytest.mark.parametrize("name,want", [("dipole_impedance_len7", 5.9 - 812j), ("dipole_impedance_len15", 32.6 - 222j),
+                                       ("dipole_impedance", 62.9 - 37j), ("dipole_impedance_len21", 87.1 + 54j)])
+def test_dipole_impedance_table(name, want, tmp_path):
+    rec = run_watch(name, 600, tmp_path)
+    for z in settled(rec, "z", last=4):
+        assert abs(z.real - want.real) < 0.1      # resistance at the quoted 0.1 ohm
+        assert abs(z.imag - want.imag) < 0.75     # reactance at the quoted 1 ohm
+
+
+@pytest.mark.parametrize("name,check", [
+    ("coax_line", lambda g, z0, ze: abs(abs(g) - 0.057) < 0.004),
+    ("coax_line_open", lambda g, z0, ze: abs(abs(g) - 0.999) < 0.003),
+    ("coax_line_short", lambda g, z0, ze: abs(abs(g) - 1.000) < 0.004 and abs(abs(math.degrees(np.angle(g))) - 180) < 0.5),
+    ("coax_line_100ohm", lambda g, z0, ze: abs(abs(g) - 0.338) < 0.002 and abs(ze.real - 94) < 0.5
+     and abs(ze.imag + 22) < 0.5),
+])
+def test_coax_line_terminations(name, check, tmp_path):
+    rec = run_watch(name, 600, tmp_path)
+    for g, z0, ze in zip(settled(rec, "gamma", 4), settled(rec, "z0m", 4), settled(rec, "zend", 4)):
+        assert abs(z0 - 50.0) < 0.2               # quoted Z0 50.0 ohm
+        assert check(g, z0, ze), (g, z0, ze)
+
+
+def test_non_finite_fields_exit_with_code_2(tmp_path, capsys):
+    """A source strong enough to overflow FP32 makes the fields non-finite: the run ends with exit
+    code 2 as the reference's (Instruments.cpp:271-275, Main.cpp:1145-1157)."""
+    res = load("hertzian_dipole", tmp_path)
+    res.scene.sources[0].amplitude = 3.0e38
+    code, _ = headless.run_result(res, 40, script_name="overflow")
+    assert code == 2
+    assert "non-finite" in capsys.readouterr().err
