@@ -61,6 +61,11 @@ class Source(C.Structure):
                 ("repeat_periods", C.c_float), ("delay_periods", C.c_float), ("enabled", C.c_int)]
 
 
+class Cpml(C.Structure):
+    """emlab_cpml: the opt-in convolutional PML's grading."""
+    _fields_ = [("sigma_max", C.c_float), ("kappa_max", C.c_float), ("alpha_max", C.c_float), ("order", C.c_float)]
+
+
 class Port(C.Structure):
     _fields_ = [("x", C.c_int), ("y", C.c_int), ("z", C.c_int), ("axis", C.c_int), ("edges", C.c_int),
                 ("sign", C.c_int)]

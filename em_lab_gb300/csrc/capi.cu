@@ -142,14 +142,15 @@ void emlab::refresh_tma(emlab_grid* g) {
 int emlab::clear_fields(emlab_grid* g) {
     EMLAB_CUDA(cudaMemsetAsync(g->fields.p, 0, g->fields.n * sizeof(float), g->stream));
     g->cur = 0;
-    return EMLAB_OK;
+    return cpml_clear(g);
 }
 
 // Absorber tables of the configured size (common.glsl:23-43). In a stack, the z entries are each
 // scene's own tables at its planes; separator planes lie outside every layer.
 int emlab::upload_pml(emlab_grid* g) {
     invalidate_graphs(g);
-    const emlab_grid_config& c = g->cfg;
+    emlab_grid_config c = g->cfg;
+    if (g->cpml_on) c.pml_sigma_max = 0.0f;  // the convolutional PML replaces the graded conductivity
     const int S = std::max(c.nx, std::max(c.ny, c.nz));
     g->pml_stride = S;
     std::vector<float> pt = pml_tables(c, S);
@@ -326,7 +327,10 @@ uint64_t enqueue_step(emlab_grid* g, int k, bool graph, const float* d_sig, cons
     uint64_t launched = 0;
     YeeArgs a = yee_args(g);
     if (ev0) cudaEventRecord(ev0, g->stream);
-    if (g->kernel == EMLAB_KERNEL_SPLIT) {
+    if (g->cpml_on) {
+        launch_cpml(g, a, g->wide, g->stream);  // in place on the current generation
+        launched += 2;
+    } else if (g->kernel == EMLAB_KERNEL_SPLIT) {
         launch_yee_split(a, g->wide, g->stream);
         launched += 2;
     } else {
@@ -464,6 +468,9 @@ int emlab_grid_configure(emlab_grid* g, const emlab_grid_config* req) {
     g->pitch = pitch, g->plane = plane, g->padded = padded;
     g->stack = StackLayout();  // a single scene
     if (int rc = upload_pml(g)) return rc;
+    if (g->cpml_on) {  // the convolutional PML follows the new size and absorber thickness
+        if (int rc = cpml_prepare(g)) return rc;
+    }
     // vacuum materials: class 0 everywhere (SimulationGrid.cpp:185-192)
     const long long n = g->cells();
     try {

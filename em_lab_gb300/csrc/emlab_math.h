@@ -143,3 +143,28 @@ static inline float emlab_half_to_float(uint16_t h) {
 
 /* Round a float through binary16 and back: the value a shader sees after unpackHalf2x16. */
 static inline float emlab_half_round(float f) { return emlab_half_to_float(emlab_float_to_half(f)); }
+
+/* Convolutional PML (the opt-in absorber; the reference's own absorber is the graded conductivity
+ * above). Coefficients of the recursive convolution of Roden & Gedney (Microwave Opt. Technol.
+ * Lett. 27, 2000) with the complex-frequency-shifted stretch s = kappa + sigma / (alpha + j w):
+ *   psi^{n+1} = b psi^n + c dF,   b = exp(-(sigma / kappa + alpha) dt),
+ *   c = sigma / (sigma kappa + kappa^2 alpha) (b - 1),
+ * and the derivative dF enters the curl as dF / kappa + psi. At coordinate u on an axis of n
+ * cells with an absorber of L cells the normalised depth is delta = clamp(max(L - u, u - (n-1-L)) / L,
+ * 0, 1) (the interior ends where the graded absorber's does, common.glsl:31-36), and
+ *   sigma = sigma_max delta^m, kappa = 1 + (kappa_max - 1) delta^m, alpha = alpha_max (1 - delta).
+ * Evaluated in FP64 on the host (library tables and the restatement alike), stored as FP32:
+ * out = (b, c, 1 / kappa). */
+static inline void emlab_cpml_coef(double u, int n, int L, double sigma_max, double kappa_max, double alpha_max,
+                                   double order, double dt, float out[3]) {
+    double d = (double)L - u, hi = u - (double)(n - 1 - L);
+    if (hi > d) d = hi;
+    double delta = L > 0 ? d / (double)L : 0.0;
+    if (!(delta > 0.0)) delta = 0.0;
+    if (delta > 1.0) delta = 1.0;
+    const double g = pow(delta, order);
+    const double sigma = sigma_max * g, kappa = 1.0 + (kappa_max - 1.0) * g, alpha = alpha_max * (1.0 - delta);
+    const double b = exp(-(sigma / kappa + alpha) * dt);
+    const double c = sigma > 0.0 ? sigma / (sigma * kappa + kappa * kappa * alpha) * (b - 1.0) : 0.0;
+    out[0] = (float)b, out[1] = (float)c, out[2] = (float)(1.0 / kappa);
+}

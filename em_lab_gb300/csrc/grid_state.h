@@ -159,6 +159,13 @@ struct emlab_grid {
     DevBuf<float> d_dft_blk;
     DevBuf<float> d_dft_bhi, d_dft_blo;  // tensor-core twiddles (split hi/lo, MMA operand layout)
     int dft_engine = EMLAB_DFT_TENSOR;
+    // opt-in convolutional PML (cpml.cu): parameters, per-axis coefficient tables, slab psi arrays
+    bool cpml_on = false;
+    emlab_cpml cpml{};
+    DevBuf<float4> cpml_coef;
+    DevBuf<float> cpml_psi;
+    int cpml_stride = 0;
+    long long cpml_slab[3] = {0, 0, 0}, cpml_psi_off[3] = {0, 0, 0};
     // scratch
     DevBuf<unsigned> d_flag;
     // asynchronous FieldAnalyzer read-back: two measurements in flight, collected in order
@@ -195,4 +202,8 @@ int upload_sources(emlab_grid* g, const std::vector<float>& packed, const std::v
                    const std::vector<int32_t>& lists, const std::vector<int32_t>& zoff);
 // stack.cu: merges per-scene materials uploaded since the last step
 int stack_commit(emlab_grid* g);
+// cpml.cu: tables and psi arrays for the configured size, psi reset, and the two in-place passes
+int cpml_prepare(emlab_grid* g);
+int cpml_clear(emlab_grid* g);
+void launch_cpml(emlab_grid* g, const YeeArgs& a, bool wide, cudaStream_t s);
 }  // namespace emlab

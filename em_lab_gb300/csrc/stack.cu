@@ -66,6 +66,8 @@ int configure_layout(emlab_grid* g, const emlab_grid_config& c, const std::vecto
     const int pitch = row_pitch(t.nx);
     const long long plane = (long long)pitch * t.ny;
     const long long padded = plane * t.nz;
+    g->cpml_on = false;  // a stack always uses the reference absorber
+    g->cpml_psi.release(), g->cpml_coef.release();
     g->fields.release();
     g->cls.release();
     if (g->fields.alloc((size_t)padded * 12) != cudaSuccess) {

@@ -98,6 +98,7 @@ def load_library() -> C.CDLL:
         "emlab_lines_read": ([P, fp, fp], I),
         "emlab_debug_expf": ([fp, fp, SZ], I),
         "emlab_debug_set_wait_limit": ([I], I),
+        "emlab_grid_set_cpml": ([P, C.POINTER(abi.Cpml)], I),
         "emlab_edge_materials": ([fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ, C.POINTER(abi.WireTerm), SZ,
                                   fp, fp, fp, fp, C.POINTER(C.c_uint32)], I),
         "emlab_source_signal": ([C.POINTER(abi.Source), D], D),
@@ -289,6 +290,15 @@ class SimulationGrid:
 
     def set_kernel(self, kernel: int):
         _check(self._lib.emlab_grid_set_kernel(self._h, int(kernel)))
+
+    def set_cpml(self, params=None):
+        """The opt-in convolutional PML: (sigma_max, kappa_max, alpha_max, order), or None for the
+        reference's graded absorber. Clears the fields, the auxiliary fields and time."""
+        if params is None:
+            _check(self._lib.emlab_grid_set_cpml(self._h, None))
+        else:
+            p = abi.Cpml(*[float(v) for v in params])
+            _check(self._lib.emlab_grid_set_cpml(self._h, C.byref(p)))
 
     def set_tiling(self, tile_rows: int):
         """Tile height of the fused kernels (8, 16, or 0 = automatic); results do not depend on it."""

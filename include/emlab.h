@@ -184,6 +184,22 @@ int emlab_grid_kernel_time(emlab_grid* g, double* ms, uint64_t* launches, int re
  * with port recording on, a chunk uses its graph when the caller has taken the series
  * (emlab_ports_take_series) since the last chunk. */
 int emlab_grid_set_graph(emlab_grid* g, int chunk);
+/* Opt-in convolutional PML (no counterpart in the reference, whose absorber is the graded
+ * conductivity with matched magnetic loss of shaders/common.glsl:15-43; that absorber stays the
+ * default and the parity path). With params, the absorber cells of the grid (pml_thickness of the
+ * configuration, plus one, at every face) stretch each spatial derivative of the curl along an axis
+ * as dF / kappa + psi, psi <- b psi + c dF (Roden & Gedney's recursive convolution with the complex
+ * frequency shift), with sigma = sigma_max d^m, kappa = 1 + (kappa_max - 1) d^m,
+ * alpha = alpha_max (1 - d) at normalised depth d; the graded conductivity is off. NULL restores the
+ * reference absorber. Either way the fields, the auxiliary fields and time are cleared. Not
+ * available for stacks of scenes. Stepping then uses two in-place passes (B, E) of its own kernels. */
+typedef struct emlab_cpml {
+    float sigma_max; /* conductivity at the outer edge (normalised); about 0.8 (m + 1) is the usual optimum */
+    float kappa_max; /* coordinate stretch at the outer edge (>= 1) */
+    float alpha_max; /* frequency shift at the inner edge (>= 0) */
+    float order;     /* grading exponent m (1 .. 8) */
+} emlab_cpml;
+int emlab_grid_set_cpml(emlab_grid* g, const emlab_cpml* params);
 /* Non-finite check over E and B on the device (Instruments::applyMeasurement's stability check,
  * src/Instruments.cpp:271-275): EMLAB_ERR_NONFINITE if any component is NaN or infinite. */
 int emlab_grid_check_finite(emlab_grid* g);

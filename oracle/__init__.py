@@ -53,6 +53,7 @@ def _grid_spec(R):
         "oracle_ntff_dft_configure": ([P, ip, ip, fp, I, ip], I),
         "oracle_ntff_dft_points": ([P], I),
         "oracle_ntff_dft_read": ([P, dp], None),
+        "oracle_set_cpml": ([P, I, F, F, F, F], I),
     }
 
 
@@ -71,7 +72,7 @@ def load_ref():
     lib = C.CDLL(str(_REF_PATH))
     for name, (args, res) in _grid_spec(C.c_float).items():
         if name in ("oracle_ports_sweep_sums", "oracle_ntff_dft_configure", "oracle_ntff_dft_points",
-                    "oracle_ntff_dft_read"):
+                    "oracle_ntff_dft_read", "oracle_set_cpml"):
             continue
         fn = getattr(lib, f"{name}_ref")
         fn.argtypes, fn.restype = args, res
@@ -332,6 +333,16 @@ class Oracle:
             raise ValueError("far-field DFT box is degenerate")
         self._dft_nf = len(wl)
         return tuple(out[:3]), tuple(out[3:])
+
+    def set_cpml(self, params=None):
+        """The opt-in convolutional PML (sigma_max, kappa_max, alpha_max, order) or None for the
+        reference absorber; clears the fields and the auxiliary fields as the library does."""
+        if params is None:
+            rc = self._fn("oracle_set_cpml")(self._h, 0, 0.0, 1.0, 0.0, 1.0)
+        else:
+            rc = self._fn("oracle_set_cpml")(self._h, 1, *[float(v) for v in params])
+        if rc:
+            raise MemoryError("oracle CPML set-up failed")
 
     def ntff_dft_info(self):
         """(box nodes, samples accumulated) like the device monitor's emlab_ntff_dft_info."""

@@ -58,6 +58,12 @@ typedef struct {
     int dft_min[3], dft_max[3], dft_face[7], dft_points, dft_nf;
     double* dft_w;       /* omega per frequency */
     double* dft;         /* [f][point][6][2] */
+    /* opt-in convolutional PML (the library's cpml.cu): per-axis (b, c, 1/kappa) at integer and
+       half-integer positions, and the slab auxiliary fields, four arrays per derivative axis */
+    int cpml_on;
+    float* cpml_coef[2][3]; /* [lattice][axis][i * 3 + {b, c, 1/kappa}] */
+    R* cpml_psi[3];         /* [axis][slot * slab + compact index] */
+    int64_t cpml_slab[3];
 } NAME(grid);
 
 static inline R NAME(exp)(const NAME(grid) * g, R x) {
@@ -69,12 +75,14 @@ static inline R NAME(exp)(const NAME(grid) * g, R x) {
 #endif
 }
 
+static void NAME(cpml_free)(NAME(grid) * g);
+
 static inline R NAME(rmax)(R a, R b) { return a > b ? a : b; } /* GLSL max(x, y): y if x < y */
 static inline R NAME(rmin)(R a, R b) { return b < a ? b : a; }
 
-/* common.glsl:23-27 */
+/* common.glsl:23-27 (off under the convolutional PML, which replaces the graded conductivity) */
 static R NAME(pml_profile)(const NAME(grid) * g, R depth) {
-    if (depth <= (R)0) return (R)0;
+    if (depth <= (R)0 || g->cpml_on) return (R)0;
     R u = NAME(rmin)(depth / (R)g->cfg.pml_thickness, (R)1);
     return (R)g->cfg.pml_sigma_max * (NAME(exp)(g, (R)g->cfg.pml_grading * u) - (R)1) /
            (NAME(exp)(g, (R)g->cfg.pml_grading) - (R)1);
@@ -167,6 +175,7 @@ void NAME(oracle_destroy)(void* h) {
     free(g->cells), free(g->lists), free(g->port_phasor), free(g->series), free(g->ntff);
     free(g->q), free(g->terms), free(g->weights), free(g->line_phasor), free(g->line_now);
     free(g->dft_w), free(g->dft);
+    NAME(cpml_free)(g);
     free(g);
 }
 
@@ -229,7 +238,126 @@ void NAME(oracle_reset_fields)(void* h) {
     NAME(grid)* g = (NAME(grid)*)h;
     for (int64_t i = 0; i < g->n; ++i)
         for (int c = 0; c < 3; ++c) g->E[i * 4 + c] = g->B[i * 4 + c] = (R)0;
+    for (int a = 0; a < 3; ++a)
+        if (g->cpml_psi[a]) memset(g->cpml_psi[a], 0, (size_t)g->cpml_slab[a] * 4 * sizeof(R));
     g->step = 0;
+}
+
+/* ---------------------------------------------------------------------------------------- */
+/* The opt-in convolutional PML, restated from its definition (Roden & Gedney's recursive
+   convolution: psi <- b psi + c dF, derivative -> dF / kappa + psi inside slabs of L + 1 cells at
+   each face), in the operation order the library's cpml.cu uses; coefficients from the shared
+   emlab_cpml_coef (FP64 -> FP32). */
+static void NAME(cpml_free)(NAME(grid) * g) {
+    for (int l = 0; l < 2; ++l)
+        for (int a = 0; a < 3; ++a) free(g->cpml_coef[l][a]), g->cpml_coef[l][a] = NULL;
+    for (int a = 0; a < 3; ++a) free(g->cpml_psi[a]), g->cpml_psi[a] = NULL;
+    g->cpml_on = 0;
+}
+
+int NAME(oracle_set_cpml)(void* h, int on, float sigma_max, float kappa_max, float alpha_max, float order) {
+    NAME(grid)* g = (NAME(grid)*)h;
+    NAME(cpml_free)(g);
+    if (on) {
+        const int n[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+        const int L = g->cfg.pml_thickness, S = 2 * (L + 1);
+        for (int l = 0; l < 2; ++l)
+            for (int a = 0; a < 3; ++a) {
+                g->cpml_coef[l][a] = (float*)malloc((size_t)n[a] * 3 * sizeof(float));
+                if (!g->cpml_coef[l][a]) return EMLAB_ERR_OOM;
+                for (int i = 0; i < n[a]; ++i)
+                    emlab_cpml_coef((double)i + (l ? 0.5 : 0.0), n[a], L, sigma_max, kappa_max, alpha_max, order,
+                                    (double)g->cfg.courant, g->cpml_coef[l][a] + (size_t)i * 3);
+            }
+        const int64_t area[3] = {(int64_t)n[1] * n[2], (int64_t)n[0] * n[2], (int64_t)n[0] * n[1]};
+        for (int a = 0; a < 3; ++a) {
+            g->cpml_slab[a] = area[a] * S;
+            g->cpml_psi[a] = (R*)calloc((size_t)g->cpml_slab[a] * 4, sizeof(R));
+            if (!g->cpml_psi[a]) return EMLAB_ERR_OOM;
+        }
+        g->cpml_on = 1;
+    }
+    NAME(oracle_reset_fields)(h);
+    return EMLAB_OK;
+}
+
+/* dF / kappa + psi for the derivative along `axis` (lattice 0: integer positions, 1: half) of the
+   component in psi slot `slot`, at (x, y, z); dF outside the slabs */
+static inline R NAME(cpml_term)(NAME(grid) * g, int lattice, int axis, int slot, int x, int y, int z, R d) {
+    const int n[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+    const int p[3] = {x, y, z};
+    const int L1 = g->cfg.pml_thickness + 1, S = 2 * L1;
+    const int i = p[axis];
+    int s = -1;
+    if (i < L1) s = i;
+    else if (i >= n[axis] - L1) s = i - n[axis] + 2 * L1;
+    if (s < 0) return d;
+    int64_t at;
+    if (axis == 0) at = ((int64_t)z * n[1] + y) * S + s;
+    else if (axis == 1) at = ((int64_t)z * S + s) * n[0] + x;
+    else at = ((int64_t)s * n[1] + y) * n[0] + x;
+    R* psi = g->cpml_psi[axis] + (int64_t)slot * g->cpml_slab[axis] + at;
+    const float* k = g->cpml_coef[lattice][axis] + (size_t)i * 3;
+    const R v = (R)k[0] * *psi + (R)k[1] * d;
+    *psi = v;
+    return d * (R)k[2] + v;
+}
+
+static void NAME(cpml_update_B)(NAME(grid) * g) {
+    const int nx = g->cfg.nx, ny = g->cfg.ny, nz = g->cfg.nz;
+    const R dt = (R)g->cfg.courant;
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const int64_t i = NAME(idx)(g, x, y, z);
+                const R* e0 = g->E + i * 4;
+                const R exy = NAME(fetchE0)(g, x + 1, y, z, 1), exz = NAME(fetchE0)(g, x + 1, y, z, 2);
+                const R eyx = NAME(fetchE0)(g, x, y + 1, z, 0), eyz = NAME(fetchE0)(g, x, y + 1, z, 2);
+                const R ezx = NAME(fetchE0)(g, x, y, z + 1, 0), ezy = NAME(fetchE0)(g, x, y, z + 1, 1);
+                R t0[3] = {eyz - e0[2], ezx - e0[0], exy - e0[1]};
+                R t1[3] = {ezy - e0[1], exz - e0[2], eyx - e0[0]};
+                if (g->thin) {
+                    for (int c = 0; c < 3; ++c) {
+                        t0[c] = t0[c] * (R)g->w0[i * 3 + c];
+                        t1[c] = t1[c] * (R)g->w1[i * 3 + c];
+                    }
+                }
+                R* b = g->B + i * 4;
+                for (int c = 0; c < 3; ++c) {
+                    const R u0 = NAME(cpml_term)(g, 1, (c + 1) % 3, 2, x, y, z, t0[c]);
+                    const R u1 = NAME(cpml_term)(g, 1, (c + 2) % 3, 3, x, y, z, t1[c]);
+                    const R curl = u0 - u1;
+                    b[c] = b[c] - dt * curl;
+                }
+            }
+}
+
+static void NAME(e_coeffs)(const NAME(grid) * g, int x, int y, int z, R ca[3], R cb[3]);
+
+static void NAME(cpml_update_E)(NAME(grid) * g) {
+    const int nx = g->cfg.nx, ny = g->cfg.ny, nz = g->cfg.nz;
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const int64_t i = NAME(idx)(g, x, y, z);
+                const R* b0 = g->B + i * 4;
+                const R bxy = NAME(fetchB0)(g, x - 1, y, z, 1), bxz = NAME(fetchB0)(g, x - 1, y, z, 2);
+                const R byx = NAME(fetchB0)(g, x, y - 1, z, 0), byz = NAME(fetchB0)(g, x, y - 1, z, 2);
+                const R bzx = NAME(fetchB0)(g, x, y, z - 1, 0), bzy = NAME(fetchB0)(g, x, y, z - 1, 1);
+                const R t0[3] = {b0[2] - byz, b0[0] - bzx, b0[1] - bxy};
+                const R t1[3] = {b0[1] - bzy, b0[2] - bxz, b0[0] - byx};
+                R ca[3], cb[3];
+                NAME(e_coeffs)(g, x, y, z, ca, cb);
+                R* e = g->E + i * 4;
+                for (int c = 0; c < 3; ++c) {
+                    const R u0 = NAME(cpml_term)(g, 0, (c + 1) % 3, 0, x, y, z, t0[c]);
+                    const R u1 = NAME(cpml_term)(g, 0, (c + 2) % 3, 1, x, y, z, t1[c]);
+                    const R curl = u0 - u1;
+                    e[c] = ca[c] * e[c] + cb[c] * curl;
+                }
+            }
 }
 
 /* ---------------------------------------------------------------------------------------- */
@@ -552,8 +680,13 @@ void NAME(oracle_step)(void* h, int count) {
     for (int k = 0; k < count; ++k) {
         const double t = ((double)(g->step) + 0.5) * (double)g->cfg.courant;
         for (int s = 0; s < g->nsrc; ++s) signals[s] = (float)oracle_signal(&g->desc[s], t);
-        NAME(update_B)(g);
-        NAME(update_E)(g);
+        if (g->cpml_on) {
+            NAME(cpml_update_B)(g);
+            NAME(cpml_update_E)(g);
+        } else {
+            NAME(update_B)(g);
+            NAME(update_E)(g);
+        }
         if (g->ncells > 0) NAME(apply_sources)(g, signals);
         ++g->step;
         if (g->ntff_on) NAME(ntff_accumulate)(g);

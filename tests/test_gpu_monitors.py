@@ -189,7 +189,7 @@ def test_plain_small_2000_steps():
         b = out["f64"]["f"][c]
         rel = np.linalg.norm(out["gpu"]["f"][c].astype(np.float64) - b) / np.linalg.norm(b)
         print(f"component {c}: relative L2 vs FP64 oracle {rel:.3e}")
-        assert rel < 1e-4
+        assert rel < 1e-5  # measured on GB300: 6.2e-7 .. 6.2e-6 (Bz largest)
     for k in ("probe", "flux", "ntff"):
         assert np.array_equal(out["gpu"][k], out["f32"][k]), k
 
