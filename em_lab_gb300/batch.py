@@ -3,8 +3,9 @@
 Scenes are grouped by cross-section (nx, ny) and each group becomes one `SceneStack`: a single grid
 whose every solver launch covers all of its scenes (csrc/stack.cu). Each group runs on its own CUDA
 stream, so the groups' launches overlap on the device. Every `chunk` steps the port series of the
-chunk is read back; a scene is done when its port voltage has stayed below `ringdown_db` (-60 dB)
-of its peak for two periods of its design wavelength. A finished scene's impedance sweep Z(f) is
+chunk is read back; a scene is done when the reference's ring-down residual (the largest |V| of
+the last 5 % of its series over the peak, Ports.cpp:206-213) is 60 dB down, after at least four
+design periods (at most 120). A finished scene's impedance sweep Z(f) is
 evaluated on the host from its whole series (Ports.cpp:187-278: the FP64 DFT of V and I with the
 half-step phase correction of I, Z = -V/I * eta0), and the scene is dropped from its stack by
 compaction once a quarter of the stack has finished.
@@ -81,34 +82,54 @@ def scene_sweep(sc, series: np.ndarray, dt: float):
     return impedance(sums, sw["wavelength_min"], sw["wavelength_max"], z0)
 
 
-class RingDown:
-    """-60 dB watch on one port voltage: peak |V| so far and the last step at which |V| exceeded the
-    threshold fraction of it; done once `window` quiet steps follow and at least `min_steps` ran."""
+def residual(v: np.ndarray) -> float:
+    """The reference's ring-down residual of a port voltage series (PortMonitor::evaluateSweep,
+    Ports.cpp:206-213): the largest |V| of the last max(n / 20, 1) samples over the largest |V| of
+    all n (1 without signal). emlab_ports_residuals computes the same on the device."""
+    a = np.abs(np.asarray(v, np.float32))
+    if a.size == 0:
+        return 1.0
+    peak = float(a.max())
+    return float(a[a.size - max(a.size // 20, 1):].max()) / peak if peak > 0.0 else 1.0
 
-    def __init__(self, window: int, min_steps: int, db: float = DB_RINGDOWN, max_steps: int = 1 << 62):
-        self.window, self.min_steps, self.max_steps = int(window), int(min_steps), int(max_steps)
+
+class RingDown:
+    """-60 dB watch on one port voltage with the reference's criterion: the sweep has settled once
+    the residual (largest |V| of the last 5 % of the series over its peak, Ports.cpp:206-213) is at
+    most -60 dB, checked wherever the runner reads the series; at least `min_steps` must have run,
+    and the watch gives up (not rung down) at `max_steps`."""
+
+    def __init__(self, min_steps: int, max_steps: int = 1 << 62, db: float = DB_RINGDOWN):
+        self.min_steps, self.max_steps = int(min_steps), int(max_steps)
         self.ratio = 10.0 ** (db / 20.0)
         self.peak = 0.0
-        self.last_loud = 0
         self.steps = 0
+        self.parts = []  # |V| of the series so far, in the chunks it arrived in
 
     def feed(self, v: np.ndarray) -> bool:
-        a = np.abs(np.asarray(v, np.float64))
+        a = np.abs(np.asarray(v, np.float32))
         if a.size:
-            # the peak grows while the pulse passes: each sample is compared with the running peak
-            peak = np.maximum.accumulate(np.maximum(a, self.peak))
-            loud = np.nonzero(a > self.ratio * peak)[0]
-            if loud.size:
-                self.last_loud = self.steps + int(loud[-1])
-            self.peak = float(peak[-1])
+            self.parts.append(a)
+            self.peak = max(self.peak, float(a.max()))
         self.steps += a.size
         return self.done()
 
+    def residual(self) -> float:
+        if not (self.peak > 0.0):
+            return 1.0
+        tail, late, k = max(self.steps // 20, 1), 0.0, len(self.parts) - 1
+        while tail > 0 and k >= 0:  # the last `tail` samples, from the newest chunk backwards
+            part = self.parts[k][-tail:]
+            late = max(late, float(part.max()))
+            tail -= part.size
+            k -= 1
+        return late / self.peak
+
     def rung_down(self) -> bool:
-        return self.peak > 0.0 and self.steps >= self.min_steps and self.steps - 1 - self.last_loud >= self.window
+        return self.peak > 0.0 and self.steps >= self.min_steps and self.residual() <= self.ratio
 
     def done(self) -> bool:
-        return self.rung_down() or self.steps >= self.max_steps
+        return self.steps >= self.max_steps or self.rung_down()
 
 
 MAX_PERIODS = 120  # a scene that has not rung down after this many design periods stops there (flagged)
@@ -116,8 +137,7 @@ MAX_PERIODS = 120  # a scene that has not rung down after this many design perio
 
 def _watch(sc, dt: float) -> RingDown:
     period = sc.wavelength / dt  # steps per period of the design wavelength
-    return RingDown(window=int(math.ceil(2.0 * period)), min_steps=int(math.ceil(4.0 * period)),
-                    max_steps=int(math.ceil(MAX_PERIODS * period)))
+    return RingDown(min_steps=int(math.ceil(4.0 * period)), max_steps=int(math.ceil(MAX_PERIODS * period)))
 
 
 TILINGS = (64, 32, 128, 8)  # 64 x 8, 64 x 4, 64 x 16 pair tiles; 32 x 8 single-cell tiles
@@ -210,7 +230,7 @@ class BatchRunner:
         if stop_steps is None:
             self.watch = [_watch(sc, float(sc.grid.courant)) for sc in self.scenes]
         else:
-            self.watch = [RingDown(window=1 << 40, min_steps=int(n), max_steps=int(n)) for n in stop_steps]
+            self.watch = [RingDown(min_steps=int(n), max_steps=int(n)) for n in stop_steps]
         self.cell_steps = 0
         self.steps = 0
 

@@ -17,6 +17,7 @@ normal distribution of the GNU C++ library, restated here (MT19937, generate_can
 """
 from __future__ import annotations
 
+import cmath
 import math
 
 import numpy as np
@@ -91,6 +92,19 @@ def _db(p):
 def _mean_power(v):
     v = np.asarray(v)
     return float(np.sum(np.abs(v) ** 2) / v.size) if v.size else 0.0
+
+
+def _dot3_f32(a, b):
+    """glm::dot of two vec3: (a.x b.x + a.y b.y) + a.z b.z, every operation rounded to FP32."""
+    a, b = np.asarray(a, f32), np.asarray(b, f32)
+    return f32(f32(f32(a[0] * b[0]) + f32(a[1] * b[1])) + f32(a[2] * b[2]))
+
+
+def _normalize_f32(v):
+    """glm::normalize: v * inversesqrt(dot(v, v)) with inversesqrt = 1 / sqrt in FP32."""
+    v = np.asarray(v, f32)
+    inv = f32(f32(1.0) / f32(np.sqrt(_dot3_f32(v, v))))
+    return (v * inv).astype(f32)
 
 
 def _dot_h(a, b):
@@ -384,18 +398,23 @@ class CrpaMonitor:
             R = np.zeros((N, N), complex)
             amp = math.sqrt(gs)
             for snap in self.baseband:
-                xk = np.array([amp * snap[i] + complex(rng(), rng()) for i in range(N)])
+                xk = np.empty(N, complex)
+                for i in range(N):
+                    # cd(gauss(rng), gauss(rng)) (Crpa.cpp:447): C++ leaves the order of the two
+                    # draws to the compiler; GCC and MSVC evaluate the imaginary part's draw first
+                    im = rng()
+                    xk[i] = amp * snap[i] + complex(rng(), im)
                 R += np.outer(xk, np.conj(xk))
             R /= len(self.baseband)
             r.update(blind=True, snapshots=len(self.baseband),
                      snapshot_us=self.setup["snapshot_periods"] * self.wl * self.cell_size / 299792458.0 * 1e6)
-        u = np.asarray(self.emitters[self.satellite]["position"], f32) - self.center
-        u = (u / f32(np.sqrt(np.sum(u * u, dtype=f32)))).astype(f32)
+        # glm::normalize and glm::dot in FP32, operation by operation (Crpa.cpp:462-466)
+        u = _normalize_f32((np.asarray(self.emitters[self.satellite]["position"], f32) - self.center).astype(f32))
         k = 2.0 * math.pi / self.wl
         if self.setup["measured_steering"]:
             a = s_raw.copy()
         else:
-            a = np.array([np.exp(1j * k * float(np.dot(np.asarray(el["center"], f32) - self.center, u)))
+            a = np.array([cmath.rect(1.0, k * float(_dot3_f32((np.asarray(el["center"], f32) - self.center).astype(f32), u)))
                           for el in self.setup["elements"]])
         Ria = solve(R, a, N)
         denom = _dot_h(a, Ria)

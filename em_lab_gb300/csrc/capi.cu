@@ -919,19 +919,29 @@ int emlab_ports_sweep_sums(emlab_grid* g, double lambda_min, double lambda_max, 
     EMLAB_CUDA(cudaMemcpyAsync(out, d_out.p, d_out.n * 8, cudaMemcpyDeviceToHost, g->stream));
     if (int rc = emlab_grid_synchronize(g, 0)) return rc;
     if (residual) {
-        // ring-down: late-time |V| of port 0 relative to its peak (Ports.cpp:206-213)
-        std::vector<float> series(g->recorded * g->nports * 2);
-        EMLAB_CUDA(cudaMemcpy(series.data(), g->d_series.p, series.size() * 4, cudaMemcpyDeviceToHost));
-        const size_t n = g->recorded, tail = std::max<size_t>(n / 20, 1);
-        double peak = 0.0, late = 0.0;
-        for (size_t k = 0; k < n; ++k) {
-            const double v = std::abs((double)series[k * g->nports * 2]);
-            peak = std::max(peak, v);
-            if (k >= n - tail) late = std::max(late, v);
-        }
-        *residual = peak > 0.0 ? late / peak : 1.0;
+        // ring-down: late-time |V| of port 0 relative to its peak (Ports.cpp:206-213), on the device
+        std::vector<double> r((size_t)g->nports);
+        if (int rc = emlab_ports_residuals(g, r.data())) return rc;
+        *residual = r[0];
     }
     return EMLAB_OK;
+}
+
+int emlab_ports_residuals(emlab_grid* g, double* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(out, "null output");
+    EMLAB_REQUIRE(g->nports > 0, "no port monitor");
+    if (g->recorded == 0) {
+        for (int p = 0; p < g->nports; ++p) out[p] = 1.0;
+        return EMLAB_OK;
+    }
+    DevBuf<double> d_out;
+    EMLAB_CUDA(d_out.alloc((size_t)g->nports));
+    launch_port_residuals(g->d_series.p, (long long)g->recorded, g->nports, d_out.p, g->stream);
+    ++g_launches;
+    if (int rc = check_launch()) return rc;
+    EMLAB_CUDA(cudaMemcpyAsync(out, d_out.p, d_out.n * 8, cudaMemcpyDeviceToHost, g->stream));
+    return emlab_grid_synchronize(g, 0);
 }
 
 // ---- far field -----------------------------------------------------------------------------

@@ -112,6 +112,7 @@ void launch_ntff_pattern_fast(const int* box, int points, const float* phasors, 
                               int count, int slices, float k, float4* partials, cudaStream_t s);
 void launch_ntff_reduce(const float4* dirs, const float4* partials, int first, int count, int slices, float* out,
                         cudaStream_t s);
+void launch_port_residuals(const float* series, long long steps, int nports, double* out, cudaStream_t s);
 void launch_sweep_sums(const float* series, long long steps, int nports, double nu_lo, double nu_hi, int points,
                        double dt, double* out, cudaStream_t s);
 void launch_check_finite(const MonitorArgs& m, unsigned* flag, cudaStream_t s);

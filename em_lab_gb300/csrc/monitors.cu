@@ -634,6 +634,35 @@ void launch_sweep_sums(const float* series, long long steps, int nports, double 
     sweep_kernel<<<nports * points, 256, 0, s>>>(series, steps, nports, nu_lo, nu_hi, points, dt, out);
 }
 
+// Ring-down residual of every port (PortMonitor::evaluateSweep, Ports.cpp:206-213): the largest |V|
+// of the last max(n / 20, 1) recorded steps over the largest |V| of all n (1 when there is no
+// signal). One block per port; |V| maxima are exact in any order, so the result equals the host's.
+__global__ void __launch_bounds__(256) residual_kernel(const float* series, long long steps, int nports, double* out) {
+    __shared__ float s_peak[256], s_late[256];
+    const int p = blockIdx.x;
+    const long long tail = steps / 20 > 1 ? steps / 20 : 1, late_from = steps - tail;
+    float peak = 0.0f, late = 0.0f;
+    for (long long k = threadIdx.x; k < steps; k += blockDim.x) {
+        const float v = fabsf(series[(k * nports + p) * 2]);
+        peak = fmaxf(peak, v);
+        if (k >= late_from) late = fmaxf(late, v);
+    }
+    s_peak[threadIdx.x] = peak, s_late[threadIdx.x] = late;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            s_peak[threadIdx.x] = fmaxf(s_peak[threadIdx.x], s_peak[threadIdx.x + w]);
+            s_late[threadIdx.x] = fmaxf(s_late[threadIdx.x], s_late[threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[p] = s_peak[0] > 0.0f ? (double)s_late[0] / (double)s_peak[0] : 1.0;
+}
+
+void launch_port_residuals(const float* series, long long steps, int nports, double* out, cudaStream_t s) {
+    residual_kernel<<<nports, 256, 0, s>>>(series, steps, nports, out);
+}
+
 void launch_check_finite(const MonitorArgs& m, unsigned* flag, cudaStream_t s) {
     finite_kernel<<<152 * 8, 256, 0, s>>>(m, flag);
 }

@@ -68,6 +68,7 @@ def load_library() -> C.CDLL:
         "emlab_ports_read_phasors": ([P, fp], I),
         "emlab_ports_read_series": ([P, fp, SZ, C.POINTER(SZ)], I),
         "emlab_ports_sweep_sums": ([P, D, D, I, dp, dp], I),
+        "emlab_ports_residuals": ([P, dp], I),
         "emlab_ntff_configure": ([P, ip, ip, F, F, ip], I),
         "emlab_ntff_point_count": ([P, ip], I),
         "emlab_ntff_read_phasors": ([P, fp], I),
@@ -444,6 +445,13 @@ class SimulationGrid:
         _check(self._lib.emlab_ports_sweep_sums(self._h, float(lambda_min), float(lambda_max), int(points),
                                                 out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res)))
         return out, res.value
+
+    def ports_residuals(self):
+        """Per port, the reference's ring-down residual of the recorded series (on the device)."""
+        n = getattr(self, "_nports", 0)
+        out = np.zeros(n, np.float64)
+        _check(self._lib.emlab_ports_residuals(self._h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
 
     def ntff_configure(self, box_min, box_max, wavelength, averaging_periods=4.0):
         mn = (C.c_int * 3)(*[int(v) for v in box_min])

@@ -225,6 +225,11 @@ int emlab_ports_take_series(emlab_grid* g, float* out, size_t max_steps, size_t*
  * (sumV re, sumV im, sumI re, sumI im). Also returns the ring-down residual of port 0. */
 int emlab_ports_sweep_sums(emlab_grid* g, double lambda_min, double lambda_max, int points, double* out,
                            double* residual);
+/* The ring-down residual of PortMonitor::evaluateSweep (src/Ports.cpp:206-213) for every port, on
+ * the device over the series recorded since the last take: out[p] = largest |V| of the last
+ * max(n / 20, 1) steps / largest |V| of all n steps (1 without signal). The reference reports a
+ * sweep as settled once the residual of its first port is at most 1e-3 (-60 dB). */
+int emlab_ports_residuals(emlab_grid* g, double* out);
 
 /* ---- far-field monitor: FarFieldMonitor (src/FarField.hpp:75-133) ------------------------ */
 /* FarFieldMonitor::configure (src/FarField.cpp:126-174): box clamped into [L+1, n-L-2];

@@ -97,9 +97,10 @@ def transform(text: str) -> str:
     return _array_ctor("\n".join(lines)) + "\n"
 
 
-def _lines_between(text: str, start: str, end: str, what: str) -> str:
-    """The lines from the first one containing `start` up to (not including) the next one containing
-    `end`. Raises if either anchor is missing, so a changed reference file fails loudly."""
+def _lines_between(text: str, start: str, end: str, what: str, include_end: bool = False) -> str:
+    """The lines from the first one containing `start` up to the next one containing `end` (that
+    line excluded, or included with include_end). Raises if either anchor is missing, so a changed
+    reference file fails loudly."""
     lines = text.splitlines()
     i = next((k for k, l in enumerate(lines) if start in l), None)
     if i is None:
@@ -107,7 +108,7 @@ def _lines_between(text: str, start: str, end: str, what: str) -> str:
     j = next((k for k in range(i + 1, len(lines)) if end in lines[k]), None)
     if j is None:
         raise RuntimeError(f"build_ref: end anchor of {what} not found: {end!r}")
-    return "\n".join(lines[i:j]) + "\n"
+    return "\n".join(lines[i:j + (1 if include_end else 0)]) + "\n"
 
 
 def _braced(text: str, start: str, what: str) -> str:
@@ -139,7 +140,17 @@ def host_sources(root: Path) -> dict[str, str]:
     hpp = (root / "src" / "SimulationGrid.hpp").read_text()
     cpp = (root / "src" / "SimulationGrid.cpp").read_text()
     radar = (root / "src" / "Radar.cpp").read_text()
+    crpa_h = (root / "src" / "Crpa.hpp").read_text()
+    crpa = (root / "src" / "Crpa.cpp").read_text()
     return {
+        # the adaptive array's weights: set-up and result types, the small dense complex algebra,
+        # the hybrid channels and computeWeights from its covariance to its SINR scores
+        "ref_crpa_types.inc": _lines_between(crpa_h, "struct EmitterSetup {", "class CrpaMonitor {", "CRPA types"),
+        "ref_crpa_algebra.inc": _braced(crpa, "namespace {", "CRPA helpers"),
+        "ref_crpa_channels.inc": _braced(crpa, "std::vector<cd> CrpaMonitor::channels(", "channels"
+                                         ).replace("CrpaMonitor::", "CrpaCore::"),
+        "ref_crpa_weights.inc": _lines_between(crpa, "const std::vector<cd> sRaw = channels(m_response",
+                                               "r.satelliteGainDb =", "computeWeights", include_end=True),
         "ref_types.inc": _lines_between(hpp, "struct GridConfig {", "class SimulationGrid {", "set-up types"),
         "ref_gpusource.inc": _braced(cpp, "struct GPUSource {", "GPUSource"),
         "ref_defs.inc": _lines_between(cpp, "MaterialVolume::MaterialVolume(const glm::ivec3& size)",

@@ -19,6 +19,8 @@
 #include <complex>
 #include <cstdint>
 #include <cstring>
+#include <random>
+#include <string>
 #include <utility>
 #include <vector>
 
@@ -99,6 +101,40 @@ struct RadarCore {
 };
 
 #include "ref_radar_members.inc"
+
+// The adaptive GPS array's weight computation (Crpa.cpp): the helpers of its anonymous namespace
+// (toDb, meanPower, dotH, solve), the hybrid channels and computeWeights up to its SINR scores.
+#include "ref_crpa_types.inc"
+namespace crpa {
+#include "ref_crpa_algebra.inc"
+}
+using crpa::cd;
+
+struct CrpaCore {
+    CrpaSetup m_setup;
+    std::vector<EmitterSetup> m_emitters;
+    std::vector<std::pair<int, int>> m_elementPorts;
+    int m_satellite = 0;
+    glm::vec3 m_center{0.0f};
+    float m_wavelength = 16.0f, m_cellSize = 1e-3f;
+    std::vector<std::vector<cd>> m_baseband;
+    std::vector<std::vector<cd>> m_response;
+    CrpaResult m_result;
+
+    std::vector<cd> channels(const std::vector<cd>& ports, bool lhcp = false) const;
+
+    void computeWeights() {
+        using namespace crpa;
+        CrpaResult r;
+        const size_t N = m_elementPorts.size(), E = m_emitters.size();
+        (void)E;
+#include "ref_crpa_weights.inc"
+        r.valid = true;
+        m_result = std::move(r);
+    }
+};
+
+#include "ref_crpa_channels.inc"
 
 SourceDesc from_c(const emlab_source& c) {
     SourceDesc s;
@@ -238,6 +274,61 @@ void ref_host_radar_backproject(const emlab_radar_geometry* geo, float wavelengt
     std::vector<double> out((size_t)img.nr * img.nel * img.naz, 0.0);
     r.backproject(img, geo->dr, zz, (size_t)M, (size_t)C, geo->dt, geo->sample_dt, out);
     std::memcpy(power, out.data(), out.size() * sizeof(double));
+}
+
+// CrpaMonitor::computeWeights from the measured responses: elements (their X, Y port indices and
+// phase centres), emitters (positions; `satellite` is the wanted one), response[e][p] as complex
+// pairs, and in blind mode the noise-free snapshots baseband[k][i]. weights receives N complex
+// pairs, scores (sinrSingleDb, sinrSteeringDb, sinrMvdrDb, satelliteGainDb).
+void ref_host_crpa_weights(int n_elem, const int* element_ports, const float* element_centers, int n_emit,
+                           const float* emitter_pos, int n_ports, const double* response, int satellite,
+                           const float center[3], float wavelength, float cell_size, float jnr_db, float snr_db,
+                           int measured_steering, int mvdr, int blind, unsigned noise_seed, float snapshot_periods,
+                           int n_snap, const double* baseband, double* weights, double* scores) {
+    CrpaCore c;
+    for (int i = 0; i < n_elem; ++i) {
+        c.m_elementPorts.emplace_back(element_ports[2 * i], element_ports[2 * i + 1]);
+        CrpaElement el;
+        el.center = glm::vec3(element_centers[3 * i], element_centers[3 * i + 1], element_centers[3 * i + 2]);
+        c.m_setup.elements.push_back(el);
+    }
+    for (int e = 0; e < n_emit; ++e) {
+        EmitterSetup em;
+        em.position = glm::vec3(emitter_pos[3 * e], emitter_pos[3 * e + 1], emitter_pos[3 * e + 2]);
+        c.m_emitters.push_back(em);
+        std::vector<cd> r((size_t)n_ports);
+        for (int p = 0; p < n_ports; ++p)
+            r[(size_t)p] = cd(response[((size_t)e * n_ports + p) * 2], response[((size_t)e * n_ports + p) * 2 + 1]);
+        c.m_response.push_back(r);
+    }
+    for (int k = 0; k < n_snap; ++k) {
+        std::vector<cd> s((size_t)n_elem);
+        for (int i = 0; i < n_elem; ++i)
+            s[(size_t)i] = cd(baseband[((size_t)k * n_elem + i) * 2], baseband[((size_t)k * n_elem + i) * 2 + 1]);
+        c.m_baseband.push_back(s);
+    }
+    c.m_satellite = satellite;
+    c.m_center = glm::vec3(center[0], center[1], center[2]);
+    c.m_wavelength = wavelength, c.m_cellSize = cell_size;
+    c.m_setup.jnrDb = jnr_db, c.m_setup.snrDb = snr_db;
+    c.m_setup.measuredSteering = measured_steering != 0, c.m_setup.mvdr = mvdr != 0, c.m_setup.blind = blind != 0;
+    c.m_setup.noiseSeed = noise_seed, c.m_setup.snapshotPeriods = snapshot_periods;
+    c.computeWeights();
+    for (int i = 0; i < n_elem; ++i) {
+        weights[2 * i] = c.m_result.weights[(size_t)i].real();
+        weights[2 * i + 1] = c.m_result.weights[(size_t)i].imag();
+    }
+    scores[0] = c.m_result.sinrSingleDb, scores[1] = c.m_result.sinrSteeringDb;
+    scores[2] = c.m_result.sinrMvdrDb, scores[3] = c.m_result.satelliteGainDb;
+}
+
+// Crpa.cpp's solve (Gaussian elimination with partial pivoting): A n x n, b n, x n, complex pairs.
+void ref_host_crpa_solve(const double* A, const double* b, int n, double* x) {
+    std::vector<cd> a((size_t)n * n), bb((size_t)n);
+    for (size_t k = 0; k < a.size(); ++k) a[k] = cd(A[2 * k], A[2 * k + 1]);
+    for (int k = 0; k < n; ++k) bb[(size_t)k] = cd(b[2 * k], b[2 * k + 1]);
+    const std::vector<cd> r = crpa::solve(a, bb, (size_t)n);
+    for (int k = 0; k < n; ++k) x[2 * k] = r[(size_t)k].real(), x[2 * k + 1] = r[(size_t)k].imag();
 }
 
 }  // extern "C"

@@ -38,8 +38,10 @@ def test_batched_scene_generator_is_seeded_and_in_range():
 
 
 def test_ringdown_watch_on_a_damped_tone():
+    """The reference's criterion (Ports.cpp:206-213): settled once the largest |V| of the last 5 %
+    of the series is 60 dB below the peak."""
     dt, period = 0.5, 40.0  # steps per period = 80
-    w = batch.RingDown(window=160, min_steps=320)
+    w = batch.RingDown(min_steps=320)
     k = np.arange(4000)
     tau = 150.0  # steps: amplitude e^{-k / tau}
     v = np.sin(2 * math.pi * k / (period / dt)) * np.exp(-k / tau)
@@ -49,12 +51,21 @@ def test_ringdown_watch_on_a_damped_tone():
             done_at = c + 64
             break
     assert done_at is not None
-    # -60 dB of the peak is reached near tau * ln(1000) steps; the watch then waits one window
-    quiet = tau * math.log(1000.0)
-    assert quiet < done_at <= quiet + 160 + 80 + 64
+    assert w.residual() == pytest.approx(batch.residual(v[:done_at]), rel=1e-6)
+    # the late window starts at 0.95 n: e^{-0.95 n / tau} <= 1e-3 from n = tau ln(1000) / 0.95
+    settle = tau * math.log(1000.0) / 0.95
+    assert settle - 80 < done_at <= settle + 64 + 80
+    assert batch.residual(v[:done_at]) <= 1e-3 < batch.residual(v[:done_at - 64])
     # a silent start (delayed pulse) does not count as ring-down
-    w2 = batch.RingDown(window=10, min_steps=20)
-    assert not w2.feed(np.zeros(200))
+    w2 = batch.RingDown(min_steps=20)
+    assert not w2.feed(np.zeros(200)) and w2.residual() == 1.0
+
+
+def test_ringdown_stops_at_the_step_cap():
+    w = batch.RingDown(min_steps=10, max_steps=256)
+    v = np.sin(np.arange(300) * 0.3)  # never decays
+    done = [w.feed(v[c:c + 64]) for c in range(0, 256, 64)]
+    assert done == [False, False, False, True] and not w.rung_down()
 
 
 def test_sweep_sums_match_a_direct_dft():

@@ -65,6 +65,24 @@ def test_sweep_sums_fp64():
     assert r_gpu == r_cpu
 
 
+def test_port_residuals_on_the_device():
+    """emlab_ports_residuals (every port's ring-down residual of Ports.cpp:206-213, on the device)
+    equals the host evaluation of the same recorded series, for several lengths."""
+    from em_lab_gb300 import batch
+    sc = configs.random_scene(size=(30, 28, 26), pml=5, seed=12)
+    sc.sources[-1].waveform = abi.WAVE_PULSE
+    g = SimulationGrid(sc.grid)
+    oracle.load_scene(g, sc)
+    g.ports_configure([p.to_c() for p in sc.ports], 12.0, 4.0, sweep=True)
+    for steps in (1, 19, 40, 333):
+        g.step(steps if steps == 1 else steps - g.step_count())
+        ser = g.ports_series()
+        got = g.ports_residuals()
+        want = [batch.residual(ser[:, p, 0]) for p in range(ser.shape[1])]
+        assert np.array_equal(got, np.asarray(want)), (steps, got, want)
+    g.close()
+
+
 def test_check_finite():
     grid = abi.GridConfig((96, 96, 96), pml_thickness=8)
     g = SimulationGrid(grid)

@@ -178,3 +178,84 @@ def test_radar_backprojection_restatement_equals_the_reference(seed):
     # FP32 geometry, FP64 sums: the restatement evaluates sinf/cosf of the angles through double
     # precision libm and rounds, so single images points may differ in the last bits
     assert np.max(np.abs(got[inside] - want[inside]) / np.max(want[inside])) < 1e-9
+
+
+def crpa_problem(seed, blind):
+    """A seeded adaptive-array problem: 5 dual-probe elements, 4 emitters (index 1 the satellite),
+    measured responses at 12 ports (two unused), and for blind mode noise-free snapshots."""
+    from em_lab_gb300 import crpa
+    rng = np.random.default_rng(seed)
+    n_el, n_em, n_ports = 5, 4, 12
+    centers = rng.uniform(20, 60, (n_el, 3)).astype(np.float32)
+    ports = [(2 * i, 2 * i + 1) for i in range(n_el - 1)] + [(11, -1)]  # the last element has one probe
+    emitters = rng.uniform(-200, 300, (n_em, 3)).astype(np.float32)
+    response = (rng.standard_normal((n_em, n_ports)) + 1j * rng.standard_normal((n_em, n_ports))) * \
+        rng.uniform(0.01, 2.0, (n_em, 1))
+    baseband = (rng.standard_normal((40, n_el)) + 1j * rng.standard_normal((40, n_el))) if blind else np.zeros((0, n_el))
+    m = crpa.CrpaMonitor.__new__(crpa.CrpaMonitor)
+    m.setup = {"jnr_db": 40.0, "snr_db": -20.0, "blind": blind, "noise_seed": 7, "measured_steering": seed % 2 == 1,
+               "mvdr": True, "snapshot_periods": 40.0, "north": (0.0, 1.0, 0.0),
+               "elements": [{"center": tuple(float(v) for v in c)} for c in centers]}
+    m.emitters = [{"name": f"e{e}", "position": tuple(float(v) for v in p)} for e, p in enumerate(emitters)]
+    m.element_ports = ports
+    m.center = (centers.sum(axis=0, dtype=np.float32) / np.float32(n_el)).astype(np.float32)
+    m.satellite, m.wl, m.cell_size = 1, 24.0, 1e-3
+    m.response = [response[e] for e in range(n_em)]
+    m.baseband = [baseband[k] for k in range(baseband.shape[0])]
+    m.settle = [1.0] * n_em
+    return m, centers, emitters, response, baseband
+
+
+@pytest.mark.parametrize("seed,blind", [(1, False), (2, False), (3, True), (4, True)])
+def test_crpa_weights_equal_the_reference(seed, blind):
+    """CrpaMonitor::computeWeights (Crpa.cpp:401-496: covariance, steering vector, MVDR weights
+    through the reference's Gaussian elimination, SINR scores) against the package's
+    compute_weights on the same measured responses; summation order differs (vectorised sums), so
+    the comparison is to 1e-9 relative."""
+    m, centers, emitters, response, baseband = crpa_problem(seed, blind)
+    m.compute_weights()
+    got = m.result
+    lib = oracle.load_ref_host()
+    n_el, n_em = len(m.element_ports), len(m.emitters)
+    fp, dp, ip = C.POINTER(C.c_float), C.POINTER(C.c_double), C.POINTER(C.c_int)
+    ports = np.ascontiguousarray(np.asarray(m.element_ports, np.int32))
+    resp = np.ascontiguousarray(np.stack([response.real, response.imag], -1), np.float64)
+    bb = np.ascontiguousarray(np.stack([baseband.real, baseband.imag], -1), np.float64)
+    ctr = np.ascontiguousarray(m.center, np.float32)
+    w = np.zeros((n_el, 2))
+    scores = np.zeros(4)
+    lib.ref_host_crpa_weights.restype = None
+    lib.ref_host_crpa_weights(n_el, ports.ctypes.data_as(ip), np.ascontiguousarray(centers).ctypes.data_as(fp), n_em,
+                              np.ascontiguousarray(emitters).ctypes.data_as(fp), response.shape[1],
+                              resp.ctypes.data_as(dp), 1, ctr.ctypes.data_as(fp), C.c_float(24.0), C.c_float(1e-3),
+                              C.c_float(40.0), C.c_float(-20.0), int(m.setup["measured_steering"]), 1, int(blind),
+                              C.c_uint(7), C.c_float(40.0), bb.shape[0], bb.ctypes.data_as(dp), w.ctypes.data_as(dp),
+                              scores.ctypes.data_as(dp))
+    want_w = w[:, 0] + 1j * w[:, 1]
+    np.testing.assert_allclose(got["weights"], want_w, rtol=1e-9, atol=1e-12 * np.abs(want_w).max())
+    mine = [got["sinr_single_db"], got["sinr_steering_db"], got["sinr_mvdr_db"], got["satellite_gain_db"]]
+    np.testing.assert_allclose(mine, scores, rtol=0, atol=1e-9)
+
+
+def test_crpa_solver_equals_the_reference():
+    """Crpa.cpp:30-54 (Gaussian elimination with partial pivoting, singular pivots skipped) against
+    the package's solve, including a singular system."""
+    from em_lab_gb300 import crpa
+    lib = oracle.load_ref_host()
+    lib.ref_host_crpa_solve.restype = None
+    dp = C.POINTER(C.c_double)
+    rng = np.random.default_rng(3)
+    cases = [rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) for n in (1, 3, 6, 9)]
+    sing = cases[2].copy()
+    sing[:, 2] = 0.0
+    cases.append(sing)
+    for A in cases:
+        n = A.shape[0]
+        b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        x = np.zeros((n, 2))
+        Ap = np.ascontiguousarray(np.stack([A.real, A.imag], -1))
+        bp = np.ascontiguousarray(np.stack([b.real, b.imag], -1))
+        lib.ref_host_crpa_solve(Ap.ctypes.data_as(dp), bp.ctypes.data_as(dp), n, x.ctypes.data_as(dp))
+        want = x[:, 0] + 1j * x[:, 1]
+        got = crpa.solve(A.reshape(-1), b, n)
+        np.testing.assert_allclose(got, want, rtol=1e-10, atol=1e-12 * max(1.0, np.abs(want).max()))
