@@ -448,6 +448,11 @@ def run_learned(args):
                    "accuracy": strict["eval"].get("with_fallback"), "fallback_scenes": strict["eval"].get("fallback_scenes"),
                    "criterion": "p90 over scenes of band-median |dZ|/|Z| <= 2 % and of the S11 error <= 0.5 dB on "
                                 "validation runs; scenes above the ensemble-spread threshold run the plain solver"}
+    # what the learned path costs once, before any sweep: generating the training runs with the
+    # batched solver, and training the ensemble of the window in use (sweeps/hr excludes both)
+    for entry, key in ((head, head.get("window", out["chosen_window"])), (strict_line, out["chosen_window"])):
+        entry["one_time_cost_s"] = {"training_runs_generation": out["train_runs"]["wall_s"],
+                                    "ensemble_training": out["windows"][key]["training"]["wall_s"]}
     line = {
         "metric": "Z(f) sweeps/hr learned vs plain (held-out scenes)", "value": head["sweeps_per_hour"],
         "unit": "sweeps/hr", "n_gpus": 1, "steps": None, "warmup": args.warmup, "ms_per_step": None,
