@@ -98,7 +98,8 @@ def test_hertzian_dipole_directivity_power_and_flux(tmp_path):
     assert covers(settled(rec, "dbi"), 1.87, 0.005, 0.02)                          # D 1.87 dBi
     hp = settled(rec, "hpbw")
     assert all(h["xy"] >= 359.0 for h in hp)                                        # omni in azimuth
-    assert covers([h["xz"] for h in hp], 87.5, 0.05, 0.5) and covers([h["yz"] for h in hp], 87.5, 0.05, 0.5)
+    # the beamwidth is read from 1-degree cut samples: it moves in steps of about 0.25 deg
+    assert covers([h["xz"] for h in hp], 87.5, 0.05, 1.0) and covers([h["yz"] for h in hp], 87.5, 0.05, 1.0)
     assert covers(settled(rec, "P_rad"), 0.34876, 5e-6, 5e-4)                       # P_rad 0.34876
     assert covers(settled(rec, "flux_avg"), 0.355, 5e-4, 0.01)                     # flux <P> 0.355
 
