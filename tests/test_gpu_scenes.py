@@ -109,7 +109,7 @@ def test_dipole_04_port_impedance_and_power(tmp_path):
     rec = run_watch("04_dipole", 3000, tmp_path)
     z = settled(rec, "z")
     assert covers([v.real for v in z], 64.3, 0.05, 0.5) and covers([v.imag for v in z], -21.1, 0.05, 0.5)
-    assert covers(settled(rec, "acc"), 0.8937, 5e-5, 0.02)                 # P_acc 8.937e-01
+    assert covers(settled(rec, "acc"), 0.8937, 1e-4, 0.02)                 # P_acc 8.937e-01 (to one unit)
     assert all(round(a, 4) == 0.9418 for a in settled(rec, "avail"))       # of 9.418e-01 available
 
 
