@@ -548,21 +548,23 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1)
         }
         prod[5] = issued;
     };
-    // every warp waits for the loads it reads itself, at the top of each plane: the per-plane barrier
-    // then carries no copy latency, and a warp's E phase overlaps the copies the next plane needs.
-    // The leader records the newest load it has seen complete in prod[6].
-    auto ready = [&](int j) -> bool {  // bounded wait for load j
-        const bool ok = mbar_wait(bars + j % S_, (j / S_) & 1, a.wait_polls);
-        if (leader && ok && j > prod[6]) prod[6] = j;
+    auto wait_upto = [&](int last) {  // false if a load did not complete within the bound
+        int waited = prod[6];
+        bool ok = true;
+        while (ok && waited < last) {
+            ++waited;
+            ok = mbar_wait(bars + waited % S_, (waited / S_) & 1, a.wait_polls);
+        }
+        prod[6] = waited;
         return ok;
     };
     // on an expired wait: record the error, then give every copy still in flight a bounded time to
-    // land before the CTA leaves and its shared memory goes: loads prod[6] + 1 .. prod[5] - 1 (the
-    // last issued) are not known to be complete.
+    // land before the CTA leaves and its shared memory goes. prod[6] is the load whose wait ran out
+    // (not complete), prod[5] - 1 the last load issued.
     auto bail = [&]() {
         if (leader) {
             atomicOr(err, 1u);
-            for (int w = prod[6] + 1; w < prod[5]; ++w) mbar_wait(bars + w % S_, (w / S_) & 1);
+            for (int w = prod[6] < 0 ? 0 : prod[6]; w < prod[5]; ++w) mbar_wait(bars + w % S_, (w / S_) & 1);
         }
     };
 
@@ -578,6 +580,11 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1)
     if (leader) {
         p_seek();
         issue_upto(S_ - 1);
+        failed = !wait_upto(1);  // the first iteration reads loads 0 and 1
+    }
+    if (__syncthreads_or(failed)) {
+        bail();
+        return;
     }
 
     constexpr int EPF = Lay::EP / 4, BPF = Lay::BP / 4, W = Lay::W, SBC = (TY + 1) * W;
@@ -639,10 +646,7 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1)
             const long long off = (long long)z * a.plane + row_off;
             float2 e0x = make_float2(0.0f, 0.0f), e0y = e0x, e0z = e0x, bx = e0x, by = e0x, bz = e0x;
             unsigned ca = 0, cb = 0;
-            failed = !ready(k) || !ready(k + 1);  // this plane and the z+1 plane
-            if (failed) {
-                // nothing read: the barrier below sends every warp to bail()
-            } else if (!ctl) {
+            if (!ctl) {
                 // update_B.comp:35-67 for both cells (halo values beyond the grid are TMA zeros)
                 e0x = *reinterpret_cast<const float2*>(Es + me);
                 e0y = *reinterpret_cast<const float2*>(Es + EPF + me);
@@ -715,6 +719,11 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1)
                     sb[SBC + ce] = hby;
                     sb[2 * SBC + ce] = hbz;
                 }
+            }
+            // the next iteration reads loads k+1, k+2 (or k+2, k+3 at the start of the next item)
+            if (leader) {  // at the last plane the next item was taken when its first load was issued
+                const int need = z + 1 < ze ? k + 2 : (queue[(ord + 1) & 7] < 0 ? -1 : k + 3);
+                if (need >= 0) failed = !wait_upto(need);
             }
             if (__syncthreads_or(failed)) {
                 bail();
