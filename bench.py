@@ -409,11 +409,12 @@ def run_batched(args):
 
 
 def run_learned(args):
-    """--workload learned: the learned ring-down extrapolator (BASELINE config 4 shapes). Training
+    """--workload learned: the learned ring-down extrapolator. Training
     runs of the batched generator's scenes (seed --seed) to -60 dB ring-down, training on the GPU
     with this library's kernels, then on held-out scenes (seed --seed + 1): sweeps/hr of the plain
-    solver to ring-down (the reference result) against the learned path (early window + inference), and the
-    |dZ| and S11 error of the network and of the early window's truncated DFT."""
+    solver to ring-down (the reference result) against the learned path (early window + inference), the
+    |dZ| and S11 error of the network and of the early window's truncated DFT, and the same for the
+    32-frequency far-field spectra (directivity and radiated energy, dB)."""
     import torch
     from em_lab_gb300 import extrap, launch_count
 
@@ -438,6 +439,8 @@ def run_learned(args):
     net_key = out["chosen_window_network_only"]
     if net_key is not None:
         head = dict(out["windows"][net_key]["network_only"], window=net_key, accuracy=out["windows"][net_key]["eval"]["network"],
+                    accuracy_far_field=out["windows"][net_key]["eval"]["network_far"],
+                    truncated_far_field=out["windows"][net_key]["eval"]["truncated_dft_far"],
                     criterion="median over scenes of band-median |dZ|/|Z| <= 2 % and S11 error <= 0.5 dB "
                               "(checked on validation runs)")
     else:
@@ -446,6 +449,7 @@ def run_learned(args):
                    "speedup_vs_batched_plain": strict["speedup_vs_batched_plain"],
                    "speedup_vs_single_plain": strict.get("speedup_vs_single_plain"),
                    "accuracy": strict["eval"].get("with_fallback"), "fallback_scenes": strict["eval"].get("fallback_scenes"),
+                   "accuracy_far_field": strict["eval"].get("with_fallback_far"),
                    "criterion": "p90 over scenes of band-median |dZ|/|Z| <= 2 % and of the S11 error <= 0.5 dB on "
                                 "validation runs; scenes above the ensemble-spread threshold run the plain solver"}
     # what the learned path costs once, before any sweep: generating the training runs with the
@@ -461,7 +465,10 @@ def run_learned(args):
         "config": {"workload": f"learned ring-down extrapolator: {args.train_scenes} training scenes (seed {args.seed}; "
                                f"{args.val_frac:g} of them held for the fallback threshold), {args.scenes} held-out "
                                f"scenes (seed {args.seed + 1}), early windows {','.join(f'{p:g}' for p in periods)} "
-                               f"design periods, ensembles of {args.members}, {args.epochs} epochs",
+                               f"design periods, ensembles of {args.members}, {args.epochs} epochs; inputs: early port "
+                               f"V, I and 32 surface-DFT channels (the Huygens box's far-field spectra over the early "
+                               f"window); outputs: Z(f) at 128 frequencies and the 32-frequency far-field spectra "
+                               f"(directivity, radiated energy)",
                    "plain_reference": "batched stacks and one SimulationGrid per scene, each run to -60 dB ring-down"},
         "headline": head, "strict": strict_line, "plain": out["plain"], "windows": windows,
         "train_runs": out["train_runs"], "gpu_launches": int(launch_count() - l0), "clocks": clk.summary(),
@@ -471,7 +478,7 @@ def run_learned(args):
 
 
 def run_phased(args):
-    """--workload phased_array: BASELINE config 5 shapes. 16 x 16 dipoles at half-wavelength pitch
+    """--workload phased_array: 16 x 16 dipoles at half-wavelength pitch
     (lambda 24 cells) a quarter wavelength over a ground sheet under a radome slab (eps_r 3.5, 6
     cells), 384 x 384 x 256 cells with a 12-cell absorber, 50-ohm feeds with a Taylor taper and
     true-time-delay steering to 8 seeded directions (8 scenes); the 32-frequency tensor-core

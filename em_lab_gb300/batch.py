@@ -38,6 +38,7 @@ class SceneResult:
     wall_s: float = 0.0
     sweep: dict | None = None
     accepted: bool = False  # stopped at its decision step (BatchRunner decide): no sweep of its own
+    far: dict = field(default_factory=dict)  # far-field spectra by step (BatchRunner far_field)
 
 
 def sweep_sums(series: np.ndarray, lambda_min: float, lambda_max: float, points: int, dt: float) -> np.ndarray:
@@ -80,6 +81,53 @@ def scene_sweep(sc, series: np.ndarray, dt: float):
     sums = sweep_sums(series, sw["wavelength_min"], sw["wavelength_max"], int(sw["points"]), dt)
     z0 = float(sc.ports[0].impedance_ohm) if sc.ports else 50.0
     return impedance(sums, sw["wavelength_min"], sw["wavelength_max"], z0)
+
+
+class FarField:
+    """The far-field spectra a batched run records per scene: a Huygens box just inside the scene's
+    absorber (FarFieldMonitor::configure's box, FarField.cpp:126-174) with the multi-frequency DFT
+    at `nf` frequencies uniform in 1/lambda over the scene's port sweep band, evaluated over a fixed
+    grid of directions (polar angle 5..175 deg and azimuth 0..350 deg in 10-degree steps, plus the
+    poles). A scene's spectra are, per frequency, the largest directivity over those directions in
+    dBi (D = k^2 |N_perp - r x L|^2 / (8 pi P), FarField.cpp:198-217) and the radiated energy
+    10 log10(P_sum / lambda0^2) dB, P_sum the radiated power of the unscaled DFT sums: the energy
+    the pulse has radiated at that frequency, over the square of the design wavelength (the feed's
+    pulse lasts a fixed number of periods, so its energy spectrum scales with lambda0^2)."""
+
+    def __init__(self, nf: int = 32, block: int = 64):
+        self.nf = int(nf)
+        self.block = int(block)  # samples per fold: 64 keeps the per-node time block small
+        th = np.radians(np.arange(5.0, 180.0, 10.0))
+        ph = np.radians(np.arange(0.0, 360.0, 10.0))
+        t, p = np.meshgrid(th, ph, indexing="ij")
+        d = np.stack([np.sin(t) * np.cos(p), np.sin(t) * np.sin(p), np.cos(t)], axis=-1).reshape(-1, 3)
+        self.dirs = np.concatenate([d, [[0.0, 0.0, 1.0], [0.0, 0.0, -1.0]]]).astype(np.float32)
+
+    def wavelengths(self, sc):
+        sw = sc.sweep
+        nu_lo = 1.0 / max(sw["wavelength_max"], sw["wavelength_min"])
+        nu_hi = 1.0 / min(sw["wavelength_max"], sw["wavelength_min"])
+        return 1.0 / (nu_lo + (nu_hi - nu_lo) * np.arange(self.nf) / max(self.nf - 1, 1))
+
+    @staticmethod
+    def box(sc, z0: int = 0):
+        """The scene's Huygens box in stack coordinates (its first plane at z0)."""
+        n, L = sc.grid.size, int(sc.grid.pml_thickness)
+        return [L + 1, L + 1, z0 + L + 1, n[0] - L - 2, n[1] - L - 2, z0 + n[2] - L - 2]
+
+    def spectra(self, sc, out: np.ndarray, samples: int):
+        """(D_max dBi, radiated energy dB) per frequency from an evaluation (nf, dirs, 2) of the sums
+        scaled by 2 / samples."""
+        wl = self.wavelengths(sc)
+        k = 2.0 * math.pi / wl
+        P = out[:, 0, 1].astype(np.float64)
+        F2 = out[:, :, 0].astype(np.float64).max(axis=1)
+        ok = P > 1e-30
+        d = np.where(ok, k * k * F2 / (8.0 * math.pi * np.where(ok, P, 1.0)), 0.0)
+        dbi = np.where(d > 1e-12, 10.0 * np.log10(np.maximum(d, 1e-300)), -120.0)
+        energy = P * (0.5 * samples) ** 2 / float(sc.wavelength) ** 2
+        db = np.where(energy > 1e-30, 10.0 * np.log10(np.maximum(energy, 1e-300)), -300.0)
+        return np.stack([dbi, db]).astype(np.float32)
 
 
 def residual(v: np.ndarray) -> float:
@@ -164,7 +212,7 @@ def autotune_tiling(grid, modes=TILINGS, steps=4):
 
 
 class _Group:
-    def __init__(self, scenes, indices, chunk, tune=True):
+    def __init__(self, scenes, indices, chunk, tune=True, far=None):
         self.indices = list(indices)  # scene indices into the batch, in stack order
         self.scenes = [scenes[i] for i in indices]
         first = self.scenes[0]
@@ -178,6 +226,11 @@ class _Group:
         self.chunk = chunk
         self.stack.set_graph(chunk)  # each chunk replays one captured graph of its launches
         self.attach_ports()
+        self.far = far
+        if far is not None:
+            z0, _ = self.stack.layout()
+            self.stack.ntff_dft_configure_boxes([far.box(sc, z) for sc, z in zip(self.scenes, z0)],
+                                                far.wavelengths(first), block=far.block)
 
     def attach_ports(self):
         z0, _ = self.stack.layout()
@@ -188,8 +241,13 @@ class _Group:
                                   int(p.edges), 1 if p.sign >= 0 else -1))
         self.stack.ports_configure(ports, self.scenes[0].wavelength, 4.0, False, self.chunk)
 
+    def far_spectra(self, k: int):
+        """The far-field spectra of the stack's scene k now."""
+        _, samples = self.stack.ntff_dft_info()
+        return self.far.spectra(self.scenes[k], self.stack.ntff_dft_spectra(k, self.far.dirs), samples)
+
     def compact(self, keep):
-        self.stack.compact(keep)
+        self.stack.compact(keep)  # the far-field boxes of the kept scenes keep their sums
         self.indices = [i for i, k in zip(self.indices, keep) if k]
         self.scenes = [s for s, k in zip(self.scenes, keep) if k]
         self.attach_ports()
@@ -199,13 +257,15 @@ class BatchRunner:
     """Steps `scenes` (each with one feed port) to port ring-down in stacks grouped by cross-section."""
 
     def __init__(self, scenes, chunk: int = 64, max_steps: int = 200_000, compact_fraction: float = 0.25,
-                 stop_steps=None, tune: bool = True, decide_at=None, decide=None):
+                 stop_steps=None, tune: bool = True, decide_at=None, decide=None, far_field=None, snap_at=None):
         """stop_steps: per scene, stop after this many steps without waiting for the ring-down (the
         early window of a learned extrapolation); None: run every scene to ring-down.
         decide_at / decide: once scene i has run decide_at[i] steps (at a chunk boundary) without
-        ringing down, decide(indices, series) is called for the scenes of a stack that reached it in
+        ringing down, decide(indices, series[, spectra]) is called for the scenes of a stack that reached it in
         the same chunk (under the runner's lock) and returns one flag per scene: True stops the scene
-        there (result.accepted), False lets it run on to ring-down from where it is."""
+        there (result.accepted), False lets it run on to ring-down from where it is.
+        far_field: a FarField; every scene then records its far-field spectra (result.far[step]) when
+        it is done and, with snap_at (per scene, a list of steps), at each of those steps on the way."""
         for sc in scenes:
             if not sc.ports:
                 raise ValueError(f"{sc.name}: a batched scene needs a feed port")
@@ -213,13 +273,19 @@ class BatchRunner:
         self.chunk = int(chunk)
         self.max_steps = int(max_steps)
         self.compact_fraction = float(compact_fraction)
+        self.far = far_field
+        if far_field is not None and decide_at is not None:  # decide() sees the decision step's spectra
+            snap_at = [list(a) + [d] for a, d in zip(snap_at or [[]] * len(self.scenes), decide_at)]
+        self.snap_at = [sorted(set(int(v) for v in a)) for a in snap_at] if snap_at is not None else None
         groups = {}
         for i, sc in enumerate(self.scenes):
             key = (sc.grid.size[0], sc.grid.size[1], sc.grid.pml_thickness, float(sc.grid.courant),
                    float(sc.grid.pml_sigma_max), float(sc.grid.pml_grading))
+            if far_field is not None:  # the boxes of one stack share the DFT frequencies
+                key += tuple(float(v) for v in far_field.wavelengths(sc))
             groups.setdefault(key, []).append(i)
         t0 = time.perf_counter()
-        self.groups = [_Group(self.scenes, idx, self.chunk, tune) for _, idx in
+        self.groups = [_Group(self.scenes, idx, self.chunk, tune, far_field) for _, idx in
                        sorted(groups.items(), key=lambda kv: kv[0])]
         self.setup_s = time.perf_counter() - t0
         self.results = [SceneResult(i) for i in range(len(self.scenes))]
@@ -246,6 +312,10 @@ class BatchRunner:
             for marks in (self.stop_steps, None if self.decide_at is None or self.decided[i] else self.decide_at):
                 if marks is not None and marks[i] > r.steps:
                     n = min(n, marks[i] - r.steps)
+            if self.snap_at is not None:
+                later = [v for v in self.snap_at[i] if v > r.steps]
+                if later:
+                    n = min(n, later[0] - r.steps)
         return n
 
     def _run_group(self, g, t0, on_done, lock):
@@ -266,6 +336,8 @@ class BatchRunner:
                     continue
                 r.series.append(ser[:, k].copy())
                 r.steps += ser.shape[0]
+                if self.snap_at is not None and r.steps in self.snap_at[i]:
+                    r.far[r.steps] = g.far_spectra(k)
                 # the ring-down watch concludes only at whole chunks, as in a run without stop or
                 # decision steps; a stop step ends the scene wherever it falls
                 fed = self.watch[i].feed(ser[:, k, 0])
@@ -275,12 +347,17 @@ class BatchRunner:
                     r.wall_s = time.perf_counter() - t0
                     sc = self.scenes[i]
                     r.sweep = scene_sweep(sc, np.concatenate(r.series), float(sc.grid.courant))
+                    if g.far is not None and r.steps not in r.far:
+                        r.far[r.steps] = g.far_spectra(k)
                     finished.append(i)
             pending = [i for i in g.indices if self.decide_at is not None and not self.results[i].done
                        and not self.decided[i] and self.results[i].steps >= self.decide_at[i]]
             with lock:
                 if pending:
-                    flags = self.decide(pending, [np.concatenate(self.results[i].series) for i in pending])
+                    args = (pending, [np.concatenate(self.results[i].series) for i in pending])
+                    if self.far is not None:
+                        args += ([self.results[i].far.get(self.decide_at[i]) for i in pending],)
+                    flags = self.decide(*args)
                     for i, stop in zip(pending, flags):
                         self.decided[i] = True
                         if stop:
@@ -327,9 +404,10 @@ class BatchRunner:
             g.stack.close()
 
 
-def run_single(sc, chunk: int = 64, max_steps: int = 200_000, timing: dict | None = None):
+def run_single(sc, chunk: int = 64, max_steps: int = 200_000, timing: dict | None = None, far_field=None):
     """One scene on its own SimulationGrid to the same ring-down rule: (series (steps, 2), sweep).
-    `timing`, if given, receives the set-up and the stepping wall-clock seconds and the steps."""
+    `timing`, if given, receives the set-up and the stepping wall-clock seconds and the steps. With a
+    FarField the grid carries its Huygens box and sweep["far"] holds the spectra at the end."""
     t0 = time.perf_counter()
     g = SimulationGrid(sc.grid)
     m = sc.materials
@@ -337,6 +415,8 @@ def run_single(sc, chunk: int = 64, max_steps: int = 200_000, timing: dict | Non
     g.set_sources(sc.sources)
     g.ports_configure([sc.ports[0].to_c()], sc.wavelength, 4.0, False, chunk)
     g.set_graph(chunk)
+    if far_field is not None:
+        g.ntff_dft_configure_boxes([far_field.box(sc)], far_field.wavelengths(sc), block=far_field.block)
     g.synchronize()
     t1 = time.perf_counter()
     dt = float(sc.grid.courant)
@@ -352,6 +432,8 @@ def run_single(sc, chunk: int = 64, max_steps: int = 200_000, timing: dict | Non
             break
     series = np.concatenate(parts)
     sweep = scene_sweep(sc, series, dt)
+    if far_field is not None:
+        sweep["far"] = far_field.spectra(sc, g.ntff_dft_spectra(0, far_field.dirs), g.ntff_dft_info()[1])
     t2 = time.perf_counter()
     g.close()
     if timing is not None:

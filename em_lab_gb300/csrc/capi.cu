@@ -279,7 +279,8 @@ constexpr int kDftCoreBlock = 64;  // samples per CUDA-core fold (that kernel's 
 // Samples per time block of the engine in use: the tensor-core fold takes up to four 64-sample
 // chunks per launch (dft_tc_block), the CUDA-core fold 64.
 int dft_block(const emlab_grid* g) {
-    return g->dft_engine == EMLAB_DFT_TENSOR ? dft_tc_block(g->dft_nf) : kDftCoreBlock;
+    const int b = g->dft_engine == EMLAB_DFT_TENSOR ? dft_tc_block(g->dft_nf) : kDftCoreBlock;
+    return g->dft_block_cap > 0 ? std::min(b, g->dft_block_cap) : b;
 }
 
 // Folds the samples gathered so far into the FP64 sums.
@@ -660,7 +661,8 @@ int emlab_grid_step(emlab_grid* g, int count) {
             g_launches += enqueue_step(g, k, false, d_sig, d_prot, d_nrot, d_lrot, d_bl, rec, ev0, ev1);
             if (g->dft_on) {
                 if (g->dft_t == 0) g->dft_n0 = (long long)g->step;  // time index of the block's first sample
-                launch_dft_sample(monitor_args(g), g->d_dft_box.p, g->dft_points, g->d_dft_blk.p, g->dft_t, g->stream);
+                launch_dft_sample(monitor_args(g), g->d_dft_box.p, g->dft_nbox, g->dft_box_max, g->dft_points,
+                                  g->d_dft_blk.p, g->dft_t, g->stream);
                 g_launches += 1;
                 if (++g->dft_t == dft_block(g)) dft_fold(g);
             }
@@ -1030,37 +1032,35 @@ int emlab_ntff_evaluate(emlab_grid* g, const float* directions, int n_dirs, floa
     return EMLAB_OK;
 }
 
-// ---- multi-frequency far-field DFT ------------------------------------------------------------
-int emlab_ntff_dft_configure(emlab_grid* g, const int box_min[3], const int box_max[3], const float* wavelengths,
-                             int n_freq, int box_out[6]) {
-    if (int rc = require_grid(g)) return rc;
-    EMLAB_CUDA(cudaSetDevice(g->device));
-    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
-    invalidate_graphs(g);
-    g->dft_on = false;
-    g->d_dft_x.release(), g->d_dft_blk.release();
-    if (n_freq <= 0) return EMLAB_OK;
-    EMLAB_REQUIRE(box_min && box_max && wavelengths, "null DFT argument");
-    EMLAB_REQUIRE(n_freq <= 128, "at most 128 DFT frequencies");
-    const int n[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
-    const int L = g->cfg.pml_thickness;
-    int* b = g->dft_box;
-    for (int a = 0; a < 3; ++a) {
-        const int lo = L + 1, hi = n[a] - L - 2;
-        b[a] = std::clamp(std::min(box_min[a], box_max[a]), lo, hi);
-        b[3 + a] = std::clamp(std::max(box_min[a], box_max[a]), lo, hi);
-        if (b[3 + a] - b[a] < 4)
-            return fail(EMLAB_ERR_INVALID, "far-field DFT box is degenerate after clamping to the region inside the "
-                                           "absorbing layer");
-        if (box_out) box_out[a] = b[a], box_out[3 + a] = b[3 + a];
+// ---- multi-frequency far-field DFT ----------------------------------------------------------------
+namespace {
+// Attaches the far-field DFT to `nbox` boxes (6 ints each, min xyz and max xyz, already checked):
+// box records with their face offsets and their places in the concatenated point list, twiddles,
+// zeroed sums and the time block.
+int dft_setup(emlab_grid* g, const int* boxes, int nbox, const float* wavelengths, int n_freq, int block_cap) {
+    g->dft_boxes.assign((size_t)nbox * kDftBoxInts, 0);
+    long long total = 0;
+    int largest = 0;
+    for (int k = 0; k < nbox; ++k) {
+        int* b = g->dft_boxes.data() + (size_t)k * kDftBoxInts;
+        for (int a = 0; a < 6; ++a) b[a] = boxes[6 * k + a];
+        b[6] = 0;
+        for (int f = 0; f < 6; ++f) {
+            const int a = f >> 1, u = a == 0 ? 1 : 0, v = a == 2 ? 1 : 2;
+            b[7 + f] = b[6 + f] + (b[3 + u] - b[u] + 1) * (b[3 + v] - b[v] + 1);
+        }
+        b[13] = (int)total;
+        b[14] = b[12];
+        total += b[12];
+        largest = std::max(largest, b[12]);
     }
-    b[6] = 0;
-    for (int f = 0; f < 6; ++f) {
-        const int a = f >> 1, u = a == 0 ? 1 : 0, v = a == 2 ? 1 : 2;
-        b[7 + f] = b[6 + f] + (b[3 + u] - b[u] + 1) * (b[3 + v] - b[v] + 1);
-    }
-    g->dft_points = b[12];
+    EMLAB_REQUIRE(total < (1ll << 28), "far-field DFT boxes have too many points");
+    g->dft_nbox = nbox;
+    g->dft_box_max = largest;
+    g->dft_points = (int)total;
     g->dft_nf = n_freq;
+    g->dft_block_cap = block_cap;
+    g->dft_wl.assign(wavelengths, wavelengths + n_freq);
     g->dft_omega.assign((size_t)n_freq, 0.0);
     std::vector<float2> w((size_t)n_freq * kDftCoreBlock);
     const double dt = (double)g->cfg.courant;
@@ -1071,8 +1071,8 @@ int emlab_ntff_dft_configure(emlab_grid* g, const int box_min[3], const int box_
             w[(size_t)f * kDftCoreBlock + k] = make_float2((float)std::cos(ph), (float)-std::sin(ph));
         }
     }
-    EMLAB_CUDA(g->d_dft_box.alloc(13));
-    EMLAB_CUDA(cudaMemcpy(g->d_dft_box.p, b, 13 * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(g->d_dft_box.alloc(g->dft_boxes.size()));
+    EMLAB_CUDA(cudaMemcpy(g->d_dft_box.p, g->dft_boxes.data(), g->dft_boxes.size() * 4, cudaMemcpyHostToDevice));
     EMLAB_CUDA(g->d_dft_w.alloc(w.size()));
     EMLAB_CUDA(cudaMemcpy(g->d_dft_w.p, w.data(), w.size() * 8, cudaMemcpyHostToDevice));
     EMLAB_CUDA(g->d_dft_omega.alloc((size_t)n_freq));
@@ -1083,14 +1083,68 @@ int emlab_ntff_dft_configure(emlab_grid* g, const int box_min[3], const int box_
     EMLAB_CUDA(g->d_dft_blo.alloc(blo.size()));
     EMLAB_CUDA(cudaMemcpy(g->d_dft_bhi.p, bhi.data(), bhi.size() * 4, cudaMemcpyHostToDevice));
     EMLAB_CUDA(cudaMemcpy(g->d_dft_blo.p, blo.data(), blo.size() * 4, cudaMemcpyHostToDevice));
-    // room for the longer of the two engines' blocks (the engine may change between folds)
-    const int block = std::max(kDftCoreBlock, dft_tc_block(n_freq));
+    // room for the longer of the two engines' blocks (the engine may change between folds), or the cap
+    const int block = block_cap > 0 ? block_cap : std::max(kDftCoreBlock, dft_tc_block(n_freq));
     EMLAB_CUDA(g->d_dft_blk.alloc((size_t)block * 6 * g->dft_points));
     EMLAB_CUDA(g->d_dft_x.alloc((size_t)n_freq * g->dft_points * 12));
     EMLAB_CUDA(cudaMemset(g->d_dft_x.p, 0, g->d_dft_x.n * 8));
     g->dft_t = 0, g->dft_samples = 0;
     g->dft_on = true;
     return EMLAB_OK;
+}
+
+int dft_detach(emlab_grid* g) {
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    invalidate_graphs(g);
+    g->dft_on = false;
+    g->dft_nbox = 0, g->dft_points = 0;
+    g->d_dft_x.release(), g->d_dft_blk.release();
+    return EMLAB_OK;
+}
+}  // namespace
+
+int emlab_ntff_dft_configure(emlab_grid* g, const int box_min[3], const int box_max[3], const float* wavelengths,
+                             int n_freq, int box_out[6]) {
+    if (int rc = require_grid(g)) return rc;
+    if (int rc = dft_detach(g)) return rc;
+    if (n_freq <= 0) return EMLAB_OK;
+    EMLAB_REQUIRE(box_min && box_max && wavelengths, "null DFT argument");
+    EMLAB_REQUIRE(n_freq <= 128, "at most 128 DFT frequencies");
+    const int n[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+    const int L = g->cfg.pml_thickness;
+    int b[6];
+    for (int a = 0; a < 3; ++a) {
+        const int lo = L + 1, hi = n[a] - L - 2;
+        b[a] = std::clamp(std::min(box_min[a], box_max[a]), lo, hi);
+        b[3 + a] = std::clamp(std::max(box_min[a], box_max[a]), lo, hi);
+        if (b[3 + a] - b[a] < 4)
+            return fail(EMLAB_ERR_INVALID, "far-field DFT box is degenerate after clamping to the region inside the "
+                                           "absorbing layer");
+        if (box_out) box_out[a] = b[a], box_out[3 + a] = b[3 + a];
+    }
+    return dft_setup(g, b, 1, wavelengths, n_freq, 0);
+}
+
+int emlab_ntff_dft_configure_boxes(emlab_grid* g, const int* boxes, int n_boxes, const float* wavelengths,
+                                   int n_freq, int block) {
+    if (int rc = require_grid(g)) return rc;
+    if (int rc = dft_detach(g)) return rc;
+    if (n_freq <= 0 || n_boxes <= 0) return EMLAB_OK;
+    EMLAB_REQUIRE(boxes && wavelengths, "null DFT argument");
+    EMLAB_REQUIRE(n_freq <= 128, "at most 128 DFT frequencies");
+    EMLAB_REQUIRE(n_boxes <= 65535, "too many far-field DFT boxes");
+    EMLAB_REQUIRE(block == 0 || (block >= kDftCoreBlock && block <= dft_tc_block(n_freq) && block % kDftCoreBlock == 0),
+                  "DFT block must be 0 or a multiple of 64 up to the tensor-core fold's block");
+    const int n[3] = {g->cfg.nx, g->cfg.ny, g->cfg.nz};
+    for (int k = 0; k < n_boxes; ++k)
+        for (int a = 0; a < 3; ++a) {
+            const int lo = boxes[6 * k + a], hi = boxes[6 * k + 3 + a];
+            if (lo < 1 || hi > n[a] - 2 || hi - lo < 4)
+                return fail(EMLAB_ERR_INVALID, "far-field DFT box " + std::to_string(k) +
+                                                   " leaves the grid's interior or is degenerate (< 4 cells)");
+        }
+    return dft_setup(g, boxes, n_boxes, wavelengths, n_freq, block);
 }
 
 int emlab_ntff_dft_info(emlab_grid* g, int* points, uint64_t* samples) {
@@ -1134,6 +1188,7 @@ int emlab_ntff_dft_engine(emlab_grid* g, int engine) {
 int emlab_ntff_dft_evaluate(emlab_grid* g, int f, const float* directions, int n_dirs, float* out) {
     if (int rc = require_grid(g)) return rc;
     EMLAB_REQUIRE(g->dft_on && f >= 0 && f < g->dft_nf, "far-field DFT frequency out of range");
+    EMLAB_REQUIRE(g->dft_nbox == 1, "the DFT has several boxes: evaluate them one by one with emlab_ntff_dft_spectra");
     EMLAB_REQUIRE(directions && out && n_dirs > 0, "bad direction arguments");
     EMLAB_CUDA(cudaSetDevice(g->device));
     if (int rc = dft_fold(g)) return rc;
@@ -1170,6 +1225,7 @@ int emlab_ntff_dft_evaluate(emlab_grid* g, int f, const float* directions, int n
 int emlab_ntff_dft_evaluate_all(emlab_grid* g, const float* directions, int n_dirs, float* out) {
     if (int rc = require_grid(g)) return rc;
     EMLAB_REQUIRE(g->dft_on, "no far-field DFT attached");
+    EMLAB_REQUIRE(g->dft_nbox == 1, "the DFT has several boxes: evaluate them one by one with emlab_ntff_dft_spectra");
     EMLAB_REQUIRE(directions && out && n_dirs > 0, "bad direction arguments");
     EMLAB_CUDA(cudaSetDevice(g->device));
     if (int rc = dft_fold(g)) return rc;
@@ -1203,6 +1259,88 @@ int emlab_ntff_dft_evaluate_all(emlab_grid* g, const float* directions, int n_di
         for (int d = 1; d < n_dirs; ++d) out[((size_t)f * n_dirs + d) * 2 + 1] = 0.0f;
     return EMLAB_OK;
 }
+
+int emlab_ntff_dft_spectra(emlab_grid* g, int box, const float* directions, int n_dirs, float* out) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(g->dft_on, "no far-field DFT attached");
+    EMLAB_REQUIRE(box >= 0 && box < g->dft_nbox, "no such far-field DFT box");
+    EMLAB_REQUIRE(directions && out && n_dirs > 0 && n_dirs <= 8192, "bad direction arguments (1 to 8192 directions)");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    if (int rc = dft_fold(g)) return rc;
+    const uint64_t samples = g->dft_samples;
+    EMLAB_REQUIRE(samples > 0, "no far-field DFT samples yet");
+    const int* rec = g->dft_boxes.data() + (size_t)box * kDftBoxInts;
+    const int first = rec[13], points = rec[14];
+    const int slices = std::clamp((points + 4095) / 4096, 1, 64);
+    const size_t part = (size_t)g->dft_nf * n_dirs * slices * 4, outs = (size_t)g->dft_nf * n_dirs * 2;
+    // the scratch grows to the largest request and stays (no allocation in a steady loop)
+    if (g->d_spec_dirs.n < (size_t)n_dirs) EMLAB_CUDA(g->d_spec_dirs.alloc((size_t)n_dirs));
+    if (g->d_spec_part.n < part) EMLAB_CUDA(g->d_spec_part.alloc(part));
+    if (g->d_spec_out.n < outs) EMLAB_CUDA(g->d_spec_out.alloc(outs));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_spec_dirs.p, directions, (size_t)n_dirs * 16, cudaMemcpyHostToDevice, g->stream));
+    launch_ntff_spectra(g->d_dft_box.p + (size_t)box * kDftBoxInts, first, points, g->dft_points, g->d_dft_x.p,
+                        g->dft_nf, g->d_dft_omega.p, 2.0 / (double)samples, g->d_spec_dirs.p, n_dirs, slices,
+                        g->d_spec_part.p, g->stream);
+    launch_ntff_reduce_multi(g->d_spec_dirs.p, g->d_spec_part.p, n_dirs, slices, g->dft_nf, g->d_spec_out.p, g->stream);
+    g_launches += 2;
+    if (int rc = check_launch()) return rc;
+    EMLAB_CUDA(cudaMemcpyAsync(out, g->d_spec_out.p, outs * 4, cudaMemcpyDeviceToHost, g->stream));
+    if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    for (int f = 0; f < g->dft_nf; ++f)  // the radiated power is reported once per frequency (first direction)
+        for (int d = 1; d < n_dirs; ++d) out[((size_t)f * n_dirs + d) * 2 + 1] = 0.0f;
+    return EMLAB_OK;
+}
+
+}  // extern "C"
+
+int emlab::dft_carry_take(emlab_grid* g, const std::vector<int>& old_z0, const std::vector<int>& old_nz,
+                          const std::vector<int>& idx, const std::vector<int>& new_z0, DftCarry& c) {
+    c = DftCarry();
+    if (!g->dft_on) return EMLAB_OK;
+    if (int rc = dft_fold(g)) return rc;
+    for (int k = 0; k < g->dft_nbox; ++k) {
+        const int* b = g->dft_boxes.data() + (size_t)k * kDftBoxInts;
+        for (size_t j = 0; j < idx.size(); ++j) {
+            const int s = idx[j], z0 = old_z0[(size_t)s];
+            if (b[2] < z0 || b[5] >= z0 + old_nz[(size_t)s]) continue;  // the box lies inside scene s
+            const int shift = new_z0[j] - z0;
+            c.boxes.insert(c.boxes.end(), {b[0], b[1], b[2] + shift, b[3], b[4], b[5] + shift});
+            c.old_first.push_back(b[13]);
+        }
+    }
+    c.on = !c.old_first.empty();
+    c.wl = g->dft_wl;
+    c.old_points = g->dft_points;
+    c.block_cap = g->dft_block_cap;
+    c.engine = g->dft_engine;
+    c.samples = g->dft_samples;
+    std::swap(c.x.p, g->d_dft_x.p), std::swap(c.x.n, g->d_dft_x.n);  // the old sums stay alive for the gather
+    return EMLAB_OK;
+}
+
+int emlab::dft_carry_restore(emlab_grid* g, DftCarry& c) {
+    if (!c.on) return EMLAB_OK;
+    const int nbox = (int)c.old_first.size();
+    if (int rc = dft_setup(g, c.boxes.data(), nbox, c.wl.data(), (int)c.wl.size(), c.block_cap)) return rc;
+    g->dft_engine = c.engine;
+    std::vector<int> map((size_t)g->dft_points);
+    for (int k = 0; k < nbox; ++k) {
+        const int* b = g->dft_boxes.data() + (size_t)k * kDftBoxInts;
+        for (int i = 0; i < b[14]; ++i) map[(size_t)b[13] + i] = c.old_first[(size_t)k] + i;
+    }
+    DevBuf<int> d_map;
+    EMLAB_CUDA(d_map.alloc(map.size()));
+    EMLAB_CUDA(cudaMemcpyAsync(d_map.p, map.data(), map.size() * 4, cudaMemcpyHostToDevice, g->stream));
+    launch_dft_gather(c.x.p, c.old_points, d_map.p, g->dft_points, g->dft_nf, g->d_dft_x.p, g->stream);
+    ++g_launches;
+    if (int rc = check_launch()) return rc;
+    EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    g->dft_samples = c.samples;
+    g->dft_t = 0;
+    return EMLAB_OK;
+}
+
+extern "C" {
 
 // ---- probes and flux ----------------------------------------------------------------------
 int emlab_probe_gather(emlab_grid* g, const int* origins, int n_probes, float* out) {

@@ -116,8 +116,24 @@ void launch_port_residuals(const float* series, long long steps, int nports, dou
 void launch_sweep_sums(const float* series, long long steps, int nports, double nu_lo, double nu_hi, int points,
                        double dt, double* out, cudaStream_t s);
 void launch_check_finite(const MonitorArgs& m, unsigned* flag, cudaStream_t s);
-// multi-frequency far-field DFT: per-step sampling into a time block, FP64 fold of a block
-void launch_dft_sample(const MonitorArgs& m, const int* box, int points, float* blk, int t, cudaStream_t s);
+// multi-frequency far-field DFT: per-step sampling into a time block, FP64 fold of a block. A box
+// record is kDftBoxInts ints: min xyz, max xyz, seven face offsets (box-local point indices), the
+// box's first point in the concatenated point list, its point count.
+constexpr int kDftBoxInts = 16;
+void launch_dft_sample(const MonitorArgs& m, const int* boxes, int nbox, int box_max, int points, float* blk, int t,
+                       cudaStream_t s);
+// far-field spectra of one box (`points` nodes from point `first` of X's `total_points`) straight
+// from the DFT sums scaled by `scale`: per frequency the partial sums of the pattern over direction
+// chunks and surface slices, then the per-direction reduction (|N_perp - r x L|^2 and the radiated
+// power at direction 0), one launch each for all frequencies; out[(f * count + d) * 2 + {0, 1}]
+void launch_ntff_spectra(const int* box, int first, int points, int total_points, const double* X, int nf,
+                         const double* omega, double scale, const float4* dirs, int count, int slices,
+                         float4* partials, cudaStream_t s);
+void launch_ntff_reduce_multi(const float4* dirs, const float4* partials, int count, int slices, int nf, float* out,
+                              cudaStream_t s);
+// X_new[f][c][j] = X_old[f][c][map[j]] for the carried boxes of a stack compaction
+void launch_dft_gather(const double* x_old, int old_points, const int* map, int new_points, int nf, double* x_new,
+                       cudaStream_t s);
 void launch_dft_fold(const float* blk, int T, int points, int nf, const float2* W, const double* omega, long long n0,
                      double dt, double* X, cudaStream_t s);
 void launch_dft_to_phasor(const double* X, int points, int f, double scale, float* ph, cudaStream_t s);

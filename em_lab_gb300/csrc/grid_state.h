@@ -148,7 +148,13 @@ struct emlab_grid {
     float line_wl = 16.0f, line_avg = 4.0f;
     // multi-frequency far-field DFT
     bool dft_on = false;
-    int dft_box[13] = {};
+    // one or more Huygens boxes; box b is dft_boxes[kDftBoxInts * b + ...]: min xyz, max xyz, the
+    // seven face offsets (box-local point indices), its first point in the concatenated point list,
+    // its point count
+    std::vector<int> dft_boxes;
+    int dft_nbox = 0, dft_box_max = 0;  // boxes, the largest box's points
+    int dft_block_cap = 0;              // samples per fold at most (0: the engine's own block)
+    std::vector<float> dft_wl;          // wavelengths as configured (kept across stack compaction)
     int dft_points = 0, dft_nf = 0, dft_t = 0;
     long long dft_n0 = 0;
     uint64_t dft_samples = 0;
@@ -159,6 +165,9 @@ struct emlab_grid {
     DevBuf<float> d_dft_blk;
     DevBuf<float> d_dft_bhi, d_dft_blo;  // tensor-core twiddles (split hi/lo, MMA operand layout)
     int dft_engine = EMLAB_DFT_TENSOR;
+    // far-field spectra scratch (emlab_ntff_dft_spectra), grown on demand and kept
+    DevBuf<float4> d_spec_dirs, d_spec_part;
+    DevBuf<float> d_spec_out;
     // opt-in convolutional PML (cpml.cu): parameters, per-axis coefficient tables, slab psi arrays
     bool cpml_on = false;
     emlab_cpml cpml{};
@@ -206,4 +215,19 @@ int stack_commit(emlab_grid* g);
 int cpml_prepare(emlab_grid* g);
 int cpml_clear(emlab_grid* g);
 void launch_cpml(emlab_grid* g, const YeeArgs& a, bool wide, cudaStream_t s);
+// capi.cu: the far-field DFT across a stack compaction. dft_carry_take folds the partial block and
+// keeps the sums of the boxes that lie inside kept scenes (old scene idx[k] becomes scene k at
+// new_z0[k]); dft_carry_restore re-attaches those boxes at their new planes with their sums.
+struct DftCarry {
+    bool on = false;
+    std::vector<int> boxes;      // kept boxes, 6 ints each, in the new layout
+    std::vector<int> old_first;  // their first point in the old point list
+    std::vector<float> wl;
+    int old_points = 0, block_cap = 0, engine = 0;
+    uint64_t samples = 0;
+    DevBuf<double> x;
+};
+int dft_carry_take(emlab_grid* g, const std::vector<int>& old_z0, const std::vector<int>& old_nz,
+                   const std::vector<int>& idx, const std::vector<int>& new_z0, DftCarry& c);
+int dft_carry_restore(emlab_grid* g, DftCarry& c);
 }  // namespace emlab

@@ -312,16 +312,53 @@ __device__ __forceinline__ void sincos_reduced(float psi, float* s, float* c) {
     __sincosf(r, s, c);
 }
 
+// Surface sources of the fast pattern sums. PhasorSource: the stage-2 phasors of ntff_pattern.comp's
+// layout (8 float4 per point). DftSource: the far-field DFT sums of frequency f straight from X
+// ([f][c][i] complex FP64), scaled and rounded to FP32 as dft_to_phasor_kernel stages them, for a
+// box whose first point in X is `first`.
+struct PhasorSource {
+    const float4* ph;
+    float k;
+    __device__ float kw(int) const { return k; }
+    __device__ void load(int, int i, float4& eR, float4& eI, float4& hR, float4& hI) const {
+        const float4* s2 = ph + 8 * (long long)i + 4;
+        eR = s2[0], eI = s2[1], hR = s2[2], hI = s2[3];
+    }
+};
+struct DftSource {
+    const double* X;
+    long long total;
+    int first;
+    const double* omega;
+    double scale;
+    __device__ float kw(int f) const { return (float)omega[f]; }
+    __device__ void load(int f, int i, float4& eR, float4& eI, float4& hR, float4& hI) const {
+        const double2* x = reinterpret_cast<const double2*>(X) + (size_t)f * 6 * total + first + i;
+        double2 v[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v[c] = x[(size_t)c * total];
+        eR = make_float4((float)(v[0].x * scale), (float)(v[1].x * scale), (float)(v[2].x * scale), 0.0f);
+        eI = make_float4((float)(v[0].y * scale), (float)(v[1].y * scale), (float)(v[2].y * scale), 0.0f);
+        hR = make_float4((float)(v[3].x * scale), (float)(v[4].x * scale), (float)(v[5].x * scale), 0.0f);
+        hI = make_float4((float)(v[3].y * scale), (float)(v[4].y * scale), (float)(v[5].y * scale), 0.0f);
+    }
+};
+
 // The same sums as ntff_pattern_kernel for 256 directions per block (two per thread, sharing every
 // staged surface point), with sincos_reduced and explicit multiply-adds: the far-field DFT's
-// pattern over large angle grids.
-__global__ void __launch_bounds__(128) ntff_pattern_fast_kernel(const int* box, int points, const float4* ph,
+// pattern over large angle grids. blockIdx.z is the source's frequency; each frequency has its own
+// block of partials (count * slices * 4 float4).
+template <class Src>
+__global__ void __launch_bounds__(128) ntff_pattern_fast_kernel(const int* box, int points, Src src,
                                                                 const float4* dirs, int first, int count, int slices,
-                                                                float kw, float4* partials) {
+                                                                float4* partials) {
     __shared__ float4 sPos[128], sJr[128], sJi[128], sMr[128], sMi[128];
     __shared__ float sP[128];
     __shared__ int sbox[13];
     const int lid = threadIdx.x;
+    const int fq = blockIdx.z;
+    const float kw = src.kw(fq);
+    partials += (size_t)fq * count * slices * 4;
     if (lid < 13) sbox[lid] = box[lid];
     __syncthreads();
     const int local0 = blockIdx.x * 256 + lid, local1 = local0 + 128;
@@ -347,8 +384,8 @@ __global__ void __launch_bounds__(128) ntff_pattern_fast_kernel(const int* box, 
             int node[3];
             float n[3], w;
             ntff_point(sbox, i, node, n, w);
-            const float4* s2 = ph + 8 * (long long)i + 4;
-            const float4 eR = s2[0], eI = s2[1], hR = s2[2], hI = s2[3];
+            float4 eR, eI, hR, hI;
+            src.load(fq, i, eR, eI, hR, hI);
             sPos[lid] = make_float4((float)node[0] - cx, (float)node[1] - cy, (float)node[2] - cz, 0.0f);
 #define EMLAB_CROSS(A0, A1, A2, B0, B1, B2) \
     make_float4(A1 * B2 - B1 * A2, A2 * B0 - B2 * A0, A0 * B1 - B0 * A1, 0.0f)
@@ -412,9 +449,12 @@ __global__ void __launch_bounds__(128) ntff_pattern_fast_kernel(const int* box, 
     }
 }
 
-// ntff_reduce.comp:19-39
+// ntff_reduce.comp:19-39 (blockIdx.y: the frequency of a multi-frequency pattern, each with its own
+// partials and outputs)
 __global__ void ntff_reduce_kernel(const float4* dirs, const float4* partials, int first, int count, int slices,
                                    float* out) {
+    partials += (size_t)blockIdx.y * count * slices * 4;
+    out += (size_t)blockIdx.y * count * 2;
     const int local = blockIdx.x * blockDim.x + threadIdx.x;
     const int d = first + local;
     if (local >= count) return;
@@ -490,16 +530,20 @@ __global__ void finite_kernel(MonitorArgs m, unsigned* flag) {
 }
 
 // Multi-frequency far-field DFT, per step: the co-located E and H (field_sampling.glsl:17-32) of
-// every Huygens-box node into slot t of the time block, component-major: blk[(t * 6 + c) * P + i].
-__global__ void __launch_bounds__(256) dft_sample_kernel(MonitorArgs m, const int* box, int points, float* blk, int t) {
-    __shared__ int sbox[13];
-    if (threadIdx.x < 13) sbox[threadIdx.x] = box[threadIdx.x];
+// every Huygens-box node into slot t of the time block, component-major: blk[(t * 6 + c) * P + i],
+// P the points of all boxes, i = the box's first point + the node's index in its box. blockIdx.y is
+// the box.
+__global__ void __launch_bounds__(256) dft_sample_kernel(MonitorArgs m, const int* boxes, int points, float* blk,
+                                                         int t) {
+    __shared__ int sbox[kDftBoxInts];
+    if (threadIdx.x < kDftBoxInts) sbox[threadIdx.x] = boxes[(size_t)blockIdx.y * kDftBoxInts + threadIdx.x];
     __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= points) return;
+    const int local = blockIdx.x * blockDim.x + threadIdx.x;
+    if (local >= sbox[14]) return;
+    const int i = sbox[13] + local;
     int node[3];
     float n[3], w;
-    ntff_point(sbox, i, node, n, w);
+    ntff_point(sbox, local, node, n, w);
     float E[3], Hh[3];
     e_at_node(m, node[0], node[1], node[2], E[0], E[1], E[2]);
     b_at_node(m, node[0], node[1], node[2], Hh[0], Hh[1], Hh[2]);
@@ -561,6 +605,15 @@ __global__ void __launch_bounds__(128) dft_fold_kernel(const float* blk, int T, 
     }
 }
 
+// The sums of the boxes a stack compaction keeps, moved to their places in the shorter point list.
+__global__ void dft_gather_kernel(const double2* x_old, int old_points, const int* map, int new_points,
+                                  double2* x_new) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= new_points) return;
+    const size_t fc = blockIdx.y;
+    x_new[fc * new_points + j] = x_old[fc * old_points + map[j]];
+}
+
 // Stage-2 phasor layout of ntff_pattern.comp (PhasorPair, 8 float4 per node) from the DFT sums of
 // one frequency, scaled by `scale` (2 / samples turns a sum into the amplitude of a steady tone).
 __global__ void dft_to_phasor_kernel(const double* X, int points, int f, double scale, float4* ph) {
@@ -620,8 +673,21 @@ void launch_ntff_pattern(const int* box, int points, const float* phasors, const
 void launch_ntff_pattern_fast(const int* box, int points, const float* phasors, const float4* dirs, int first,
                               int count, int slices, float k, float4* partials, cudaStream_t s) {
     const dim3 grid((count + 255) / 256, slices);
-    ntff_pattern_fast_kernel<<<grid, 128, 0, s>>>(box, points, reinterpret_cast<const float4*>(phasors), dirs, first,
-                                                  count, slices, k, partials);
+    ntff_pattern_fast_kernel<<<grid, 128, 0, s>>>(box, points, PhasorSource{reinterpret_cast<const float4*>(phasors), k},
+                                                  dirs, first, count, slices, partials);
+}
+
+void launch_ntff_spectra(const int* box, int first, int points, int total_points, const double* X, int nf,
+                         const double* omega, double scale, const float4* dirs, int count, int slices,
+                         float4* partials, cudaStream_t s) {
+    const dim3 grid((count + 255) / 256, slices, nf);
+    ntff_pattern_fast_kernel<<<grid, 128, 0, s>>>(box, points, DftSource{X, total_points, first, omega, scale}, dirs,
+                                                  0, count, slices, partials);
+}
+
+void launch_ntff_reduce_multi(const float4* dirs, const float4* partials, int count, int slices, int nf, float* out,
+                              cudaStream_t s) {
+    ntff_reduce_kernel<<<dim3((count + 63) / 64, nf), 64, 0, s>>>(dirs, partials, 0, count, slices, out);
 }
 
 void launch_ntff_reduce(const float4* dirs, const float4* partials, int first, int count, int slices, float* out,
@@ -667,8 +733,15 @@ void launch_check_finite(const MonitorArgs& m, unsigned* flag, cudaStream_t s) {
     finite_kernel<<<152 * 8, 256, 0, s>>>(m, flag);
 }
 
-void launch_dft_sample(const MonitorArgs& m, const int* box, int points, float* blk, int t, cudaStream_t s) {
-    dft_sample_kernel<<<(points + 255) / 256, 256, 0, s>>>(m, box, points, blk, t);
+void launch_dft_sample(const MonitorArgs& m, const int* boxes, int nbox, int box_max, int points, float* blk, int t,
+                       cudaStream_t s) {
+    dft_sample_kernel<<<dim3((box_max + 255) / 256, nbox), 256, 0, s>>>(m, boxes, points, blk, t);
+}
+
+void launch_dft_gather(const double* x_old, int old_points, const int* map, int new_points, int nf, double* x_new,
+                       cudaStream_t s) {
+    dft_gather_kernel<<<dim3((new_points + 255) / 256, nf * 6), 256, 0, s>>>(
+        reinterpret_cast<const double2*>(x_old), old_points, map, new_points, reinterpret_cast<double2*>(x_new));
 }
 
 void launch_dft_fold(const float* blk, int T, int points, int nf, const float2* W, const double* omega, long long n0,

@@ -315,7 +315,7 @@ int emlab_stack_compact(emlab_grid* g, const unsigned char* keep) {
     DevBuf<uint8_t> old_cls;
     std::swap(old_fields.p, g->fields.p), std::swap(old_fields.n, g->fields.n);
     std::swap(old_cls.p, g->cls.p), std::swap(old_cls.n, g->cls.n);
-    const std::vector<int> old_z0 = s.z0;
+    const std::vector<int> old_z0 = s.z0, old_nz = s.nz;
     const long long old_padded = g->padded;
     const int old_cur = g->cur;
     std::vector<int> nz;
@@ -364,7 +364,12 @@ int emlab_stack_compact(emlab_grid* g, const unsigned char* keep) {
     refresh_tma(g);
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
     if (int rc = merge_sources(g)) return rc;
-    if (int rc = reset_monitors(g)) return rc;  // the caller re-attaches its ports at the new planes
+    // far-field DFT boxes inside kept scenes carry their sums over; the other monitors are reset
+    // and the caller re-attaches its ports at the new planes
+    DftCarry carry;
+    if (int rc = dft_carry_take(g, old_z0, old_nz, idx, s.z0, carry)) return rc;
+    if (int rc = reset_monitors(g)) return rc;
+    if (int rc = dft_carry_restore(g, carry)) return rc;
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
     return EMLAB_OK;
 }

@@ -1,16 +1,23 @@
-"""Learned ring-down extrapolator: predicts a scene's converged port impedance Z(f) from the first few
-periods of its port V(t), I(t), so an antenna sweep can stop each scene early.
+"""Learned ring-down extrapolator: predicts a scene's converged port impedance Z(f) and far-field
+spectra from the first few periods of its port V(t), I(t) and of its surface DFT, so an antenna
+sweep can stop each scene early.
 
 Network (every layer a GEMM on the tcgen05 tensor cores with BF16 operands and FP32 accumulation,
 csrc/learn.cu; FP32 master weights and Adam):
   encoder  conv1d 2 -> 32 channels (kernel 8, stride 4, pad 2, ReLU): 256 samples -> 64 positions
            conv1d 32 -> 64 channels (kernel 8, stride 4, pad 2, ReLU): 64 -> 16 positions
-  head     [1024 encoder features | 256 truncated-DFT features] -> 256 -> 256 -> 256 -> 256 (ReLU)
-           -> 256 outputs: Re, Im of Z(f) / 100 ohm at the 128 sweep frequencies.
+  head     [1024 encoder features | 256 truncated-DFT Z features | 64 surface-DFT features]
+           -> 256 -> 256 -> 256 -> 256 (ReLU)
+           -> 320 outputs: Re, Im of Z(f) / 100 ohm at the 128 sweep frequencies, then the far-field
+              spectra at the 32 surface-DFT frequencies: directivity (dBi / 10) and radiated energy
+              (dB / 10, batch.FarField).
 Inputs (host, from the early window of `PERIODS_IN` design periods): V and I resampled to 256
-points in units of the period (I scaled by eta0 / 100, both by the window's peak), and the "method
-without the network": Z_trunc(f) = -V(f) / I(f) * eta0 from the DFT of the early window alone.
-Targets: Z(f) of the whole series run to -60 dB ring-down (the plain solver is the reference result).
+points in units of the period (I scaled by eta0 / 100, both by the window's peak); the "method
+without the network": Z_trunc(f) = -V(f) / I(f) * eta0 from the DFT of the early window alone, and
+the far-field spectra of the Huygens box's DFT over the early window alone (32 surface-DFT channels:
+the directivity and the radiated energy at each frequency).
+Targets: Z(f) and the far-field spectra of the whole run to -60 dB ring-down (the plain solver is
+the reference result).
 PyTorch only allocates the device buffers and moves the batches; every forward and backward
 operation is a kernel of this library.
 """
@@ -22,23 +29,32 @@ import time
 
 import numpy as np
 
-from .batch import K_ETA0, sweep_sums
+from .batch import K_ETA0, FarField, sweep_sums
 from .grid import _check, load_library
 
 T_IN = 256             # resampled early-window samples per channel
 PERIODS_IN = 4.0       # early window, design periods
 NF = 128               # sweep frequencies
+NFF = 32               # far-field (surface-DFT) frequencies
 Z_SCALE = 100.0        # ohm per output unit
 Z_CLIP = 10.0          # feature / target clip (units of Z_SCALE)
+DB_SCALE = 10.0        # dB per far-field output unit
 I_SCALE = K_ETA0 / 100.0
+AUX = 2 * NF + 2 * NFF  # head inputs beside the encoder: truncated Z(f), truncated far-field spectra
+OUT = 2 * NF + 2 * NFF  # outputs: Z(f), far-field spectra
 
 CONV = [  # (name, c_in, c_out, kernel, stride, pad, L_in, L_out)
     ("conv1", 2, 32, 8, 4, 2, 256, 64),
     ("conv2", 32, 64, 8, 4, 2, 64, 16),
 ]
 ENC = CONV[-1][2] * CONV[-1][7]  # 1024 encoder features
-HEAD = [("fc1", ENC + 2 * NF, 256, True), ("fc2", 256, 256, True), ("fc3", 256, 256, True),
-        ("fc4", 256, 256, True), ("out", 256, 2 * NF, False)]
+HEAD = [("fc1", ENC + AUX, 256, True), ("fc2", 256, 256, True), ("fc3", 256, 256, True),
+        ("fc4", 256, 256, True), ("out", 256, OUT, False)]
+
+
+def far_field() -> FarField:
+    """The surface DFT the extrapolator reads and predicts: NFF frequencies over the sweep band."""
+    return FarField(NFF)
 
 
 def layer_shapes():
@@ -59,8 +75,9 @@ def init_params(seed: int = 0):
 
 
 # ---- features ------------------------------------------------------------------------------------
-def early_steps(sc) -> int:
-    return int(math.ceil(PERIODS_IN * sc.wavelength / float(sc.grid.courant)))
+def early_steps(sc, periods: float | None = None) -> int:
+    p = PERIODS_IN if periods is None else float(periods)
+    return int(math.ceil(p * sc.wavelength / float(sc.grid.courant)))
 
 
 def truncated_z(sc, series_early):
@@ -71,9 +88,15 @@ def truncated_z(sc, series_early):
     return impedance(sums, sw["wavelength_min"], sw["wavelength_max"], float(sc.ports[0].impedance_ohm))["z"]
 
 
-def features(sc, series):
-    """(x (T_IN, 2) float32 position-major, zt (2 NF,) float32, Z_trunc complex (NF,)) from the first
-    early_steps(sc) rows of a scene's (V, I) series."""
+def far_units(spec):
+    """Far-field spectra (2, NFF) (dBi, dB) -> 2 NFF network units (clipped)."""
+    return np.clip(np.asarray(spec, np.float64).reshape(-1) / DB_SCALE, -Z_CLIP, Z_CLIP).astype(np.float32)
+
+
+def features(sc, series, far_early):
+    """(x (T_IN, 2) float32 position-major, aux (AUX,) float32, Z_trunc complex (NF,)) from the first
+    early_steps(sc) rows of a scene's (V, I) series and the far-field spectra (2, NFF) of its
+    surface DFT over the same steps."""
     n = early_steps(sc)
     ser = np.asarray(series[:n], np.float64)
     if ser.shape[0] < n:
@@ -85,18 +108,25 @@ def features(sc, series):
     peak = max(np.abs(v).max(), np.abs(i).max(), 1e-30)
     x = np.stack([v / peak, i / peak], axis=1).astype(np.float32)
     zt = truncated_z(sc, ser.astype(np.float32))
-    zf = np.concatenate([np.clip(zt.real / Z_SCALE, -Z_CLIP, Z_CLIP), np.clip(zt.imag / Z_SCALE, -Z_CLIP, Z_CLIP)])
+    zf = np.concatenate([np.clip(zt.real / Z_SCALE, -Z_CLIP, Z_CLIP), np.clip(zt.imag / Z_SCALE, -Z_CLIP, Z_CLIP),
+                         far_units(far_early)])
     return x, zf.astype(np.float32), zt
 
 
-def target(z_conv):
+def target(z_conv, far_conv):
     return np.concatenate([np.clip(z_conv.real / Z_SCALE, -Z_CLIP, Z_CLIP),
-                           np.clip(z_conv.imag / Z_SCALE, -Z_CLIP, Z_CLIP)]).astype(np.float32)
+                           np.clip(z_conv.imag / Z_SCALE, -Z_CLIP, Z_CLIP), far_units(far_conv)]).astype(np.float32)
 
 
 def to_z(y):
     y = np.asarray(y, np.float64)
-    return (y[..., :NF] + 1j * y[..., NF:]) * Z_SCALE
+    return (y[..., :NF] + 1j * y[..., NF:2 * NF]) * Z_SCALE
+
+
+def to_far(y):
+    """Network outputs -> far-field spectra (..., 2, NFF): dBi, dB."""
+    y = np.asarray(y, np.float64)[..., 2 * NF:2 * NF + 2 * NFF] * DB_SCALE
+    return y.reshape(y.shape[:-1] + (2, NFF))
 
 
 # ---- device network --------------------------------------------------------------------------------
@@ -129,12 +159,12 @@ class Net:
         self.a1 = z(B * 64, 32, dt=bf16)
         self.cols2 = z(B * 16, 256, dt=bf16)
         self.z2 = z(B * 16, 64)
-        self.X0 = z(B, ENC + 2 * NF, dt=bf16)
+        self.X0 = z(B, ENC + AUX, dt=bf16)
         self.zh = {n: z(B, o) for n, i, o, _ in HEAD}
         self.ah = {n: z(B, o, dt=bf16) for n, i, o, r in HEAD if r}
         self.y = self.zh["out"]
-        self.t = z(B, 2 * NF)
-        self.dy = z(B, 2 * NF)
+        self.t = z(B, OUT)
+        self.dy = z(B, OUT)
         self.dz = {n: z(B, o) for n, i, o, _ in HEAD}
         self.dzb = {n: z(B, o, dt=bf16) for n, i, o, _ in HEAD}
         self.dx = {n: z(B, i) for n, i, o, _ in HEAD}
@@ -173,17 +203,17 @@ class Net:
                                           self._p(out) if out is not None else None, ldo, off, self.stream))
 
     def load(self, x, zt, t=None):
-        """A batch: x (n, T_IN, 2), zt (n, 2 NF), targets t (n, 2 NF) (float32 host arrays)."""
+        """A batch: x (n, T_IN, 2), head inputs zt (n, AUX), targets t (n, OUT) (float32 host arrays)."""
         torch = self.torch
         n = x.shape[0]
         assert n <= self.B
         self.n = n
         xs = torch.zeros((self.B, T_IN, 2), dtype=torch.float32, device=self.dev)
         xs[:n] = torch.from_numpy(np.ascontiguousarray(x, np.float32)).to(self.dev)
-        zs = torch.zeros((self.B, 2 * NF), dtype=torch.float32, device=self.dev)
+        zs = torch.zeros((self.B, AUX), dtype=torch.float32, device=self.dev)
         zs[:n] = torch.from_numpy(np.ascontiguousarray(zt, np.float32)).to(self.dev)
         self._conv(xs.view(self.B * T_IN, 2), self.x0.view(self.B * T_IN, 2))
-        self._conv(zs, self.X0, ldo=ENC + 2 * NF, cols=2 * NF, off=ENC)
+        self._conv(zs, self.X0, ldo=ENC + AUX, cols=AUX, off=ENC)
         self.t.zero_()
         if t is not None:
             self.t[:n] = torch.from_numpy(np.ascontiguousarray(t, np.float32)).to(self.dev)
@@ -198,7 +228,7 @@ class Net:
         _check(lib.emlab_nn_im2col(self._p(self.a1), B, c2[6], c2[1], c2[3], c2[4], c2[5], c2[7], self._p(self.cols2), s))
         self._gemm(B * 16, 64, 256, self.cols2, 256, 1, self.Wb["conv2"], 256, 1, self.z2, 64)
         # rows (b, l) of z2 are the encoder features of sample b at columns l * 64 + c
-        self._bias_act(self.z2, self.b["conv2"], B, ENC, True, self.X0, ENC + 2 * NF, 0, 64)
+        self._bias_act(self.z2, self.b["conv2"], B, ENC, True, self.X0, ENC + AUX, 0, 64)
         x = self.X0
         for name, i, o, relu in HEAD:
             self._gemm(B, o, i, x, i, 1, self.Wb[name], i, 1, self.zh[name], o)
@@ -215,7 +245,7 @@ class Net:
         self.loss.zero_()
         # only the loaded rows contribute: gradient rows beyond n are zero
         self.dy.zero_()
-        _check(lib.emlab_nn_mse(self._fp(self.y), self._fp(self.t), n * 2 * NF, self._fp(self.dy),
+        _check(lib.emlab_nn_mse(self._fp(self.y), self._fp(self.t), n * OUT, self._fp(self.dy),
                                 self._fp(self.loss), s))
         up = self.dy
         ins = {"fc1": self.X0}
@@ -231,7 +261,7 @@ class Net:
             up = self.dx[name]
         c1, c2 = CONV
         # conv2: dz2 over rows (b, l) x 64 channels = the encoder part of d(X0)
-        _check(lib.emlab_nn_act_grad(self._fp(up), ENC + 2 * NF, 0, self._fp(self.z2), B, ENC, 1, self._fp(self.dz2),
+        _check(lib.emlab_nn_act_grad(self._fp(up), ENC + AUX, 0, self._fp(self.z2), B, ENC, 1, self._fp(self.dz2),
                                      self._p(self.dz2b), s))
         self._gemm(64, 256, B * 16, self.dz2b, 1, 64, self.cols2, 1, 256, self.gW["conv2"], 256)
         _check(lib.emlab_nn_col_sum(self._fp(self.dz2), B * 16, 64, self._fp(self.gb["conv2"]), s))
@@ -263,7 +293,7 @@ class Net:
             self.forward()
             out.append(self.y[: self.n].cpu().numpy())
         self.status()
-        return np.concatenate(out) if out else np.zeros((0, 2 * NF), np.float32)
+        return np.concatenate(out) if out else np.zeros((0, OUT), np.float32)
 
     def params(self):
         return {n: (self.W[n].cpu().numpy(), self.b[n].cpu().numpy()) for n, _, _ in layer_shapes()}
@@ -343,55 +373,81 @@ def summary(z_pred, z_ref):
             "s11_db_p90": float(np.percentile(ds11, 90)), "scenes": int(rel.size)}
 
 
+def far_errors(f_pred, f_ref):
+    """Per-scene band medians of the far-field errors: |dD| (dB) and |d radiated energy| (dB)."""
+    f_pred, f_ref = np.asarray(f_pred, np.float64), np.asarray(f_ref, np.float64)
+    return np.median(np.abs(f_pred[:, 0] - f_ref[:, 0]), axis=1), np.median(np.abs(f_pred[:, 1] - f_ref[:, 1]), axis=1)
+
+
+def far_summary(f_pred, f_ref):
+    dd, dp = far_errors(f_pred, f_ref)
+    return {"directivity_db_median": float(np.median(dd)), "directivity_db_p90": float(np.percentile(dd, 90)),
+            "energy_db_median": float(np.median(dp)), "energy_db_p90": float(np.percentile(dp, 90)),
+            "scenes": int(dd.size)}
+
+
 def run_scenes(scenes, early: bool):
-    """Steps scenes in stacks: to ring-down (early False) or for their early window only; returns
-    (results, wall seconds of the run, stack set-up excluded)."""
+    """Steps scenes in stacks, each with its surface DFT: to ring-down (early False) or for their
+    early window only; returns (results, wall seconds of the run, stack set-up excluded). The
+    results hold the far-field spectra at the last step (result.far)."""
     from .batch import BatchRunner
     stop = [early_steps(sc) for sc in scenes] if early else None
-    r = BatchRunner(scenes, chunk=64, stop_steps=stop)
+    r = BatchRunner(scenes, chunk=64, stop_steps=stop, far_field=far_field())
     res = r.run()
     r.close()
     return res, r.wall_s
 
 
-WAVE = 512  # scenes stepped together at most (device memory: about 50 GB of stacks per wave)
+WAVE = 256  # scenes stepped together at most (device memory: stacks and their surface DFTs)
 
 
 def record(sc, r):
-    """What the extrapolator keeps of a run that rang down: the scene quantities features() reads
-    and the whole (V, I) series with its converged Z(f); None for a run that did not ring down."""
+    """What the extrapolator keeps of a run that rang down: the scene quantities features() reads,
+    the whole (V, I) series with its converged Z(f), and the far-field spectra by step (the early
+    windows and the last step); None for a run that did not ring down."""
     from types import SimpleNamespace as NS
     if not (r.done and r.rung_down and r.sweep is not None):
         return None
+    series = np.ascontiguousarray(np.concatenate(r.series), np.float32)
+    far = dict(getattr(r, "far", {}) or {})
     return NS(wavelength=sc.wavelength, grid=NS(courant=sc.grid.courant), sweep=dict(sc.sweep),
               cells=int(np.prod(sc.grid.size)),
               ports=[NS(impedance_ohm=sc.ports[0].impedance_ohm)],
-              series=np.ascontiguousarray(np.concatenate(r.series), np.float32), z=r.sweep["z"])
+              series=series, z=r.sweep["z"], far=far, far_final=far.get(series.shape[0]))
 
 
-def generate(seed, n, edges, log=None):
-    """Runs scenes 0..n-1 of the generator's `seed` to ring-down with the batched solver, in waves;
-    returns (records of the runs that rang down, wall seconds of stepping)."""
+def generate(seed, n, edges, log=None, periods=None):
+    """Runs scenes 0..n-1 of the generator's `seed` to ring-down with the batched solver, in waves,
+    recording the far-field spectra at the end of each early window in `periods` (design periods)
+    and at the last step; returns (records of the runs that rang down, wall seconds of stepping)."""
     from . import configs
+    from .batch import BatchRunner
+    periods = list(periods) if periods else [PERIODS_IN]
     recs, wall = [], 0.0
     for w0 in range(0, n, WAVE):
         scenes = [configs.batched_scene(seed, i, edges=edges) for i in range(w0, min(n, w0 + WAVE))]
-        res, w = run_scenes(scenes, early=False)
-        wall += w
-        recs += [q for q in (record(sc, r) for sc, r in zip(scenes, res)) if q is not None]
+        r = BatchRunner(scenes, chunk=64, far_field=far_field(),
+                        snap_at=[[early_steps(sc, P) for P in periods] for sc in scenes])
+        res = r.run()
+        r.close()
+        wall += r.wall_s
+        recs += [q for q in (record(sc, x) for sc, x in zip(scenes, res)) if q is not None]
         if log:
-            log(f"training runs {w0 + len(scenes)}/{n}: {w:.1f} s")
+            log(f"training runs {w0 + len(scenes)}/{n}: {r.wall_s:.1f} s")
     return recs, wall
 
 
 def dataset_of(records):
-    """(x, zt, t, z_trunc, z_conv) of the records whose series covers the current early window."""
-    rows = [[], [], [], [], []]
+    """(x, aux, t, z_trunc, z_conv, far_trunc, far_conv) of the records whose series and far-field
+    snapshots cover the current early window."""
+    rows = [[] for _ in range(7)]
     for q in records:
-        if q.series.shape[0] < early_steps(q):
+        n = early_steps(q)
+        far_e = q.far.get(n)
+        if q.series.shape[0] < n or far_e is None or q.far_final is None:
             continue
-        x, zf, ztrunc = features(q, q.series)
-        for k, v in enumerate((x, zf, target(q.z), ztrunc, q.z)):
+        x, zf, ztrunc = features(q, q.series, far_e)
+        for k, v in enumerate((x, zf, target(q.z, q.far_final), ztrunc, q.z, far_e, q.far_final)):
             rows[k].append(v)
     if not rows[0]:
         return None
@@ -400,11 +456,13 @@ def dataset_of(records):
 
 def ensemble_predict(nets, x, zt):
     """(mean Z(f) of the members, per-scene spread = band median of the largest member deviation
-    |Z_m - Z_mean| / |Z_mean|): the spread is the extrapolator's own estimate of its error."""
-    zs = np.stack([to_z(n.predict(x, zt)) for n in nets])
+    |Z_m - Z_mean| / |Z_mean|, mean far-field spectra (n, 2, NFF)): the spread is the extrapolator's
+    own estimate of its error."""
+    ys = np.stack([n.predict(x, zt) for n in nets])
+    zs = to_z(ys)
     zm = zs.mean(axis=0)
     dev = np.abs(zs - zm[None]).max(axis=0) / np.maximum(np.abs(zm), 1e-9)
-    return zm, np.median(dev, axis=1)
+    return zm, np.median(dev, axis=1), to_far(ys).mean(axis=0)
 
 
 def per_scene_errors(z_pred, z_ref):
@@ -430,56 +488,58 @@ def run_with_fallback(scenes, nets, tau):
     """The learned path with the plain solver as its fallback, in one batched run: at its early
     window each scene's ensemble prediction and spread are computed (one batched inference per stack
     and chunk); a spread within `tau` stops the scene there, otherwise it steps on from where it is
-    to ring-down and its Z(f) is the plain solver's. Returns ({scene: Z(f)}, wall seconds including
-    the inference, number of fallback scenes)."""
+    to ring-down and its Z(f) and far-field spectra are the plain solver's. Returns ({scene: Z(f)},
+    {scene: far-field spectra}, wall seconds including the inference, number of fallback scenes)."""
     from .batch import BatchRunner
-    pred = {}
+    pred, pred_far = {}, {}
 
-    def decide(idx, series):
+    def decide(idx, series, fars):
         xs, zts = [], []
-        for i, ser in zip(idx, series):
-            x, zf, _ = features(scenes[i], ser)
+        for i, ser, fe in zip(idx, series, fars):
+            x, zf, _ = features(scenes[i], ser, fe)
             xs.append(x), zts.append(zf)
-        zm, spread = ensemble_predict(nets, np.stack(xs), np.stack(zts))
-        for i, z in zip(idx, zm):
-            pred[i] = z
+        zm, spread, fm = ensemble_predict(nets, np.stack(xs), np.stack(zts))
+        for i, z, f in zip(idx, zm, fm):
+            pred[i], pred_far[i] = z, f
         return [bool(v <= tau) for v in spread]
 
-    r = BatchRunner(scenes, chunk=64, decide_at=[early_steps(sc) for sc in scenes], decide=decide)
+    r = BatchRunner(scenes, chunk=64, decide_at=[early_steps(sc) for sc in scenes], decide=decide,
+                    far_field=far_field())
     res = r.run()
     r.close()
-    z = {}
+    z, far = {}, {}
     for i, q in enumerate(res):
         if q.accepted:
-            z[i] = pred[i]
+            z[i], far[i] = pred[i], pred_far[i]
         elif q.sweep is not None:
-            z[i] = q.sweep["z"]
-    return z, r.wall_s, sum(1 for q in res if not q.accepted)
+            z[i], far[i] = q.sweep["z"], q.far.get(q.steps)
+    return z, far, r.wall_s, sum(1 for q in res if not q.accepted)
 
 
 def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=1e-3, seed=0, edges=None, log=None,
                periods=None, members=1, val_frac=0.0, single=False):
     """Generates training runs with the batched solver (every scene to -60 dB ring-down, in waves of
-    WAVE scenes) and, for each early window in `periods` (design periods; default PERIODS_IN),
-    trains `members` networks on them and evaluates on held-out scenes against the reference result, the plain
-    solver run to ring-down:
+    WAVE scenes, each with its surface DFT) and, for each early window in `periods` (design periods;
+    default PERIODS_IN), trains `members` networks on them and evaluates on held-out scenes against
+    the reference result, the plain solver run to ring-down:
       (a) the plain solver: batched stacks (and with `single`, one SimulationGrid per scene, the
-          reference's way) — sweeps/hr and the converged Z(f);
-      (b) the early window's truncated DFT (the method without the network);
+          reference's way) — sweeps/hr, the converged Z(f) and far-field spectra;
+      (b) the early window's truncated DFTs (the method without the network);
       (c) the network's prediction (the ensemble mean) from the same early window;
       (d) with members > 1 and val_frac > 0, the learned path with its fallback: scenes whose
           ensemble spread exceeds a threshold chosen on a validation split of the training runs
           (p90 |dZ| <= 2 % and p90 S11 error <= 0.5 dB over all validation scenes) continue with
-          the plain solver, and their Z(f) is the plain solver's.
-    Sweeps/hr are wall-clock figures of stepping, read-back, features and inference (stack set-up
-    excluded). Returns (result dict, parameters of the first member of the last window)."""
+          the plain solver, and their Z(f) and spectra are the plain solver's.
+    Sweeps/hr are wall-clock figures of stepping, read-back, far-field evaluation, features and
+    inference (stack set-up excluded). Returns (result dict, parameters of the first member of the
+    last window)."""
     from . import batch as batch_solver, configs
     global PERIODS_IN
     edges = edges or configs.BATCH_EDGES
     periods = list(periods) if periods else [PERIODS_IN]
     out = {}
     t0 = time.perf_counter()
-    recs, tr_wall = generate(train_seed, n_train, edges, log)
+    recs, tr_wall = generate(train_seed, n_train, edges, log, periods)
     out["train_runs"] = {"scenes": n_train, "usable": len(recs), "wall_s": tr_wall}
     n_val = int(round(val_frac * len(recs))) if members > 1 else 0
     val_recs, fit_recs = recs[:n_val], recs[n_val:]
@@ -490,9 +550,10 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
                     "steps_median": float(np.median([r.steps for r in ev_res]))}
     if single:
         run_s = 0.0
+        ff = far_field()
         for sc in eval_scenes:
             tm = {}
-            batch_solver.run_single(sc, chunk=64, timing=tm)
+            batch_solver.run_single(sc, chunk=64, timing=tm, far_field=ff)
             run_s += tm["run_s"]
         out["plain"].update(single_s=run_s, single_sweeps_per_hour=n_eval / run_s * 3600.0)
 
@@ -502,7 +563,7 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
         for P in periods:
             PERIODS_IN = float(P)
             w = {"periods": float(P)}
-            x, zt, t, _, _ = dataset_of(fit_recs)
+            x, zt, t = dataset_of(fit_recs)[:3]
             t1 = time.perf_counter()
             nets, last = [], []
             for m in range(members):
@@ -514,46 +575,55 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
             params = nets[0].params()
             tau = None
             if n_val:
-                vx, vzt, _, _, vz = dataset_of(val_recs)
-                vzm, vspread = ensemble_predict(nets, vx, vzt)
+                vx, vzt, _, _, vz, _, vfar = dataset_of(val_recs)
+                vzm, vspread, vfm = ensemble_predict(nets, vx, vzt)
                 vdz, vds = per_scene_errors(vzm, vz)
                 tau = select_threshold(vspread, vdz, vds)
                 # cell-steps of the learned path with fallback relative to the plain runs (a rejected
                 # scene runs on from its early window)
-                usable = [q for q in val_recs if q.series.shape[0] >= early_steps(q)]
+                usable = [q for q in val_recs if q.series.shape[0] >= early_steps(q) and early_steps(q) in q.far
+                          and q.far_final is not None]
                 full = np.array([q.cells * q.series.shape[0] for q in usable], np.float64)
                 early = np.array([q.cells * early_steps(q) for q in usable], np.float64)
                 cost = float(np.where(vspread > tau, full, early).sum() / full.sum())
                 w["validation"] = {"scenes": int(vx.shape[0]), "threshold": tau,
                                    "accepted": float(np.mean(vspread <= tau)), "cell_steps_vs_plain": cost,
                                    "network_dz_median": float(np.median(vdz)),
-                                   "network_s11_db_median": float(np.median(vds))}
-            # the learned path on the held-out scenes: early window, features, inference
+                                   "network_s11_db_median": float(np.median(vds)),
+                                   "network_far": far_summary(vfm, vfar)}
+            # the learned path on the held-out scenes: early window (with its surface DFT), features,
+            # inference
             early_res, early_wall = run_scenes(eval_scenes, early=True)
             t2 = time.perf_counter()
-            xs, zts, ztr, keep = [], [], [], []
+            xs, zts, ztr, ftr, keep = [], [], [], [], []
             for k, (sc, r) in enumerate(zip(eval_scenes, early_res)):
                 ser = np.concatenate(r.series)
-                if ser.shape[0] < early_steps(sc):
+                fe = r.far.get(early_steps(sc))
+                if ser.shape[0] < early_steps(sc) or fe is None:
                     continue
-                xe, ze, zr = features(sc, ser)
-                xs.append(xe), zts.append(ze), ztr.append(zr), keep.append(k)
-            z_pred, spread = ensemble_predict(nets, np.stack(xs), np.stack(zts))
+                xe, ze, zr = features(sc, ser, fe)
+                xs.append(xe), zts.append(ze), ztr.append(zr), ftr.append(fe), keep.append(k)
+            z_pred, spread, f_pred = ensemble_predict(nets, np.stack(xs), np.stack(zts))
             infer_wall = time.perf_counter() - t2
             # the learned path with its fallback, in one run: every scene is stopped at its early
             # window if the ensemble's spread is within the threshold, else it runs on to ring-down
-            fb_wall, n_fallback, z_hyb_of = 0.0, 0, {}
+            fb_wall, n_fallback, z_hyb_of, f_hyb_of = 0.0, 0, {}, {}
             if tau is not None:
-                z_hyb_of, fb_wall, n_fallback = run_with_fallback(eval_scenes, nets, tau)
+                z_hyb_of, f_hyb_of, fb_wall, n_fallback = run_with_fallback(eval_scenes, nets, tau)
             learned_wall = (early_wall + infer_wall) if tau is None else fb_wall
-            z_trunc = np.stack(ztr)
+            z_trunc, f_trunc = np.stack(ztr), np.stack(ftr)
             ok = [j for j, k in enumerate(keep) if ev_res[k].rung_down]
             z_conv = np.stack([ev_res[keep[j]].sweep["z"] for j in ok])
+            f_conv = np.stack([ev_res[keep[j]].far[ev_res[keep[j]].steps] for j in ok])
             w["eval"] = {"scenes": n_eval, "compared": len(ok), "network": summary(z_pred[ok], z_conv),
-                         "truncated_dft": summary(z_trunc[ok], z_conv)}
+                         "truncated_dft": summary(z_trunc[ok], z_conv),
+                         "network_far": far_summary(f_pred[ok], f_conv),
+                         "truncated_dft_far": far_summary(f_trunc[ok], f_conv)}
             if tau is not None:
                 z_hyb = np.stack([z_hyb_of[keep[j]] for j in ok])
+                f_hyb = np.stack([f_hyb_of[keep[j]] for j in ok])
                 w["eval"]["with_fallback"] = summary(z_hyb, z_conv)
+                w["eval"]["with_fallback_far"] = far_summary(f_hyb, f_conv)
                 w["eval"]["fallback_scenes"] = n_fallback
             w["wall"] = {"early_s": early_wall, "features_inference_s": infer_wall, "with_fallback_s": fb_wall}
             net_wall = early_wall + infer_wall  # every scene stops at the early window

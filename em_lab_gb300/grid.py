@@ -79,6 +79,8 @@ def load_library() -> C.CDLL:
         "emlab_ntff_dft_read": ([P, dp], I),
         "emlab_ntff_dft_evaluate": ([P, I, fp, I, fp], I),
         "emlab_ntff_dft_evaluate_all": ([P, fp, I, fp], I),
+        "emlab_ntff_dft_configure_boxes": ([P, ip, I, fp, I, I], I),
+        "emlab_ntff_dft_spectra": ([P, I, fp, I, fp], I),
         "emlab_probe_gather": ([P, ip, I, fp], I),
         "emlab_flux_planes": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
@@ -517,6 +519,23 @@ class SimulationGrid:
         d[:, :3] = np.asarray(directions, np.float32)[:, :3]
         out = np.zeros((self._dft_nf, len(directions), 2), np.float32)
         _check(self._lib.emlab_ntff_dft_evaluate_all(self._h, _fptr(d), len(d), _fptr(out)))
+        return out
+
+    def ntff_dft_configure_boxes(self, boxes, wavelengths, block: int = 0):
+        """The far-field DFT on several boxes ((k, 6) ints: min xyz, max xyz each, not clamped);
+        block: samples per fold at most (0: the engine's own)."""
+        b = np.ascontiguousarray(np.asarray(boxes, np.int32).reshape(-1, 6))
+        wl = _f32(wavelengths)
+        _check(self._lib.emlab_ntff_dft_configure_boxes(self._h, b.ctypes.data_as(C.POINTER(C.c_int)), len(b),
+                                                        _fptr(wl), len(wl), int(block)))
+        self._dft_nf = len(wl) if len(b) else 0
+
+    def ntff_dft_spectra(self, box: int, directions) -> np.ndarray:
+        """(frequencies, directions, 2) of one box of several, as ntff_dft_evaluate_all."""
+        d = np.zeros((len(directions), 4), np.float32)
+        d[:, :3] = np.asarray(directions, np.float32)[:, :3]
+        out = np.zeros((self._dft_nf, len(directions), 2), np.float32)
+        _check(self._lib.emlab_ntff_dft_spectra(self._h, int(box), _fptr(d), len(d), _fptr(out)))
         return out
 
     def probe_gather(self, origins) -> np.ndarray:

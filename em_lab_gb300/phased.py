@@ -1,4 +1,4 @@
-"""Planar phased-array workload (BASELINE config 5): N x N dipoles over a ground sheet under a radome,
+"""Planar phased-array workload: N x N dipoles over a ground sheet under a radome,
 Taylor-tapered and steered by true time delays, in eight seeded directions; the far field at
 181 x 361 angles and 32 frequencies from the tensor-core DFT of the Huygens-box fields.
 

@@ -272,6 +272,22 @@ int emlab_ntff_dft_evaluate(emlab_grid* g, int f, const float* directions, int n
  * surface phases from a 2-pi range reduction and hardware sin/cos (relative difference about 1e-5),
  * two directions per thread: for large angle grids. */
 int emlab_ntff_dft_evaluate_all(emlab_grid* g, const float* directions, int n_dirs, float* out);
+/* The far-field DFT on several Huygens boxes at once (the boxes of the scenes of a stack): boxes[6k ..
+ * 6k + 5] = min xyz, max xyz of box k in grid coordinates, each inside [1, n - 2] on every axis with
+ * at least 4 cells (no clamping: the caller keeps each box inside its scene's absorber);
+ * EMLAB_ERR_INVALID otherwise. Their nodes are sampled and folded together, box after box in one
+ * point list (emlab_ntff_dft_read returns them in that order). block: samples per fold at most, 0
+ * for the engine's own block or a multiple of 64 (a shorter block holds fewer samples per node in
+ * device memory). A stack compaction keeps the boxes of the kept scenes with their sums.
+ * emlab_ntff_dft_evaluate and _evaluate_all need a single box; emlab_ntff_dft_spectra evaluates one
+ * box of several. */
+int emlab_ntff_dft_configure_boxes(emlab_grid* g, const int* boxes, int n_boxes, const float* wavelengths,
+                                   int n_freq, int block);
+/* The pattern of box `box` at every configured frequency (1 to 8192 directions, 4 floats each, xyz
+ * used), in the layout of emlab_ntff_dft_evaluate_all: out[(f * n_dirs + d) * 2] = |N_perp - r x L|^2,
+ * out[f * n_dirs * 2 + 1] = radiated power at f, from the sums scaled by 2 / samples. Two launches
+ * for all frequencies; the device scratch grows to the largest request and is kept. */
+int emlab_ntff_dft_spectra(emlab_grid* g, int box, const float* directions, int n_dirs, float* out);
 
 /* ---- volume rendering: VolumeRenderer (src/VolumeRenderer.cpp:66-118, shaders/raymarch.frag) */
 /* Camera and look of one rendered frame. inv_view_proj: inverse of projection * view, column-

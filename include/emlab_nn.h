@@ -1,5 +1,5 @@
 /* emlab_nn.h - kernels of the learned ring-down extrapolator (no reference counterpart: the
- * reference has no learned component; BASELINE config 4).
+ * reference has no learned component; the learned antenna-sweep workload).
  *
  * Device pointers and sizes only; `stream` is a cudaStream_t (NULL = the legacy default stream).
  * BF16 operands are __nv_bfloat16 arrays, everything else FP32. Return EMLAB_OK or an error code

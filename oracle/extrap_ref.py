@@ -48,7 +48,7 @@ def col2im(dcols, B, Lin, C, k, stride, pad, Lout):
 
 
 def forward(params, x, zt, exact=False):
-    """x (B, T_IN, 2), zt (B, 2 NF): every intermediate the backward pass needs, and y."""
+    """x (B, T_IN, 2), zt (B, AUX): every intermediate the backward pass needs, and y."""
     B = x.shape[0]
     W = {n: _r(params[n][0], exact) for n in params}
     b = {n: np.asarray(params[n][1], np.float64) for n in params}
@@ -74,12 +74,12 @@ def forward(params, x, zt, exact=False):
 
 
 def backward(params, cache, t, n, exact=False):
-    """Gradients {name: (dW, db)} of the MSE over the first n rows (2 NF outputs each)."""
+    """Gradients {name: (dW, db)} of the MSE over the first n rows (OUT outputs each)."""
     y = cache["z"]["out"]
     B = y.shape[0]
     W = cache["W"]
     dy = np.zeros_like(y)
-    dy[:n] = 2.0 * (y[:n] - np.asarray(t[:n], np.float64)) / (n * 2 * X.NF)
+    dy[:n] = 2.0 * (y[:n] - np.asarray(t[:n], np.float64)) / (n * X.OUT)
     grads = {}
     up = dy
     for name, i, o, relu in reversed(X.HEAD):
@@ -101,4 +101,4 @@ def backward(params, cache, t, n, exact=False):
 
 def loss(params, x, zt, t, n, exact=True):
     y, _ = forward(params, x, zt, exact)
-    return float(np.sum((y[:n] - t[:n]) ** 2) / (n * 2 * X.NF))
+    return float(np.sum((y[:n] - t[:n]) ** 2) / (n * X.OUT))

@@ -49,8 +49,8 @@ def test_forward_and_gradients_match_the_cpu_restatement():
     params = {k: (w, (rng.standard_normal(b.shape) * 0.05).astype(np.float32)) for k, (w, b) in params.items()}
     n = 37  # fewer rows than the batch: padding rows must not contribute
     x = rng.standard_normal((n, extrap.T_IN, 2)).astype(np.float32)
-    zt = (rng.standard_normal((n, 2 * extrap.NF)) * 0.5).astype(np.float32)
-    t = (rng.standard_normal((n, 2 * extrap.NF)) * 0.5).astype(np.float32)
+    zt = (rng.standard_normal((n, extrap.AUX)) * 0.5).astype(np.float32)
+    t = (rng.standard_normal((n, extrap.OUT)) * 0.5).astype(np.float32)
     net = extrap.Net(params, batch=64)
     net.load(x, zt, t)
     y = net.forward()[:n].cpu().numpy()
@@ -77,9 +77,9 @@ def test_training_reduces_the_loss():
     rng = np.random.default_rng(0)
     n = 512
     x = rng.standard_normal((n, extrap.T_IN, 2)).astype(np.float32) * 0.3
-    zt = rng.standard_normal((n, 2 * extrap.NF)).astype(np.float32) * 0.5
-    t = (0.8 * zt + 0.2 * np.tanh(zt[:, ::-1]) + 0.1 * x[:, :1, 0]).astype(np.float32)
-    net, losses = extrap.train(x, zt, t, epochs=80, batch=64, lr=2e-3, seed=1)
+    zt = rng.standard_normal((n, extrap.AUX)).astype(np.float32) * 0.5
+    t = (0.8 * zt[:, :extrap.OUT] + 0.2 * np.tanh(zt[:, ::-1][:, :extrap.OUT]) + 0.1 * x[:, :1, 0]).astype(np.float32)
+    net, losses = extrap.train(x, zt, t, epochs=200, batch=64, lr=2e-3, seed=1)
     assert losses[-1] < 0.2 * losses[0]
     assert all(np.isfinite(losses))
 
