@@ -360,11 +360,12 @@ def run_batched(args):
     scenes = configs.batched_scenes(n, seed=args.seed)
     build_s = time.perf_counter() - t0
     # warm-up: a few chunks of a small batch (kernel loading, allocator)
-    warm = batch.BatchRunner([configs.batched_scene(args.seed + 1, i) for i in range(4)], max_steps=64 * args.warmup)
+    warm = batch.BatchRunner([configs.batched_scene(args.seed + 1, i) for i in range(4)], max_steps=64 * args.warmup,
+                             layout=args.layout)
     warm.run()
     warm.close()
     l0 = launch_count()
-    runner = batch.BatchRunner(scenes, chunk=64)
+    runner = batch.BatchRunner(scenes, chunk=64, layout=args.layout)
     with ClockSampler(local) as clk:
         results = runner.run()
     launches = launch_count() - l0
@@ -373,6 +374,17 @@ def run_batched(args):
     scene_cells = [int(np.prod(sc.grid.size)) for sc in scenes]
     useful = float(sum(c * st for c, st in zip(scene_cells, steps)))
     value = done / runner.wall_s * 3600.0
+    other = None
+    if args.layout == "ragged" and not args.no_single:
+        # the same scenes in one stack per cross-section, each on its own stream and host thread
+        alt = batch.BatchRunner(scenes, chunk=64, layout="cross_section")
+        alt_res = alt.run()
+        alt.close()
+        other = {"layout": "one stack per cross-section, each on its own CUDA stream", "groups": len(alt.groups),
+                 "sweeps_per_hour": sum(r.done for r in alt_res) / alt.wall_s * 3600.0,
+                 "mcells_per_s": float(sum(c * r.steps for c, r in zip(scene_cells, alt_res))) / alt.wall_s / 1e6,
+                 "identical_results": all(np.array_equal(a.sweep["z"], b.sweep["z"]) for a, b in zip(results, alt_res)
+                                          if a.sweep is not None and b.sweep is not None)}
     single = None
     if not args.no_single:
         ts = []
@@ -393,12 +405,18 @@ def run_batched(args):
         "config": {"workload": f"batched antenna sweep: {n} seeded scenes (seed {args.seed}), cube edges 48-160 cells, "
                                "8-cell absorber, thin-wire dipole or monopole over ground, 50-ohm Gaussian-pulse feed, "
                                "one random dielectric sphere or box, 128-point Z(f) sweep per scene",
-                   "groups": len(runner.groups), "chunk_steps": 64, "l2": "inputs larger than L2 (stack state > 129 MB)"},
+                   "groups": len(runner.groups), "chunk_steps": 64, "l2": "inputs larger than L2 (stack state > 129 MB)",
+                   "layout": ("one stack of scenes with their own cross-sections per solver setting: one persistent "
+                              "Yee launch per step for all scenes" if args.layout == "ragged" else
+                              "one stack per cross-section, each on its own CUDA stream")},
         "scenes_done": done, "scenes_rung_down": sum(r.rung_down for r in results), "scene_steps": {"min": int(min(steps)), "median": int(np.median(steps)), "max": int(max(steps))},
         "mcells_per_s": useful / runner.wall_s / 1e6,
         "setup_s": {"scene_build": build_s, "stack_upload_and_tiling": runner.setup_s},
-        "tiling": {f"{g.scenes[0].grid.size[0]}": min(g.tiling, key=g.tiling.get) if g.tiling else None
-                   for g in runner.groups},
+        "host_s": {"between_chunks": runner.host_s, "of_which_compaction": runner.compact_s,
+                   "note": "summed over the stacks' host threads"},
+        "tiling": {"x".join(str(v) for v in g.scenes[0].grid.size) if args.layout != "ragged" else f"stack {k}":
+                   min(g.tiling, key=g.tiling.get) if g.tiling else None for k, g in enumerate(runner.groups)},
+        "per_cross_section": other,
         "single_grid": single,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
@@ -541,6 +559,8 @@ def main():
     ap.add_argument("--seed", type=int, default=2024, help="batched: scene seed")
     ap.add_argument("--no-single", action="store_true", help="batched: skip the one-grid-per-scene comparison")
     ap.add_argument("--single-all", action="store_true", help="batched: compare on every scene, not a sample")
+    ap.add_argument("--layout", default="ragged", choices=["ragged", "cross_section"],
+                    help="batched: one stack of all cross-sections (one launch per step) or one stack per cross-section")
     ap.add_argument("--train-scenes", type=int, default=20000, help="learned: training scenes")
     ap.add_argument("--epochs", type=int, default=100, help="learned: training epochs")
     ap.add_argument("--periods", default="1.5,2,3,4", help="learned: early windows to try, design periods")

@@ -1,8 +1,10 @@
 """Batched antenna sweeps: many independent scenes stepped together until their ports ring down.
 
-Scenes are grouped by cross-section (nx, ny) and each group becomes one `SceneStack`: a single grid
-whose every solver launch covers all of its scenes (csrc/stack.cu). Each group runs on its own CUDA
-stream, so the groups' launches overlap on the device. Every `chunk` steps the port series of the
+Scenes of equal solver settings become one `SceneStack` of scenes with their own cross-sections: a
+single grid whose every solver launch covers all of its scenes (csrc/stack.cu), one launch of the
+persistent pair kernel per step whose work items are the tiles of each scene's own nx x ny. With
+layout="cross_section" the scenes are instead grouped by (nx, ny), one stack per group, each group
+on its own CUDA stream so that the groups' launches overlap on the device. Every `chunk` steps the port series of the
 chunk is read back; a scene is done when the reference's ring-down residual (the largest |V| of
 the last 5 % of its series over the peak, Ports.cpp:206-213) is 60 dB down, after at least four
 design periods (at most 120). A finished scene's impedance sweep Z(f) is
@@ -189,6 +191,7 @@ def _watch(sc, dt: float) -> RingDown:
 
 
 TILINGS = (64, 32, 128, 8)  # 64 x 8, 64 x 4, 64 x 16 pair tiles; 32 x 8 single-cell tiles
+PAIR_TILINGS = (64, 32, 128)  # a stack of scenes with their own cross-sections: pair tiles only
 
 
 def autotune_tiling(grid, modes=TILINGS, steps=4):
@@ -212,17 +215,20 @@ def autotune_tiling(grid, modes=TILINGS, steps=4):
 
 
 class _Group:
-    def __init__(self, scenes, indices, chunk, tune=True, far=None):
+    def __init__(self, scenes, indices, chunk, tune=True, far=None, ragged=False):
         self.indices = list(indices)  # scene indices into the batch, in stack order
         self.scenes = [scenes[i] for i in indices]
         first = self.scenes[0]
-        self.stack = SceneStack(first.grid, [sc.grid.size[2] for sc in self.scenes])
+        if ragged:
+            self.stack = SceneStack(first.grid, scene_dims=[tuple(sc.grid.size) for sc in self.scenes])
+        else:
+            self.stack = SceneStack(first.grid, [sc.grid.size[2] for sc in self.scenes])
         for k, sc in enumerate(self.scenes):
             m = sc.materials
             self.stack.upload_scene_materials(k, m.sigma, m.epsilon_r, sc.edges, sc.wires)
         self.stack.set_scene_sources([sc.sources for sc in self.scenes])
         self.stack.commit()
-        self.tiling = autotune_tiling(self.stack) if tune else None
+        self.tiling = autotune_tiling(self.stack, PAIR_TILINGS if ragged else TILINGS) if tune else None
         self.chunk = chunk
         self.stack.set_graph(chunk)  # each chunk replays one captured graph of its launches
         self.attach_ports()
@@ -257,7 +263,8 @@ class BatchRunner:
     """Steps `scenes` (each with one feed port) to port ring-down in stacks grouped by cross-section."""
 
     def __init__(self, scenes, chunk: int = 64, max_steps: int = 200_000, compact_fraction: float = 0.25,
-                 stop_steps=None, tune: bool = True, decide_at=None, decide=None, far_field=None, snap_at=None):
+                 stop_steps=None, tune: bool = True, decide_at=None, decide=None, far_field=None, snap_at=None,
+                 layout: str = "ragged"):
         """stop_steps: per scene, stop after this many steps without waiting for the ring-down (the
         early window of a learned extrapolation); None: run every scene to ring-down.
         decide_at / decide: once scene i has run decide_at[i] steps (at a chunk boundary) without
@@ -265,7 +272,13 @@ class BatchRunner:
         the same chunk (under the runner's lock) and returns one flag per scene: True stops the scene
         there (result.accepted), False lets it run on to ring-down from where it is.
         far_field: a FarField; every scene then records its far-field spectra (result.far[step]) when
-        it is done and, with snap_at (per scene, a list of steps), at each of those steps on the way."""
+        it is done and, with snap_at (per scene, a list of steps), at each of those steps on the way.
+        The boxes of one stack share the DFT's frequencies, so scenes of other sweep bands go to other
+        stacks.
+        layout: "ragged" (scenes of all cross-sections in one stack per solver setting) or
+        "cross_section" (one stack per (nx, ny))."""
+        if layout not in ("ragged", "cross_section"):
+            raise ValueError("layout must be 'ragged' or 'cross_section'")
         for sc in scenes:
             if not sc.ports:
                 raise ValueError(f"{sc.name}: a batched scene needs a feed port")
@@ -278,14 +291,17 @@ class BatchRunner:
             snap_at = [list(a) + [d] for a, d in zip(snap_at or [[]] * len(self.scenes), decide_at)]
         self.snap_at = [sorted(set(int(v) for v in a)) for a in snap_at] if snap_at is not None else None
         groups = {}
+        ragged = layout == "ragged"
         for i, sc in enumerate(self.scenes):
-            key = (sc.grid.size[0], sc.grid.size[1], sc.grid.pml_thickness, float(sc.grid.courant),
-                   float(sc.grid.pml_sigma_max), float(sc.grid.pml_grading))
+            key = (sc.grid.pml_thickness, float(sc.grid.courant), float(sc.grid.pml_sigma_max),
+                   float(sc.grid.pml_grading))
+            if not ragged:
+                key += (sc.grid.size[0], sc.grid.size[1])
             if far_field is not None:  # the boxes of one stack share the DFT frequencies
                 key += tuple(float(v) for v in far_field.wavelengths(sc))
             groups.setdefault(key, []).append(i)
         t0 = time.perf_counter()
-        self.groups = [_Group(self.scenes, idx, self.chunk, tune, far_field) for _, idx in
+        self.groups = [_Group(self.scenes, idx, self.chunk, tune, far_field, ragged) for _, idx in
                        sorted(groups.items(), key=lambda kv: kv[0])]
         self.setup_s = time.perf_counter() - t0
         self.results = [SceneResult(i) for i in range(len(self.scenes))]
@@ -299,6 +315,8 @@ class BatchRunner:
             self.watch = [RingDown(min_steps=int(n), max_steps=int(n)) for n in stop_steps]
         self.cell_steps = 0
         self.steps = 0
+        self.host_s = 0.0     # host seconds between a chunk's read-back and the next chunk's launch
+        self.compact_s = 0.0  # of which in compaction
 
     def _next_chunk(self, g, steps):
         """Steps of the stack's next chunk: up to the next multiple of the chunk length (a whole
@@ -318,17 +336,25 @@ class BatchRunner:
                     n = min(n, later[0] - r.steps)
         return n
 
+    def _compact_now(self, g, keep) -> bool:
+        """Compact once the finished scenes hold compact_fraction of the stack's cells (their steps
+        are wasted until then; each compaction copies the rest of the stack)."""
+        cells = [int(np.prod(sc.grid.size)) for sc in g.scenes]
+        done = sum(c for c, k in zip(cells, keep) if not k)
+        return done > 0 and done >= self.compact_fraction * sum(cells)
+
     def _run_group(self, g, t0, on_done, lock):
         """One stack's loop (its own host thread and CUDA stream): step a chunk, read the chunk's port
         series back, watch every scene, evaluate the finished ones, compact. The library releases the
         interpreter lock inside its calls, so the stacks' chunks overlap on the device."""
         steps = 0
+        host = comp = 0.0
         while g.indices and steps < self.max_steps:
             n = self._next_chunk(g, steps)
             g.stack.step(n)
             ser = g.stack.ports_take_series(n)
-            nx, ny, _ = g.stack.size()
-            cells = nx * ny * sum(g.stack.layout()[1]) * ser.shape[0]
+            th = time.perf_counter()
+            cells = sum(int(np.prod(sc.grid.size)) for sc in g.scenes) * ser.shape[0]  # the scenes' own cells
             finished = []
             for k, i in enumerate(g.indices):
                 r = self.results[i]
@@ -373,10 +399,15 @@ class BatchRunner:
             keep = [not self.results[i].done for i in g.indices]
             if not any(keep):
                 g.indices = []
-            elif keep.count(False) >= max(1, int(self.compact_fraction * len(keep))):
+            elif self._compact_now(g, keep):
+                tc = time.perf_counter()
                 g.compact(keep)
+                comp += time.perf_counter() - tc
+            host += time.perf_counter() - th
         with lock:
             self.steps = max(self.steps, steps)
+            self.host_s += host
+            self.compact_s += comp
 
     def run(self, on_done=None):
         import threading

@@ -76,6 +76,15 @@ YeeArgs yee_args(emlab_grid* g) {
     a.work = g->d_work.p;
     a.work_base = g->work_base;
     a.wait_polls = wait_limit();
+    a.pml_cls_xy = g->pml_cls.p, a.pml_xy = g->pml.p, a.pml_xy_stride = g->pml_stride, a.pml_xy_scene = 0;
+    a.items = nullptr, a.n_items = 0, a.scene_xy = nullptr;
+    if (g->stack.ragged) {
+        const int ti = ty == 4 ? 0 : (ty == 8 ? 1 : 2);
+        a.pml_cls_xy = g->d_pml_cls_xy.p, a.pml_xy = g->d_pml_xy.p;
+        a.pml_xy_stride = g->pml_xy_stride, a.pml_xy_scene = 6 * g->pml_xy_stride;
+        a.items = g->d_items[ti].p, a.n_items = g->n_items[ti];
+        a.scene_xy = g->d_scene_xy.p;
+    }
     return a;
 }
 
@@ -185,6 +194,57 @@ int emlab::upload_pml(emlab_grid* g) {
             }
         }
     }
+    if (g->stack.ragged) {
+        // every scene's own x / y profiles and depth classes ([6][SXY] per scene, rows 0, 1, 3, 4 used),
+        // its nx, ny, and the pair kernel's work items for each tile height
+        const StackLayout& st = g->stack;
+        const int n = st.scenes(), SXY = std::max(c.nx, c.ny);
+        std::vector<float> pxy((size_t)n * 6 * SXY, 0.0f);
+        std::vector<uint8_t> cxy((size_t)n * 6 * SXY, 0);
+        std::vector<int2> dims((size_t)n);
+        for (int i = 0; i < n; ++i) {
+            emlab_grid_config ci = c;
+            ci.nx = st.nx[(size_t)i], ci.ny = st.ny[(size_t)i], ci.nz = st.nz[(size_t)i];
+            const int Si = std::max(ci.nx, std::max(ci.ny, ci.nz));
+            const std::vector<float> ti = pml_tables(ci, Si);
+            std::vector<uint8_t> ci_cls;
+            std::vector<float> ci_coef;
+            int Ki = 0;
+            pml_class_tables(ci, Si, ci_cls, ci_coef, Ki);
+            if (Ki != g->pml_K || ci_coef != coef)
+                return fail(EMLAB_ERR_INVALID, "stack: scenes' absorber coefficient tables differ");
+            for (int r : {0, 1, 3, 4}) {
+                const int len = (r == 0 || r == 3) ? ci.nx : ci.ny;
+                for (int p = 0; p < len; ++p) {
+                    pxy[((size_t)i * 6 + r) * SXY + p] = ti[(size_t)r * Si + p];
+                    cxy[((size_t)i * 6 + r) * SXY + p] = ci_cls[(size_t)r * Si + p];
+                }
+            }
+            dims[(size_t)i] = make_int2(ci.nx, ci.ny);
+        }
+        g->pml_xy_stride = SXY;
+        EMLAB_CUDA(g->d_pml_xy.alloc(pxy.size()));
+        EMLAB_CUDA(cudaMemcpy(g->d_pml_xy.p, pxy.data(), pxy.size() * 4, cudaMemcpyHostToDevice));
+        EMLAB_CUDA(g->d_pml_cls_xy.alloc(cxy.size()));
+        EMLAB_CUDA(cudaMemcpy(g->d_pml_cls_xy.p, cxy.data(), cxy.size(), cudaMemcpyHostToDevice));
+        EMLAB_CUDA(g->d_scene_xy.alloc(dims.size()));
+        EMLAB_CUDA(cudaMemcpy(g->d_scene_xy.p, dims.data(), dims.size() * 8, cudaMemcpyHostToDevice));
+        int dev = 0, sms = 0;
+        EMLAB_CUDA(cudaGetDevice(&dev));
+        EMLAB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int tys[3] = {4, 8, 16}, per_sm[3] = {4, 2, 1};
+        for (int t = 0; t < 3; ++t) {
+            const std::vector<int4> items = ragged_items(st.z0, st.nx, st.ny, st.nz, tys[t], per_sm[t] * sms);
+            EMLAB_REQUIRE(!items.empty(), "stack: no work items");
+            EMLAB_CUDA(g->d_items[t].alloc(items.size()));
+            EMLAB_CUDA(cudaMemcpy(g->d_items[t].p, items.data(), items.size() * 16, cudaMemcpyHostToDevice));
+            g->n_items[t] = (int)items.size();
+        }
+    } else {
+        for (auto& d : g->d_items) d.release();
+        g->n_items[0] = g->n_items[1] = g->n_items[2] = 0;
+        g->d_scene_xy.release(), g->d_pml_cls_xy.release(), g->d_pml_xy.release();
+    }
     EMLAB_CUDA(g->pml.alloc(pt.size()));
     EMLAB_CUDA(cudaMemcpy(g->pml.p, pt.data(), pt.size() * 4, cudaMemcpyHostToDevice));
     EMLAB_CUDA(g->pml_cls.alloc(pcls.size()));
@@ -198,7 +258,8 @@ int emlab::upload_pml(emlab_grid* g) {
 
 // Packed sources and their per-cell lists on the device (zoff: empty for a single scene).
 int emlab::upload_sources(emlab_grid* g, const std::vector<float>& packed, const std::vector<int32_t>& cells,
-                          const std::vector<int32_t>& lists, const std::vector<int32_t>& zoff) {
+                          const std::vector<int32_t>& lists, const std::vector<int32_t>& zoff,
+                          const std::vector<int32_t>& scene) {
     invalidate_graphs(g);
     g->ncells = (int)(cells.size() / 4) - 1;
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));  // buffers may be in use by queued steps
@@ -214,6 +275,11 @@ int emlab::upload_sources(emlab_grid* g, const std::vector<float>& packed, const
     if (!zoff.empty()) {
         EMLAB_CUDA(g->d_zoff.alloc(zoff.size()));
         EMLAB_CUDA(cudaMemcpy(g->d_zoff.p, zoff.data(), zoff.size() * 4, cudaMemcpyHostToDevice));
+    }
+    g->d_cell_scene.release();
+    if (!scene.empty()) {
+        EMLAB_CUDA(g->d_cell_scene.alloc(scene.size()));
+        EMLAB_CUDA(cudaMemcpy(g->d_cell_scene.p, scene.data(), scene.size() * 4, cudaMemcpyHostToDevice));
     }
     return EMLAB_OK;
 }
@@ -346,7 +412,8 @@ uint64_t enqueue_step(emlab_grid* g, int k, bool graph, const float* d_sig, cons
         }
         if (graph) g->graph_tickets = tickets;
         else g->work_base += tickets;
-        if (!tma) launch_yee_fused(a, g->wide, g->stream);
+        if (!tma && g->stack.ragged) g->launch_failed = true;  // no kernel here knows the scenes' cross-sections
+        else if (!tma) launch_yee_fused(a, g->wide, g->stream);
         launched += 1;
         g->cur ^= 1;
         a = yee_args(g);  // sources act on the new generation
@@ -355,6 +422,7 @@ uint64_t enqueue_step(emlab_grid* g, int k, bool graph, const float* d_sig, cons
     if (g->ncells > 0) {
         SourceArgs sa{};
         sa.cells = g->d_cells.p, sa.zoff = g->d_zoff.p, sa.lists = g->d_lists.p, sa.src = g->d_src.p;
+        sa.scene = g->stack.ragged ? g->d_cell_scene.p : nullptr;
         sa.signals = d_sig, sa.nsrc = g->nsrc, sa.ncells = g->ncells;
         launch_sources(a, sa, k, g->wide, g->stream);
         launched += 1;
@@ -573,6 +641,9 @@ int emlab_grid_step(emlab_grid* g, int count) {
     if (count <= 0) return EMLAB_OK;
     EMLAB_CUDA(cudaSetDevice(g->device));
     if (int rc = stack_commit(g)) return rc;
+    if (g->stack.ragged && !(tma_maps_ready(g->tma, 0) && tma_maps_ready(g->tma, 1)))
+        return fail(EMLAB_ERR_CUDA, "a stack of scenes with different cross-sections needs the TMA pair kernel, "
+                                    "and its tensor maps could not be encoded");
     const double dt = (double)g->cfg.courant;
     const int nsrc = g->nsrc;
     for (int base = 0; base < count; base += kChunk) {
@@ -633,6 +704,13 @@ int emlab_grid_step(emlab_grid* g, int count) {
                 if (ce == cudaSuccess) ie = cudaGraphInstantiate(&ex, graph_def, 0);
                 if (graph_def) cudaGraphDestroy(graph_def);
                 cudaGetLastError();
+                if (g->launch_failed) {  // the captured chunk lacks its solver launches: never replay it
+                    g->launch_failed = false;
+                    if (ex) cudaGraphExecDestroy(ex);
+                    ex = nullptr;
+                    return fail(EMLAB_ERR_CUDA, "the pair kernel could not be launched for a stack of scenes with "
+                                                "different cross-sections");
+                }
                 if (ie != cudaSuccess) {
                     ex = nullptr;
                     return fail(EMLAB_ERR_CUDA, std::string("step graph capture: ") + cudaGetErrorString(ie));
@@ -659,6 +737,11 @@ int emlab_grid_step(emlab_grid* g, int count) {
             if (g->timing)
                 if (int rc = timing_pair(g, &ev0, &ev1)) return rc;
             g_launches += enqueue_step(g, k, false, d_sig, d_prot, d_nrot, d_lrot, d_bl, rec, ev0, ev1);
+            if (g->launch_failed) {
+                g->launch_failed = false;
+                return fail(EMLAB_ERR_CUDA, "the pair kernel could not be launched for a stack of scenes with "
+                                            "different cross-sections");
+            }
             if (g->dft_on) {
                 if (g->dft_t == 0) g->dft_n0 = (long long)g->step;  // time index of the block's first sample
                 launch_dft_sample(monitor_args(g), g->d_dft_box.p, g->dft_nbox, g->dft_box_max, g->dft_points,
@@ -735,6 +818,7 @@ int emlab_grid_read_fields(emlab_grid* g, float* e_rgba, float* b_rgba) {
     if (int rc = require_grid(g)) return rc;
     EMLAB_CUDA(cudaSetDevice(g->device));
     const long long n = g->cells();
+    if (int rc = ensure_cell_materials(g)) return rc;
     for (int c = 0; c < 6; ++c) {
         float* dst = c < 3 ? e_rgba : b_rgba;
         if (!dst) continue;
@@ -781,6 +865,8 @@ int emlab_grid_set_kernel(emlab_grid* g, int kernel) {
     if (!g) return fail(EMLAB_ERR_INVALID, "null grid handle");
     EMLAB_REQUIRE(kernel == EMLAB_KERNEL_FUSED || kernel == EMLAB_KERNEL_SPLIT || kernel == EMLAB_KERNEL_FUSED_LDG,
                   "unknown kernel");
+    EMLAB_REQUIRE(!g->stack.ragged || kernel == EMLAB_KERNEL_FUSED,
+                  "a stack of scenes with different cross-sections steps with the fused kernel only");
     g->kernel = kernel;
     if (g->configured) refresh_tma(g);
     return EMLAB_OK;
@@ -792,6 +878,8 @@ int emlab_grid_set_tiling(emlab_grid* g, int tile_rows) {
                       tile_rows == 128,
                   "tiling must be 0 (automatic), 8 or 16 (32-cell rows), 32, 64 or 128 (64 x 4, 64 x 8 or 64 x 16 "
                   "tiles of cell pairs)");
+    EMLAB_REQUIRE(!g->stack.ragged || tile_rows == 0 || tile_rows == 32 || tile_rows == 64 || tile_rows == 128,
+                  "a stack of scenes with different cross-sections steps with tiles of cell pairs only (0, 32, 64, 128)");
     g->tile_rows = tile_rows;
     if (g->configured) refresh_tma(g);  // the TMA boxes depend on the tile height
     return EMLAB_OK;
@@ -1357,6 +1445,7 @@ int emlab_probe_gather(emlab_grid* g, const int* origins, int n_probes, float* o
     if (int rc = check_launch()) return rc;
     EMLAB_CUDA(cudaMemcpyAsync(out, d_out.p, (size_t)n_probes * 54 * 16, cudaMemcpyDeviceToHost, g->stream));
     if (int rc = emlab_grid_synchronize(g, 0)) return rc;
+    if (int rc = ensure_cell_materials(g)) return rc;
     const int nx = g->cfg.nx, ny = g->cfg.ny, nz = g->cfg.nz;
     for (int id = 0; id < n_probes * 54; ++id) {
         const int probe = id / 54, k = id % 54, t = k % 27;
@@ -1384,6 +1473,7 @@ int emlab_render(emlab_grid* g, const emlab_render_params* params, unsigned char
     const size_t pixels = (size_t)q.width * q.height;
     DevBuf<float> d_sigma, d_eps;
     DevBuf<unsigned char> d_img;
+    if (int rc = ensure_cell_materials(g)) return rc;
     const bool mats = g->cell_sigma.size() == cells && g->cell_eps.size() == cells;
     if (mats) {
         EMLAB_CUDA(d_sigma.alloc(cells));
@@ -1518,6 +1608,7 @@ int emlab_analyzer_collect(emlab_grid* g, float* probe_out, double* flux_out, in
     EMLAB_REQUIRE((probe_out || !a.n_probes) && (flux_out || a.planes.empty()), "null analyzer output");
     EMLAB_CUDA(cudaSetDevice(g->device));
     EMLAB_CUDA(cudaEventSynchronize(a.done));
+    if (int rc = ensure_cell_materials(g)) return rc;
     const int nx = g->cfg.nx, ny = g->cfg.ny, nz = g->cfg.nz;
     for (int id = 0; id < a.n_probes * 54; ++id) {
         const int probe = id / 54, k = id % 54, t = k % 27;

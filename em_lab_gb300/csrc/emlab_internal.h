@@ -54,6 +54,18 @@ struct YeeArgs {
     unsigned long long* work;      // work-item ticket counter of the persistent kernel (monotonic)
     unsigned long long work_base;  // tickets consumed by all earlier launches on this counter
     int wait_polls;                // polls of a plane's copy barrier before the CTA gives up (wait_limit())
+    // x / y absorber lookups of the pair kernel: rows 0 (I_x), 1 (I_y), 3 (H_x), 4 (H_y) of a
+    // [6][pml_xy_stride] table pair, one pair per scene of a stack whose scenes have their own
+    // cross-sections (pml_xy_scene elements apart), else the grid's own tables (pml_xy_scene 0)
+    const unsigned char* pml_cls_xy;
+    const float* pml_xy;
+    int pml_xy_stride;
+    int pml_xy_scene;
+    // such a stack's pair-kernel work items (x0 | y0 << 16, first plane, end plane, scene), each inside
+    // one scene, and every scene's nx, ny; null for a grid whose items follow from its size
+    const int4* items;
+    int n_items;
+    const int2* scene_xy;
 };
 
 // Polls of an on-device wait (mbarrier) before a kernel reports EMLAB_ERR_TIMEOUT: about a second by
@@ -65,6 +77,7 @@ int wait_limit();
 struct SourceArgs {
     const int4* cells;       // xyz = cell (scene coordinates), w = first list entry; entry n is the sentinel
     const int* zoff;         // per cell: first plane of its scene in a stack of scenes (null: 0)
+    const int* scene;        // per cell: its scene in a stack of scenes with their own cross-sections (or null)
     const int* lists;
     const float4* src;       // 4 float4 per source: center, halfExtent, polAmp, softness
     const float* signals;    // [step][nsrc]
@@ -87,6 +100,12 @@ TmaMaps* tma_maps_create();
 void tma_maps_destroy(TmaMaps* m);
 // Encodes the maps for generation `gen` (0 or 1); returns false if TMA cannot be used.
 bool tma_maps_encode(TmaMaps* m, int gen, const YeeArgs& a, bool wide);
+bool tma_maps_ready(const TmaMaps* m, int gen);
+// pair-kernel work items of a stack of scenes with their own cross-sections (scene by scene, z
+// chunk by chunk, tile by tile): tiles of 64 x ty cells over each scene's nx x ny, z chunks of one
+// length for all scenes, chosen for g CTAs as the uniform schedule chooses it
+std::vector<int4> ragged_items(const std::vector<int>& z0, const std::vector<int>& nx, const std::vector<int>& ny,
+                               const std::vector<int>& nz, int ty, int g);
 // Launches the TMA kernel reading generation `gen`; err receives a nonzero word if a wait timed out.
 // *tickets receives the work-counter tickets the launch consumes (0 for the non-persistent kernels)
 bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsigned* err, cudaStream_t s,

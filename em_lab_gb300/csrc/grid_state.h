@@ -70,9 +70,15 @@ struct AnalyzerSlot {
 // between consecutive scenes.
 struct StackLayout {
     std::vector<int> z0, nz;
+    std::vector<int> nx, ny;  // per scene; below the grid's own nx, ny only in a ragged stack
+    bool ragged = false;      // scenes of different cross-sections (each at x = y = 0, the rest frozen)
     std::vector<ClassTable> tabs;                    // per-scene class tables until they are merged
     std::vector<bool> has_tab;
     std::vector<std::vector<emlab_source>> sources;  // per-scene sources (scene coordinates)
+    // per-scene conductivity / permittivity as uploaded (empty: vacuum); the grid's host copies
+    // (cell_sigma, cell_eps: read-back only) are assembled from them on demand
+    std::vector<std::vector<float>> sig, eps;
+    bool cells_stale = true;
     bool dirty = false;                              // per-scene tables not merged yet
     int scenes() const { return (int)z0.size(); }
 };
@@ -116,10 +122,20 @@ struct emlab_grid {
     DevBuf<int4> d_cells;
     DevBuf<int> d_lists;
     DevBuf<int> d_zoff;  // stacks: per source cell, the first plane of its scene
+    DevBuf<int> d_cell_scene;  // ragged stacks: per source cell, its scene
     int nsrc = 0, ncells = 0;
     // stack of scenes (empty: a single scene)
     emlab::StackLayout stack;
     uint32_t stack_sep = 0;  // class of the separator planes
+    // ragged stack: pair-kernel work items per tile height (4, 8, 16 rows), every scene's nx, ny,
+    // and per-scene x / y absorber tables
+    DevBuf<int4> d_items[3];
+    int n_items[3] = {0, 0, 0};
+    DevBuf<int2> d_scene_xy;
+    DevBuf<uint8_t> d_pml_cls_xy;
+    DevBuf<float> d_pml_xy;
+    int pml_xy_stride = 0;
+    bool launch_failed = false;  // set by a step whose solver launch was impossible (ragged stack)
     // per-chunk scalars: signals[k][nsrc], port rot[k], ntff rot[k], line rot[k], blends
     DevBuf<uint8_t> d_stage;
     uint8_t* h_stage[2] = {nullptr, nullptr};
@@ -208,9 +224,12 @@ int reset_monitors(emlab_grid* g);
 // drops the captured step graphs (any change of a buffer, a monitor or a launch setting)
 void invalidate_graphs(emlab_grid* g);
 int upload_sources(emlab_grid* g, const std::vector<float>& packed, const std::vector<int32_t>& cells,
-                   const std::vector<int32_t>& lists, const std::vector<int32_t>& zoff);
+                   const std::vector<int32_t>& lists, const std::vector<int32_t>& zoff,
+                   const std::vector<int32_t>& scene = {});
 // stack.cu: merges per-scene materials uploaded since the last step
 int stack_commit(emlab_grid* g);
+// the host copies of a stack's per-cell materials, assembled from the scenes' own (no-op for a grid)
+int ensure_cell_materials(emlab_grid* g);
 // cpml.cu: tables and psi arrays for the configured size, psi reset, and the two in-place passes
 int cpml_prepare(emlab_grid* g);
 int cpml_clear(emlab_grid* g);

@@ -111,27 +111,44 @@ __device__ __forceinline__ void ntff_point(const int* box, int index, int node[3
 }
 
 // ntff_accumulate.comp:30-52: 32 floats per point (stage1 eRe, eIm, hRe, hIm, stage2 ...). The
-// block's 256 x 128 B of state move between HBM and shared memory as one contiguous chunk
+// block's 128 x 128 B of state move between HBM and shared memory as one contiguous chunk
 // (consecutive threads, consecutive float4s), rows padded to 9 float4s against bank conflicts;
-// each thread then updates its own point there. Same arithmetic per point.
-__global__ void __launch_bounds__(256) ntff_kernel(MonitorArgs m, const int* box, int points, float4* ph,
-                                                   const float4* rot, const float* blend, int k) {
+// each thread then updates its own point there. Every load a thread makes (its eight float4s of
+// the block's state and the 18 field values of its node) is issued before the first is used, so
+// the kernel waits one memory round trip instead of nine. Same arithmetic per point.
+constexpr int kNtffThreads = 128;
+__global__ void __launch_bounds__(kNtffThreads) ntff_kernel(MonitorArgs m, const int* box, int points, float4* ph,
+                                                            const float4* rot, const float* blend, int k) {
     __shared__ int sbox[13];
-    __shared__ float4 st[256 * 9];
+    __shared__ float4 st[kNtffThreads * 9];
     if (threadIdx.x < 13) sbox[threadIdx.x] = box[threadIdx.x];
-    const int first = blockIdx.x * blockDim.x;
-    const int count = min((int)blockDim.x, points - first);
+    const int first = blockIdx.x * kNtffThreads;
+    const int count = min(kNtffThreads, points - first);
     float4* base = ph + 8 * (long long)first;
-    for (int j = threadIdx.x; j < 8 * count; j += blockDim.x) st[9 * (j >> 3) + (j & 7)] = base[j];
-    __syncthreads();
+    float4 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int j = threadIdx.x + q * kNtffThreads;
+        if (j < 8 * count) v[q] = base[j];
+    }
+    __syncthreads();  // sbox
     const int i = first + threadIdx.x;
-    if (i < points) {
+    const bool live = i < points;
+    float E[3], Hh[3];
+    if (live) {
         int node[3];
         float n[3], w;
         ntff_point(sbox, i, node, n, w);
-        float E[3], Hh[3];
         e_at_node(m, node[0], node[1], node[2], E[0], E[1], E[2]);
         b_at_node(m, node[0], node[1], node[2], Hh[0], Hh[1], Hh[2]);
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int j = threadIdx.x + q * kNtffThreads;
+        if (j < 8 * count) st[9 * (j >> 3) + (j & 7)] = v[q];
+    }
+    __syncthreads();
+    if (live) {
         const float4 r = rot[k];
         const float b = blend[k];
         float4* p = st + 9 * threadIdx.x;
@@ -151,7 +168,11 @@ __global__ void __launch_bounds__(256) ntff_kernel(MonitorArgs m, const int* box
         for (int q = 0; q < 4; ++q) p[q] = s1[q], p[4 + q] = s2[q];
     }
     __syncthreads();
-    for (int j = threadIdx.x; j < 8 * count; j += blockDim.x) base[j] = st[9 * (j >> 3) + (j & 7)];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int j = threadIdx.x + q * kNtffThreads;
+        if (j < 8 * count) base[j] = st[9 * (j >> 3) + (j & 7)];
+    }
 }
 
 // line_accumulate.comp:30-48
@@ -643,7 +664,8 @@ void launch_ports(const MonitorArgs& m, const int4* ports, int n, float* phasors
 
 void launch_ntff(const MonitorArgs& m, const int* box, int points, float* phasors, const float4* rot,
                  const float* blend, int k, cudaStream_t s) {
-    ntff_kernel<<<(points + 255) / 256, 256, 0, s>>>(m, box, points, reinterpret_cast<float4*>(phasors), rot, blend, k);
+    ntff_kernel<<<(points + kNtffThreads - 1) / kNtffThreads, kNtffThreads, 0, s>>>(
+        m, box, points, reinterpret_cast<float4*>(phasors), rot, blend, k);
 }
 
 void launch_lines(const MonitorArgs& m, const int4* q, int nq, const int4* terms, const float* weights,

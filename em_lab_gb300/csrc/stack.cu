@@ -56,7 +56,10 @@ ClassKey key_of(const ClassTable& t, uint32_t c) {
     return k;
 }
 
-int configure_layout(emlab_grid* g, const emlab_grid_config& c, const std::vector<int>& nz) {
+// c.nx, c.ny: the grid's cross-section (the largest scene's in a ragged stack); nx, ny: every
+// scene's own (equal to c's in a uniform stack).
+int configure_layout(emlab_grid* g, const emlab_grid_config& c, const std::vector<int>& nz, const std::vector<int>& nx,
+                     const std::vector<int>& ny) {
     const int n = (int)nz.size();
     emlab_grid_config t = c;
     long long total = n - 1;
@@ -78,12 +81,19 @@ int configure_layout(emlab_grid* g, const emlab_grid_config& c, const std::vecto
     g->pitch = pitch, g->plane = plane, g->padded = padded;
     StackLayout s;
     s.nz = nz;
+    s.nx = nx, s.ny = ny;
+    for (int i = 0; i < n; ++i) s.ragged = s.ragged || nx[(size_t)i] != t.nx || ny[(size_t)i] != t.ny;
+    if (s.ragged) {
+        g->kernel = EMLAB_KERNEL_FUSED;  // the pair kernel reads each item's scene; the others do not
+        if (g->tile_rows != 0 && g->tile_rows != 32 && g->tile_rows != 64 && g->tile_rows != 128) g->tile_rows = 0;
+    }
     s.z0.resize((size_t)n);
     int z = 0;
     for (int i = 0; i < n; ++i) s.z0[(size_t)i] = z, z += nz[(size_t)i] + 1;
     s.tabs.resize((size_t)n);
     s.has_tab.assign((size_t)n, false);
     s.sources.resize((size_t)n);
+    s.sig.resize((size_t)n), s.eps.resize((size_t)n);
     s.dirty = true;
     g->stack = std::move(s);
     return upload_pml(g);
@@ -140,23 +150,32 @@ int commit(emlab_grid* g) {
     } catch (const std::bad_alloc&) {
         return fail(EMLAB_ERR_OOM, "host allocation failed while merging the scene classes");
     }
-    const size_t plane = (size_t)g->plane;
+    const size_t plane = (size_t)g->plane, pitch = (size_t)g->pitch;
     for (int i = 0; i < n; ++i) {
+        // the scene's cells (x < its nx, y < its ny); the rest of its planes keeps the frozen class
         uint32_t* dst = m.cls.data() + (size_t)s.z0[(size_t)i] * plane;
-        const size_t count = (size_t)s.nz[(size_t)i] * plane;
-        if (!s.has_tab[(size_t)i]) {
-            std::fill(dst, dst + count, 0u);
-            continue;
-        }
-        const std::vector<uint32_t>& r = remap[(size_t)i];
-        const uint32_t* src = s.tabs[(size_t)i].cls.data();
+        const int sx = s.nx[(size_t)i], sy = s.ny[(size_t)i], sz = s.nz[(size_t)i];
+        const size_t spitch = (size_t)row_pitch(sx);
+        const std::vector<uint32_t>* r = s.has_tab[(size_t)i] ? &remap[(size_t)i] : nullptr;
+        const uint32_t* src = r ? s.tabs[(size_t)i].cls.data() : nullptr;
 #pragma omp parallel for schedule(static)
-        for (long long j = 0; j < (long long)count; ++j) {
-            const uint32_t v = r[src[j]];
-            dst[j] = v & 0x80000000u ? wire_start + (v & 0x7fffffffu) : v;
+        for (long long row = 0; row < (long long)sz * sy; ++row) {
+            const size_t z = (size_t)row / sy, y = (size_t)row % sy;
+            uint32_t* d = dst + z * plane + y * pitch;
+            if (!r) {
+                std::fill(d, d + sx, 0u);
+                continue;
+            }
+            const uint32_t* q = src + (z * sy + y) * spitch;
+            for (int x = 0; x < sx; ++x) {
+                const uint32_t v = (*r)[q[x]];
+                d[x] = v & 0x80000000u ? wire_start + (v & 0x7fffffffu) : v;
+            }
         }
-        s.tabs[(size_t)i] = ClassTable();  // merged: the per-scene copy is no longer needed
-        s.has_tab[(size_t)i] = false;
+        if (r) {
+            s.tabs[(size_t)i] = ClassTable();  // merged: the per-scene copy is no longer needed
+            s.has_tab[(size_t)i] = false;
+        }
     }
     if (int rc = upload_class_table(g, m)) return rc;
     g->stack_sep = sep;
@@ -171,7 +190,7 @@ int merge_sources(emlab_grid* g) {
     StackLayout& s = g->stack;
     std::vector<emlab_source> all_desc;
     std::vector<float> all_packed;
-    std::vector<int32_t> cells, lists, zoff;
+    std::vector<int32_t> cells, lists, zoff, scene;
     for (int i = 0; i < s.scenes(); ++i) {
         const std::vector<emlab_source>& in = s.sources[(size_t)i];
         if (in.empty()) continue;
@@ -179,13 +198,14 @@ int merge_sources(emlab_grid* g) {
         std::vector<float> packed;
         const int ns = pack_sources(in.data(), in.size(), desc, packed);
         std::vector<int32_t> c, l;
-        const int dims[3] = {g->cfg.nx, g->cfg.ny, s.nz[(size_t)i]};
+        const int dims[3] = {s.nx[(size_t)i], s.ny[(size_t)i], s.nz[(size_t)i]};
         source_lists(packed, ns, dims, c, l);
         const int32_t src0 = (int32_t)all_desc.size(), list0 = (int32_t)lists.size();
         const size_t nc = c.size() / 4 - 1;
         for (size_t k = 0; k < nc; ++k) {
             cells.insert(cells.end(), {c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3] + list0});
             zoff.push_back(s.z0[(size_t)i]);
+            scene.push_back(i);
         }
         const int32_t used = c[4 * nc + 3];  // the sentinel: list entries of this scene
         for (int32_t k = 0; k < used; ++k) lists.push_back(l[(size_t)k] + src0);
@@ -195,40 +215,66 @@ int merge_sources(emlab_grid* g) {
     cells.insert(cells.end(), {0, 0, 0, (int32_t)lists.size()});
     if (lists.empty()) lists.push_back(0);
     if (zoff.empty()) zoff.push_back(0);
+    if (scene.empty()) scene.push_back(0);
     g->nsrc = (int)all_desc.size();
     g->desc = all_desc;
     g->packed = all_packed;
-    return upload_sources(g, all_packed, cells, lists, zoff);
+    return upload_sources(g, all_packed, cells, lists, zoff, s.ragged ? scene : std::vector<int32_t>());
 }
 
 }  // namespace
 
 int emlab::stack_commit(emlab_grid* g) { return g->stack.dirty ? commit(g) : EMLAB_OK; }
 
+int emlab::ensure_cell_materials(emlab_grid* g) {
+    StackLayout& s = g->stack;
+    const size_t cells = (size_t)g->cells();
+    if (s.scenes() == 0 || (!s.cells_stale && g->cell_sigma.size() == cells)) return EMLAB_OK;
+    try {
+        g->cell_sigma.assign(cells, 0.0f);
+        g->cell_eps.assign(cells, 1.0f);
+    } catch (const std::bad_alloc&) {
+        return fail(EMLAB_ERR_OOM, "host allocation failed");
+    }
+    const size_t gx = (size_t)g->cfg.nx, gy = (size_t)g->cfg.ny;
+    for (int i = 0; i < s.scenes(); ++i) {
+        const std::vector<float>& sg = s.sig[(size_t)i];
+        const std::vector<float>& ep = s.eps[(size_t)i];
+        if (sg.empty()) continue;  // vacuum
+        const size_t nx = (size_t)s.nx[(size_t)i], ny = (size_t)s.ny[(size_t)i], nz = (size_t)s.nz[(size_t)i];
+        for (size_t z = 0; z < nz; ++z)
+            for (size_t y = 0; y < ny; ++y) {
+                const size_t d = (((size_t)s.z0[(size_t)i] + z) * gy + y) * gx, q = (z * ny + y) * nx;
+                std::memcpy(g->cell_sigma.data() + d, sg.data() + q, nx * 4);
+                std::memcpy(g->cell_eps.data() + d, ep.data() + q, nx * 4);
+            }
+    }
+    s.cells_stale = false;
+    return EMLAB_OK;
+}
+
 extern "C" {
 
-int emlab_stack_configure(emlab_grid* g, const emlab_grid_config* req, const int* scene_nz, int n_scenes) {
-    if (!g || !req || !scene_nz) return fail(EMLAB_ERR_INVALID, "null argument");
+namespace {
+int configure_scenes(emlab_grid* g, const emlab_grid_config* req, const int* dims, int n_scenes) {
     EMLAB_REQUIRE(n_scenes >= 1, "a stack needs at least one scene");
     EMLAB_CUDA(cudaSetDevice(g->device));
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
     emlab_grid_config c = *req;
-    std::vector<int> nz((size_t)n_scenes);
+    std::vector<int> nx((size_t)n_scenes), ny((size_t)n_scenes), nz((size_t)n_scenes);
+    int mx = 0, my = 0;
     for (int i = 0; i < n_scenes; ++i) {  // each scene is clamped as SimulationGrid::configure clamps it
         emlab_grid_config ci = *req;
-        ci.nz = scene_nz[i];
+        ci.nx = dims[3 * i], ci.ny = dims[3 * i + 1], ci.nz = dims[3 * i + 2];
         clamp_config(ci);
-        nz[(size_t)i] = ci.nz;
+        nx[(size_t)i] = ci.nx, ny[(size_t)i] = ci.ny, nz[(size_t)i] = ci.nz;
+        mx = std::max(mx, ci.nx), my = std::max(my, ci.ny);
         c = ci;
     }
-    if (int rc = configure_layout(g, c, nz)) return rc;
-    const long long cells = g->cells();
-    try {
-        g->cell_sigma.assign((size_t)cells, 0.0f);
-        g->cell_eps.assign((size_t)cells, 1.0f);
-    } catch (const std::bad_alloc&) {
-        return fail(EMLAB_ERR_OOM, "host allocation failed");
-    }
+    EMLAB_REQUIRE(mx < 65536 && my < 65536, "stack cross-section too large");
+    c.nx = mx, c.ny = my;
+    if (int rc = configure_layout(g, c, nz, nx, ny)) return rc;
+    g->cell_sigma.clear(), g->cell_eps.clear();  // assembled from the scenes' materials when read back
     if (int rc = commit(g)) return rc;
     if (int rc = clear_fields(g)) return rc;
     g->step = 0;
@@ -236,6 +282,28 @@ int emlab_stack_configure(emlab_grid* g, const emlab_grid_config* req, const int
     if (int rc = merge_sources(g)) return rc;
     if (int rc = reset_monitors(g)) return rc;
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
+    return EMLAB_OK;
+}
+}  // namespace
+
+int emlab_stack_configure(emlab_grid* g, const emlab_grid_config* req, const int* scene_nz, int n_scenes) {
+    if (!g || !req || !scene_nz) return fail(EMLAB_ERR_INVALID, "null argument");
+    std::vector<int> dims;
+    for (int i = 0; i < n_scenes; ++i) dims.insert(dims.end(), {req->nx, req->ny, scene_nz[i]});
+    return configure_scenes(g, req, dims.data(), n_scenes);
+}
+
+int emlab_stack_configure_scenes(emlab_grid* g, const emlab_grid_config* req, const int* dims, int n_scenes) {
+    if (!g || !req || !dims) return fail(EMLAB_ERR_INVALID, "null argument");
+    return configure_scenes(g, req, dims, n_scenes);
+}
+
+int emlab_stack_scene_dims(const emlab_grid* g, int* dims) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(dims, "null argument");
+    const StackLayout& s = g->stack;
+    for (int i = 0; i < s.scenes(); ++i)
+        dims[3 * i] = s.nx[(size_t)i], dims[3 * i + 1] = s.ny[(size_t)i], dims[3 * i + 2] = s.nz[(size_t)i];
     return EMLAB_OK;
 }
 
@@ -256,7 +324,7 @@ int emlab_stack_upload_materials(emlab_grid* g, int scene, const float* sigma, c
     if (int rc = require_grid(g)) return rc;
     StackLayout& s = g->stack;
     EMLAB_REQUIRE(scene >= 0 && scene < s.scenes(), "no such scene in the stack");
-    if (nx != g->cfg.nx || ny != g->cfg.ny || nz != s.nz[(size_t)scene])
+    if (nx != s.nx[(size_t)scene] || ny != s.ny[(size_t)scene] || nz != s.nz[(size_t)scene])
         return fail(EMLAB_ERR_INVALID, "SimulationGrid: material volume size does not match the grid");
     EMLAB_REQUIRE(sigma && eps_r, "null material array");
     EMLAB_REQUIRE((edges || n_edges == 0) && (wires || n_wires == 0), "null override array");
@@ -267,9 +335,11 @@ int emlab_stack_upload_materials(emlab_grid* g, int scene, const float* sigma, c
     s.tabs[(size_t)scene] = std::move(t);
     s.has_tab[(size_t)scene] = true;
     s.dirty = true;
-    const size_t off = (size_t)s.z0[(size_t)scene] * nx * ny, count = (size_t)nx * ny * nz;
-    std::memcpy(g->cell_sigma.data() + off, sigma, count * 4);
-    std::memcpy(g->cell_eps.data() + off, eps_r, count * 4);
+    // the scene's own copies (read-back only)
+    const size_t count = (size_t)nx * ny * nz;
+    s.sig[(size_t)scene].assign(sigma, sigma + count);
+    s.eps[(size_t)scene].assign(eps_r, eps_r + count);
+    s.cells_stale = true;
     EMLAB_CUDA(cudaSetDevice(g->device));
     if (int rc = clear_fields(g)) return rc;  // uploadMaterials starts the scenes over
     g->step = 0;
@@ -318,13 +388,19 @@ int emlab_stack_compact(emlab_grid* g, const unsigned char* keep) {
     const std::vector<int> old_z0 = s.z0, old_nz = s.nz;
     const long long old_padded = g->padded;
     const int old_cur = g->cur;
-    std::vector<int> nz;
+    std::vector<int> nz, nxk, nyk;
     std::vector<std::vector<emlab_source>> src;
-    for (int i : idx) nz.push_back(s.nz[(size_t)i]), src.push_back(s.sources[(size_t)i]);
-    const std::vector<float> old_sig = std::move(g->cell_sigma), old_eps = std::move(g->cell_eps);
+    std::vector<std::vector<float>> sigk, epsk;
+    for (int i : idx) {
+        nz.push_back(s.nz[(size_t)i]), nxk.push_back(s.nx[(size_t)i]), nyk.push_back(s.ny[(size_t)i]);
+        src.push_back(s.sources[(size_t)i]);
+        sigk.push_back(std::move(s.sig[(size_t)i])), epsk.push_back(std::move(s.eps[(size_t)i]));
+    }
     const emlab_grid_config c = g->cfg;
-    if (int rc = configure_layout(g, c, nz)) return rc;
+    if (int rc = configure_layout(g, c, nz, nxk, nyk)) return rc;
     s.sources = src;
+    s.sig = std::move(sigk), s.eps = std::move(epsk);
+    g->cell_sigma.clear(), g->cell_eps.clear();
     s.dirty = false;
     const size_t plane = (size_t)g->plane, esize = g->wide ? 4 : 2;
     EMLAB_CUDA(cudaMemsetAsync(g->fields.p, 0, g->fields.n * 4, g->stream));
@@ -344,9 +420,6 @@ int emlab_stack_compact(emlab_grid* g, const unsigned char* keep) {
                                   cudaMemcpyHostToDevice));
         }
     }
-    const size_t cells_plane = (size_t)c.nx * c.ny;
-    g->cell_sigma.assign((size_t)g->cells(), 0.0f);
-    g->cell_eps.assign((size_t)g->cells(), 1.0f);
     for (size_t k = 0; k < idx.size(); ++k) {
         const size_t zo = (size_t)old_z0[(size_t)idx[k]], zn = (size_t)s.z0[k], depth = (size_t)s.nz[k];
         for (int comp = 0; comp < 6; ++comp) {
@@ -356,9 +429,6 @@ int emlab_stack_compact(emlab_grid* g, const unsigned char* keep) {
         }
         EMLAB_CUDA(cudaMemcpyAsync(g->cls.p + zn * plane * esize, old_cls.p + zo * plane * esize,
                                    depth * plane * esize, cudaMemcpyDeviceToDevice, g->stream));
-        std::memcpy(g->cell_sigma.data() + zn * cells_plane, old_sig.data() + zo * cells_plane,
-                    depth * cells_plane * 4);
-        std::memcpy(g->cell_eps.data() + zn * cells_plane, old_eps.data() + zo * cells_plane, depth * cells_plane * 4);
     }
     g->cur = 0;
     refresh_tma(g);

@@ -190,15 +190,27 @@ __global__ void __launch_bounds__(64) apply_sources(YeeArgs a, SourceArgs sa, in
     const int x = entry.x, y = entry.y, z = entry.z + (sa.zoff ? sa.zoff[id] : 0);
     const long long i = (long long)z * a.plane + (long long)y * a.pitch + x;
     const unsigned c = load_class<Idx>(a, i);
+    // the absorber of the cell's scene: in a stack of scenes with their own cross-sections its nx,
+    // ny and x / y profiles (common.glsl:40-43 and 15-27 on the scene's own grid)
+    int snx = a.nx, sny = a.ny;
+    const float* pxy = a.pml;
+    int SX = a.pml_stride;
+    if (sa.scene && a.scene_xy) {
+        const int sc = sa.scene[id];
+        const int2 d = __ldg(a.scene_xy + sc);
+        snx = d.x, sny = d.y;
+        pxy = a.pml_xy + (long long)sc * a.pml_xy_scene, SX = a.pml_xy_stride;
+    }
+    const bool inp = x < a.L || y < a.L || x >= snx - (a.L + 1) || y >= sny - (a.L + 1) || __ldg(a.pml_z + z) != 0;
     float cbx, cby, cbz;
-    if (!in_pml(a, x, y, z)) {
+    if (!inp) {
         const float4 t0 = __ldg(a.tabE + 2 * c), t1 = __ldg(a.tabE + 2 * c + 1);
         cbx = t0.w, cby = t1.x, cbz = t1.y;
     } else {
         const float4 m0 = __ldg(a.tabM + 2 * c), m1 = __ldg(a.tabM + 2 * c + 1);
         const int S = a.pml_stride;
-        const float ix = a.pml[x], iy = a.pml[S + y], iz = a.pml[2 * S + z];
-        const float hx = a.pml[3 * S + x], hy = a.pml[4 * S + y], hz = a.pml[5 * S + z];
+        const float ix = pxy[x], iy = pxy[SX + y], iz = a.pml[2 * S + z];
+        const float hx = pxy[3 * SX + x], hy = pxy[4 * SX + y], hz = a.pml[5 * S + z];
         const float sx = m0.x + ((hx + iy) + iz), sy = m0.y + ((ix + hy) + iz), sz = m0.z + ((ix + iy) + hz);
         const float dx = a.dt / m0.w, dy = a.dt / m1.x, dz = a.dt / m1.y;
         cbx = dx * emlab_phi(sx * dx), cby = dy * emlab_phi(sy * dy), cbz = dz * emlab_phi(sz * dz);

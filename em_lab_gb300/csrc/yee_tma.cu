@@ -425,7 +425,7 @@ __device__ __forceinline__ void b_update(const YeeArgs& a, float& bx, float& by,
 // E^{n+1} of one cell from its curl (update_E.comp:41-64).
 __device__ __forceinline__ void e_update(const YeeArgs& a, float& ex, float& ey, float& ez, float cx, float cy,
                                          float cz, unsigned c, bool inp, int R1, int R2, int R4, int iz, int hz, int x,
-                                         int y, int z) {
+                                         int y, int z, int scene) {
     if (!inp) {
         if (c == 0) {  // vacuum: ca = 1 and cb = dt exactly, so 1 * e + dt * curl == e + dt * curl
             const float dt = a.dt;
@@ -445,7 +445,16 @@ __device__ __forceinline__ void e_update(const YeeArgs& a, float& ex, float& ey,
         ey = ky.x * ey + ky.y * cy;
         ez = kz.x * ez + kz.y * cz;
     } else {
-        e_cell(a, ex, ey, ez, cx, cy, cz, c, x, y, z);
+        // a non-vacuum edge material inside the absorber (update_E.comp:51-64), the x / y profiles
+        // those of the cell's scene: e_cell's arithmetic
+        const float4 m0 = __ldg(a.tabM + 2 * c), m1 = __ldg(a.tabM + 2 * c + 1);
+        const float* pxy = a.pml_xy + (long long)scene * a.pml_xy_scene;
+        const int SX = a.pml_xy_stride, S = a.pml_stride;
+        const float ix = __ldg(pxy + x), iy = __ldg(pxy + SX + y), izv = __ldg(a.pml + 2 * S + z);
+        const float hx = __ldg(pxy + 3 * SX + x), hy = __ldg(pxy + 4 * SX + y), hzv = __ldg(a.pml + 5 * S + z);
+        ex = e_pml(ex, cx, m0.x + ((hx + iy) + izv), m0.w, a.dt);
+        ey = e_pml(ey, cy, m0.y + ((ix + hy) + izv), m1.x, a.dt);
+        ez = e_pml(ez, cz, m0.z + ((ix + iy) + hzv), m1.y, a.dt);
     }
 }
 
@@ -463,20 +472,27 @@ struct PairSched {
     int zc;       // planes per z chunk
     unsigned long long* work;
     unsigned long long base;
+    const int4* tab;  // a stack of scenes with their own cross-sections: the items themselves
 };
 
 struct PairItem {
-    int x0, y0, zs, ze, zstart;
+    int x0, y0, zs, ze, zstart, scene;
 };
 
 template <int TY>
 __device__ __forceinline__ PairItem pair_item(const PairSched& ps, int nz, int item) {
-    const int c = item / ps.tiles, t = item - c * ps.tiles;
     PairItem it;
-    it.x0 = (t % ps.tiles_x) * 64;
-    it.y0 = (t / ps.tiles_x) * TY;
-    it.zs = c * ps.zc;
-    it.ze = min(nz, it.zs + ps.zc);
+    if (ps.tab) {
+        const int4 t = __ldg(ps.tab + item);
+        it.x0 = t.x & 0xffff, it.y0 = (int)((unsigned)t.x >> 16), it.zs = t.y, it.ze = t.z, it.scene = t.w;
+    } else {
+        const int c = item / ps.tiles, t = item - c * ps.tiles;
+        it.x0 = (t % ps.tiles_x) * 64;
+        it.y0 = (t / ps.tiles_x) * TY;
+        it.zs = c * ps.zc;
+        it.ze = min(nz, it.zs + ps.zc);
+        it.scene = 0;
+    }
     it.zstart = it.zs > 0 ? it.zs - 1 : 0;  // a chunk above z = 0 first rebuilds B^{n+1/2}(zs-1)
     return it;
 }
@@ -594,35 +610,46 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1)
     // box is DC elements further) and of the column cell (x0-1, y0+lane); B tile slot = element - 2
     const int me = (ctl ? 0 : warp + 1) * W + 2 * lane + 4;
     const int ce = (lane + 1) * W + 3;
-    auto pml_rows = [&](int px, int py, int& R1, int& R2, int& R3, int& R4) {
-        const int ix = __ldg(pcls + px), iy = __ldg(pcls + PS + py), hx = __ldg(pcls + 3 * PS + px),
-                  hy = __ldg(pcls + 4 * PS + py);
+    const int SX = a.pml_xy_stride;
+    // x / y depth classes from the item's scene's table (pcx), z from the grid's
+    auto pml_rows = [&](const unsigned char* pcx, int px, int py, int& R1, int& R2, int& R3, int& R4) {
+        const int ix = __ldg(pcx + px), iy = __ldg(pcx + SX + py), hx = __ldg(pcx + 3 * SX + px),
+                  hy = __ldg(pcx + 4 * SX + py);
         R1 = (ix * K + hy) * K, R2 = (hx * K + iy) * K, R3 = (hx * K + hy) * K, R4 = (ix * K + iy) * K;
     };
-    auto pml_xy_of = [&](int px, int py) { return px < L || py < L || px >= a.nx - (L + 1) || py >= a.ny - (L + 1); };
 
     int k = 0;     // load index of the current iteration's plane z
     int iter = 0;  // iteration counter: parity selects the B tile buffer
     for (int ord = 0, item = queue[0]; item >= 0; item = queue[++ord & 7]) {
         const PairItem itm = pair_item<TY>(ps, a.nz, item);
-        const int x0 = itm.x0, y0 = itm.y0, zs = itm.zs, ze = itm.ze;
+        const int x0 = itm.x0, y0 = itm.y0, zs = itm.zs, ze = itm.ze, scene = itm.scene;
+        // the absorber of the item's scene (common.glsl:40-43 with the scene's own nx, ny)
+        const unsigned char* pcx = a.pml_cls_xy + (long long)scene * a.pml_xy_scene;
+        int snx = a.nx, sny = a.ny;
+        if (a.scene_xy) {
+            const int2 d = __ldg(a.scene_xy + scene);
+            snx = d.x, sny = d.y;
+        }
+        auto pml_xy_of = [&](int px, int py) { return px < L || py < L || px >= snx - (L + 1) || py >= sny - (L + 1); };
 
         // per-item invariants: own warps hold cells (xa, y), (xa+1, y); the halo warp holds the row
         // cells (xa, y0-1), (xa+1, y0-1) and the column cell (x0-1, y0+lane)
+        // cells outside the item's scene (a ragged stack's frozen cells) are neither updated nor
+        // written: they keep their initial 0 in both field generations
         const int xa = x0 + 2 * lane;
         const int y = ctl ? y0 - 1 : y0 + warp;
-        const bool rowok = ctl ? y0 > 0 : y < a.ny;
-        const bool o0 = rowok && xa < a.nx, o1 = rowok && xa + 1 < a.nx;
+        const bool rowok = ctl ? y0 > 0 : y < sny;
+        const bool o0 = rowok && xa < snx, o1 = rowok && xa + 1 < snx;
         int A1 = 0, A2 = 0, A3 = 0, A4 = 0, B1 = 0, B2 = 0, B3 = 0, B4 = 0;
-        if (o0) pml_rows(xa, y, A1, A2, A3, A4);
-        if (o1) pml_rows(xa + 1, y, B1, B2, B3, B4);
+        if (o0) pml_rows(pcx, xa, y, A1, A2, A3, A4);
+        if (o1) pml_rows(pcx, xa + 1, y, B1, B2, B3, B4);
         const bool pxy0 = o0 && pml_xy_of(xa, y), pxy1 = o1 && pml_xy_of(xa + 1, y);
         if (ctl && lane < TY) {  // column cell: live flag | absorber flag, then its table rows
             const int cy = y0 + lane;
             int4 cr = make_int4(0, 0, 0, 0);
-            if (x0 > 0 && cy < a.ny) {
+            if (x0 > 0 && cy < sny) {
                 int r4;
-                pml_rows(x0 - 1, cy, cr.y, cr.z, cr.w, r4);
+                pml_rows(pcx, x0 - 1, cy, cr.y, cr.z, cr.w, r4);
                 cr.x = 1 | (pml_xy_of(x0 - 1, cy) ? 2 : 0);
             }
             colrow[lane] = cr;  // read by the same thread only
@@ -741,9 +768,9 @@ __global__ void __launch_bounds__(32 * (TY + 1), TY == 4 ? 4 : (TY == 8 ? 2 : 1)
                 const float2 bym_z = *reinterpret_cast<const float2*>(sb + 2 * SBC + me - W);  // B(y-1).z
                 float2 ex = e0x, ey = e0y, ez = e0z;
                 e_update(a, ex.x, ey.x, ez.x, (bz.x - bym_z.x) - (by.x - bp_y.x), (bx.x - bp_x.x) - (bz.x - bxm_z),
-                         (by.x - bxm_y) - (bx.x - bym_x.x), ca, pxy0 || pz, A1, A2, A4, iz, hz, xa, y, z);
+                         (by.x - bxm_y) - (bx.x - bym_x.x), ca, pxy0 || pz, A1, A2, A4, iz, hz, xa, y, z, scene);
                 e_update(a, ex.y, ey.y, ez.y, (bz.y - bym_z.y) - (by.y - bp_y.y), (bx.y - bp_x.y) - (bz.y - bz.x),
-                         (by.y - by.x) - (bx.y - bym_x.y), cb, pxy1 || pz, B1, B2, B4, iz, hz, xa + 1, y, z);
+                         (by.y - by.x) - (bx.y - bym_x.y), cb, pxy1 || pz, B1, B2, B4, iz, hz, xa + 1, y, z, scene);
                 const uint64_t evict_first = evict_first_policy();
                 if (o1) {
                     st_pair(a.nex + off, ex, evict_first);
@@ -862,7 +889,15 @@ bool launch_p(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaSt
         }
     }
     lk.unlock();
-    PairSched ps = pair_schedule(a, TY, resident * sms);
+    PairSched ps{};
+    if (a.items) {
+        ps.items = a.n_items;
+        ps.tab = a.items;
+    } else {
+        ps = pair_schedule(a, TY, resident * sms);
+        ps.tab = nullptr;
+    }
+    if (ps.items <= 0) return false;
     const int grid = std::min(ps.items, resident * sms);
     ps.work = a.work, ps.base = a.work_base;
     yee_tma2<TY, Idx><<<grid, dim3(32, TY + 1), Lay::SMEM, s>>>(m->e[gen][0], m->e[gen][1], m->e[gen][2],
@@ -894,6 +929,42 @@ bool tma_maps_encode(TmaMaps* m, int gen, const YeeArgs& a, bool wide) {
     m->ok[gen] = ok;
     m->cls_ok = ok;
     return ok;
+}
+
+bool tma_maps_ready(const TmaMaps* m, int gen) { return m && m->ok[gen] && m->cls_ok; }
+
+std::vector<int4> ragged_items(const std::vector<int>& z0, const std::vector<int>& nx, const std::vector<int>& ny,
+                               const std::vector<int>& nz, int ty, int g) {
+    const size_t n = z0.size();
+    std::vector<long long> tiles(n);
+    int deepest = 1;
+    for (size_t i = 0; i < n; ++i) {
+        tiles[i] = (long long)((nx[i] + 63) / 64) * ((ny[i] + ty - 1) / ty);
+        deepest = std::max(deepest, nz[i]);
+    }
+    // one chunk length for every scene: the CTA with the most items bounds the launch, and every
+    // chunk above a scene's first plane re-reads one plane
+    int zc_best = deepest;
+    long long best = -1;
+    for (int zc = std::min(deepest, 4); zc <= deepest; ++zc) {
+        long long items = 0, extra = 0;
+        for (size_t i = 0; i < n; ++i) {
+            const long long c = (nz[i] + zc - 1) / zc;
+            items += tiles[i] * c;
+            extra += c > 1 ? 1 : 0;
+        }
+        const long long cost = (items + g - 1) / g * (zc + (extra ? 1 : 0));
+        if (best < 0 || cost < best) best = cost, zc_best = zc;
+    }
+    std::vector<int4> out;
+    for (size_t i = 0; i < n; ++i) {
+        const int tx = (nx[i] + 63) / 64, tyn = (ny[i] + ty - 1) / ty;
+        for (int zs = 0; zs < nz[i]; zs += zc_best)
+            for (int t = 0; t < tx * tyn; ++t)
+                out.push_back(make_int4((t % tx) * 64 | ((t / tx) * ty) << 16, z0[i] + zs,
+                                        z0[i] + std::min(nz[i], zs + zc_best), (int)i));
+    }
+    return out;
 }
 
 bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsigned* err, cudaStream_t s,

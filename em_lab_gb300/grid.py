@@ -92,6 +92,8 @@ def load_library() -> C.CDLL:
         "emlab_grid_set_graph": ([P, I], I),
         "emlab_stack_configure": ([P, C.POINTER(abi.GridConfig), ip, I], I),
         "emlab_stack_info": ([P, ip, ip, ip], I),
+        "emlab_stack_configure_scenes": ([P, C.POINTER(abi.GridConfig), ip, I], I),
+        "emlab_stack_scene_dims": ([P, ip], I),
         "emlab_stack_upload_materials": ([P, I, fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ,
                                           C.POINTER(abi.WireTerm), SZ], I),
         "emlab_stack_commit": ([P], I),
@@ -585,17 +587,31 @@ class SimulationGrid:
 
 
 class SceneStack(SimulationGrid):
-    """Independent scenes of equal nx x ny stepped as one grid (emlab_stack_*): scene i occupies
-    planes z0[i] .. z0[i] + nz[i] - 1 with a frozen separator plane between scenes, and evolves bit for
-    bit as it would on a SimulationGrid of its own. Materials and sources are given per scene in the
-    scene's own coordinates; ports are attached in stack planes (scene z + z0)."""
+    """Independent scenes stepped as one grid (emlab_stack_*): scene i occupies planes z0[i] ..
+    z0[i] + nz[i] - 1 with a frozen separator plane between scenes, and evolves bit for bit as it
+    would on a SimulationGrid of its own. Scenes of equal nx x ny (`scene_nz`: their depths) or of
+    their own cross-sections (`scene_dims`: (nx, ny, nz) each; every scene at x = y = 0 of its planes,
+    the rest of the planes frozen). Materials and sources are given per scene in the scene's own
+    coordinates; ports are attached in stack planes (scene z + z0)."""
 
-    def __init__(self, config: abi.GridConfig, scene_nz):
+    def __init__(self, config: abi.GridConfig, scene_nz=None, scene_dims=None):
         super().__init__(None)
         cfg = abi.GridConfig()
         C.memmove(C.byref(cfg), C.byref(config), C.sizeof(cfg))
-        nz = (C.c_int * len(scene_nz))(*[int(v) for v in scene_nz])
-        _check(self._lib.emlab_stack_configure(self._h, C.byref(cfg), nz, len(scene_nz)))
+        if scene_dims is not None:
+            d = [int(v) for t in scene_dims for v in t]
+            arr = (C.c_int * len(d))(*d)
+            _check(self._lib.emlab_stack_configure_scenes(self._h, C.byref(cfg), arr, len(d) // 3))
+        else:
+            nz = (C.c_int * len(scene_nz))(*[int(v) for v in scene_nz])
+            _check(self._lib.emlab_stack_configure(self._h, C.byref(cfg), nz, len(scene_nz)))
+
+    def scene_dims(self):
+        """(nx, ny, nz) of every scene now in the stack."""
+        n = self.scenes()
+        out = (C.c_int * max(3, 3 * n))()
+        _check(self._lib.emlab_stack_scene_dims(self._h, out))
+        return [tuple(out[3 * i: 3 * i + 3]) for i in range(n)]
 
     def layout(self):
         """(z0, nz) lists of the scenes now in the stack."""
@@ -638,7 +654,8 @@ class SceneStack(SimulationGrid):
         self._nports = 0
 
     def scene_components(self, scene: int, comps=None):
-        """The six components of one scene, each (nz_i, ny, nx)."""
+        """The six components of one scene, each (nz_i, ny_i, nx_i)."""
         z0, nz = self.layout()
+        nx, ny, _ = self.scene_dims()[scene]
         comps = self.read_components() if comps is None else comps
-        return [c[z0[scene]: z0[scene] + nz[scene]] for c in comps]
+        return [c[z0[scene]: z0[scene] + nz[scene], :ny, :nx] for c in comps]

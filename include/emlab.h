@@ -337,9 +337,20 @@ int emlab_radar_backproject(const emlab_radar_geometry* geo, const float* z, int
  * the depth of each scene (each clamped as SimulationGrid::configure clamps). Fields cleared, every
  * scene vacuum, no sources, monitors detached. */
 int emlab_stack_configure(emlab_grid* g, const emlab_grid_config* cfg, const int* scene_nz, int n_scenes);
+/* A stack of scenes of different cross-sections: dims[3i .. 3i + 2] = nx, ny, nz of scene i (each
+ * clamped as SimulationGrid::configure clamps), the solver settings from cfg (its nx, ny, nz are
+ * ignored). The grid's cross-section is the largest scene's; every scene lies at x = y = 0 of its
+ * planes, and the cells of its planes outside its nx x ny hold the separator's frozen class (E and B
+ * stay 0 there, as outside a grid of its own). Each scene keeps its own absorber on all six faces.
+ * One launch of the persistent pair kernel steps every scene: its work items are the tiles of each
+ * scene's own cross-section. Such a stack runs the fused kernel with tiles of cell pairs only
+ * (emlab_grid_set_kernel / _set_tiling refuse the others). Otherwise as emlab_stack_configure. */
+int emlab_stack_configure_scenes(emlab_grid* g, const emlab_grid_config* cfg, const int* dims, int n_scenes);
+/* nx, ny, nz of every scene (3 ints per scene). */
+int emlab_stack_scene_dims(const emlab_grid* g, int* dims);
 /* Layout: number of scenes, first plane and depth of each (arrays of n_scenes entries, or NULL). */
 int emlab_stack_info(const emlab_grid* g, int* n_scenes, int* z0, int* nz);
-/* uploadMaterials for one scene, in the scene's own coordinates (nz = the scene's depth). Clears the
+/* uploadMaterials for one scene, in the scene's own coordinates (nx, ny, nz = the scene's). Clears the
  * fields of the stack and its step count. The merged class table is built at the next step or
  * emlab_stack_commit. */
 int emlab_stack_upload_materials(emlab_grid* g, int scene, const float* sigma, const float* eps_r, int nx, int ny,

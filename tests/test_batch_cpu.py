@@ -97,3 +97,32 @@ def test_impedance_of_a_resistive_port():
     np.testing.assert_allclose(z["z"].imag, 0.0, atol=1e-9)
     g = (r - 50.0) / (r + 50.0)
     np.testing.assert_allclose(z["s11"], 20 * math.log10(g), rtol=1e-12)
+
+
+def test_far_field_spectra_of_a_dipole_pattern():
+    """FarField: the direction grid, the frequencies over the sweep band, the scene's box inside its
+    absorber, and the spectra formula on a synthetic short-dipole pattern |F|^2 ~ sin^2(theta):
+    D = 1.5 (1.76 dBi) and the radiated energy in dB over lambda0^2 of the unscaled sums."""
+    ff = batch.FarField(8)
+    d = ff.dirs.astype(np.float64)
+    assert d.shape == (18 * 36 + 2, 3) and np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-6)
+    sc = configs.batched_scene(4, 2)
+    wl = ff.wavelengths(sc)
+    sw = sc.sweep
+    assert wl[0] == pytest.approx(sw["wavelength_max"]) and wl[-1] == pytest.approx(sw["wavelength_min"])
+    assert np.all(np.diff(1.0 / wl) > 0)
+    n, L = sc.grid.size, sc.grid.pml_thickness
+    assert batch.FarField.box(sc, 100) == [L + 1, L + 1, 100 + L + 1, n[0] - L - 2, n[1] - L - 2, 100 + n[2] - L - 2]
+    # a pattern |F|^2 = A sin^2(theta) whose peak gives D = k^2 A / (8 pi P) = 1.5 (a short dipole)
+    k = 2.0 * math.pi / wl
+    P = np.linspace(1.0, 2.0, 8)
+    A = 1.5 * 8.0 * math.pi * P / (k * k)
+    sin2 = 1.0 - d[:, 2] ** 2
+    out = np.zeros((8, len(d), 2), np.float32)
+    out[:, :, 0] = A[:, None] * sin2[None, :]
+    out[:, 0, 1] = P
+    samples = 1000
+    spec = ff.spectra(sc, out, samples)
+    assert spec.shape == (2, 8)
+    np.testing.assert_allclose(spec[0], 10.0 * math.log10(1.5) + 10.0 * np.log10(sin2.max()), atol=1e-4)
+    np.testing.assert_allclose(spec[1], 10.0 * np.log10(P * (samples / 2.0) ** 2 / sc.wavelength ** 2), rtol=1e-5)
