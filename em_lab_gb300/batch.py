@@ -319,21 +319,21 @@ class BatchRunner:
         self.compact_s = 0.0  # of which in compaction
 
     def _next_chunk(self, g, steps):
-        """Steps of the stack's next chunk: up to the next multiple of the chunk length (a whole
-        chunk replays one captured graph), or fewer when a scene's stop or decision step comes
-        sooner, so an early window ends exactly there and the chunk grid stays where it was."""
+        """Steps of the stack's next chunk after the `steps` already queued (every scene of a stack
+        has run the same steps): up to the next multiple of the chunk length (a whole chunk replays
+        one captured graph), or fewer when a scene's stop, decision or snapshot step comes sooner,
+        so an early window ends exactly there and the chunk grid stays where it was."""
         n = self.chunk - steps % self.chunk
         for i in g.indices:
-            r = self.results[i]
-            if r.done:
+            if self.results[i].done:
                 continue
             for marks in (self.stop_steps, None if self.decide_at is None or self.decided[i] else self.decide_at):
-                if marks is not None and marks[i] > r.steps:
-                    n = min(n, marks[i] - r.steps)
+                if marks is not None and marks[i] > steps:
+                    n = min(n, marks[i] - steps)
             if self.snap_at is not None:
-                later = [v for v in self.snap_at[i] if v > r.steps]
+                later = [v for v in self.snap_at[i] if v > steps]
                 if later:
-                    n = min(n, later[0] - r.steps)
+                    n = min(n, later[0] - steps)
         return n
 
     def _compact_now(self, g, keep) -> bool:
@@ -343,66 +343,91 @@ class BatchRunner:
         done = sum(c for c, k in zip(cells, keep) if not k)
         return done > 0 and done >= self.compact_fraction * sum(cells)
 
+    def _process(self, g, ser, t0, on_done, lock):
+        """One chunk's port series of stack g: watch every scene, evaluate the finished ones, call
+        decide() for the scenes at their decision step."""
+        cells = sum(int(np.prod(sc.grid.size)) for sc in g.scenes) * ser.shape[0]  # the scenes' own cells
+        finished = []
+        for k, i in enumerate(g.indices):
+            r = self.results[i]
+            if r.done:
+                continue
+            r.series.append(ser[:, k].copy())
+            r.steps += ser.shape[0]
+            if self.snap_at is not None and r.steps in self.snap_at[i]:
+                r.far[r.steps] = g.far_spectra(k)
+            # the ring-down watch concludes only at whole chunks, as in a run without stop or
+            # decision steps; a stop step ends the scene wherever it falls
+            fed = self.watch[i].feed(ser[:, k, 0])
+            if fed and (self.stop_steps is not None or r.steps % self.chunk == 0):
+                r.done = True
+                r.rung_down = self.watch[i].rung_down()
+                r.wall_s = time.perf_counter() - t0
+                sc = self.scenes[i]
+                r.sweep = scene_sweep(sc, np.concatenate(r.series), float(sc.grid.courant))
+                if g.far is not None and r.steps not in r.far:
+                    r.far[r.steps] = g.far_spectra(k)
+                finished.append(i)
+        pending = [i for i in g.indices if self.decide_at is not None and not self.results[i].done
+                   and not self.decided[i] and self.results[i].steps >= self.decide_at[i]]
+        with lock:
+            if pending:
+                args = (pending, [np.concatenate(self.results[i].series) for i in pending])
+                if self.far is not None:
+                    args += ([self.results[i].far.get(self.decide_at[i]) for i in pending],)
+                flags = self.decide(*args)
+                for i, stop in zip(pending, flags):
+                    self.decided[i] = True
+                    if stop:
+                        r = self.results[i]
+                        r.done = r.accepted = True
+                        r.wall_s = time.perf_counter() - t0
+                        finished.append(i)
+            self.cell_steps += cells
+            if on_done:
+                for i in finished:
+                    on_done(i, self.results[i])
+
     def _run_group(self, g, t0, on_done, lock):
         """One stack's loop (its own host thread and CUDA stream): step a chunk, read the chunk's port
         series back, watch every scene, evaluate the finished ones, compact. The library releases the
-        interpreter lock inside its calls, so the stacks' chunks overlap on the device."""
+        interpreter lock inside its calls, so the stacks' chunks overlap on the device.
+
+        Without far-field monitors the loop runs one chunk ahead: chunk n+1 is queued before the
+        series of chunk n is processed (asynchronous takes), so the device never waits for the host.
+        A scene found done in chunk n has been stepped through chunk n+1 as well; that chunk's rows
+        are not added to its series (its results are those of the chunk that finished it), and the
+        compaction waits until the chunk in flight has been processed. With far-field monitors every
+        chunk is processed before the next is queued (a snapshot reads the sums at its own step)."""
+        from collections import deque
         steps = 0
         host = comp = 0.0
-        while g.indices and steps < self.max_steps:
-            n = self._next_chunk(g, steps)
-            g.stack.step(n)
-            ser = g.stack.ports_take_series(n)
+        ahead = 1 if self.far is None else 0
+        inflight = deque()  # (slot, steps) of queued chunks not processed yet
+        while True:
+            while g.indices and steps < self.max_steps and len(inflight) <= ahead:
+                n = self._next_chunk(g, steps)
+                g.stack.step(n)
+                inflight.append(g.stack.ports_take_series_async())
+                steps += n
+            if not inflight:
+                break
+            slot, rows = inflight.popleft()
+            ser = g.stack.ports_collect_series(slot, rows)
             th = time.perf_counter()
-            cells = sum(int(np.prod(sc.grid.size)) for sc in g.scenes) * ser.shape[0]  # the scenes' own cells
-            finished = []
-            for k, i in enumerate(g.indices):
-                r = self.results[i]
-                if r.done:
-                    continue
-                r.series.append(ser[:, k].copy())
-                r.steps += ser.shape[0]
-                if self.snap_at is not None and r.steps in self.snap_at[i]:
-                    r.far[r.steps] = g.far_spectra(k)
-                # the ring-down watch concludes only at whole chunks, as in a run without stop or
-                # decision steps; a stop step ends the scene wherever it falls
-                fed = self.watch[i].feed(ser[:, k, 0])
-                if fed and (self.stop_steps is not None or r.steps % self.chunk == 0):
-                    r.done = True
-                    r.rung_down = self.watch[i].rung_down()
-                    r.wall_s = time.perf_counter() - t0
-                    sc = self.scenes[i]
-                    r.sweep = scene_sweep(sc, np.concatenate(r.series), float(sc.grid.courant))
-                    if g.far is not None and r.steps not in r.far:
-                        r.far[r.steps] = g.far_spectra(k)
-                    finished.append(i)
-            pending = [i for i in g.indices if self.decide_at is not None and not self.results[i].done
-                       and not self.decided[i] and self.results[i].steps >= self.decide_at[i]]
-            with lock:
-                if pending:
-                    args = (pending, [np.concatenate(self.results[i].series) for i in pending])
-                    if self.far is not None:
-                        args += ([self.results[i].far.get(self.decide_at[i]) for i in pending],)
-                    flags = self.decide(*args)
-                    for i, stop in zip(pending, flags):
-                        self.decided[i] = True
-                        if stop:
-                            r = self.results[i]
-                            r.done = r.accepted = True
-                            r.wall_s = time.perf_counter() - t0
-                            finished.append(i)
-                self.cell_steps += cells
-                if on_done:
-                    for i in finished:
-                        on_done(i, self.results[i])
-            steps += n
+            self._process(g, ser, t0, on_done, lock)
             keep = [not self.results[i].done for i in g.indices]
-            if not any(keep):
-                g.indices = []
-            elif self._compact_now(g, keep):
-                tc = time.perf_counter()
-                g.compact(keep)
-                comp += time.perf_counter() - tc
+            if not any(keep) or self._compact_now(g, keep):
+                while inflight:  # the chunk in flight ran with this layout: process it first
+                    slot, rows = inflight.popleft()
+                    self._process(g, g.stack.ports_collect_series(slot, rows), t0, on_done, lock)
+                keep = [not self.results[i].done for i in g.indices]
+                if not any(keep):
+                    g.indices = []
+                else:
+                    tc = time.perf_counter()
+                    g.compact(keep)
+                    comp += time.perf_counter() - tc
             host += time.perf_counter() - th
         with lock:
             self.steps = max(self.steps, steps)

@@ -501,6 +501,8 @@ int emlab_grid_destroy(emlab_grid* g) {
     for (int s = 0; s < 2; ++s) {
         if (g->h_stage[s]) cudaFreeHost(g->h_stage[s]);
         if (g->stage_done[s]) cudaEventDestroy(g->stage_done[s]);
+        if (g->h_series[s]) cudaFreeHost(g->h_series[s]);
+        if (g->series_done[s]) cudaEventDestroy(g->series_done[s]);
     }
     for (size_t i = 0; i < g->ev_start.size(); ++i) cudaEventDestroy(g->ev_start[i]), cudaEventDestroy(g->ev_stop[i]);
     if (g->tma) tma_maps_destroy(g->tma);
@@ -990,6 +992,55 @@ int emlab_ports_take_series(emlab_grid* g, float* out, size_t max_steps, size_t*
     if (s) EMLAB_CUDA(cudaMemcpyAsync(out, g->d_series.p, s * g->nports * 8, cudaMemcpyDeviceToHost, g->stream));
     if (int rc = emlab_grid_synchronize(g, 0)) return rc;
     g->recorded = 0;  // the next step records from the start of the buffer again
+    return EMLAB_OK;
+}
+
+int emlab_ports_take_series_async(emlab_grid* g, int* slot, size_t* steps) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(slot && steps, "null output");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    const int k = g->series_next;
+    EMLAB_REQUIRE(!g->series_busy[k], "both series slots are waiting to be collected");
+    const size_t s = g->recorded, bytes = s * (size_t)g->nports * 8;
+    if (!g->series_done[k]) EMLAB_CUDA(cudaEventCreateWithFlags(&g->series_done[k], cudaEventDisableTiming));
+    if (bytes > g->h_series_cap[k]) {
+        if (g->h_series[k]) cudaFreeHost(g->h_series[k]);
+        g->h_series[k] = nullptr, g->h_series_cap[k] = 0;
+        EMLAB_CUDA(cudaMallocHost(&g->h_series[k], bytes));
+        g->h_series_cap[k] = bytes;
+    }
+    if (bytes) EMLAB_CUDA(cudaMemcpyAsync(g->h_series[k], g->d_series.p, bytes, cudaMemcpyDeviceToHost, g->stream));
+    EMLAB_CUDA(cudaEventRecord(g->series_done[k], g->stream));
+    g->h_series_rows[k] = s;
+    g->series_busy[k] = true;
+    g->series_next ^= 1;
+    g->recorded = 0;  // the next step records from the start of the buffer again (after this copy, in stream order)
+    *slot = k, *steps = s;
+    return EMLAB_OK;
+}
+
+int emlab_ports_collect_series(emlab_grid* g, int slot, float* out, size_t max_steps, int timeout_ms) {
+    if (int rc = require_grid(g)) return rc;
+    EMLAB_REQUIRE(slot == 0 || slot == 1, "no such series slot");
+    EMLAB_REQUIRE(g->series_busy[slot], "the series slot holds no pending take");
+    EMLAB_REQUIRE(out || max_steps == 0, "null output");
+    EMLAB_CUDA(cudaSetDevice(g->device));
+    const auto limit = std::chrono::milliseconds(timeout_ms > 0 ? timeout_ms : 60000);
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        const cudaError_t e = cudaEventQuery(g->series_done[slot]);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return fail(EMLAB_ERR_CUDA, std::string("series copy: ") + cudaGetErrorString(e));
+        if (std::chrono::steady_clock::now() - t0 > limit)
+            return fail(EMLAB_ERR_TIMEOUT, "series copy did not complete within the timeout");
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    unsigned err = 0;
+    EMLAB_CUDA(cudaMemcpy(&err, g->d_err.p, 4, cudaMemcpyDeviceToHost));
+    if (err) return fail(EMLAB_ERR_TIMEOUT, "a solver kernel's bounded wait ran out");
+    const size_t s = std::min(max_steps, g->h_series_rows[slot]);
+    if (s) std::memcpy(out, g->h_series[slot], s * (size_t)g->nports * 8);
+    g->series_busy[slot] = false;
     return EMLAB_OK;
 }
 

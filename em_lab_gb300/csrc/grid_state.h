@@ -148,6 +148,12 @@ struct emlab_grid {
     DevBuf<int4> d_ports;
     DevBuf<float> d_port_ph, d_series;
     size_t series_cap = 0, recorded = 0;
+    // asynchronous takes of the recorded series: two pinned slots, each with its copy's event
+    float* h_series[2] = {nullptr, nullptr};
+    size_t h_series_cap[2] = {0, 0}, h_series_rows[2] = {0, 0};
+    cudaEvent_t series_done[2] = {nullptr, nullptr};
+    bool series_busy[2] = {false, false};
+    int series_next = 0;
     bool recording = false;
     float port_wl = 16.0f, port_avg = 4.0f;
     // ntff

@@ -92,6 +92,8 @@ def load_library() -> C.CDLL:
         "emlab_grid_set_graph": ([P, I], I),
         "emlab_stack_configure": ([P, C.POINTER(abi.GridConfig), ip, I], I),
         "emlab_stack_info": ([P, ip, ip, ip], I),
+        "emlab_ports_take_series_async": ([P, ip, C.POINTER(SZ)], I),
+        "emlab_ports_collect_series": ([P, I, fp, SZ, I], I),
         "emlab_stack_configure_scenes": ([P, C.POINTER(abi.GridConfig), ip, I], I),
         "emlab_stack_scene_dims": ([P, ip], I),
         "emlab_stack_upload_materials": ([P, I, fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ,
@@ -441,6 +443,20 @@ class SimulationGrid:
         steps = C.c_size_t()
         _check(self._lib.emlab_ports_take_series(self._h, _fptr(out), int(max_steps), C.byref(steps)))
         return out[: steps.value, :n]
+
+    def ports_take_series_async(self):
+        """Queues the copy of the steps recorded since the last take; returns (slot, steps) for
+        ports_collect_series. Recording restarts at the start of the buffer."""
+        slot, steps = C.c_int(), C.c_size_t()
+        _check(self._lib.emlab_ports_take_series_async(self._h, C.byref(slot), C.byref(steps)))
+        return slot.value, steps.value
+
+    def ports_collect_series(self, slot: int, steps: int, timeout_ms: int = 0) -> np.ndarray:
+        """Waits for a queued take and returns its (steps, ports, 2) series."""
+        n = getattr(self, "_nports", 0)
+        out = np.zeros((max(1, int(steps)), max(1, n), 2), np.float32)
+        _check(self._lib.emlab_ports_collect_series(self._h, int(slot), _fptr(out), int(steps), int(timeout_ms)))
+        return out[: int(steps), :n]
 
     def ports_sweep_sums(self, lambda_min, lambda_max, points):
         n = getattr(self, "_nports", 0)

@@ -219,6 +219,15 @@ int emlab_ports_read_series(emlab_grid* g, float* out, size_t max_steps, size_t*
 /* Copies the recorded steps (at most max_steps) like emlab_ports_read_series, then restarts the
  * recording at the start of the buffer: chunked read-back of long runs (a ring-down watch). */
 int emlab_ports_take_series(emlab_grid* g, float* out, size_t max_steps, size_t* steps);
+/* The same take without waiting: queues the copy of the series recorded since the last take into one
+ * of two pinned host slots behind the work already queued on the grid's stream, and restarts the
+ * recording (the steps queued next record from the start of the buffer). *slot names the slot,
+ * *steps the rows it will hold. At most two takes may wait to be collected. */
+int emlab_ports_take_series_async(emlab_grid* g, int* slot, size_t* steps);
+/* Waits (bounded: EMLAB_ERR_TIMEOUT after timeout_ms; <= 0 waits 60 s) for a slot's copy, copies at
+ * most max_steps rows to out ((steps, ports, 2) floats) and frees the slot. Work queued after the
+ * take keeps running. EMLAB_ERR_TIMEOUT also if a solver kernel gave up a bounded wait. */
+int emlab_ports_collect_series(emlab_grid* g, int slot, float* out, size_t max_steps, int timeout_ms);
 /* Running DFT of the recorded series at `points` frequencies evenly spaced in 1/lambda between
  * 1/lambda_max and 1/lambda_min, in FP64 on the device (the sums of PortMonitor::evaluateSweep,
  * src/Ports.cpp:215-242, I corrected by e^{i w dt/2}): out[(port * points + f) * 4 + {0..3}] =
