@@ -707,8 +707,9 @@ def main():
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_kind,
-                         "traffic_source": ("DRAM bytes read + written per launch from one ncu capture "
-                                            "(profiles/traffic.txt), not measured in this run") if traffic else None,
+                         "traffic_source": ("DRAM bytes read + written per launch from one ncu capture of the "
+                                            "256^3 case, scaled by the cells a launch updates (profiles/traffic.txt); "
+                                            "not measured in this run") if traffic else None,
                          "kernel": kname, "kernel_ms_per_launch": per_launch_ms,
                          "algorithmic_bytes_per_cell_step": BYTES_PER_CELL_STEP},
             "cpu_baseline": cpu,

@@ -222,3 +222,38 @@ def test_graph_chunks_on_a_stack_after_compaction():
         for c, (a, b) in enumerate(zip(st.scene_components(k, comps), ref)):
             np.testing.assert_array_equal(a, b, err_msg=f"scene {k} component {c}")
     st.close()
+
+
+def test_asynchronous_series_takes_equal_the_synchronous_take():
+    """emlab_ports_take_series_async / _collect_series: two takes may wait at once, each holds the
+    rows recorded before it, and the series equals the synchronous take of the same steps; a third
+    take while both slots wait, or collecting a free slot, is refused."""
+    sc = configs.batched_scene(3, 0)
+    out = []
+    for mode in ("sync", "async"):
+        g = SimulationGrid(sc.grid)
+        oracle.load_scene(g, sc)
+        g.ports_configure([sc.ports[0].to_c()], sc.wavelength, 4.0, False, 64)
+        g.set_graph(64)
+        if mode == "sync":
+            parts = []
+            for _ in range(3):
+                g.step(64)
+                parts.append(g.ports_take_series(64))
+        else:
+            g.step(64)
+            a = g.ports_take_series_async()
+            g.step(64)
+            b = g.ports_take_series_async()
+            with pytest.raises(RuntimeError, match="both series slots"):
+                g.ports_take_series_async()
+            parts = [g.ports_collect_series(*a)]
+            with pytest.raises(RuntimeError, match="no pending take"):
+                g.ports_collect_series(a[0], a[1])
+            g.step(64)
+            c = g.ports_take_series_async()
+            parts += [g.ports_collect_series(*b), g.ports_collect_series(*c)]
+            assert a[1] == b[1] == c[1] == 64
+        out.append(np.concatenate(parts))
+        g.close()
+    np.testing.assert_array_equal(out[0], out[1])
