@@ -272,6 +272,11 @@ def parity_sample(steps: int = 200, size: int = 128):
                                              np.array_equal(gpu_s, f32_s)),
             "max_abs_vs_fp32_oracle": float(max(np.abs(a - b).max() for a, b in zip(gpu_f, f32_f))),
             "rel_l2_vs_fp64_oracle": {n: rel(a, b) for n, a, b in zip(COMPONENTS, gpu_f, f64_f)},
+            # the same per field vector (E, B): a component much smaller than its field's others (Bz of a
+            # z dipole, 1 % of |B| here) has a larger error relative to its own norm at the same absolute error
+            "rel_l2_vs_fp64_oracle_per_field": {
+                "E": rel(np.stack(gpu_f[:3]), np.stack(f64_f[:3])), "B": rel(np.stack(gpu_f[3:]), np.stack(f64_f[3:]))},
+            "rms_abs_error_vs_fp64_oracle": {n: float(np.sqrt(np.mean((a - b) ** 2))) for n, a, b in zip(COMPONENTS, gpu_f, f64_f)},
             "port_series_rel_l2_vs_fp64_oracle": rel(gpu_s, f64_s),
             "seconds": round(time.perf_counter() - t0, 1)}
 
