@@ -128,9 +128,9 @@ int emlab::upload_class_table(emlab_grid* g, const ClassTable& t) {
     EMLAB_CUDA(g->tabE.alloc(t.classes * 2));
     EMLAB_CUDA(g->tabM.alloc(t.classes * 2));
     EMLAB_CUDA(g->tabW.alloc(t.classes * 2));
-    EMLAB_CUDA(cudaMemcpy(g->tabE.p, t.tabE.data(), t.tabE.size() * 4, cudaMemcpyHostToDevice));
-    EMLAB_CUDA(cudaMemcpy(g->tabM.p, t.tabM.data(), t.tabM.size() * 4, cudaMemcpyHostToDevice));
-    EMLAB_CUDA(cudaMemcpy(g->tabW.p, t.tabW.data(), t.tabW.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->tabE.p, t.tabE.data(), t.tabE.size() * 4, cudaMemcpyHostToDevice, g->stream));
+    EMLAB_CUDA(cudaMemcpyAsync(g->tabM.p, t.tabM.data(), t.tabM.size() * 4, cudaMemcpyHostToDevice, g->stream));
+    EMLAB_CUDA(cudaMemcpyAsync(g->tabW.p, t.tabW.data(), t.tabW.size() * 4, cudaMemcpyHostToDevice, g->stream));
     g->classes = t.classes;
     g->wire_start = t.wire_start;
     return EMLAB_OK;
@@ -224,11 +224,11 @@ int emlab::upload_pml(emlab_grid* g) {
         }
         g->pml_xy_stride = SXY;
         EMLAB_CUDA(g->d_pml_xy.alloc(pxy.size()));
-        EMLAB_CUDA(cudaMemcpy(g->d_pml_xy.p, pxy.data(), pxy.size() * 4, cudaMemcpyHostToDevice));
+        EMLAB_CUDA(cudaMemcpyAsync(g->d_pml_xy.p, pxy.data(), pxy.size() * 4, cudaMemcpyHostToDevice, g->stream));
         EMLAB_CUDA(g->d_pml_cls_xy.alloc(cxy.size()));
-        EMLAB_CUDA(cudaMemcpy(g->d_pml_cls_xy.p, cxy.data(), cxy.size(), cudaMemcpyHostToDevice));
+        EMLAB_CUDA(cudaMemcpyAsync(g->d_pml_cls_xy.p, cxy.data(), cxy.size(), cudaMemcpyHostToDevice, g->stream));
         EMLAB_CUDA(g->d_scene_xy.alloc(dims.size()));
-        EMLAB_CUDA(cudaMemcpy(g->d_scene_xy.p, dims.data(), dims.size() * 8, cudaMemcpyHostToDevice));
+        EMLAB_CUDA(cudaMemcpyAsync(g->d_scene_xy.p, dims.data(), dims.size() * 8, cudaMemcpyHostToDevice, g->stream));
         int dev = 0, sms = 0;
         EMLAB_CUDA(cudaGetDevice(&dev));
         EMLAB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -237,7 +237,7 @@ int emlab::upload_pml(emlab_grid* g) {
             const std::vector<int4> items = ragged_items(st.z0, st.nx, st.ny, st.nz, tys[t], per_sm[t] * sms);
             EMLAB_REQUIRE(!items.empty(), "stack: no work items");
             EMLAB_CUDA(g->d_items[t].alloc(items.size()));
-            EMLAB_CUDA(cudaMemcpy(g->d_items[t].p, items.data(), items.size() * 16, cudaMemcpyHostToDevice));
+            EMLAB_CUDA(cudaMemcpyAsync(g->d_items[t].p, items.data(), items.size() * 16, cudaMemcpyHostToDevice, g->stream));
             g->n_items[t] = (int)items.size();
         }
     } else {
@@ -246,13 +246,13 @@ int emlab::upload_pml(emlab_grid* g) {
         g->d_scene_xy.release(), g->d_pml_cls_xy.release(), g->d_pml_xy.release();
     }
     EMLAB_CUDA(g->pml.alloc(pt.size()));
-    EMLAB_CUDA(cudaMemcpy(g->pml.p, pt.data(), pt.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->pml.p, pt.data(), pt.size() * 4, cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->pml_cls.alloc(pcls.size()));
-    EMLAB_CUDA(cudaMemcpy(g->pml_cls.p, pcls.data(), pcls.size(), cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->pml_cls.p, pcls.data(), pcls.size(), cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->pml_coef.alloc(coef.size() / 2));
-    EMLAB_CUDA(cudaMemcpy(g->pml_coef.p, coef.data(), coef.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->pml_coef.p, coef.data(), coef.size() * 4, cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->pml_z.alloc(pz.size()));
-    EMLAB_CUDA(cudaMemcpy(g->pml_z.p, pz.data(), pz.size(), cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->pml_z.p, pz.data(), pz.size(), cudaMemcpyHostToDevice, g->stream));
     return EMLAB_OK;
 }
 
@@ -265,21 +265,21 @@ int emlab::upload_sources(emlab_grid* g, const std::vector<float>& packed, const
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));  // buffers may be in use by queued steps
     EMLAB_CUDA(g->d_src.alloc(std::max<size_t>(1, packed.size() / 4)));
     if (!packed.empty())
-        EMLAB_CUDA(cudaMemcpy(g->d_src.p, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice));
+        EMLAB_CUDA(cudaMemcpyAsync(g->d_src.p, packed.data(), packed.size() * 4, cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->d_cells.alloc(cells.size() / 4));
-    EMLAB_CUDA(cudaMemcpy(g->d_cells.p, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_cells.p, cells.data(), cells.size() * 4, cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->d_lists.alloc(std::max<size_t>(1, lists.size())));
     if (!lists.empty())
-        EMLAB_CUDA(cudaMemcpy(g->d_lists.p, lists.data(), lists.size() * 4, cudaMemcpyHostToDevice));
+        EMLAB_CUDA(cudaMemcpyAsync(g->d_lists.p, lists.data(), lists.size() * 4, cudaMemcpyHostToDevice, g->stream));
     g->d_zoff.release();
     if (!zoff.empty()) {
         EMLAB_CUDA(g->d_zoff.alloc(zoff.size()));
-        EMLAB_CUDA(cudaMemcpy(g->d_zoff.p, zoff.data(), zoff.size() * 4, cudaMemcpyHostToDevice));
+        EMLAB_CUDA(cudaMemcpyAsync(g->d_zoff.p, zoff.data(), zoff.size() * 4, cudaMemcpyHostToDevice, g->stream));
     }
     g->d_cell_scene.release();
     if (!scene.empty()) {
         EMLAB_CUDA(g->d_cell_scene.alloc(scene.size()));
-        EMLAB_CUDA(cudaMemcpy(g->d_cell_scene.p, scene.data(), scene.size() * 4, cudaMemcpyHostToDevice));
+        EMLAB_CUDA(cudaMemcpyAsync(g->d_cell_scene.p, scene.data(), scene.size() * 4, cudaMemcpyHostToDevice, g->stream));
     }
     return EMLAB_OK;
 }
@@ -485,8 +485,8 @@ int emlab_grid_create(emlab_grid** out) {
         cudaEventCreateWithFlags(&g->stage_done[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&g->stage_done[1], cudaEventDisableTiming) != cudaSuccess ||
         g->d_flag.alloc(1) != cudaSuccess || g->d_err.alloc(1) != cudaSuccess ||
-        cudaMemset(g->d_err.p, 0, 4) != cudaSuccess || g->d_work.alloc(1) != cudaSuccess ||
-        cudaMemset(g->d_work.p, 0, 8) != cudaSuccess) {
+        cudaMemsetAsync(g->d_err.p, 0, 4, g->stream) != cudaSuccess || g->d_work.alloc(1) != cudaSuccess ||
+        cudaMemsetAsync(g->d_work.p, 0, 8, g->stream) != cudaSuccess) {
         delete g;
         return fail(EMLAB_ERR_CUDA, "stream or event creation failed");
     }
@@ -562,9 +562,9 @@ int emlab_grid_configure(emlab_grid* g, const emlab_grid_config* req) {
     EMLAB_CUDA(g->tabE.alloc(2));
     EMLAB_CUDA(g->tabM.alloc(2));
     EMLAB_CUDA(g->tabW.alloc(2));
-    EMLAB_CUDA(cudaMemcpy(g->tabE.p, t.tabE.data(), 32, cudaMemcpyHostToDevice));
-    EMLAB_CUDA(cudaMemcpy(g->tabM.p, t.tabM.data(), 32, cudaMemcpyHostToDevice));
-    EMLAB_CUDA(cudaMemcpy(g->tabW.p, t.tabW.data(), 32, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->tabE.p, t.tabE.data(), 32, cudaMemcpyHostToDevice, g->stream));
+    EMLAB_CUDA(cudaMemcpyAsync(g->tabM.p, t.tabM.data(), 32, cudaMemcpyHostToDevice, g->stream));
+    EMLAB_CUDA(cudaMemcpyAsync(g->tabW.p, t.tabW.data(), 32, cudaMemcpyHostToDevice, g->stream));
     g->classes = 1, g->wire_start = 1;
     int rc = clear_fields(g);
     if (rc) return rc;
@@ -777,7 +777,7 @@ int emlab_grid_synchronize(emlab_grid* g, int timeout_ms) {
             unsigned err = 0;
             EMLAB_CUDA(cudaMemcpy(&err, g->d_err.p, 4, cudaMemcpyDeviceToHost));
             if (err) {
-                EMLAB_CUDA(cudaMemset(g->d_err.p, 0, 4));
+                EMLAB_CUDA(cudaMemsetAsync(g->d_err.p, 0, 4, g->stream));
                 return fail(EMLAB_ERR_TIMEOUT, "a solver kernel gave up a bounded wait on the device");
             }
             return EMLAB_OK;
@@ -954,9 +954,9 @@ int emlab_ports_configure(emlab_grid* g, const emlab_port* ports, size_t n, floa
         pk.push_back(make_int4(ports[i].edges, ports[i].sign >= 0 ? 1 : -1, 0, 0));
     }
     EMLAB_CUDA(g->d_ports.alloc(pk.size()));
-    EMLAB_CUDA(cudaMemcpy(g->d_ports.p, pk.data(), pk.size() * 16, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_ports.p, pk.data(), pk.size() * 16, cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->d_port_ph.alloc(n * 8));
-    EMLAB_CUDA(cudaMemset(g->d_port_ph.p, 0, n * 32));
+    EMLAB_CUDA(cudaMemsetAsync(g->d_port_ph.p, 0, n * 32, g->stream));
     if (sweep || record_steps > 0) {
         size_t cap = ((size_t)1 << 23) / (2 * n);  // Ports.cpp:16, 209-210
         if (!sweep) cap = std::min(cap, record_steps);
@@ -1120,9 +1120,9 @@ int emlab_ntff_configure(emlab_grid* g, const int box_min[3], const int box_max[
     g->ntff_wl = std::max(wavelength, 2.0f);
     g->ntff_avg = std::max(averaging_periods, 0.5f);
     EMLAB_CUDA(g->d_box.alloc(13));
-    EMLAB_CUDA(cudaMemcpy(g->d_box.p, g->box, 13 * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_box.p, g->box, 13 * 4, cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->d_ntff.alloc((size_t)g->points * 32));
-    EMLAB_CUDA(cudaMemset(g->d_ntff.p, 0, (size_t)g->points * 128));
+    EMLAB_CUDA(cudaMemsetAsync(g->d_ntff.p, 0, (size_t)g->points * 128, g->stream));
     g->ntff_on = true;
     return EMLAB_OK;
 }
@@ -1211,22 +1211,22 @@ int dft_setup(emlab_grid* g, const int* boxes, int nbox, const float* wavelength
         }
     }
     EMLAB_CUDA(g->d_dft_box.alloc(g->dft_boxes.size()));
-    EMLAB_CUDA(cudaMemcpy(g->d_dft_box.p, g->dft_boxes.data(), g->dft_boxes.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_dft_box.p, g->dft_boxes.data(), g->dft_boxes.size() * 4, cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->d_dft_w.alloc(w.size()));
-    EMLAB_CUDA(cudaMemcpy(g->d_dft_w.p, w.data(), w.size() * 8, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_dft_w.p, w.data(), w.size() * 8, cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->d_dft_omega.alloc((size_t)n_freq));
-    EMLAB_CUDA(cudaMemcpy(g->d_dft_omega.p, g->dft_omega.data(), (size_t)n_freq * 8, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_dft_omega.p, g->dft_omega.data(), (size_t)n_freq * 8, cudaMemcpyHostToDevice, g->stream));
     std::vector<float> bhi, blo;
     dft_tc_twiddles(n_freq, g->dft_omega.data(), dt, bhi, blo);
     EMLAB_CUDA(g->d_dft_bhi.alloc(bhi.size()));
     EMLAB_CUDA(g->d_dft_blo.alloc(blo.size()));
-    EMLAB_CUDA(cudaMemcpy(g->d_dft_bhi.p, bhi.data(), bhi.size() * 4, cudaMemcpyHostToDevice));
-    EMLAB_CUDA(cudaMemcpy(g->d_dft_blo.p, blo.data(), blo.size() * 4, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_dft_bhi.p, bhi.data(), bhi.size() * 4, cudaMemcpyHostToDevice, g->stream));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_dft_blo.p, blo.data(), blo.size() * 4, cudaMemcpyHostToDevice, g->stream));
     // room for the longer of the two engines' blocks (the engine may change between folds), or the cap
     const int block = block_cap > 0 ? block_cap : std::max(kDftCoreBlock, dft_tc_block(n_freq));
     EMLAB_CUDA(g->d_dft_blk.alloc((size_t)block * 6 * g->dft_points));
     EMLAB_CUDA(g->d_dft_x.alloc((size_t)n_freq * g->dft_points * 12));
-    EMLAB_CUDA(cudaMemset(g->d_dft_x.p, 0, g->d_dft_x.n * 8));
+    EMLAB_CUDA(cudaMemsetAsync(g->d_dft_x.p, 0, g->d_dft_x.n * 8, g->stream));
     g->dft_t = 0, g->dft_samples = 0;
     g->dft_on = true;
     return EMLAB_OK;
@@ -1700,17 +1700,17 @@ int emlab_lines_configure(emlab_grid* g, const int* quantities, int n_quantities
     }
     for (int t = 0; t < n_terms; ++t) EMLAB_REQUIRE(terms[4 * t + 3] >= 0 && terms[4 * t + 3] < 6, "line term component");
     EMLAB_CUDA(g->d_q.alloc((size_t)n_quantities));
-    EMLAB_CUDA(cudaMemcpy(g->d_q.p, quantities, (size_t)n_quantities * 16, cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->d_q.p, quantities, (size_t)n_quantities * 16, cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->d_terms.alloc((size_t)std::max(n_terms, 1)));
     EMLAB_CUDA(g->d_weights.alloc((size_t)std::max(n_terms, 1)));
     if (n_terms > 0) {
-        EMLAB_CUDA(cudaMemcpy(g->d_terms.p, terms, (size_t)n_terms * 16, cudaMemcpyHostToDevice));
-        EMLAB_CUDA(cudaMemcpy(g->d_weights.p, weights, (size_t)n_terms * 4, cudaMemcpyHostToDevice));
+        EMLAB_CUDA(cudaMemcpyAsync(g->d_terms.p, terms, (size_t)n_terms * 16, cudaMemcpyHostToDevice, g->stream));
+        EMLAB_CUDA(cudaMemcpyAsync(g->d_weights.p, weights, (size_t)n_terms * 4, cudaMemcpyHostToDevice, g->stream));
     }
     EMLAB_CUDA(g->d_line_ph.alloc((size_t)n_quantities * 4));
-    EMLAB_CUDA(cudaMemset(g->d_line_ph.p, 0, (size_t)n_quantities * 16));
+    EMLAB_CUDA(cudaMemsetAsync(g->d_line_ph.p, 0, (size_t)n_quantities * 16, g->stream));
     EMLAB_CUDA(g->d_line_now.alloc((size_t)n_quantities));
-    EMLAB_CUDA(cudaMemset(g->d_line_now.p, 0, (size_t)n_quantities * 4));
+    EMLAB_CUDA(cudaMemsetAsync(g->d_line_now.p, 0, (size_t)n_quantities * 4, g->stream));
     g->nq = n_quantities;
     g->line_wl = std::max(wavelength, 2.0f);
     g->line_avg = averaging_periods;

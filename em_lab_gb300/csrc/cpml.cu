@@ -167,9 +167,9 @@ int cpml_prepare(emlab_grid* g) {
         total += 4 * g->cpml_slab[ax];
     }
     EMLAB_CUDA(g->cpml_coef.alloc(coef.size()));
-    EMLAB_CUDA(cudaMemcpy(g->cpml_coef.p, coef.data(), coef.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    EMLAB_CUDA(cudaMemcpyAsync(g->cpml_coef.p, coef.data(), coef.size() * sizeof(float4), cudaMemcpyHostToDevice, g->stream));
     EMLAB_CUDA(g->cpml_psi.alloc((size_t)total));
-    EMLAB_CUDA(cudaMemset(g->cpml_psi.p, 0, (size_t)total * sizeof(float)));
+    EMLAB_CUDA(cudaMemsetAsync(g->cpml_psi.p, 0, (size_t)total * sizeof(float), g->stream));
     return EMLAB_OK;
 }
 

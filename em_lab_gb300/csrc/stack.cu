@@ -416,8 +416,7 @@ int emlab_stack_compact(emlab_grid* g, const unsigned char* keep) {
         }
         for (size_t k = 0; k + 1 < idx.size(); ++k) {
             const size_t z = (size_t)s.z0[k] + (size_t)s.nz[k];
-            EMLAB_CUDA(cudaMemcpy(g->cls.p + z * plane * esize, sep_plane.data(), plane * esize,
-                                  cudaMemcpyHostToDevice));
+            EMLAB_CUDA(cudaMemcpyAsync(g->cls.p + z * plane * esize, sep_plane.data(), plane * esize, cudaMemcpyHostToDevice, g->stream));
         }
     }
     for (size_t k = 0; k < idx.size(); ++k) {
