@@ -5,9 +5,8 @@ calls into a `scene.Scene`: src/ScriptEngine.cpp (SceneSettings :90-101, Args :2
 :409-520, scene/view/material/param :605-842, geometry :843-1075, sources and antennas :1077-1460,
 plane waves :1526-1590, instruments :1737-1805, far_field :2160-2190, final checks :2420-2520).
 The vector prelude (vec, X/Y/Z, deg, wavelengths, meters, mm, lerp, clamp, range) is provided as
-native functions with the same behaviour. Functions of the reference's API that drive subsystems
-this build does not implement (radar, crpa, emitter, loop, frame) raise a script error that
-names them.
+native functions with the same behaviour. Every function of the reference's API is
+provided, loop{} and frame{} included (:1022-1030, :1456-1524).
 """
 from __future__ import annotations
 
@@ -44,7 +43,6 @@ BUILTIN_MATERIALS = {
     "ground_wet": (25.0, None, 0.02, None), "water": (78.0, None, None, 0.1), "seawater": (74.0, None, 4.0, None),
 }
 
-UNSUPPORTED = ("loop", "frame")
 WAVEFORM_KEYS = ["wavelength", "frequency", "phase", "waveform", "ramp", "pulse_width", "interval", "delay", "enabled"]
 
 
@@ -679,7 +677,8 @@ class ScriptEngine:
         api = {"radar": self.api_radar, "emitter": self.api_emitter, "crpa": self.api_crpa, "scene": self.api_scene, "view": self.api_view, "material": self.api_material, "param": self.api_param,
                "box": self.api_box, "sphere": self.api_sphere, "cylinder": self.api_cylinder,
                "wall": self.api_wall, "grating": self.api_grating, "shape": self.api_shape,
-               "cage": self.api_cage, "array": self.api_array, "coax": self.api_coax,
+               "cage": self.api_cage, "frame": self.api_frame, "loop": self.api_loop,
+               "array": self.api_array, "coax": self.api_coax,
                "dipole": self.api_dipole, "monopole": self.api_monopole, "wire": self.api_wire,
                "sheet": self.api_sheet, "sweep": self.api_sweep, "plane_wave": self.api_plane_wave,
                "gaussian_beam": self.api_gaussian_beam, "current_source": self.api_current_source,
@@ -687,11 +686,6 @@ class ScriptEngine:
                "far_field": self.api_far_field, "warning": self.api_warning}
         for name, fn in api.items():
             I.register(name, fn)
-        for name in UNSUPPORTED:
-            def unsupported(*args, _n=name):
-                raise LuaError(f"{_n}{{}}: not supported by this build (it drives a subsystem outside the FDTD "
-                               f"time-stepping path)")
-            I.register(name, unsupported)
 
     # -- radar (ScriptEngine.cpp:1804-1848)
     def api_radar(self, t=None, *r):
@@ -1193,6 +1187,97 @@ class ScriptEngine:
             written = self.env().materials.set_mask(solid, (int(clo[0]), int(clo[1]), int(clo[2])), m)
         if written == 0:
             self.warn(f"{a.what}: shape is empty or lies completely outside the grid")
+        a.check_unknown()
+
+    def api_frame(self, t=None, *r):
+        """frame{} (ScriptEngine.cpp:1022-1030) with EnvironmentBuilder::wireframeBox
+        (Environment.cpp:111-127): the twelve edges of a box as square bars `bar` cells thick."""
+        a = Args(self, "frame", ["min", "max", "center", "size", "bar", "material", "name"], t)
+        mn, mx = self.read_box(a)
+        bar = float(f32(a.positive("bar", 2.0)))
+        m = self.read_material(a, "metal")
+        mn = [float(f32(v)) for v in mn]
+        mx = [float(f32(v)) for v in mx]
+        written = 0
+        for axis in range(3):
+            u, v = (axis + 1) % 3, (axis + 2) % 3
+            for su in (0, 1):
+                for sv in (0, 1):
+                    lo, hi = list(mn), list(mx)
+                    lo[u] = float(f32(mx[u] - bar)) if su else mn[u]
+                    hi[u] = float(f32(lo[u] + bar))
+                    lo[v] = float(f32(mx[v] - bar)) if sv else mn[v]
+                    hi[v] = float(f32(lo[v] + bar))
+                    written += self.env_builder().box(tuple(lo), tuple(hi), m)
+        if written == 0:
+            self.warn(f"{a.what}: shape is empty or lies completely outside the grid")
+        a.check_unknown()
+
+    def api_loop(self, t=None, *r):
+        """loop{} (ScriptEngine.cpp:1456-1524): a square loop antenna of `size` cells in the plane normal
+        to `normal`, current counter-clockwise about +normal. model "thin": four thin wires on the
+        node lattice fed across one edge in the middle of the -v side; "rod": a ring of 1x1-cell rods
+        fed in the middle of the -v side (4-edge gap); "current": four ideal current segments."""
+        a = Args(self, "loop", ["center", "normal", "size", "amplitude", "name", "model", "radius", "feed",
+                                "impedance", "material", *WAVEFORM_KEYS], t)
+        self.lock()
+        base = SourceDesc()
+        self.read_waveform(a, base)
+        c = [float(f32(v)) for v in a.vec("center", tuple(float(f32(v)) * 0.5 for v in self.settings.size))]
+        n = a.axis("normal", 2)
+        side = float(f32(a.positive("size", 4.0)))
+        u, v = (n + 1) % 3, (n + 2) % 3  # u x v = n (right-handed)
+        model = self.read_conductor(a)
+        name = a.str("name", "loop")
+        if model == "thin":
+            sz = _round_half_away(side)
+            if sz < 2:
+                a.fail("a thin-wire loop needs size >= 2 cells")
+            radius = self.read_radius(a, base.wavelength)
+            n0 = [_round_half_away(x) for x in c]
+            u0, v0 = n0[u] - sz // 2, n0[v] - sz // 2
+            ug = u0 + sz // 2
+            bottom, top, left, right = list(n0), list(n0), list(n0), list(n0)
+            bottom[v], top[v], left[u], right[u] = v0, v0 + sz, u0, u0 + sz
+            self.add_thin_wire(bottom, u, u0, u0 + sz, radius, ug)
+            self.add_thin_wire(top, u, u0, u0 + sz, radius)
+            self.add_thin_wire(left, v, v0, v0 + sz, radius)
+            self.add_thin_wire(right, v, v0, v0 + sz, radius)
+            gap = list(bottom)
+            gap[u] = ug
+            self.add_feed(base, gap, u, 1.0, 1, self.read_feed(a), name)
+            a.check_unknown()
+            return
+        if model == "rod":
+            sz = _round_half_away(side)
+            if sz < 3:
+                a.fail("a rod loop needs size >= 3 cells")
+            m = self.read_material(a, "metal")
+            g0 = [int(math.floor(x)) for x in c]
+            u0, v0 = g0[u] - sz // 2, g0[v] - sz // 2
+            ug = u0 + sz // 2
+            bottom, top, left, right = list(g0), list(g0), list(g0), list(g0)
+            bottom[v], top[v], left[u], right[u] = v0, v0 + sz - 1, u0, u0 + sz - 1
+            self.fill_rod(bottom, u, u0, ug, m)
+            self.fill_rod(bottom, u, ug + 1, u0 + sz, m)
+            self.fill_rod(top, u, u0, u0 + sz, m)
+            self.fill_rod(left, v, v0 + 1, v0 + sz - 1, m)
+            self.fill_rod(right, v, v0 + 1, v0 + sz - 1, m)
+            gap = list(bottom)
+            gap[u] = ug
+            self.add_feed(base, gap, u, 1.0, 4, self.read_feed(a), name)
+            a.check_unknown()
+            return
+        amp = float(f32(a.num("amplitude", 1.0)))
+        for along, at, at_sign, dir_sign in ((u, v, -1.0, 1.0), (v, u, 1.0, 1.0), (u, v, 1.0, -1.0), (v, u, -1.0, -1.0)):
+            center = list(c)
+            center[at] = float(f32(center[at] + f32(f32(at_sign * 0.5) * f32(side))))
+            axis_vec = [0.0, 0.0, 0.0]
+            axis_vec[along] = dir_sign
+            d = SourceDesc.dipole(tuple(center), tuple(axis_vec), base.wavelength, amp, side)
+            for k in ("wavelength", "phase", "waveform", "ramp_periods", "repeat_periods", "delay_periods", "enabled"):
+                setattr(d, k, getattr(base, k))
+            self.add_source(d)
         a.check_unknown()
 
     def taper_weights(self, a, n):

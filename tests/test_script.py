@@ -115,7 +115,9 @@ def test_array_and_cage():
     ("scene { courant = 0.6 }", "courant must be < 1/sqrt(3)"),
     ("dipole { length = 4 }", "thin-wire dipole needs length >= 5"),
     ("wire { from = {1, 1, 1}, to = {2, 2, 1} }", "differ along exactly one axis"),
-    ("loop {}", "loop{}: not supported"),
+    ("loop { size = 1 }", "a thin-wire loop needs size >= 2 cells"),
+    ("loop { size = 2, model = 'rod' }", "a rod loop needs size >= 3 cells"),
+    ("frame { min = {1, 1, 1}, max = {9, 9, 9}, bar = 0 }", "'bar' must be > 0"),
     ("radar { taper = 'kaiser' }", "taper must be \"uniform\", \"hamming\" or \"hann\""),
     ("view { mode = 'poyntng' }", "mode must be one of \"fields\", \"e\", \"b\", \"poynting\", \"signed\" "
                                   "(did you mean 'poynting'?)"),
@@ -204,3 +206,54 @@ def test_coax_builder_and_monitor_layout():
     kinds = [q[2] for q in g.q[:3]]
     assert kinds == [0, 1, 1]
     assert g.q[0][1] == 4 * 2 * 2 and g.q[1][1] == 8     # V: 4 sides x 2 node rows x 2 cells; I: 8 B terms
+
+
+def test_frame_builds_the_twelve_edges_of_a_box():
+    """frame{} (ScriptEngine.cpp:1022-1030, Environment.cpp:111-127): bars `bar` cells thick along the
+    twelve edges of the box; faces and interior stay empty."""
+    sc = run("""
+        scene { size = 48, pml = 4 }
+        frame { min = {10, 12, 14}, max = {30, 28, 34}, bar = 2, material = "pec" }
+    """).scene
+    sig = sc.materials.sigma  # (z, y, x)
+    metal = sig > 0
+    assert metal[14, 12, 10] and metal[33, 27, 29] and metal[20, 12, 10] and metal[14, 20, 29]
+    assert not metal[20, 20, 20] and not metal[20, 20, 10] and not metal[14, 20, 20]
+    # each edge bar: 2 x 2 cells across; edge lengths 20, 16, 20: 4 bars each, corners shared
+    onx = np.isin(np.arange(48), [10, 11, 28, 29])
+    ony = np.isin(np.arange(48), [12, 13, 26, 27])
+    onz = np.isin(np.arange(48), [14, 15, 32, 33])
+    inx = (np.arange(48) >= 10) & (np.arange(48) < 30)
+    iny = (np.arange(48) >= 12) & (np.arange(48) < 28)
+    inz = (np.arange(48) >= 14) & (np.arange(48) < 34)
+    Z, Y, X = np.meshgrid(np.arange(48), np.arange(48), np.arange(48), indexing="ij")
+    edge = inx[X] & iny[Y] & inz[Z] & ((onx[X] & ony[Y]) | (ony[Y] & onz[Z]) | (onx[X] & onz[Z]))
+    np.testing.assert_array_equal(metal, edge)
+
+
+def test_loop_models():
+    """loop{} (ScriptEngine.cpp:1456-1524): thin-wire square fed across one edge of the -v side, a ring
+    of rods with a four-edge gap, or four ideal current segments counter-clockwise about +normal."""
+    thin = run("""
+        scene { size = 48, pml = 4, wavelength = 24 }
+        loop { center = {24, 24, 24}, normal = "z", size = 8, radius = 0.1 }
+    """).scene
+    assert len(thin.ports) == 1 and thin.ports[0].axis == 0 and thin.ports[0].edges == 1
+    p = thin.ports[0]
+    assert tuple(p.texel) == (24, 20, 24)      # the middle of the -y side (u = x, v = y)
+    assert len(thin.wires) > 0 and all(w.z == 24 or w.z == 23 for w in thin.wires)
+    rod = run("""
+        scene { size = 48, pml = 4, wavelength = 24 }
+        loop { center = {24, 24, 24}, normal = "x", size = 6, model = "rod" }
+    """).scene
+    assert len(rod.ports) == 1 and rod.ports[0].edges == 4 and rod.ports[0].axis == 1
+    metal = rod.materials.sigma > 0  # (z, y, x): the ring lies in the plane x = 24
+    assert metal[:, :, 24].sum() == 4 * 6 - 4 - 1 and not metal[:, :, 23].any()
+    ideal = run("""
+        scene { size = 48, pml = 4, wavelength = 24 }
+        loop { center = {24, 24, 24}, normal = "z", size = 8, model = "current", amplitude = 2 }
+    """).scene
+    assert len(ideal.sources) == 4 and not ideal.ports
+    cs = sorted((tuple(round(v, 3) for v in s.center), tuple(round(v, 3) for v in s.polarization)) for s in ideal.sources)
+    assert cs == sorted([((24.0, 20.0, 24.0), (1.0, 0.0, 0.0)), ((28.0, 24.0, 24.0), (0.0, 1.0, 0.0)),
+                         ((24.0, 28.0, 24.0), (-1.0, 0.0, 0.0)), ((20.0, 24.0, 24.0), (0.0, -1.0, 0.0))])
