@@ -520,9 +520,9 @@ def run_phased(args):
     l0 = launch_count()
     res = []
     with ClockSampler(local) as clk:
-        for th, ph in dirs:
+        for k, (th, ph) in enumerate(dirs):
             sc = phased.build(th, ph)
-            r = phased.run_scene(sc, args.array_steps)
+            r = phased.run_scene(sc, args.array_steps, compare=(k == 0))
             r.pop("pattern")
             r["steer"] = (th, ph)
             r["pointing_error_deg"] = phased.angular_error(r["beam_theta"], r["beam_phi"], th, ph)
@@ -541,7 +541,12 @@ def run_phased(args):
                                "time-delay-steered feeds, 32-frequency far-field DFT, pattern 181x361 x 32 frequencies",
                    "directions_seed": args.seed, "l2": "inputs larger than L2 (1.8 GB of field state per scene)"},
         "pattern": {"evaluations": sum(r["pattern_evaluations"] for r in res), "seconds": pat_s,
-                    "huygens_points": res[0]["points"]},
+                    "huygens_points": res[0]["points"],
+                    "method": "per-face tensor-core GEMMs (emlab_ntff_dft_pattern_gemm)",
+                    "first_scene_direct_sums_s": res[0].get("other_pattern_s"),
+                    "first_scene_gemm_s": res[0]["pattern_s"],
+                    "first_scene_max_diff_of_peak": res[0].get("max_diff_of_peak"),
+                    "first_scene_power_rel_diff": res[0].get("power_rel_diff")},
         "beams": [{"steer": r["steer"], "beam": (r["beam_theta"], r["beam_phi"]),
                    "error_deg": round(r["pointing_error_deg"], 2)} for r in res],
         "gpu_launches": int(launches), "clocks": clk.summary(), "finite": all(r["finite"] for r in res),

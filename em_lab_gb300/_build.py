@@ -28,8 +28,8 @@ HOST_FLAGS = "-fPIC,-fopenmp,-ffp-contract=off,-O2"
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", HOST_FLAGS,
               "-I", str(ROOT / "include"), "-I", str(CSRC)]
 
-SOURCES = ["yee.cu", "yee_tma.cu", "monitors.cu", "capi.cu", "noalloc.cu", "dft_tc.cu", "render.cu", "stack.cu", "learn.cu", "radar.cu", "cpml.cu", "setup.cpp"]
-HEADERS = ["emlab_math.h", "emlab_internal.h", "setup.h", "yee_common.cuh", "grid_state.h"]
+SOURCES = ["yee.cu", "yee_tma.cu", "monitors.cu", "capi.cu", "noalloc.cu", "dft_tc.cu", "render.cu", "stack.cu", "learn.cu", "radar.cu", "cpml.cu", "pattern_tc.cu", "setup.cpp"]
+HEADERS = ["emlab_math.h", "emlab_internal.h", "setup.h", "yee_common.cuh", "grid_state.h", "sincos_reduced.cuh"]
 
 
 def _nvcc() -> str:

@@ -1432,6 +1432,11 @@ int emlab_ntff_dft_spectra(emlab_grid* g, int box, const float* directions, int 
 
 }  // extern "C"
 
+int emlab::dft_fold_now(emlab_grid* g) {
+    if (int rc = dft_fold(g)) return rc;
+    return check_launch();
+}
+
 int emlab::dft_carry_take(emlab_grid* g, const std::vector<int>& old_z0, const std::vector<int>& old_nz,
                           const std::vector<int>& idx, const std::vector<int>& new_z0, DftCarry& c) {
     c = DftCarry();

@@ -255,4 +255,6 @@ struct DftCarry {
 int dft_carry_take(emlab_grid* g, const std::vector<int>& old_z0, const std::vector<int>& old_nz,
                    const std::vector<int>& idx, const std::vector<int>& new_z0, DftCarry& c);
 int dft_carry_restore(emlab_grid* g, DftCarry& c);
+// folds the samples of the far-field DFT's partial block into its sums (capi.cu)
+int dft_fold_now(emlab_grid* g);
 }  // namespace emlab

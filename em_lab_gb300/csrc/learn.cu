@@ -74,10 +74,22 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }
 
 // One row (of A or B) of a 64-wide K chunk into the K-major core-matrix layout: the row's eight
-// 16-byte pieces go to (row / 8) * 1024 + piece * 128 + (row % 8) * 16.
+// 16-byte pieces go to (row / 8) * 1024 + piece * 128 + (row % 8) * 16. A row that is contiguous
+// along K and 16-byte aligned (vec) is read as eight 16-byte pieces, all in flight together; any
+// other stride, and the chunk that reaches past K, element by element.
 __device__ __forceinline__ void stage_row(unsigned char* tile, int row, const __nv_bfloat16* src, long long s_k,
-                                          bool live, int k0, int K) {
+                                          bool live, int k0, int K, bool vec) {
     const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+    if (vec && k0 + kTK <= K) {
+        uint4 piece[kTK / 8];
+#pragma unroll
+        for (int j = 0; j < kTK / 8; ++j)
+            piece[j] = live ? __ldg(reinterpret_cast<const uint4*>(src + k0 + j * 8)) : make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int j = 0; j < kTK / 8; ++j)
+            *reinterpret_cast<uint4*>(tile + (row >> 3) * 1024 + j * 128 + (row & 7) * 16) = piece[j];
+        return;
+    }
 #pragma unroll
     for (int j = 0; j < kTK / 8; ++j) {
         __align__(16) __nv_bfloat16 v[8];
@@ -117,12 +129,14 @@ __global__ void __launch_bounds__(128) nn_gemm_kernel(int M, int N, int K, const
     const int am = m0 + tid, bn = n0 + tid;  // the A row and the B row this thread stages
     const __nv_bfloat16* arow = A + (long long)min(am, M - 1) * sam;
     const __nv_bfloat16* brow = B + (long long)min(bn, N - 1) * sbn;
+    const bool vec_a = sak == 1 && (sam % 8) == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0;
+    const bool vec_b = sbk == 1 && (sbn % 8) == 0 && (reinterpret_cast<uintptr_t>(B) & 15) == 0;
     uint32_t phase = 0;
     bool ok = true;
     const int chunks = (K + kTK - 1) / kTK;
     for (int c = 0; c < chunks && ok; ++c) {
-        stage_row(sa, tid, arow, sak, am < M, c * kTK, K);
-        stage_row(sb, tid, brow, sbk, bn < N, c * kTK, K);
+        stage_row(sa, tid, arow, sak, am < M, c * kTK, K, vec_a);
+        stage_row(sb, tid, brow, sbk, bn < N, c * kTK, K, vec_b);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic stores -> tensor-core reads
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
@@ -160,9 +174,16 @@ __global__ void __launch_bounds__(128) nn_gemm_kernel(int M, int N, int K, const
             tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(j * 32), d);
             if (m >= M) continue;
             float* crow = C + (long long)m * ldc;
+            const int nb = n0 + j * 32;
+            if (nb + 32 <= N && (ldc % 4) == 0 && (reinterpret_cast<uintptr_t>(C) & 15) == 0) {
+#pragma unroll
+                for (int q = 0; q < 32; q += 4)
+                    *reinterpret_cast<float4*>(crow + nb + q) = make_float4(d[q], d[q + 1], d[q + 2], d[q + 3]);
+                continue;
+            }
 #pragma unroll
             for (int q = 0; q < 32; ++q) {
-                const int n = n0 + j * 32 + q;
+                const int n = nb + q;
                 if (n < N) crow[n] = d[q];
             }
         }

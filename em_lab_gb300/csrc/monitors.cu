@@ -4,6 +4,7 @@
 // with -fmad=false so its per-step FP32 arithmetic matches the CPU restatement bit for bit.
 // Monitors read the field generation that the step just produced.
 #include "emlab_internal.h"
+#include "sincos_reduced.cuh"
 
 namespace emlab {
 
@@ -323,15 +324,6 @@ __global__ void __launch_bounds__(128) ntff_pattern_kernel(const int* box, int p
     }
 }
 
-// sin and cos of psi: Cody-Waite reduction by 2 pi (2 pi split into its nearest float and the
-// remainder), then the hardware approximations on [-pi, pi]. Absolute error about |psi| 2^-24 +
-// 2^-21 (6e-6 at |psi| = 100), for pattern evaluations that do not restate a reference shader.
-__device__ __forceinline__ void sincos_reduced(float psi, float* s, float* c) {
-    const float n = rintf(psi * 0.159154943091895336f);
-    float r = fmaf(-n, 6.28318548202514648f, psi);
-    r = fmaf(-n, -1.74845560007441e-07f, r);
-    __sincosf(r, s, c);
-}
 
 // Surface sources of the fast pattern sums. PhasorSource: the stage-2 phasors of ntff_pattern.comp's
 // layout (8 float4 per point). DftSource: the far-field DFT sums of frequency f straight from X

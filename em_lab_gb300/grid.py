@@ -81,6 +81,7 @@ def load_library() -> C.CDLL:
         "emlab_ntff_dft_evaluate_all": ([P, fp, I, fp], I),
         "emlab_ntff_dft_configure_boxes": ([P, ip, I, fp, I, I], I),
         "emlab_ntff_dft_spectra": ([P, I, fp, I, fp], I),
+        "emlab_ntff_dft_pattern_gemm": ([P, I, fp, I, fp], I),
         "emlab_probe_gather": ([P, ip, I, fp], I),
         "emlab_flux_planes": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
         "emlab_flux_planes_noalloc": ([P, C.POINTER(abi.FluxPlane), I, dp], I),
@@ -554,6 +555,15 @@ class SimulationGrid:
         d[:, :3] = np.asarray(directions, np.float32)[:, :3]
         out = np.zeros((self._dft_nf, len(directions), 2), np.float32)
         _check(self._lib.emlab_ntff_dft_spectra(self._h, int(box), _fptr(d), len(d), _fptr(out)))
+        return out
+
+    def ntff_dft_pattern_gemm(self, box: int, directions) -> np.ndarray:
+        """(frequencies, directions, 2) as ntff_dft_spectra, the sums factorised into per-face
+        tensor-core GEMMs (emlab_ntff_dft_pattern_gemm)."""
+        d = np.zeros((len(directions), 4), np.float32)
+        d[:, :3] = np.asarray(directions, np.float32)[:, :3]
+        out = np.zeros((self._dft_nf, len(directions), 2), np.float32)
+        _check(self._lib.emlab_ntff_dft_pattern_gemm(self._h, int(box), _fptr(d), len(d), _fptr(out)))
         return out
 
     def probe_gather(self, origins) -> np.ndarray:

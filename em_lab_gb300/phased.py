@@ -1,12 +1,14 @@
 """Planar phased-array workload: N x N dipoles over a ground sheet under a radome,
 Taylor-tapered and steered by true time delays, in eight seeded directions; the far field at
-181 x 361 angles and 32 frequencies from the tensor-core DFT of the Huygens-box fields.
+181 x 361 angles and 32 frequencies from the tensor-core DFT of the Huygens-box fields, the pattern
+sums factorised face by face into tensor-core GEMMs.
 
 The scene is the script `scenes/phased_array.lua`; each steering direction is one scene on a grid
 of its own (a 384 x 384 x 256 scene fills the GPU by itself), stepped with the far-field DFT
-attached, then evaluated at every frequency over the full angle grid by emlab_ntff_dft_evaluate_all (the
-sums of ntff_pattern.comp / ntff_reduce.comp with range-reduced hardware sin/cos, two directions
-per thread, csrc/monitors.cu).
+attached, then evaluated at every frequency over the full angle grid by emlab_ntff_dft_pattern_gemm
+(the sums of ntff_pattern.comp / ntff_reduce.comp split per face into a u and a v factor: the sum over
+v one complex GEMM on the tcgen05 tensor cores, csrc/pattern_tc.cu) or, with pattern="direct",
+emlab_ntff_dft_evaluate_all (the direct sums with range-reduced hardware sin/cos, csrc/monitors.cu).
 """
 from __future__ import annotations
 
@@ -45,9 +47,11 @@ def angle_grid(n_theta: int = 181, n_phi: int = 361):
     return d.astype(np.float32), np.degrees(th), np.degrees(ph)
 
 
-def run_scene(sc, steps: int, n_theta: int = 181, n_phi: int = 361, freqs=None):
+def run_scene(sc, steps: int, n_theta: int = 181, n_phi: int = 361, freqs=None, pattern: str = "gemm",
+              compare: bool = False):
     """Steps one scene with the 32-frequency far-field DFT and evaluates the pattern. Returns timing,
-    the main-beam direction at the frequency nearest the design frequency and the pattern there."""
+    the main-beam direction at the frequency nearest the design frequency and the pattern there.
+    compare: also evaluate the direct sums and report the largest difference and their time."""
     L = sc.grid.pml_thickness
     g = SimulationGrid(sc.grid)
     m = sc.materials
@@ -66,9 +70,22 @@ def run_scene(sc, steps: int, n_theta: int = 181, n_phi: int = 361, freqs=None):
     t1 = time.perf_counter()
     dirs, th, ph = angle_grid(n_theta, n_phi)
     f0 = int(np.argmin(np.abs(rel - 1.0)))
-    if freqs is None:  # every frequency in one call (the fast pattern sums)
+    extra = {}
+    if freqs is None:  # every frequency in one call
         which = range(DFT_FREQS)
-        pat0 = g.ntff_dft_evaluate_all(dirs)[f0, :, 0].reshape(n_theta, n_phi)
+        full = g.ntff_dft_pattern_gemm(0, dirs) if pattern == "gemm" else g.ntff_dft_evaluate_all(dirs)
+        pat0 = full[f0, :, 0].reshape(n_theta, n_phi)
+        if compare:
+            g.synchronize()
+            tc = time.perf_counter()
+            other = g.ntff_dft_evaluate_all(dirs) if pattern == "gemm" else g.ntff_dft_pattern_gemm(0, dirs)
+            g.synchronize()
+            extra = {"other_pattern_s": time.perf_counter() - tc,
+                     "max_diff_of_peak": float(np.max(np.abs(full[:, :, 0] - other[:, :, 0]).max(axis=1) /
+                                                      np.maximum(np.abs(other[:, :, 0]).max(axis=1), 1e-30))),
+                     "power_rel_diff": float(np.max(np.abs(full[:, 0, 1] - other[:, 0, 1]) /
+                                                    np.maximum(np.abs(other[:, 0, 1]), 1e-30)))}
+            t_extra = time.perf_counter() - tc
     else:
         which = freqs
         pat0 = None
@@ -79,7 +96,7 @@ def run_scene(sc, steps: int, n_theta: int = 181, n_phi: int = 361, freqs=None):
         if pat0 is None:
             pat0 = g.ntff_dft_evaluate(f0, dirs)[:, 0].reshape(n_theta, n_phi)
     g.synchronize()
-    t2 = time.perf_counter()
+    t2 = time.perf_counter() - (t_extra if extra else 0.0)
     finite = g.check_finite()
     g.close()
     upper = pat0[: n_theta // 2 + 1]  # theta <= 90 deg: the half space above the ground sheet
@@ -87,7 +104,7 @@ def run_scene(sc, steps: int, n_theta: int = 181, n_phi: int = 361, freqs=None):
     return {"cells": int(np.prod(sc.grid.size)), "steps": steps, "points": points, "step_s": t1 - t0,
             "pattern_s": t2 - t1, "pattern_evaluations": len(list(which)) * len(dirs),
             "beam_theta": float(th[i]), "beam_phi": float(ph[j]), "f_rel": float(rel[f0]), "finite": bool(finite),
-            "pattern": pat0}
+            "pattern": pat0, **extra}
 
 
 def angular_error(t1, p1, t2, p2):

@@ -297,6 +297,13 @@ int emlab_ntff_dft_configure_boxes(emlab_grid* g, const int* boxes, int n_boxes,
  * out[f * n_dirs * 2 + 1] = radiated power at f, from the sums scaled by 2 / samples. Two launches
  * for all frequencies; the device scratch grows to the largest request and is kept. */
 int emlab_ntff_dft_spectra(emlab_grid* g, int box, const float* directions, int n_dirs, float* out);
+/* The same pattern as emlab_ntff_dft_spectra (all frequencies, one box, out in its layout), the sums
+ * factorised face by face: on each face the phase e^{jk r.p} splits into a u and a v factor, the sum
+ * over v is one complex GEMM over all directions on the tcgen05 tensor cores (BF16 operands split
+ * into high and low halves, FP32 accumulation) and the sum over u a per-direction dot product; the
+ * sines and cosines drop from directions x points to directions x (nu + nv) per face. Within about
+ * 1e-4 of the pattern maximum of the direct sums. 1 to 2^20 directions. */
+int emlab_ntff_dft_pattern_gemm(emlab_grid* g, int box, const float* directions, int n_dirs, float* out);
 
 /* ---- volume rendering: VolumeRenderer (src/VolumeRenderer.cpp:66-118, shaders/raymarch.frag) */
 /* Camera and look of one rendered frame. inv_view_proj: inverse of projection * view, column-
