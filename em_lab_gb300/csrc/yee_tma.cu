@@ -847,17 +847,32 @@ bool launch_t(const YeeArgs& a, const TmaMaps* m, int gen, unsigned* err, cudaSt
 
 // Chooses the z chunk length of the persistent schedule: the CTA with the most items bounds the
 // launch, and every chunk above z = 0 re-reads one plane, so minimise ceil(items / G) * (zc + 1).
+// Items differ in cost (a tile with absorber or material cells takes longer per plane), and the
+// ticket schedule evens them out only when every CTA takes several: the chunk length is chosen among
+// those giving at least kItemsPerCta items per CTA, as far as chunks of kMinBalancedPlanes planes
+// allow (shorter chunks would re-read too many planes: every chunk above z = 0 re-reads one).
+constexpr int kItemsPerCta = 4;
+constexpr int kMinBalancedPlanes = 16;
+
 PairSched pair_schedule(const YeeArgs& a, int TY, int G) {
     PairSched ps;
     ps.tiles_x = (a.nx + 63) / 64;
     ps.tiles = ps.tiles_x * ((a.ny + TY - 1) / TY);
+    const int max_chunks = std::max(1, a.nz / 4);
+    const long long want = std::min((long long)kItemsPerCta * G,
+                                    (long long)std::max(1, a.nz / kMinBalancedPlanes) * ps.tiles);
     long long best = -1;
-    for (int chunks = 1; chunks <= std::max(1, a.nz / 4); ++chunks) {
+    for (int chunks = 1; chunks <= max_chunks; ++chunks) {
         const int zc = (a.nz + chunks - 1) / chunks;
         const int n = (a.nz + zc - 1) / zc;
         const long long items = (long long)n * ps.tiles;
+        if (items < want) continue;
         const long long cost = (items + G - 1) / G * (zc + (n > 1 ? 1 : 0));
         if (best < 0 || cost < best) best = cost, ps.zc = zc, ps.items = (int)items;
+    }
+    if (best < 0) {  // no chunk count reaches `want` exactly (zc rounding): the finest split
+        ps.zc = (a.nz + max_chunks - 1) / max_chunks;
+        ps.items = (int)((long long)((a.nz + ps.zc - 1) / ps.zc) * ps.tiles);
     }
     return ps;
 }
@@ -944,7 +959,11 @@ std::vector<int4> ragged_items(const std::vector<int>& z0, const std::vector<int
     }
     // one chunk length for every scene: the CTA with the most items bounds the launch, and every
     // chunk above a scene's first plane re-reads one plane
-    int zc_best = deepest;
+    // as pair_schedule: at least kItemsPerCta items per CTA where the scenes allow it
+    long long finest = 0;
+    for (size_t i = 0; i < n; ++i) finest += tiles[i] * std::max(1, nz[i] / kMinBalancedPlanes);
+    const long long want = std::min((long long)kItemsPerCta * g, finest);
+    int zc_best = std::min(deepest, 4);
     long long best = -1;
     for (int zc = std::min(deepest, 4); zc <= deepest; ++zc) {
         long long items = 0, extra = 0;
@@ -953,6 +972,7 @@ std::vector<int4> ragged_items(const std::vector<int>& z0, const std::vector<int
             items += tiles[i] * c;
             extra += c > 1 ? 1 : 0;
         }
+        if (items < want) continue;
         const long long cost = (items + g - 1) / g * (zc + (extra ? 1 : 0));
         if (best < 0 || cost < best) best = cost, zc_best = zc;
     }
