@@ -377,8 +377,9 @@ int emlab_stack_commit(emlab_grid* g);
  * sources are filtered and capped as setSources does for one grid. */
 int emlab_stack_set_sources(emlab_grid* g, const emlab_source* sources, const int* scene_of, size_t n);
 /* Drops the scenes whose keep[i] is 0: the others' fields, materials and sources move to a shorter
- * stack (device copies; step count kept). Monitors are detached: ports are re-attached by the
- * caller at the scenes' new planes (emlab_stack_info). */
+ * stack (device copies; step count kept). The far-field DFT boxes that lie inside kept scenes move
+ * with them, sums included (emlab_ntff_dft_configure_boxes); the other monitors are detached: ports
+ * are re-attached by the caller at the scenes' new planes (emlab_stack_info). */
 int emlab_stack_compact(emlab_grid* g, const unsigned char* keep);
 
 /* ---- probes and flux: FieldAnalyzer (src/FieldAnalyzer.hpp:73-130) ----------------------- */
