@@ -110,6 +110,19 @@ def analyse_cut(cut, dbi):
     cut["front_back"] = dbi[peak] - at(peak + n // 2)
 
 
+def _len32(v) -> float:
+    """|v| of a float vector in float32, as glm::length: a diverged field gives inf (the non-finite
+    check reports it), without numpy's overflow warnings."""
+    a = np.asarray(v, np.float32)
+    with np.errstate(over="ignore", invalid="ignore"):
+        return math.sqrt(float(np.float32(np.dot(a, a))))
+
+
+def _cross32(a, b):
+    with np.errstate(over="ignore", invalid="ignore"):
+        return np.cross(np.asarray(a, np.float32), np.asarray(b, np.float32))
+
+
 def probe_origin(pos, size):
     p = [min(max(float(v), 0.0), float(n - 1)) for v, n in zip(pos, size)]
     return [min(max(int(math.floor(v)) - 1, 0), max(n - 3, 0)) for v, n in zip(p, size)]
@@ -415,14 +428,14 @@ class Instruments:
                 B = [sample_block(b, o, extent, (pos[0], pos[1] - 0.5, pos[2] - 0.5), 0),
                      sample_block(b, o, extent, (pos[0] - 0.5, pos[1], pos[2] - 0.5), 1),
                      sample_block(b, o, extent, (pos[0] - 0.5, pos[1] - 0.5, pos[2]), 2)]
-                S = np.cross(np.asarray(E, np.float32), np.asarray(B, np.float32))
+                S = _cross32(E, B)
                 cell = [min(max(int(math.floor(v)), 0), n - 1) for v, n in zip(pos, self.size)]
                 m = self.sc.materials.get(cell)
                 p["sample"] = {"E": E, "B": B, "S": [float(v) for v in S], "sigma": m.sigma, "eps": m.epsilon_r}
                 finite = finite and all(math.isfinite(v) for v in E + B)
                 if p["log"]:
-                    em = math.sqrt(float(np.float32(np.dot(np.asarray(E, np.float32), np.asarray(E, np.float32)))))
-                    bm = math.sqrt(float(np.float32(np.dot(np.asarray(B, np.float32), np.asarray(B, np.float32)))))
+                    em = _len32(E)
+                    bm = _len32(B)
                     p["log"].write(",".join([str(self.measure_step), _g(self.measure_time)] +
                                             [_g(v) for v in E + B + [em, bm] + list(p["sample"]["S"])]) + "\n")
         if self.planes:
@@ -640,8 +653,8 @@ class Instruments:
             if s is None:
                 continue
             E, B, S = s["E"], s["B"], s["S"]
-            em = math.sqrt(float(np.float32(np.dot(np.asarray(E, np.float32), np.asarray(E, np.float32)))))
-            bm = math.sqrt(float(np.float32(np.dot(np.asarray(B, np.float32), np.asarray(B, np.float32)))))
+            em = _len32(E)
+            bm = _len32(B)
             pos = p["pos"]
             out(f"  {'>' if i == 0 else ' '} probe {p['name']:<14s} ({pos[0]:6.1f} {pos[1]:6.1f} {pos[2]:6.1f}): "
                 f"|E|={em:.5f} E=({E[0]:+.4f} {E[1]:+.4f} {E[2]:+.4f}) |B|={bm:.5f} S=({S[0]:+.2e} {S[1]:+.2e} "
