@@ -674,7 +674,7 @@ def main():
     else:
         tail.append(grid.ntff_evaluate(dirs))
     barrier()
-    e2e_value, e2e_s = replica_throughput(cells * frames * frame, time.perf_counter() - t0, dist, "cuda")
+    e2e_value, _ = replica_throughput(cells * frames * frame, time.perf_counter() - t0, dist, "cuda")
     # per step: FP64-evaluated source signals (FP32) and the monitor rotations (cos/sin pairs)
     h2d = 4 * len(sc.sources) + 16 * (1 if sc.ports else 0) + 16 * (1 if args.workload == "plain_small" else 0)
     # per frame: the probe's 54 texels and the flux planes' 16 x 16 workgroup partials; per step: the

@@ -43,7 +43,6 @@ def random_blocks(builder: EnvironmentBuilder, fraction: float, seed: int, lo: i
     """Seeded dielectric blocks until `fraction` of the cells is filled: edges uniform in
     edge_range, eps_r uniform in [1, 10], sigma log-uniform in [1e-4, 1e-1] S/m."""
     rng = np.random.default_rng(seed)
-    mats = builder.scene.materials
     nx, ny, nz = builder.scene.grid.size
     target = fraction * nx * ny * nz
     filled = np.zeros((nz, ny, nx), bool)

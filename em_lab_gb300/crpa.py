@@ -22,8 +22,6 @@ import math
 
 import numpy as np
 
-from . import abi
-
 f32 = np.float32
 MAP_SIZE = 61
 

@@ -259,7 +259,7 @@ class Net:
             _check(lib.emlab_nn_col_sum(self._fp(dz), B, o, self._fp(self.gb[name]), s))
             self._gemm(B, i, o, dzb, o, 1, self.Wb[name], 1, i, self.dx[name], i)
             up = self.dx[name]
-        c1, c2 = CONV
+        c2 = CONV[1]
         # conv2: dz2 over rows (b, l) x 64 channels = the encoder part of d(X0)
         _check(lib.emlab_nn_act_grad(self._fp(up), ENC + AUX, 0, self._fp(self.z2), B, ENC, 1, self._fp(self.dz2),
                                      self._p(self.dz2b), s))
@@ -603,7 +603,7 @@ def experiment(train_seed, n_train, eval_seed, n_eval, epochs=60, batch=256, lr=
                     continue
                 xe, ze, zr = features(sc, ser, fe)
                 xs.append(xe), zts.append(ze), ztr.append(zr), ftr.append(fe), keep.append(k)
-            z_pred, spread, f_pred = ensemble_predict(nets, np.stack(xs), np.stack(zts))
+            z_pred, _, f_pred = ensemble_predict(nets, np.stack(xs), np.stack(zts))
             infer_wall = time.perf_counter() - t2
             # the learned path with its fallback, in one run: every scene is stopped at its early
             # window if the ensemble's spread is within the threshold, else it runs on to ring-down

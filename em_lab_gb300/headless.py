@@ -19,8 +19,6 @@ import os
 import sys
 import time
 
-import numpy as np
-
 
 def _load(path, overrides):
     from .script import ScriptEngine

@@ -1057,7 +1057,6 @@ class Compiler:
 
     def suffixed_expr(self):
         e = self.primary_expr()
-        I = self.I
         while True:
             tok = self.peek()
             if tok.kind == "op":
@@ -1149,9 +1148,7 @@ class Compiler:
 
     def table_cons(self):
         self.expect("op", "{")
-        pos = []  # positional expressions
-        keyed = []  # (key expr, value expr, order)
-        items = []
+        items = []  # ("p", None, value) positional, ("k", key, value) keyed, in source order
         while not self.check_op("}"):
             tok = self.peek()
             if tok.kind == "op" and tok.val == "[":
@@ -1501,7 +1498,7 @@ class Interpreter:
                 return (None,)
             kk = keys[idx]
             return (_unkey(kk), t.hash[kk])
-        nextf = self.register("next", l_next)
+        self.register("next", l_next)
 
         def l_pairs(t=None, *r):
             h = self.metamethod(t, "__pairs")

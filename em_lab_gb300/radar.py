@@ -406,7 +406,7 @@ class RadarMonitor:
         echo = np.abs(meas[:N, :Cn].astype(np.float64) - self.cal[:N, :Cn].astype(np.float64)).max()
         img["echo_db"] = _to_db((echo / self.peak_tx) ** 2)
         img["complete_range"] = self.range_max
-        z, D, M = self.baseband(meas, N)
+        z, D, _ = self.baseband(meas, N)
         dr = f32(0.125) * f32(self.wl)
         nr = max(2, int((f32(self.range_max) - f32(self.range_min)) / dr) + 1)
         naz = 2 * int(_round_half_away(float(self.setup["fov_az"]) / 1.5)) + 1

@@ -17,7 +17,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import abi
-from .lua import Interpreter, LuaError, LuaFunction, LuaTable, lua_type, tostr
+from .lua import Interpreter, LuaError, LuaFunction, LuaTable, tostr
 from .scene import (K_PERFECT_EDGE_SIGMA, BoxShape, CoaxSetup, CylinderShape, DifferenceShape, EllipsoidShape,
                     EnvironmentBuilder, FluxSetup, LambdaShape, Material, SourceDesc, TransformedShape, WallShape,
                     rotation_from_euler_degrees)

@@ -144,8 +144,7 @@ def load():
         from em_lab_gb300 import _build
         _build.build_oracle()
     lib = C.CDLL(str(_PATH))
-    P, I, SZ, F, D = C.c_void_p, C.c_int, C.c_size_t, C.c_float, C.c_double
-    ip, dp, fp = C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_float)
+    I, F, D = C.c_int, C.c_float, C.c_double
     lib.oracle_expf.argtypes, lib.oracle_expf.restype = [F], F
     lib.oracle_float_to_half.argtypes, lib.oracle_float_to_half.restype = [F], C.c_uint16
     lib.oracle_half_to_float.argtypes, lib.oracle_half_to_float.restype = [C.c_uint16], F

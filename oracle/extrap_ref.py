@@ -64,7 +64,7 @@ def forward(params, x, zt, exact=False):
     h = np.concatenate([enc, _r(zt, exact)], axis=1)
     cache.update(cols1=cols1, z1=z1, cols2=cols2, z2=z2, h0=h)
     zs, hs = {}, {"fc1": h}
-    for k, (name, i, o, relu) in enumerate(X.HEAD):
+    for k, (name, _, _, relu) in enumerate(X.HEAD):
         z = hs[name] @ W[name].T + b[name]
         zs[name] = z
         if k + 1 < len(X.HEAD):
@@ -82,7 +82,7 @@ def backward(params, cache, t, n, exact=False):
     dy[:n] = 2.0 * (y[:n] - np.asarray(t[:n], np.float64)) / (n * X.OUT)
     grads = {}
     up = dy
-    for name, i, o, relu in reversed(X.HEAD):
+    for name, _, _, relu in reversed(X.HEAD):
         dz = up * (cache["z"][name] > 0.0) if relu else up
         dzr = _r(dz, exact)
         grads[name] = (dzr.T @ cache["h"][name], dz.sum(axis=0))
