@@ -937,6 +937,8 @@ int emlab_grid_check_finite(emlab_grid* g) {
 int emlab_ports_configure(emlab_grid* g, const emlab_port* ports, size_t n, float wavelength, float averaging_periods,
                           int sweep, size_t record_steps) {
     if (int rc = require_grid(g)) return rc;
+    // a pending take's rows are laid out for the current ports
+    EMLAB_REQUIRE(!g->series_busy[0] && !g->series_busy[1], "collect the pending series takes before configuring ports");
     invalidate_graphs(g);
     EMLAB_REQUIRE(ports || n == 0, "null port array");
     EMLAB_CUDA(cudaSetDevice(g->device));

@@ -372,6 +372,7 @@ int emlab_stack_compact(emlab_grid* g, const unsigned char* keep) {
     StackLayout& s = g->stack;
     const int n = s.scenes();
     EMLAB_REQUIRE(n > 0, "not a stack of scenes");
+    EMLAB_REQUIRE(!g->series_busy[0] && !g->series_busy[1], "collect the pending series takes before compacting");
     EMLAB_CUDA(cudaSetDevice(g->device));
     EMLAB_CUDA(cudaStreamSynchronize(g->stream));
     if (int rc = stack_commit(g)) return rc;

@@ -222,7 +222,9 @@ int emlab_ports_take_series(emlab_grid* g, float* out, size_t max_steps, size_t*
 /* The same take without waiting: queues the copy of the series recorded since the last take into one
  * of two pinned host slots behind the work already queued on the grid's stream, and restarts the
  * recording (the steps queued next record from the start of the buffer). *slot names the slot,
- * *steps the rows it will hold. At most two takes may wait to be collected. */
+ * *steps the rows it will hold. At most two takes may wait to be collected; while one waits,
+ * emlab_ports_configure and emlab_stack_compact are refused (its rows are laid out for the current
+ * ports). */
 int emlab_ports_take_series_async(emlab_grid* g, int* slot, size_t* steps);
 /* Waits (bounded: EMLAB_ERR_TIMEOUT after timeout_ms; <= 0 waits 60 s) for a slot's copy, copies at
  * most max_steps rows to out ((steps, ports, 2) floats) and frees the slot. Work queued after the
@@ -379,7 +381,8 @@ int emlab_stack_set_sources(emlab_grid* g, const emlab_source* sources, const in
 /* Drops the scenes whose keep[i] is 0: the others' fields, materials and sources move to a shorter
  * stack (device copies; step count kept). The far-field DFT boxes that lie inside kept scenes move
  * with them, sums included (emlab_ntff_dft_configure_boxes); the other monitors are detached: ports
- * are re-attached by the caller at the scenes' new planes (emlab_stack_info). */
+ * are re-attached by the caller at the scenes' new planes (emlab_stack_info). Refused while an
+ * asynchronous series take waits to be collected. */
 int emlab_stack_compact(emlab_grid* g, const unsigned char* keep);
 
 /* ---- probes and flux: FieldAnalyzer (src/FieldAnalyzer.hpp:73-130) ----------------------- */

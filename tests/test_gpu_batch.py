@@ -227,7 +227,8 @@ def test_graph_chunks_on_a_stack_after_compaction():
 def test_asynchronous_series_takes_equal_the_synchronous_take():
     """emlab_ports_take_series_async / _collect_series: two takes may wait at once, each holds the
     rows recorded before it, and the series equals the synchronous take of the same steps; a third
-    take while both slots wait, or collecting a free slot, is refused."""
+    take while both slots wait, collecting a free slot, or configuring ports while a take waits, is
+    refused."""
     sc = configs.batched_scene(3, 0)
     out = []
     for mode in ("sync", "async"):
@@ -252,6 +253,8 @@ def test_asynchronous_series_takes_equal_the_synchronous_take():
                 g.ports_collect_series(a[0], a[1])
             g.step(64)
             c = g.ports_take_series_async()
+            with pytest.raises(RuntimeError, match="pending series takes"):
+                g.ports_configure([sc.ports[0].to_c()], sc.wavelength, 4.0, False, 64)
             parts += [g.ports_collect_series(*b), g.ports_collect_series(*c)]
             assert a[1] == b[1] == c[1] == 64
         out.append(np.concatenate(parts))
