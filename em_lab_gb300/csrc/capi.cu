@@ -1791,6 +1791,36 @@ int emlab_debug_set_wait_limit(int polls) {
     return EMLAB_OK;
 }
 
+int emlab_debug_pair_schedule(int nx, int ny, int nz, int tile_rows, int ctas, int* zc, int* items) {
+    EMLAB_REQUIRE(zc && items, "null output");
+    EMLAB_REQUIRE(nx > 0 && ny > 0 && nz > 0, "empty grid");
+    EMLAB_REQUIRE(tile_rows == 4 || tile_rows == 8 || tile_rows == 16, "pair tiles have 4, 8 or 16 rows");
+    EMLAB_REQUIRE(ctas > 0, "no CTAs");
+    pair_schedule_shape(nx, ny, nz, tile_rows, ctas, zc, items);
+    return EMLAB_OK;
+}
+
+int emlab_debug_ragged_items(const int* z0, const int* nx, const int* ny, const int* nz, int n_scenes, int tile_rows,
+                             int ctas, int* out, size_t cap, size_t* n_items) {
+    EMLAB_REQUIRE(z0 && nx && ny && nz && n_items && n_scenes > 0, "null argument or no scenes");
+    EMLAB_REQUIRE(tile_rows == 4 || tile_rows == 8 || tile_rows == 16, "pair tiles have 4, 8 or 16 rows");
+    EMLAB_REQUIRE(ctas > 0, "no CTAs");
+    std::vector<int> vz0(z0, z0 + n_scenes), vnx(nx, nx + n_scenes), vny(ny, ny + n_scenes), vnz(nz, nz + n_scenes);
+    for (int i = 0; i < n_scenes; ++i)
+        EMLAB_REQUIRE(vnx[i] > 0 && vny[i] > 0 && vnz[i] > 0 && vnx[i] < 65536 && vny[i] < 65536 && vz0[i] >= 0,
+                      "scene extents out of range");
+    const std::vector<int4> items = ragged_items(vz0, vnx, vny, vnz, tile_rows, ctas);
+    *n_items = items.size();
+    if (!out) return EMLAB_OK;
+    EMLAB_REQUIRE(cap >= items.size(), "output too small");
+    for (size_t k = 0; k < items.size(); ++k) {
+        const int4 t = items[k];
+        int* o = out + 5 * k;
+        o[0] = t.x & 0xffff, o[1] = (int)((unsigned)t.x >> 16), o[2] = t.y, o[3] = t.z, o[4] = t.w;
+    }
+    return EMLAB_OK;
+}
+
 int emlab_debug_expf(const float* in, float* out, size_t n) {
     if (!in || !out) return fail(EMLAB_ERR_INVALID, "null argument");
     if (!n) return EMLAB_OK;

@@ -106,6 +106,8 @@ bool tma_maps_ready(const TmaMaps* m, int gen);
 // length for all scenes, chosen for g CTAs as the uniform schedule chooses it
 std::vector<int4> ragged_items(const std::vector<int>& z0, const std::vector<int>& nx, const std::vector<int>& ny,
                                const std::vector<int>& nz, int ty, int g);
+// the uniform grid's pair-kernel schedule for g CTAs: planes per z chunk and work items
+void pair_schedule_shape(int nx, int ny, int nz, int ty, int g, int* zc, int* items);
 // Launches the TMA kernel reading generation `gen`; err receives a nonzero word if a wait timed out.
 // *tickets receives the work-counter tickets the launch consumes (0 for the non-persistent kernels)
 bool launch_yee_tma(const YeeArgs& a, const TmaMaps* m, int gen, bool wide, unsigned* err, cudaStream_t s,

@@ -948,6 +948,13 @@ bool tma_maps_encode(TmaMaps* m, int gen, const YeeArgs& a, bool wide) {
 
 bool tma_maps_ready(const TmaMaps* m, int gen) { return m && m->ok[gen] && m->cls_ok; }
 
+void pair_schedule_shape(int nx, int ny, int nz, int ty, int g, int* zc, int* items) {
+    YeeArgs a{};
+    a.nx = nx, a.ny = ny, a.nz = nz;
+    const PairSched ps = pair_schedule(a, ty, g);
+    *zc = ps.zc, *items = ps.items;
+}
+
 std::vector<int4> ragged_items(const std::vector<int>& z0, const std::vector<int>& nx, const std::vector<int>& ny,
                                const std::vector<int>& nz, int ty, int g) {
     const size_t n = z0.size();

@@ -106,6 +106,8 @@ def load_library() -> C.CDLL:
         "emlab_lines_read": ([P, fp, fp], I),
         "emlab_debug_expf": ([fp, fp, SZ], I),
         "emlab_debug_set_wait_limit": ([I], I),
+        "emlab_debug_pair_schedule": ([I, I, I, I, I, ip, ip], I),
+        "emlab_debug_ragged_items": ([ip, ip, ip, ip, I, I, I, ip, SZ, C.POINTER(SZ)], I),
         "emlab_grid_set_cpml": ([P, C.POINTER(abi.Cpml)], I),
         "emlab_edge_materials": ([fp, fp, I, I, I, C.POINTER(abi.EdgeOverride), SZ, C.POINTER(abi.WireTerm), SZ,
                                   fp, fp, fp, fp, C.POINTER(C.c_uint32)], I),
@@ -148,6 +150,28 @@ def debug_set_wait_limit(polls: int) -> None:
     """Test hook: polls of an on-device barrier wait before a kernel gives up and the grid reports
     EMLAB_ERR_TIMEOUT (0: the first wait of every launch gives up; WAIT_POLLS_DEFAULT restores)."""
     _check(load_library().emlab_debug_set_wait_limit(int(polls)))
+
+
+def pair_schedule(nx: int, ny: int, nz: int, tile_rows: int, ctas: int):
+    """The persistent pair kernel's schedule on a single grid (host arithmetic): (planes per z chunk,
+    work items)."""
+    zc, items = C.c_int(), C.c_int()
+    _check(load_library().emlab_debug_pair_schedule(int(nx), int(ny), int(nz), int(tile_rows), int(ctas),
+                                                    C.byref(zc), C.byref(items)))
+    return zc.value, items.value
+
+
+def ragged_items(z0, nx, ny, nz, tile_rows: int, ctas: int) -> np.ndarray:
+    """The persistent pair kernel's work items on a stack of scenes with their own cross-sections
+    (host arithmetic): (items, 5) int32 rows (x0, y0, first plane, end plane, scene)."""
+    arrs = [np.ascontiguousarray(v, np.int32) for v in (z0, nx, ny, nz)]
+    ptr = [a.ctypes.data_as(C.POINTER(C.c_int)) for a in arrs]
+    lib, n = load_library(), C.c_size_t()
+    _check(lib.emlab_debug_ragged_items(*ptr, len(arrs[0]), int(tile_rows), int(ctas), None, 0, C.byref(n)))
+    out = np.zeros((n.value, 5), np.int32)
+    _check(lib.emlab_debug_ragged_items(*ptr, len(arrs[0]), int(tile_rows), int(ctas),
+                                        out.ctypes.data_as(C.POINTER(C.c_int)), n.value, C.byref(n)))
+    return out
 
 
 def device_expf(x) -> np.ndarray:

@@ -459,6 +459,14 @@ int emlab_source_lists(const emlab_source* sources, size_t n, int nx, int ny, in
 int emlab_debug_set_wait_limit(int polls);
 /* Evaluates the device emlab_expf on n inputs (bit-exactness check against the host). */
 int emlab_debug_expf(const float* in, float* out, size_t n);
+/* Host-side schedule of the persistent pair kernel (no device needed), for `ctas` resident CTAs and
+ * 64 x tile_rows tiles: on a single grid, the planes per z chunk and the number of work items;
+ * on a stack of scenes with their own cross-sections (emlab_stack_configure_scenes), the work items
+ * themselves, 5 ints each (x0, y0, first plane, end plane, scene) in launch order. *n_items receives
+ * the count; out may be NULL to query it, else it holds cap items. */
+int emlab_debug_pair_schedule(int nx, int ny, int nz, int tile_rows, int ctas, int* zc, int* items);
+int emlab_debug_ragged_items(const int* z0, const int* nx, const int* ny, const int* nz, int n_scenes, int tile_rows,
+                             int ctas, int* out, size_t cap, size_t* n_items);
 
 #ifdef __cplusplus
 }
